@@ -1,0 +1,87 @@
+"""Builds libdegpu.so in place: every CUDA translation unit for sm_103a, in parallel.
+
+Usage: python build.py [--jobs N] [--verbose]
+The parity translation units (inst_parity_*.cu) are compiled with -fmad=false so that no
+multiply-add on that path is contracted into an FMA.
+"""
+import argparse
+import concurrent.futures as cf
+import glob
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "libdegpu.so")
+BUILD = os.path.join(HERE, "_build")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+          "-diag-suppress", "20091", "-I", os.path.join(HERE, "..", "..", "include")]
+PARITY = ["-fmad=false", "-DDEGPU_NO_FMAD"]
+
+
+def nvcc():
+    import shutil
+    found = shutil.which("nvcc")
+    if found:
+        return found
+    for root in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if root and os.path.exists(os.path.join(root, "bin", "nvcc")):
+            return os.path.join(root, "bin", "nvcc")
+    raise RuntimeError("nvcc not found")
+
+
+def sources():
+    return sorted(glob.glob(os.path.join(HERE, "*.cu")))
+
+
+def flags_for(src):
+    name = os.path.basename(src)
+    f = list(ARCH) + list(COMMON)
+    if name.startswith("inst_parity"):
+        f += PARITY
+    return f
+
+
+def needs(obj, src):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    deps = [src] + glob.glob(os.path.join(HERE, "*.cuh")) + glob.glob(os.path.join(HERE, "*.inc")) + \
+        glob.glob(os.path.join(HERE, "..", "..", "include", "*.h"))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def compile_one(src, verbose):
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    if not needs(obj, src):
+        return obj, ""
+    cmd = [nvcc()] + flags_for(src) + ["-c", src, "-o", obj]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build(jobs=None, verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sources()
+    jobs = jobs or min(len(srcs), os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        objs = [f.result()[0] for f in [ex.submit(compile_one, s, verbose) for s in srcs]]
+    if not os.path.exists(OUT) or any(os.path.getmtime(o) > os.path.getmtime(OUT) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart", "-lnvrtc", "-lcuda"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return OUT
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--jobs", type=int, default=None)
+    ap.add_argument("--verbose", action="store_true")
+    args = ap.parse_args()
+    print(build(args.jobs, args.verbose))

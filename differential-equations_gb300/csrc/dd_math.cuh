@@ -1,0 +1,237 @@
+// dd_math.cuh — correctly rounded (in practice) FP64 pow, sin and cos for the parity path.
+//
+// The crate computes `err.powf(-1/order)` in its step-size controller
+// (src/methods/erk/dormandprince/ordinary.rs:152-157), `(0.01/der12).powf(1/order)` in its
+// initial step heuristic (src/methods/h_init.rs:116-125), and user right-hand sides call
+// `sin`/`cos`.  All of these go to the platform libm.  A GPU integrator can only reproduce the
+// crate's accept/reject sequence bit for bit if these values are the same on both sides, so the
+// parity path rounds them correctly: each function evaluates its result in double-double
+// arithmetic to a relative accuracy near 2^-100 and rounds once.  The rounded result then equals
+// the correctly rounded value except when the exact value lies within ~2^-100 of a rounding
+// boundary, which for the inputs an integrator produces does not happen in practice.
+//
+// Methods (all standard published techniques):
+//  - error-free transformations TwoSum / FastTwoSum (Knuth; Dekker) and TwoProduct via FMA
+//    (Ogita, Rump, Oishi 2005), double-double arithmetic (Dekker 1971; Hida, Li, Bailey 2001);
+//  - x^(±1/5): one double-double Newton step on r^5 = x from a few-ulp starting value
+//    (quadratic convergence), then the factor x^(2^-54/5) = exp(2^-54 ln(x)/5) that turns 1/5
+//    into the binary64 value 0.2 = (1/5)(1 + 2^-54) (truncated exponential series);
+//  - x^(±1/8): three double-double square roots (Karp–Markstein correction);
+//  - sin/cos: Cody–Waite reduction by pi/2 split into 33+33+53+53 bits (valid for |x| < 2^20),
+//    reduction to |u| <= 1/128 around the table point j/64, double-double Taylor series and
+//    the angle-addition formulas with the table sin(j/64), cos(j/64).
+//
+// Everything is written with explicit fma() where an exact product is needed and compiled
+// without FMA contraction on the parity path, so host and device builds agree.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define DD_HD __host__ __device__ __forceinline__
+#else
+#define DD_HD static inline
+#endif
+
+namespace degpu {
+namespace ddm {
+
+#include "dd_tables.inc"
+
+// sin(j/64), cos(j/64) as double-doubles: one copy for device code, one for host builds.
+#if defined(__CUDACC__)
+static __device__ const double dd_sincos_tab_dev[DD_TAB_N][4] = {DD_SINCOS_ROWS};
+#endif
+static const double dd_sincos_tab_host[DD_TAB_N][4] = {DD_SINCOS_ROWS};
+DD_HD const double* dd_tab_row(int j) {
+#if defined(__CUDA_ARCH__)
+    return dd_sincos_tab_dev[j];
+#else
+    return dd_sincos_tab_host[j];
+#endif
+}
+
+struct dd {
+    double hi, lo;
+};
+
+DD_HD dd two_sum(double a, double b) {
+    double s = a + b;
+    double bb = s - a;
+    double e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+// requires |a| >= |b| (or a == 0)
+DD_HD dd fast_two_sum(double a, double b) {
+    double s = a + b;
+    double e = b - (s - a);
+    return {s, e};
+}
+DD_HD dd two_prod(double a, double b) {
+    double p = a * b;
+    double e = fma(a, b, -p);
+    return {p, e};
+}
+DD_HD dd dd_mul(dd a, dd b) {
+    dd p = two_prod(a.hi, b.hi);
+    double t = a.hi * b.lo;
+    t = t + a.lo * b.hi;
+    p.lo = p.lo + t;
+    return fast_two_sum(p.hi, p.lo);
+}
+DD_HD dd dd_mul_d(dd a, double b) {
+    dd p = two_prod(a.hi, b);
+    p.lo = p.lo + a.lo * b;
+    return fast_two_sum(p.hi, p.lo);
+}
+DD_HD dd dd_add(dd a, dd b) {
+    dd s = two_sum(a.hi, b.hi);
+    dd t = two_sum(a.lo, b.lo);
+    s.lo = s.lo + t.hi;
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo = s.lo + t.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+DD_HD dd dd_neg(dd a) { return {-a.hi, -a.lo}; }
+
+// Square root of a double-double (a.hi > 0).
+DD_HD dd dd_sqrt(dd a) {
+    double s = sqrt(a.hi);
+    double e = fma(-s, s, a.hi);
+    e = e + a.lo;
+    double c = e / (s + s);
+    return fast_two_sum(s, c);
+}
+
+// Reciprocal of a double-double (a.hi != 0, finite).
+DD_HD dd dd_recip(dd a) {
+    double q = 1.0 / a.hi;
+    double r = fma(-q, a.hi, 1.0);  // exact residual of the rounded quotient
+    r = r - q * a.lo;
+    return fast_two_sum(q, q * r);
+}
+
+// x^(1/5) as a double-double for finite x in [2^-800, 2^800].
+DD_HD dd fifth_root_dd(double x, double r0) {
+    dd r2 = two_prod(r0, r0);
+    dd r4 = dd_mul(r2, r2);
+    dd r5 = dd_mul_d(r4, r0);
+    double e = (r5.hi - x) + r5.lo;
+    double c = e / (5.0 * r4.hi);
+    return fast_two_sum(r0, -c);
+}
+
+// pow(x, y) for the exponents of the crate's controller and initial-step heuristic:
+// y in {0.2, -0.2, 0.125, -0.125} (binary64 values of ±1/5 and ±1/8).  Other y fall back to the
+// platform pow and are not guaranteed to be correctly rounded.
+DD_HD double pow_ctrl(double x, double y) {
+    const bool fifth = (y == 0.2 || y == -0.2);
+    const bool eighth = (y == 0.125 || y == -0.125);
+    if (!(fifth || eighth)) return pow(x, y);
+    // IEEE special cases of pow for these y
+    if (x != x) return x;
+    if (x < 0.0) return (x - x) / (x - x);  // NaN
+    if (x == 0.0) return y < 0.0 ? 1.0 / 0.0 : 0.0;
+    if (x == 1.0 / 0.0) return y < 0.0 ? 0.0 : x;
+    // bring x into [2^-800, 2^800]; the scale is a multiple of 5 and 8 binades
+    double xs = x, post = 1.0;
+    if (x < 0x1p-800) {
+        xs = ldexp(x, 800);
+        post = ldexp(1.0, fifth ? -160 : -100);
+    } else if (x > 0x1p+800) {
+        xs = ldexp(x, -800);
+        post = ldexp(1.0, fifth ? 160 : 100);
+    }
+    dd r;
+    if (fifth) {
+        double r0 = pow(xs, 0.2);  // starting value, a few ulp from x^(1/5)
+        r = fifth_root_dd(xs, r0);
+    } else {
+        r = dd_sqrt(dd_sqrt(dd_sqrt(dd{xs, 0.0})));
+    }
+    if (y < 0.0) {
+        r = dd_recip(r);
+        post = 1.0 / post;  // exact: power of two
+    }
+    if (fifth) {
+        // binary64 0.2 = (1/5)(1 + 2^-54): multiply by exp(+-2^-54 ln(x) / 5)
+        double g = 1.1102230246251566e-17 /* 2^-54 / 5 */ * log(x);
+        if (y < 0.0) g = -g;
+        g = g + 0.5 * g * g;
+        double t = r.lo + r.hi * g;
+        return (r.hi + t) * post;
+    }
+    return (r.hi + r.lo) * post;
+}
+
+// sin(u), cos(u) as double-doubles for |u.hi| <= 1/128.
+DD_HD void sincos_small(dd u, dd& s, dd& c) {
+    dd z = dd_mul(u, u);
+    double zh = z.hi;
+    // sin u = u + u z (-1/6 + z (1/120 + z Q)),  Q = -1/5040 + z/9! - z^2/11! + z^3/13!
+    double Q = -1.0 / 5040.0 + zh * (1.0 / 362880.0 + zh * (-1.0 / 39916800.0 + zh * (1.0 / 6227020800.0)));
+    dd R = dd_add(dd{DD_INV120_HI, DD_INV120_LO}, dd_mul_d(z, Q));
+    dd T = dd_add(dd{-DD_INV6_HI, -DD_INV6_LO}, dd_mul(z, R));
+    dd V = dd_mul(z, T);
+    s = dd_add(u, dd_mul(u, V));
+    // cos u = 1 + z (-1/2 + z (1/24 + z P)),  P = -1/720 + z/8! - z^2/10! + z^3/12!
+    double P = -1.0 / 720.0 + zh * (1.0 / 40320.0 + zh * (-1.0 / 3628800.0 + zh * (1.0 / 479001600.0)));
+    dd R2 = dd_add(dd{DD_INV24_HI, DD_INV24_LO}, dd_mul_d(z, P));
+    dd T2 = dd_add(dd{-0.5, 0.0}, dd_mul(z, R2));
+    c = dd_add(dd{1.0, 0.0}, dd_mul(z, T2));
+}
+
+// Reduce x (|x| < 2^20) to r = x - k pi/2 as a double-double; returns k mod 4.
+DD_HD int reduce_pio2(double x, dd& r) {
+    double k = rint(x * DD_TWO_OVER_PI);
+    double t1 = fma(-k, DD_PIO2_1, x);  // exact: k*PIO2_1 has <= 53 bits and t1 is small
+    double kp2 = k * DD_PIO2_2;         // exact
+    dd s = two_sum(t1, -kp2);
+    dd p3 = two_prod(k, DD_PIO2_3);
+    dd u = two_sum(s.hi, -p3.hi);
+    double lo = s.lo + u.lo;
+    lo = lo - p3.lo;
+    lo = lo - k * DD_PIO2_4;
+    r = fast_two_sum(u.hi, lo);
+    long long ki = (long long)k;
+    return (int)(ki & 3);
+}
+
+// sin or cos (want_cos) of x, correctly rounded in practice for |x| < 2^20.
+DD_HD double sincos_cr(double x, bool want_cos) {
+    if (x != x) return x;
+    double ax = fabs(x);
+    if (!(ax < 1048576.0)) return want_cos ? cos(x) : sin(x);  // outside the reduction's range
+    dd r;
+    int q = reduce_pio2(x, r);
+    bool neg = r.hi < 0.0;
+    dd a = neg ? dd_neg(r) : r;
+    int j = (int)rint(a.hi * 64.0);
+    if (j > DD_TAB_N - 1) j = DD_TAB_N - 1;
+    dd u = {a.hi - (double)j * 0.015625, a.lo};  // exact difference
+    u = fast_two_sum(u.hi, u.lo);
+    dd su, cu;
+    sincos_small(u, su, cu);
+    const double* row = dd_tab_row(j);
+    dd sj = {row[0], row[1]};
+    dd cj = {row[2], row[3]};
+    // sin(a) = sj cu + cj su ; cos(a) = cj cu - sj su
+    dd sa = dd_add(dd_mul(sj, cu), dd_mul(cj, su));
+    dd ca = dd_add(dd_mul(cj, cu), dd_neg(dd_mul(sj, su)));
+    dd sr = neg ? dd_neg(sa) : sa;  // sin(r)
+    dd cr = ca;                      // cos(r)
+    dd res;
+    if (!want_cos) {
+        res = q == 0 ? sr : q == 1 ? cr : q == 2 ? dd_neg(sr) : dd_neg(cr);
+    } else {
+        res = q == 0 ? cr : q == 1 ? dd_neg(sr) : q == 2 ? dd_neg(cr) : sr;
+    }
+    return res.hi + res.lo;
+}
+
+DD_HD double sin_cr(double x) { return sincos_cr(x, false); }
+DD_HD double cos_cr(double x) { return sincos_cr(x, true); }
+
+}  // namespace ddm
+}  // namespace degpu

@@ -1,0 +1,16 @@
+// Host build of dd_math.cuh so that its correct rounding can be tested without a GPU.
+// Compiled with -ffp-contract=off, like the parity device code (-fmad=false).
+#include <stdint.h>
+#include "dd_math.cuh"
+
+extern "C" {
+void degpu_host_pow_ctrl(const double* x, double y, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) out[i] = degpu::ddm::pow_ctrl(x[i], y);
+}
+void degpu_host_sincos_cr(const double* x, double* s, double* c, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        s[i] = degpu::ddm::sin_cr(x[i]);
+        c[i] = degpu::ddm::cos_cr(x[i]);
+    }
+}
+}

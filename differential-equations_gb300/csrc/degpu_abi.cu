@@ -1,0 +1,381 @@
+// degpu_abi.cu — the extern "C" boundary (include/degpu.h) over the ensemble kernels.
+//
+// Host-side responsibilities, before any launch:
+//  - argument validation (null pointers, sizes, enum ranges) -> DEGPU_BAD_INPUT;
+//  - TEvalSolout::new's sort of the requested times (src/solout/t_eval.rs:154-171), done once
+//    for the batch, with the permutation back to the caller's order;
+//  - grouping of a mixed-family batch into one work list per family;
+//  - choice of the kernel layout.
+// Per-instance checks (BadInput of src/utils.rs:60-157) run on the device and are reported in
+// status[i].
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <vector>
+
+#include "registry.cuh"
+#include "wps.cuh"
+
+namespace degpu {
+
+std::map<VariantKey, EnsLaunchFn>& ens_registry() {
+    static std::map<VariantKey, EnsLaunchFn> m;
+    return m;
+}
+std::map<std::pair<int, int>, RhsLaunchFn>& rhs_registry() {
+    static std::map<std::pair<int, int>, RhsLaunchFn> m;
+    return m;
+}
+
+int device_sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+static void ensure_registered() {
+    static std::once_flag once;
+    std::call_once(once, []() {
+        register_parity_main();
+        register_parity_tests();
+        register_fast();
+        register_mixed();
+    });
+}
+
+// Stream-ordered scratch allocations released at the end of a call.
+struct Scratch {
+    cudaStream_t s;
+    std::vector<void*> ptrs;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    template <class T>
+    T* alloc(size_t count) {
+        void* p = nullptr;
+        if (count == 0) count = 1;
+        if (cudaMallocAsync(&p, count * sizeof(T), s) != cudaSuccess) return nullptr;
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    ~Scratch() {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+    }
+};
+
+static bool valid_method(int m) { return m == DEGPU_RK4 || m == DEGPU_DOPRI5 || m == DEGPU_DOP853; }
+static bool valid_prec(int p) { return p == DEGPU_FP64_PARITY || p == DEGPU_FP64_FAST || p == DEGPU_MIXED; }
+
+static void builtin_info(int id, int& dim, int& np) {
+    switch (id) {
+        case DEGPU_RHS_LORENZ: dim = 3; np = 3; return;
+        case DEGPU_RHS_VAN_DER_POL: dim = 2; np = 1; return;
+        case DEGPU_RHS_PENDULUM: dim = 2; np = 3; return;
+        case DEGPU_RHS_FPU_BETA: dim = -1; np = 1; return;
+        case DEGPU_RHS_EXP_GROWTH: dim = 1; np = 1; return;
+        case DEGPU_RHS_LINEAR: dim = 1; np = 2; return;
+        case DEGPU_RHS_HARMONIC: dim = 2; np = 1; return;
+        case DEGPU_RHS_LOGISTIC: dim = 1; np = 2; return;
+        case DEGPU_RHS_ROBERTSON: dim = 3; np = 0; return;
+        case DEGPU_RHS_HIRES: dim = 8; np = 0; return;
+        case DEGPU_RHS_BRUSSELATOR: dim = 2; np = 2; return;
+        case DEGPU_RHS_CR3BP: dim = 6; np = 1; return;
+        default: dim = 0; np = -1; return;
+    }
+}
+
+// Core of degpu_solve_ensemble.  `family_host` / `t_eval_host` are host copies of the
+// corresponding device arrays (or NULL when absent).
+static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                               degpu_batch_out* out, cudaStream_t s, const int32_t* family_host,
+                               const double* t_eval_host, const int32_t* dims_host) {
+    ensure_registered();
+    const int64_t n = in->n;
+    if (n == 0) return DEGPU_OK;
+    Scratch scratch(s);
+
+    EnsArgs a{};
+    a.n = n;
+    a.t0 = in->t0;
+    a.tf = in->tf;
+    a.y0 = in->y0;
+    a.params = in->params;
+    a.rtol = in->rtol;
+    a.atol = in->atol;
+    a.n_eval = (in->n_eval > 0 && in->t_eval) ? in->n_eval : 0;
+    a.dmax = pb->dim;
+    a.y_final = out->y_final;
+    a.t_final = out->t_final;
+    a.dense = out->dense;
+    a.accepted = out->accepted;
+    a.rejected = out->rejected;
+    a.fevals = out->fevals;
+    a.status = out->status;
+    a.h0 = cfg->h0;
+    a.h_min = cfg->h_min;
+    a.h_max = cfg->h_max;
+    a.max_steps = cfg->max_steps;
+    a.safety = cfg->safety_factor;
+    a.min_scale = cfg->min_scale;
+    a.max_scale = cfg->max_scale;
+    a.dense_mode = cfg->dense_mode;
+    a.n_params = pb->n_params;
+    const bool dense = a.n_eval > 0 && out->dense;
+    if (a.n_eval > 0 && !out->dense) a.n_eval = 0;
+
+    // TEvalSolout::new: stable sort ascending; descending instances walk it backwards
+    if (a.n_eval > 0) {
+        std::vector<int32_t> perm(a.n_eval);
+        std::iota(perm.begin(), perm.end(), 0);
+        std::stable_sort(perm.begin(), perm.end(),
+                         [&](int32_t x, int32_t y) { return t_eval_host[x] < t_eval_host[y]; });
+        std::vector<double> sorted(a.n_eval);
+        for (int e = 0; e < a.n_eval; ++e) sorted[e] = t_eval_host[perm[e]];
+        double* d_t = scratch.alloc<double>(a.n_eval);
+        int32_t* d_p = scratch.alloc<int32_t>(a.n_eval);
+        if (!d_t || !d_p) return DEGPU_OOM;
+        if (cudaMemcpyAsync(d_t, sorted.data(), a.n_eval * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_p, perm.data(), a.n_eval * sizeof(int32_t), cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+        a.t_eval = d_t;
+        a.eval_perm = d_p;
+        // the host vectors must outlive the async copies
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return DEGPU_CUDA_ERROR;
+        // every output time starts as NaN: points the solve never reaches stay NaN
+    }
+    if (dense) {
+        size_t bytes = (size_t)in->n_eval * pb->dim * n * sizeof(double);
+        // 0xFF bytes form a quiet NaN
+        if (cudaMemsetAsync(out->dense, 0xFF, bytes, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    }
+
+    // ragged (per-instance dimension) problems go to the warp-per-system kernel
+    if (pb->rhs_id == DEGPU_RHS_FPU_BETA) {
+        return wps_solve(pb, cfg, a, in->dims, s);
+    }
+
+    // work lists per family
+    std::vector<std::pair<int, std::vector<int64_t>>> groups;
+    if (family_host) {
+        std::map<int, std::vector<int64_t>> by;
+        for (int64_t i = 0; i < n; ++i) by[family_host[i]].push_back(i);
+        for (auto& kv : by) groups.emplace_back(kv.first, std::move(kv.second));
+    } else {
+        groups.emplace_back(pb->rhs_id, std::vector<int64_t>());
+    }
+
+    int kernel = cfg->kernel;
+    if (kernel == DEGPU_KERNEL_AUTO) kernel = (cfg->method != DEGPU_RK4 && n >= 32768) ? DEGPU_KERNEL_PERSISTENT
+                                                                                        : DEGPU_KERNEL_THREAD;
+    if (kernel == DEGPU_KERNEL_WARP) kernel = DEGPU_KERNEL_THREAD;  // fixed-size families: one system per thread
+
+    for (auto& g : groups) {
+        int dim, np;
+        builtin_info(g.first, dim, np);
+        if (np < 0) return DEGPU_BAD_INPUT;
+        if (dim > pb->dim || np > pb->n_params) return DEGPU_BAD_INPUT;
+        auto it = ens_registry().find(VariantKey{cfg->method, g.first, cfg->precision, dense ? 1 : 0});
+        if (it == ens_registry().end()) return DEGPU_UNSUPPORTED;
+        EnsArgs ga = a;
+        if (family_host) {
+            int64_t* d_idx = scratch.alloc<int64_t>(g.second.size());
+            if (!d_idx) return DEGPU_OOM;
+            if (cudaMemcpyAsync(d_idx, g.second.data(), g.second.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                s) != cudaSuccess)
+                return DEGPU_CUDA_ERROR;
+            ga.index = d_idx;
+            ga.count = (int64_t)g.second.size();
+        } else {
+            ga.index = nullptr;
+            ga.count = n;
+        }
+        if (kernel == DEGPU_KERNEL_PERSISTENT) {
+            unsigned long long* tk = scratch.alloc<unsigned long long>(1);
+            if (!tk) return DEGPU_OOM;
+            if (cudaMemsetAsync(tk, 0, sizeof(unsigned long long), s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+            ga.ticket = tk;
+        }
+        cudaError_t e = it->second(ga, kernel, s);
+        if (e != cudaSuccess) return DEGPU_CUDA_ERROR;
+    }
+    if (family_host) {
+        // index lists were copied from host vectors that die with this call
+        if (cudaStreamSynchronize(s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    }
+    return DEGPU_OK;
+}
+
+static degpu_status validate(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                             const degpu_batch_out* out) {
+    if (!pb || !cfg || !in || !out) return DEGPU_BAD_INPUT;
+    if (in->n < 0) return DEGPU_BAD_INPUT;
+    if (in->n == 0) return DEGPU_OK;
+    if (!valid_method(cfg->method) || !valid_prec(cfg->precision)) return DEGPU_BAD_INPUT;
+    if (cfg->kernel < DEGPU_KERNEL_AUTO || cfg->kernel > DEGPU_KERNEL_PERSISTENT) return DEGPU_BAD_INPUT;
+    if (pb->dim <= 0 || pb->n_params < 0) return DEGPU_BAD_INPUT;
+    if (!in->t0 || !in->tf || !in->y0 || !in->rtol || !in->atol) return DEGPU_BAD_INPUT;
+    if (pb->n_params > 0 && !in->params) return DEGPU_BAD_INPUT;
+    if (!out->y_final) return DEGPU_BAD_INPUT;
+    if (in->n_eval < 0 || (in->n_eval > 0 && !in->t_eval)) return DEGPU_BAD_INPUT;
+    if (cfg->max_steps < 0) return DEGPU_BAD_INPUT;
+    if (!in->family) {
+        int dim, np;
+        builtin_info(pb->rhs_id, dim, np);
+        if (np < 0) return DEGPU_BAD_INPUT;
+        if (dim > 0 && dim != pb->dim) return DEGPU_BAD_INPUT;
+        if (np > pb->n_params) return DEGPU_BAD_INPUT;
+        if (dim < 0 && !in->dims) return DEGPU_BAD_INPUT;
+    }
+    return DEGPU_OK;
+}
+
+}  // namespace degpu
+
+using namespace degpu;
+
+extern "C" {
+
+void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method) {
+    if (!cfg) return;
+    cfg->method = method;
+    cfg->precision = DEGPU_FP64_PARITY;
+    cfg->kernel = DEGPU_KERNEL_AUTO;
+    cfg->dense_mode = DEGPU_DENSE_REFERENCE;
+    cfg->h0 = 0.0;
+    cfg->h_min = 0.0;
+    cfg->h_max = INFINITY;
+    cfg->max_steps = 10000;
+    cfg->safety_factor = 0.9;
+    cfg->min_scale = 0.2;
+    cfg->max_scale = 10.0;
+}
+
+degpu_status degpu_rhs_info(int32_t rhs_id, int32_t* dim, int32_t* n_params) {
+    int d, np;
+    builtin_info(rhs_id, d, np);
+    if (np < 0) {
+        if (rhs_id >= DEGPU_RHS_NVRTC_BASE) return nvrtc_rhs_info(rhs_id, dim, n_params);
+        return DEGPU_BAD_INPUT;
+    }
+    if (dim) *dim = d;
+    if (n_params) *n_params = np;
+    return DEGPU_OK;
+}
+
+degpu_status degpu_solve_ensemble(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                  degpu_batch_out* out, void* stream) {
+    degpu_status v = validate(pb, cfg, in, out);
+    if (v != DEGPU_OK || in->n == 0) return v;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return nvrtc_solve(pb, cfg, in, out, s);
+    // small host copies: the family map and the requested times
+    std::vector<int32_t> fam;
+    std::vector<double> te;
+    if (in->family) {
+        fam.resize(in->n);
+        if (cudaMemcpyAsync(fam.data(), in->family, in->n * sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    if (in->n_eval > 0) {
+        te.resize(in->n_eval);
+        if (cudaMemcpyAsync(te.data(), in->t_eval, in->n_eval * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    if ((in->family || in->n_eval > 0) && cudaStreamSynchronize(s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    return solve_impl(pb, cfg, in, out, s, in->family ? fam.data() : nullptr, in->n_eval > 0 ? te.data() : nullptr,
+                      nullptr);
+}
+
+degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                       degpu_batch_out* out) {
+    degpu_status v = validate(pb, cfg, in, out);
+    if (v != DEGPU_OK || in->n == 0) return v;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    degpu_status st = DEGPU_OK;
+    {
+        const int64_t n = in->n;
+        const int d = pb->dim, np = pb->n_params, m = in->n_eval;
+        Scratch sc(s);
+        degpu_batch_in din = *in;
+        degpu_batch_out dout{};
+        auto up = [&](const void* src, size_t bytes) -> void* {
+            if (!src) return nullptr;
+            void* p = sc.alloc<char>(bytes);
+            if (!p) return nullptr;
+            cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, s);
+            return p;
+        };
+        din.t0 = (const double*)up(in->t0, n * 8);
+        din.tf = (const double*)up(in->tf, n * 8);
+        din.y0 = (const double*)up(in->y0, (size_t)d * n * 8);
+        din.params = np > 0 ? (const double*)up(in->params, (size_t)np * n * 8) : nullptr;
+        din.rtol = (const double*)up(in->rtol, n * 8);
+        din.atol = (const double*)up(in->atol, n * 8);
+        din.dims = in->dims ? (const int32_t*)up(in->dims, n * 4) : nullptr;
+        din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
+        din.t_eval = m > 0 ? (const double*)up(in->t_eval, (size_t)m * 8) : nullptr;
+        dout.y_final = sc.alloc<double>((size_t)d * n);
+        dout.t_final = out->t_final ? sc.alloc<double>(n) : nullptr;
+        dout.dense = (m > 0 && out->dense) ? sc.alloc<double>((size_t)m * d * n) : nullptr;
+        dout.accepted = out->accepted ? sc.alloc<int64_t>(n) : nullptr;
+        dout.rejected = out->rejected ? sc.alloc<int64_t>(n) : nullptr;
+        dout.fevals = out->fevals ? sc.alloc<int64_t>(n) : nullptr;
+        dout.status = out->status ? sc.alloc<int32_t>(n) : nullptr;
+        if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final) {
+            st = DEGPU_OOM;
+        } else if (pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) {
+            st = nvrtc_solve(pb, cfg, &din, &dout, s);
+        } else {
+            st = solve_impl(pb, cfg, &din, &dout, s, in->family, m > 0 ? in->t_eval : nullptr, in->dims);
+        }
+        if (st == DEGPU_OK) {
+            auto down = [&](void* dst, const void* src, size_t bytes) {
+                if (dst && src) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+            };
+            down(out->y_final, dout.y_final, (size_t)d * n * 8);
+            down(out->t_final, dout.t_final, n * 8);
+            down(out->dense, dout.dense, (size_t)m * d * n * 8);
+            down(out->accepted, dout.accepted, n * 8);
+            down(out->rejected, dout.rejected, n * 8);
+            down(out->fevals, dout.fevals, n * 8);
+            down(out->status, dout.status, n * 4);
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess && st == DEGPU_OK) st = DEGPU_CUDA_ERROR;
+    }
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return st;
+}
+
+degpu_status degpu_eval_rhs(int32_t rhs_id, int32_t precision, int64_t n, int32_t dim, int32_t n_params,
+                            const double* t, const double* y, const double* params, double* dydt, void* stream) {
+    ensure_registered();
+    if (n < 0 || !t || !y || !dydt || !valid_prec(precision)) return DEGPU_BAD_INPUT;
+    int d, np;
+    builtin_info(rhs_id, d, np);
+    if (np < 0 || d != dim || np > n_params || (np > 0 && !params)) return DEGPU_BAD_INPUT;
+    auto it = rhs_registry().find({rhs_id, precision});
+    if (it == rhs_registry().end()) return DEGPU_UNSUPPORTED;
+    return it->second(n, t, y, params, dydt, (cudaStream_t)stream) == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
+}
+
+const char* degpu_status_string(degpu_status s) {
+    switch (s) {
+        case DEGPU_OK: return "ok";
+        case DEGPU_BAD_INPUT: return "bad input";
+        case DEGPU_OOM: return "out of device memory";
+        case DEGPU_TIMEOUT: return "device wait timed out";
+        case DEGPU_CUDA_ERROR: return "CUDA error";
+        case DEGPU_UNSUPPORTED: return "unsupported combination";
+    }
+    return "unknown status";
+}
+
+const char* degpu_version(void) { return "degpu 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

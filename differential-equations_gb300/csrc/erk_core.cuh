@@ -1,0 +1,658 @@
+// erk_core.cuh — one instance of the crate's explicit Runge–Kutta solve, as a per-lane state
+// machine in registers.
+//
+// Mirrors, operation for operation on the parity path:
+//   driver loop ............ src/ode/solve_ivp.rs:138-277
+//   DormandPrince init ..... src/methods/erk/dormandprince/ordinary.rs:16-61
+//   DormandPrince step ..... src/methods/erk/dormandprince/ordinary.rs:63-268
+//   DormandPrince interp ... src/methods/erk/dormandprince/ordinary.rs:301-336
+//   Fixed (RK4) init/step .. src/methods/erk/fixed/ordinary.rs:16-138
+//   Hermite interpolation .. src/interpolate.rs:40-60 (fixed/ordinary.rs:206-218)
+//   h_init ................. src/methods/h_init.rs:45-136
+//   validate / constrain ... src/utils.rs:22-157
+//   error_norm ............. src/traits.rs:394-410
+//   TEvalSolout ............ src/solout/t_eval.rs:82-137
+//
+// The state (y, the derivative k0, counters, controller state and, with dense output, the
+// dense coefficients) stays in registers for the whole solve; the stage vectors k[1..I) live in
+// registers for the duration of one step.  Nothing is allocated.
+//
+// Work the crate does whose results nothing reads is not repeated: without requested output
+// times the three DOP853 dense-output stages (ordinary.rs:210-225) and the dense coefficients are
+// skipped, and their three function evaluations are still counted in `fevals` so that the
+// counters equal the crate's.
+#pragma once
+
+#include <stdint.h>
+
+#include "rhs.cuh"
+#include "tableau.cuh"
+#include "../../include/degpu.h"
+
+namespace degpu {
+
+struct EnsArgs {
+    int64_t n;               // SoA stride (instances in the batch)
+    int64_t count;           // work items (entries of `index`, or n)
+    const int64_t* index;    // optional work-item -> instance map
+    const double* t0;
+    const double* tf;
+    const double* y0;
+    const double* params;
+    const double* rtol;
+    const double* atol;
+    const double* t_eval;      // ascending, [n_eval]
+    const int32_t* eval_perm;  // ascending position -> caller's index
+    int32_t n_eval;
+    int32_t dmax;
+    double* y_final;
+    double* t_final;
+    double* dense;
+    int64_t* accepted;
+    int64_t* rejected;
+    int64_t* fevals;
+    int32_t* status;
+    double h0, h_min, h_max;
+    int64_t max_steps;
+    double safety, min_scale, max_scale;
+    int32_t dense_mode;
+    int32_t n_params;
+    const int32_t* family;           // per-instance family id (multi-family persistent kernel)
+    unsigned long long* ticket;      // persistent queue head
+};
+
+// f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
+__device__ __forceinline__ double rs_signum(double x) { return x != x ? x : copysign(1.0, x); }
+
+template <class Tab, class Rhs, class P, bool DENSE>
+struct Lane {
+    static constexpr int D = Rhs::D;
+    static constexpr int I = Tab::I;
+    static constexpr int NS = Tab::S;
+    static constexpr int O = Tab::ORDER;
+    static constexpr int NC = DENSE ? (Tab::ADAPTIVE ? O : 2) : 1;  // RK4 keeps y_prev, dydt_prev
+    static constexpr int NPP = Rhs::NP > 0 ? Rhs::NP : 1;
+    using S = typename P::S;
+
+    int64_t inst;
+    double t, tf, h, h_prev, t_prev, dir, rtol, atol;
+    double p[NPP];
+    S y[D];
+    S yc[D];  // Kahan compensation of y (mixed precision only)
+    S k0[D];  // derivative at (t, y): k[0] of the next step
+    S cont[NC][D];
+    int64_t steps, acc, rej, fev;
+    int stiff, nonstiff;
+    int next_eval;
+    int status;
+    bool last_rejected;
+    bool done;
+
+    __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const { Rhs::template diff<P>(tt, yy, dd, p); }
+
+    __device__ __forceinline__ double norm_term(S e, S yv, S ynv) const {
+        // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407), in FP64
+        double sk = atol + rtol * fmax(fabs((double)yv), fabs((double)ynv));
+        double q = (double)e / sk;
+        return q * q;
+    }
+
+    // ----- h_init: src/methods/h_init.rs:45-136 --------------------------------------------
+    __device__ double initial_step(double t0, const EnsArgs& a) {
+        double posneg = rs_signum(tf - t0);
+        S f0[D], f1[D], y1[D];
+        rhs(t0, y, f0);
+        fev += 1;
+        double dnf = 0.0, dny = 0.0;
+        double sk[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            sk[c] = atol + rtol * fabs((double)y[c]);
+            double q = (double)f0[c] / sk[c];
+            dnf = dnf + q * q;
+            double r = (double)y[c] / sk[c];
+            dny = dny + r * r;
+        }
+        double hh;
+        if (dnf <= 1.0e-10 || dny <= 1.0e-10)
+            hh = 1.0e-6;
+        else
+            hh = sqrt(dny / dnf) * 0.01;
+        hh = fmin(hh, a.h_max);
+        hh = hh * posneg;
+        S hs = P::from(hh);
+#pragma unroll
+        for (int c = 0; c < D; ++c) y1[c] = y[c] + hs * f0[c];
+        rhs(t0 + hh, y1, f1);
+        fev += 1;
+        double der2 = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            double q = ((double)f1[c] - (double)f0[c]) / sk[c];
+            if constexpr (P::ID == PrecMixed::ID) q = (double)(f1[c] - f0[c]) / sk[c];
+            der2 = der2 + q * q;
+        }
+        der2 = sqrt(der2) / fabs(hh);
+        double der12 = fmax(sqrt(dnf), der2);
+        double h1;
+        if (der12 <= 1.0e-15)
+            h1 = fabs(hh) * fmax(1.0e-3, 1.0e-6);
+        else
+            h1 = P::pow(0.01 / der12, 1.0 / (double)O);
+        double interval = fabs(tf - t0);
+        hh = fmin(fmax(fmin(fmin(fabs(hh) * 100.0, h1), a.h_max), a.h_min), interval);
+        return hh * posneg;
+    }
+
+    // ----- validate_step_size_parameters: src/utils.rs:60-157 ------------------------------
+    __device__ __forceinline__ bool valid_h0(double h0, double t0, const EnsArgs& a) const {
+        if (tf == t0) return false;
+        double sign = rs_signum(tf - t0);
+        if (rs_signum(h0) != sign) return false;
+        if (a.h_min < 0.0 || a.h_max < 0.0 || a.h_min > a.h_max) return false;
+        if (fabs(h0) < a.h_min || fabs(h0) > a.h_max) return false;
+        if (fabs(h0) > fabs(tf - t0)) return false;
+        if (h0 == 0.0) return false;
+        return true;
+    }
+
+    // ----- dense output at the requested times: src/solout/t_eval.rs:82-137 ------------------
+    __device__ __forceinline__ double eval_time(int idx, const EnsArgs& a) const {
+        return dir > 0.0 ? a.t_eval[idx] : a.t_eval[a.n_eval - 1 - idx];
+    }
+    __device__ __forceinline__ int eval_slot(int idx, const EnsArgs& a) const {
+        return dir > 0.0 ? a.eval_perm[idx] : a.eval_perm[a.n_eval - 1 - idx];
+    }
+    __device__ void write_dense(int idx, const S* v, const EnsArgs& a) const {
+        int slot = eval_slot(idx, a);
+        double* out = a.dense + ((int64_t)slot * a.dmax) * a.n + inst;
+#pragma unroll
+        for (int c = 0; c < D; ++c) out[(int64_t)c * a.n] = (double)v[c];
+    }
+    __device__ void interpolate(double te, S* out, const EnsArgs& a) const {
+        if constexpr (DENSE) {
+            if constexpr (Tab::ADAPTIVE) {
+                // ordinary.rs:312-333
+                double s = (te - t_prev) / h_prev;
+                double s1 = 1.0 - s;
+                S ss = P::from(s), ss1 = P::from(s1);
+                const bool hairer = a.dense_mode == DEGPU_DENSE_HAIRER;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    S accv = cont[O - 1][c];
+#pragma unroll
+                    for (int i = O - 2; i >= 1; --i) {
+                        S f;
+                        if (i >= 4) {
+                            bool odd = ((O - 1 - i) % 2) == 1;
+                            if (hairer) odd = !odd;
+                            f = odd ? ss1 : ss;
+                        } else {
+                            f = (i % 2 == 1) ? ss1 : ss;
+                        }
+                        accv = accv * f;
+                        accv = accv + cont[i][c];
+                    }
+                    out[c] = cont[0][c] + ss * accv;
+                }
+            } else {
+                // cubic Hermite over [t_prev, t] with y_prev=cont[0], dydt_prev=cont[1], y, k0
+                double t0 = t_prev, t1 = t;
+                double hh = t1 - t0;
+                double s = (te - t0) / hh;
+                double s2 = s * s;
+                double s3 = s2 * s;
+                double h00 = 2.0 * s3 - 3.0 * s2 + 1.0;
+                double h10 = s3 - 2.0 * s2 + s;
+                double h01 = -2.0 * s3 + 3.0 * s2;
+                double h11 = s3 - s2;
+                S c00 = P::from(h00), c10 = P::from(h10 * hh), c01 = P::from(h01), c11 = P::from(h11 * hh);
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    S o = (S)0;
+                    o = o + c00 * cont[0][c];
+                    o = o + c10 * cont[1][c];
+                    o = o + c01 * y[c];
+                    o = o + c11 * k0[c];
+                    out[c] = o;
+                }
+            }
+        }
+    }
+    __device__ void solout(const EnsArgs& a) {
+        if constexpr (DENSE) {
+            int idx = next_eval;
+            while (idx < a.n_eval) {
+                double te = eval_time(idx, a);
+                bool in_range = dir > 0.0 ? ((te == t_prev && idx == 0) || (te > t_prev && te <= t))
+                                          : ((te == t_prev && idx == 0) || (te < t_prev && te >= t));
+                if (in_range) {
+                    if (te == t) {
+                        write_dense(idx, y, a);
+                    } else {
+                        S v[D];
+                        interpolate(te, v, a);
+                        write_dense(idx, v, a);
+                    }
+                    idx += 1;
+                } else {
+                    if ((dir > 0.0 && te > t) || (dir < 0.0 && te < t)) break;
+                    idx += 1;
+                }
+            }
+            next_eval = idx;
+        }
+    }
+
+    // ----- start one instance ------------------------------------------------------------------
+    __device__ void begin(int64_t instance, const EnsArgs& a) {
+        inst = instance;
+        const int64_t n = a.n;
+        double t0 = a.t0[inst];
+        tf = a.tf[inst];
+        rtol = a.rtol[inst];
+        atol = a.atol[inst];
+#pragma unroll
+        for (int q = 0; q < Rhs::NP; ++q) p[q] = a.params[(int64_t)q * n + inst];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            y[c] = P::from(a.y0[(int64_t)c * n + inst]);
+            yc[c] = (S)0;
+        }
+        t = t0;
+        t_prev = t0;
+        h_prev = 0.0;
+        steps = acc = rej = fev = 0;
+        stiff = nonstiff = 0;
+        next_eval = 0;
+        last_rejected = false;
+        done = false;
+        status = DEGPU_COMPLETE;
+        // direction (solve_ivp.rs:139-147): signum(tf - t0) must be +-1
+        double sg = rs_signum(tf - t0);
+        if (!(sg == 1.0 || sg == -1.0)) {
+            status = DEGPU_ERR_BAD_INPUT;
+            done = true;
+            return;
+        }
+        dir = sg;
+        double h0 = a.h0;
+        if constexpr (Tab::ADAPTIVE) {
+            if (h0 == 0.0) h0 = initial_step(t0, a);
+        } else {
+            if (h0 == 0.0) h0 = fabs(tf - t0) / 100.0;
+        }
+        if (!valid_h0(h0, t0, a)) {
+            status = DEGPU_ERR_BAD_INPUT;
+            done = true;
+            return;
+        }
+        h = h0;
+        rhs(t, y, k0);
+        fev += 1;
+        if constexpr (DENSE && !Tab::ADAPTIVE) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                cont[0][c] = y[c];
+                cont[1][c] = k0[c];
+            }
+        }
+        solout(a);  // t == t_prev == t0
+    }
+
+    // ----- one Dormand–Prince step attempt: ordinary.rs:63-268 -------------------------------
+    // returns 1 accepted, 2 rejected, 3 error
+    __device__ int step_dp(const EnsArgs& a) {
+        if (fabs(h) < fabs(h_prev) * 1e-14) {
+            status = DEGPU_ERR_STEP_SIZE;
+            return 3;
+        }
+        if (steps >= a.max_steps) {
+            status = DEGPU_ERR_MAX_STEPS;
+            return 3;
+        }
+        steps += 1;
+        S k[I][D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) k[0][c] = k0[c];
+        S ys[D];
+        static_for<1, NS>([&](auto i) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = y[c];
+            static_for<0, i>([&](auto j) {
+                constexpr double aij = Tab::a(i, j);
+                if constexpr (aij != 0.0) {
+                    S ah = stage_coef(aij);
+#pragma unroll
+                    for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                }
+            });
+            rhs(t + Tab::c(i) * h, ys, k[i]);
+        });
+        // ys now holds the last stage state (ysti, ordinary.rs:107)
+        S yseg[D], ynew[D], ycn[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) yseg[c] = (S)0;
+        static_for<0, NS>([&](auto i) {
+            constexpr double bi_ = Tab::b(i);
+            if constexpr (bi_ != 0.0) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) yseg[c] = yseg[c] + (S)bi_ * k[i][c];
+            }
+        });
+        S hs = P::from(h);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            if constexpr (P::KAHAN) {
+                S inc = hs * yseg[c];
+                S yk = inc - yc[c];
+                S ts = y[c] + yk;
+                ycn[c] = (ts - y[c]) - yk;
+                ynew[c] = ts;
+            } else {
+                ynew[c] = y[c] + hs * yseg[c];
+                ycn[c] = (S)0;
+            }
+        }
+        double t_new = t + h;
+        fev += NS - 1;
+
+        double err = 0.0, err2 = 0.0;
+        {
+            S es[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) es[c] = (S)0;
+            static_for<0, NS>([&](auto j) {
+                constexpr double e_ = Tab::er(j);
+                if constexpr (e_ != 0.0) {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) es[c] = es[c] + (S)e_ * k[j][c];
+                }
+            });
+#pragma unroll
+            for (int c = 0; c < D; ++c) err = err + norm_term(es[c], y[c], ynew[c]);
+        }
+        if constexpr (Tab::HAS_BH) {
+            S es[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) es[c] = yseg[c];
+            static_for<0, NS>([&](auto j) {
+                constexpr double bh_ = Tab::bh(j);
+                if constexpr (bh_ != 0.0) {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) es[c] = es[c] + (S)(-bh_) * k[j][c];
+                }
+            });
+#pragma unroll
+            for (int c = 0; c < D; ++c) err2 = err2 + norm_term(es[c], y[c], ynew[c]);
+        }
+        double deno = Tab::HAS_BH ? err + 0.01 * err2 : err;
+        if (deno <= 0.0) deno = 1.0;
+        err = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
+
+        double error_exponent = 1.0 / (double)O;
+        double scale = a.safety * P::pow(err, -error_exponent);
+        scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+
+        int result;
+        if (err <= 1.0) {
+            S dydt[D];
+            rhs(t_new, ynew, dydt);
+            fev += 1;
+            // stiffness detection, ordinary.rs:165-194
+            if (steps % 100 == 0) {
+                double stdnum = 0.0, stden = 0.0;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    double d1 = (double)yseg[c] - (double)k[NS - 1][c];
+                    stdnum = stdnum + d1 * d1;
+                    double d2 = (double)dydt[c] - (double)ys[c];
+                    stden = stden + d2 * d2;
+                }
+                if (stden > 0.0) {
+                    double h_lamb = h * sqrt(stdnum / stden);
+                    if (h_lamb > 6.1) {
+                        nonstiff = 0;
+                        stiff += 1;
+                        if (stiff == 15) {
+                            status = DEGPU_ERR_STIFFNESS;
+                            return 3;
+                        }
+                    }
+                } else {
+                    nonstiff += 1;
+                    if (nonstiff == 6) stiff = 0;
+                }
+            }
+            if constexpr (DENSE) {
+                dense_coefficients(k, ynew, dydt);
+            } else {
+                fev += I - NS - (I > NS ? 1 : 0);  // DOP853: three dense stages the crate evaluates
+            }
+            t_prev = t;
+            h_prev = h;
+            t = t_new;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                y[c] = ynew[c];
+                yc[c] = ycn[c];
+                k0[c] = dydt[c];
+            }
+            if (last_rejected) {
+                last_rejected = false;
+                scale = fmin(scale, 1.0);
+            }
+            result = 1;
+        } else {
+            last_rejected = true;
+            result = 2;
+        }
+        h = h * scale;
+        // constrain_step_size, utils.rs:22-33
+        if (fabs(h) < a.h_min)
+            h = rs_signum(h) * a.h_min;
+        else if (fabs(h) > a.h_max)
+            h = rs_signum(h) * a.h_max;
+        return result;
+    }
+
+    __device__ __forceinline__ S stage_coef(double aij) const {
+        if constexpr (P::KAHAN)
+            return (float)aij * (float)h;
+        else
+            return aij * h;
+    }
+
+    // dense-output preparation, ordinary.rs:196-235 (k[S..I) computed here for DOP853)
+    __device__ void dense_coefficients(S (&k)[I][D], const S* ynew, const S* dydt) {
+        if constexpr (DENSE && Tab::ADAPTIVE) {
+            S hs = P::from(h);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                cont[0][c] = y[c];
+                S ydiff = ynew[c] - y[c];
+                cont[1][c] = ydiff;
+                S bspl = hs * k[0][c];
+                bspl = bspl - ydiff;
+                cont[2][c] = bspl;
+                S c3 = ydiff - hs * dydt[c];
+                c3 = c3 - bspl;
+                cont[3][c] = c3;
+            }
+            if constexpr (I > NS) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) k[NS][c] = dydt[c];
+                S ys[D];
+                static_for<NS + 1, I>([&](auto i) {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) ys[c] = y[c];
+                    static_for<0, i>([&](auto j) {
+                        constexpr double aij = Tab::a(i, j);
+                        if constexpr (aij != 0.0) {
+                            S ah = stage_coef(aij);
+#pragma unroll
+                            for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                        }
+                    });
+                    rhs(t + Tab::c(i) * h, ys, k[i]);
+                    fev += 1;
+                });
+            }
+            static_for<4, O>([&](auto i) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    S s = (S)0;
+                    static_for<0, I>([&](auto j) {
+                        constexpr double v = Tab::bi(i, j);
+                        if constexpr (v != 0.0) s = s + (S)v * k[j][c];
+                    });
+                    cont[i][c] = s * hs;
+                }
+            });
+        }
+    }
+
+    // ----- one fixed RK4 step: fixed/ordinary.rs:58-138 -----------------------------------------
+    __device__ int step_fixed(const EnsArgs& a) {
+        if (steps >= a.max_steps) {
+            status = DEGPU_ERR_MAX_STEPS;
+            return 3;
+        }
+        steps += 1;
+        S k[I][D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) k[0][c] = k0[c];
+        S ys[D];
+        static_for<1, NS>([&](auto i) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = y[c];
+            static_for<0, i>([&](auto j) {
+                constexpr double aij = Tab::a(i, j);
+                if constexpr (aij != 0.0) {
+                    S ah = stage_coef(aij);
+#pragma unroll
+                    for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                }
+            });
+            rhs(t + Tab::c(i) * h, ys, k[i]);
+        });
+        fev += NS - 1;
+        t_prev = t;
+        h_prev = h;
+        if constexpr (DENSE) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                cont[0][c] = y[c];
+                cont[1][c] = k0[c];
+            }
+        }
+        S yn[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) yn[c] = y[c];
+        if constexpr (P::KAHAN) {
+            S inc[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) inc[c] = (S)0;
+            static_for<0, NS>([&](auto i) {
+                S bh_ = (float)Tab::b(i) * (float)h;
+#pragma unroll
+                for (int c = 0; c < D; ++c) inc[c] = inc[c] + bh_ * k[i][c];
+            });
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                S yk = inc[c] - yc[c];
+                S ts = yn[c] + yk;
+                yc[c] = (ts - yn[c]) - yk;
+                yn[c] = ts;
+            }
+        } else {
+            static_for<0, NS>([&](auto i) {
+                S bh_ = Tab::b(i) * h;
+#pragma unroll
+                for (int c = 0; c < D; ++c) yn[c] = yn[c] + bh_ * k[i][c];
+            });
+        }
+        t = t + h;
+#pragma unroll
+        for (int c = 0; c < D; ++c) y[c] = yn[c];
+        rhs(t, y, k0);
+        fev += 1;
+        return 1;
+    }
+
+    // ----- one iteration of the driver loop: solve_ivp.rs:191-266 ----------------------------
+    __device__ __forceinline__ void iterate(const EnsArgs& a) {
+        const double eps10 = 2.220446049250313e-16 * 10.0;
+        if ((t + h - tf) * dir > 0.0) {
+            double h_new = tf - t;
+            if (fabs(h_new) < eps10) {
+                done = true;
+                return;
+            }
+            h = h_new;
+        }
+        int r = Tab::ADAPTIVE ? step_dp(a) : step_fixed(a);
+        if (r == 3) {
+            done = true;
+            return;
+        }
+        if (r == 2) {
+            rej += 1;
+            return;
+        }
+        acc += 1;
+        solout(a);
+        if (fabs(tf - t) <= eps10) done = true;
+    }
+
+    __device__ void finish(const EnsArgs& a) const {
+        const int64_t n = a.n;
+#pragma unroll
+        for (int c = 0; c < D; ++c) a.y_final[(int64_t)c * n + inst] = (double)y[c] - (double)yc[c];
+        for (int c = D; c < a.dmax; ++c) a.y_final[(int64_t)c * n + inst] = 0.0;
+        if (a.t_final) a.t_final[inst] = t;
+        if (a.accepted) a.accepted[inst] = acc;
+        if (a.rejected) a.rejected[inst] = rej;
+        if (a.fevals) a.fevals[inst] = fev;
+        if (a.status) a.status[inst] = status;
+    }
+};
+
+// One instance per thread, run to completion.
+template <class Tab, class Rhs, class P, bool DENSE>
+__global__ void __launch_bounds__(128) erk_thread_kernel(EnsArgs a) {
+    int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= a.count) return;
+    Lane<Tab, Rhs, P, DENSE> L;
+    L.begin(a.index ? a.index[w] : w, a);
+    while (!L.done) L.iterate(a);
+    L.finish(a);
+}
+
+// Persistent form: a fixed grid; each lane takes a work item from the device queue, steps it,
+// and as soon as its instance finishes takes the next one (lane refill), so lanes whose instance
+// needs few steps do not idle while their warp-mates finish long ones.
+template <class Tab, class Rhs, class P, bool DENSE>
+__global__ void __launch_bounds__(128) erk_persistent_kernel(EnsArgs a) {
+    Lane<Tab, Rhs, P, DENSE> L;
+    bool active = false;
+    for (;;) {
+        if (!active) {
+            unsigned long long w = atomicAdd(a.ticket, 1ULL);
+            if (w >= (unsigned long long)a.count) break;
+            L.begin(a.index ? a.index[w] : (int64_t)w, a);
+            if (L.done) {
+                L.finish(a);
+                continue;
+            }
+            active = true;
+        }
+        L.iterate(a);
+        if (L.done) {
+            L.finish(a);
+            active = false;
+        }
+    }
+}
+
+}  // namespace degpu

@@ -1,0 +1,99 @@
+// registry.cuh — table of compiled (method, family, precision, dense) kernel variants.
+//
+// Each instantiation translation unit registers launchers for the variants it compiles; the ABI
+// looks a variant up by key.  The parity variants live in translation units compiled with
+// -fmad=false, so that no multiply-add is contracted into an FMA anywhere on that path.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <tuple>
+
+#include "erk_core.cuh"
+
+namespace degpu {
+
+using EnsLaunchFn = cudaError_t (*)(const EnsArgs& a, int kernel, cudaStream_t s);
+
+struct VariantKey {
+    int method, rhs, prec, dense;
+    bool operator<(const VariantKey& o) const {
+        return std::tie(method, rhs, prec, dense) < std::tie(o.method, o.rhs, o.prec, o.dense);
+    }
+};
+
+std::map<VariantKey, EnsLaunchFn>& ens_registry();
+
+template <class Tab>
+constexpr int method_id() {
+    return std::is_same<Tab, TabRK4>::value ? DEGPU_RK4 : std::is_same<Tab, TabDopri5>::value ? DEGPU_DOPRI5 : DEGPU_DOP853;
+}
+
+int device_sm_count();
+
+template <class Tab, class Rhs, class P, bool DENSE>
+cudaError_t launch_ens(const EnsArgs& a, int kernel, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    if (kernel == DEGPU_KERNEL_PERSISTENT) {
+        static int blocks_per_sm = -1;
+        if (blocks_per_sm < 0) {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &blocks_per_sm, erk_persistent_kernel<Tab, Rhs, P, DENSE>, 128, 0);
+            if (e != cudaSuccess) return e;
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+        }
+        long long grid = (long long)blocks_per_sm * device_sm_count();
+        long long need = (a.count + 127) / 128;
+        if (grid > need) grid = need;
+        erk_persistent_kernel<Tab, Rhs, P, DENSE><<<(unsigned)grid, 128, 0, s>>>(a);
+    } else {
+        long long blocks = (a.count + 127) / 128;
+        erk_thread_kernel<Tab, Rhs, P, DENSE><<<(unsigned)blocks, 128, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+template <class Tab, class Rhs, class P>
+void register_variant() {
+    ens_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 0}] = &launch_ens<Tab, Rhs, P, false>;
+    ens_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 1}] = &launch_ens<Tab, Rhs, P, true>;
+}
+
+// Per-translation-unit registration hooks (called once by the ABI).
+void register_parity_main();
+void register_parity_tests();
+void register_fast();
+void register_mixed();
+
+// Right-hand-side evaluation kernels (degpu_eval_rhs)
+using RhsLaunchFn = cudaError_t (*)(int64_t n, const double* t, const double* y, const double* p, double* dydt,
+                                    cudaStream_t s);
+std::map<std::pair<int, int>, RhsLaunchFn>& rhs_registry();
+
+template <class Rhs, class P>
+__global__ void eval_rhs_kernel(int64_t n, const double* t, const double* y, const double* p, double* dydt) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    using S = typename P::S;
+    S yy[Rhs::D], dd[Rhs::D];
+    double pp[Rhs::NP > 0 ? Rhs::NP : 1];
+    for (int q = 0; q < Rhs::NP; ++q) pp[q] = p[(int64_t)q * n + i];
+    for (int c = 0; c < Rhs::D; ++c) yy[c] = (S)y[(int64_t)c * n + i];
+    Rhs::template diff<P>(t[i], yy, dd, pp);
+    for (int c = 0; c < Rhs::D; ++c) dydt[(int64_t)c * n + i] = (double)dd[c];
+}
+
+template <class Rhs, class P>
+cudaError_t launch_rhs(int64_t n, const double* t, const double* y, const double* p, double* dydt, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    eval_rhs_kernel<Rhs, P><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, t, y, p, dydt);
+    return cudaGetLastError();
+}
+
+template <class Rhs, class P>
+void register_rhs() {
+    rhs_registry()[{Rhs::ID, P::ID}] = &launch_rhs<Rhs, P>;
+}
+
+}  // namespace degpu

@@ -1,0 +1,218 @@
+// rhs.cuh — CUDA __device__ twins of `ODE::diff(&self, t, &y, &mut dydt)` (src/ode/ode.rs:20-44)
+// for the built-in families, and the precision policies they are evaluated under.
+//
+// Each family is a struct with the state dimension D, the parameter count NP and
+//     template <class P> static void diff(double t, const typename P::S* y, typename P::S* dydt,
+//                                         const double* p);
+// The expressions keep the evaluation order of the crate's test systems (tests/ode/systems.rs),
+// which is what the parity path (compiled without FMA contraction) must reproduce.
+#pragma once
+
+#include "dd_math.cuh"
+
+namespace degpu {
+
+// Precision policies --------------------------------------------------------------------------
+// Parity: FP64, crate operation order, correctly rounded pow/sin/cos, no FMA contraction (the
+// translation units that instantiate it are compiled with -fmad=false).
+struct PrecParity {
+    using S = double;
+    static constexpr int ID = 0;
+    static constexpr bool KAHAN = false;
+    __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl(x, y); }
+    __device__ static __forceinline__ double sin(double x) { return ddm::sin_cr(x); }
+    __device__ static __forceinline__ double cos(double x) { return ddm::cos_cr(x); }
+    __device__ static __forceinline__ S from(double x) { return x; }
+};
+// Fast FP64: FMA contraction and the CUDA math library.
+struct PrecFast {
+    using S = double;
+    static constexpr int ID = 1;
+    static constexpr bool KAHAN = false;
+    __device__ static __forceinline__ double pow(double x, double y) { return ::pow(x, y); }
+    __device__ static __forceinline__ double sin(double x) { return ::sin(x); }
+    __device__ static __forceinline__ double cos(double x) { return ::cos(x); }
+    __device__ static __forceinline__ S from(double x) { return x; }
+};
+// Mixed: stages in FP32, y accumulated with Kahan compensation, t/h/norm/controller in FP64.
+struct PrecMixed {
+    using S = float;
+    static constexpr int ID = 2;
+    static constexpr bool KAHAN = true;
+    // x^(-1/order) of the controller: FP64 result from an FP32 log2/exp2 estimate refined by
+    // one FP64 Newton step on r^q = x^-1 (q = 5 or 8); general y falls back to FP64 pow.
+    __device__ static __forceinline__ double pow(double x, double y) {
+        if ((y == -0.2 || y == -0.125) && x > 1e-300 && x < 1e300) {
+            double q = (y == -0.2) ? 5.0 : 8.0;
+            float lx = __log2f((float)x);
+            double r = (double)exp2f(lx * (float)y);
+            double rq = r * r;  // r^2
+            rq = rq * rq;       // r^4
+            if (q == 8.0) rq = rq * rq;
+            else rq = rq * r;
+            // Newton: r <- r (1 + (1 - x r^q)/q)
+            double e = fma(-x, rq, 1.0);
+            return fma(r, e / q, r);
+        }
+        return ::pow(x, y);
+    }
+    __device__ static __forceinline__ float sin(float x) { return ::sinf(x); }
+    __device__ static __forceinline__ float cos(float x) { return ::cosf(x); }
+    __device__ static __forceinline__ S from(double x) { return (float)x; }
+};
+
+// Families -------------------------------------------------------------------------------------
+// tests/ode/systems.rs:85-101
+struct RhsLorenz {
+    static constexpr int ID = 1, D = 3, NP = 3;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        S sigma = (S)p[0], rho = (S)p[1], beta = (S)p[2];
+        S x = y[0], yv = y[1], z = y[2];
+        dydt[0] = sigma * (yv - x);
+        dydt[1] = x * (rho - z) - yv;
+        dydt[2] = x * yv - beta * z;
+    }
+};
+
+// tests/ode/systems.rs:62-78
+struct RhsVanDerPol {
+    static constexpr int ID = 2, D = 2, NP = 1;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        S mu = (S)p[0];
+        S y1 = y[0], y2 = y[1];
+        dydt[0] = y2;
+        dydt[1] = mu * ((S)1 - y1 * y1) * y2 - y1;
+    }
+};
+
+// Damped driven pendulum, g/l = 1: theta' = omega, omega' = -gamma omega - sin(theta) + A cos(Omega t)
+// (the model of examples/ode/05_damped_pendulum/main.rs:34-40 plus a periodic drive).
+struct RhsPendulum {
+    static constexpr int ID = 3, D = 2, NP = 3;
+    template <class P>
+    __device__ static __forceinline__ void diff(double t, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        S theta = y[0], omega = y[1];
+        dydt[0] = omega;
+        if constexpr (P::KAHAN) {
+            // FP32 stage arithmetic; the drive phase Omega t is formed and reduced in FP64 so that
+            // the long horizon does not cost phase accuracy.
+            double ph = p[2] * t;
+            double k = rint(ph * 0.15915494309189535);
+            float r = (float)fma(-k, 6.283185307179586, ph);
+            dydt[1] = -(float)p[0] * omega - P::sin(theta) + (float)p[1] * P::cos(r);
+        } else {
+            double gamma = p[0], A = p[1], Omega = p[2];
+            dydt[1] = -gamma * omega - P::sin(theta) + A * P::cos(Omega * t);
+        }
+    }
+};
+
+// tests/ode/systems.rs:6-17
+struct RhsExpGrowth {
+    static constexpr int ID = 5, D = 1, NP = 1;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        dydt[0] = (typename P::S)p[0] * y[0];
+    }
+};
+
+// tests/ode/systems.rs:19-31
+struct RhsLinear {
+    static constexpr int ID = 6, D = 1, NP = 2;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        dydt[0] = (S)p[0] + (S)p[1] * y[0];
+    }
+};
+
+// tests/ode/systems.rs:33-46
+struct RhsHarmonic {
+    static constexpr int ID = 7, D = 2, NP = 1;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        dydt[0] = y[1];
+        dydt[1] = -(S)p[0] * y[0];
+    }
+};
+
+// tests/ode/systems.rs:48-60
+struct RhsLogistic {
+    static constexpr int ID = 8, D = 1, NP = 2;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        dydt[0] = (S)p[0] * y[0] * ((S)1 - y[0] / (S)p[1]);
+    }
+};
+
+// tests/ode/systems.rs:155-173
+struct RhsRobertson {
+    static constexpr int ID = 9, D = 3, NP = 0;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double*) {
+        using S = typename P::S;
+        S y1 = y[0], y2 = y[1], y3 = y[2];
+        dydt[0] = (S)-0.04 * y1 + (S)1.0e4 * y2 * y3;
+        dydt[1] = (S)0.04 * y1 - (S)1.0e4 * y2 * y3 - (S)3.0e7 * y2 * y2;
+        dydt[2] = (S)3.0e7 * y2 * y2;
+    }
+};
+
+// tests/ode/systems.rs:175-190
+struct RhsHires {
+    static constexpr int ID = 10, D = 8, NP = 0;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double*) {
+        using S = typename P::S;
+        dydt[0] = (S)-1.71 * y[0] + (S)0.43 * y[1] + (S)8.32 * y[2] + (S)0.0007;
+        dydt[1] = (S)1.71 * y[0] - (S)8.75 * y[1];
+        dydt[2] = (S)-10.03 * y[2] + (S)0.43 * y[3] + (S)0.035 * y[4];
+        dydt[3] = (S)8.32 * y[1] + (S)1.71 * y[2] - (S)1.12 * y[3];
+        dydt[4] = (S)-1.745 * y[4] + (S)0.43 * y[5] + (S)0.43 * y[6];
+        dydt[5] = (S)-280.0 * y[5] * y[7] + (S)0.69 * y[3] + (S)1.71 * y[4] - (S)0.43 * y[5] + (S)0.69 * y[6];
+        dydt[6] = (S)280.0 * y[5] * y[7] - (S)1.81 * y[6];
+        dydt[7] = (S)-280.0 * y[5] * y[7] + (S)1.81 * y[6];
+    }
+};
+
+// tests/ode/systems.rs:103-120
+struct RhsBrusselator {
+    static constexpr int ID = 11, D = 2, NP = 2;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        S a = (S)p[0], b = (S)p[1], y1 = y[0], y2 = y[1];
+        dydt[0] = a + y1 * y1 * y2 - (b + (S)1) * y1;
+        dydt[1] = b * y1 - y1 * y1 * y2;
+    }
+};
+
+// tests/ode/systems.rs:122-153; powi(2) -> x*x, powi(3) -> x*(x*x) as LLVM expands them.
+struct RhsCr3bp {
+    static constexpr int ID = 12, D = 6, NP = 1;
+    template <class P>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+        using S = typename P::S;
+        S mu = (S)p[0];
+        S rx = y[0], ry = y[1], rz = y[2], vx = y[3], vy = y[4], vz = y[5];
+        S a = rx + mu, b = rx - (S)1 + mu;
+        S r13 = sqrt(a * a + ry * ry + rz * rz);
+        S r23 = sqrt(b * b + ry * ry + rz * rz);
+        S c13 = r13 * (r13 * r13), c23 = r23 * (r23 * r23);
+        dydt[0] = vx;
+        dydt[1] = vy;
+        dydt[2] = vz;
+        dydt[3] = rx + (S)2 * vy - ((S)1 - mu) * (rx + mu) / c13 - mu * (rx - (S)1 + mu) / c23;
+        dydt[4] = ry - (S)2 * vx - ((S)1 - mu) * ry / c13 - mu * ry / c23;
+        dydt[5] = -((S)1 - mu) * rz / c13 - mu * rz / c23;
+    }
+};
+
+}  // namespace degpu

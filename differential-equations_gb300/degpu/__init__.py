@@ -1,0 +1,238 @@
+"""degpu — Python bindings of the GB300 ensemble explicit Runge–Kutta integrator.
+
+Thin ctypes layer over the C ABI (include/degpu.h).  The builder mirrors the crate's surface:
+
+    m = ExplicitRungeKutta.dopri5().rtol(1e-8).atol(1e-10)       # src/methods/erk/mod.rs:165-174
+    sol = IVP.ode(System.lorenz(10, 28, 8/3), 0.0, 20.0, [1, 1, 1]).method(m).t_eval(pts).solve()
+
+and `solve_ensemble` solves many instances of a family in one call.  Every solve runs on the GPU
+through libdegpu.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import abi
+
+__all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
+           "Solution"]
+
+STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
+                abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness"}
+
+
+class DegpuError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        lib = abi.load()
+        super().__init__(f"{what}: {lib.degpu_status_string(code).decode()} ({code})")
+        self.code = code
+
+
+class ExplicitRungeKutta:
+    """Method configuration, mirroring ExplicitRungeKutta's constructors and setters
+    (src/methods/erk/fixed/mod.rs:69-75, src/methods/erk/dormandprince/mod.rs:45-58,
+    src/methods/erk/mod.rs:165-228)."""
+
+    def __init__(self, method: int, h0: float = 0.0):
+        self.cfg = abi.default_cfg(method)
+        self.cfg.h0 = h0
+        self._rtol = 1e-6
+        self._atol = 1e-6
+
+    @classmethod
+    def rk4(cls, h0: float):
+        return cls(abi.RK4, h0)
+
+    @classmethod
+    def dopri5(cls):
+        return cls(abi.DOPRI5)
+
+    @classmethod
+    def dop853(cls):
+        return cls(abi.DOP853)
+
+    def rtol(self, v):
+        self._rtol = v
+        return self
+
+    def atol(self, v):
+        self._atol = v
+        return self
+
+    def h0(self, v):
+        self.cfg.h0 = v
+        return self
+
+    def h_min(self, v):
+        self.cfg.h_min = v
+        return self
+
+    def h_max(self, v):
+        self.cfg.h_max = v
+        return self
+
+    def max_steps(self, v):
+        self.cfg.max_steps = int(v)
+        return self
+
+    def safety_factor(self, v):
+        self.cfg.safety_factor = v
+        return self
+
+    def min_scale(self, v):
+        self.cfg.min_scale = v
+        return self
+
+    def max_scale(self, v):
+        self.cfg.max_scale = v
+        return self
+
+    # GPU-specific knobs
+    def precision(self, p: int):
+        self.cfg.precision = p
+        return self
+
+    def kernel(self, k: int):
+        self.cfg.kernel = k
+        return self
+
+    def dense_mode(self, d: int):
+        self.cfg.dense_mode = d
+        return self
+
+
+@dataclass
+class System:
+    """A built-in right-hand side (a CUDA __device__ twin of `ODE::diff`) and its parameters."""
+    rhs_id: int
+    params: Sequence[float]
+    dim: int
+
+    @staticmethod
+    def lorenz(sigma, rho, beta):
+        return System(abi.RHS["LORENZ"], [sigma, rho, beta], 3)
+
+    @staticmethod
+    def van_der_pol(mu):
+        return System(abi.RHS["VAN_DER_POL"], [mu], 2)
+
+    @staticmethod
+    def pendulum(gamma, A, Omega):
+        return System(abi.RHS["PENDULUM"], [gamma, A, Omega], 2)
+
+    @staticmethod
+    def exponential_growth(k):
+        return System(abi.RHS["EXP_GROWTH"], [k], 1)
+
+    @staticmethod
+    def harmonic(k):
+        return System(abi.RHS["HARMONIC"], [k], 2)
+
+    @staticmethod
+    def fpu_beta(beta, masses):
+        return System(abi.RHS["FPU_BETA"], [beta], 2 * masses)
+
+
+@dataclass
+class EnsembleResult:
+    y_final: np.ndarray      # [dim, n]
+    t_final: np.ndarray      # [n]
+    dense: Optional[np.ndarray]  # [n_eval, dim, n]
+    accepted: np.ndarray
+    rejected: np.ndarray
+    fevals: np.ndarray
+    status: np.ndarray
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(shape) if shape is not None else a
+
+
+def solve_ensemble(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
+                   t_eval=None, dims=None, family=None, n_params: Optional[int] = None) -> EnsembleResult:
+    """Solve n IVPs (host arrays) through degpu_solve_ensemble_host.
+
+    y0 is [dim, n] (structure of arrays), params [n_params, n]; t0, tf, rtol, atol are [n] or
+    scalars broadcast to n.
+    """
+    lib = abi.load()
+    y0 = np.asarray(y0, dtype=np.float64)
+    n = y0.shape[1]
+    bc = lambda v: _f64(np.broadcast_to(np.asarray(v, dtype=np.float64), (n,)).copy())
+    t0, tf, rtol, atol = bc(t0), bc(tf), bc(rtol), bc(atol)
+    y0 = _f64(y0)
+    params = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, n)) if params is not None \
+        and np.size(params) else np.zeros((1, n))
+    np_ = n_params if n_params is not None else (params.shape[0] if params is not None else 0)
+    te = None if t_eval is None else _f64(t_eval)
+    m = 0 if te is None else len(te)
+    dims_a = None if dims is None else np.ascontiguousarray(dims, dtype=np.int32)
+    fam_a = None if family is None else np.ascontiguousarray(family, dtype=np.int32)
+    out = dict(y_final=np.empty((dim, n)), t_final=np.empty(n), dense=np.empty((m, dim, n)) if m else None,
+               accepted=np.empty(n, np.int64), rejected=np.empty(n, np.int64), fevals=np.empty(n, np.int64),
+               status=np.empty(n, np.int32))
+    prob = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=np_)
+    bi = abi.BatchIn(n=n, t0=abi.ptr(t0), tf=abi.ptr(tf), y0=abi.ptr(y0), params=abi.ptr(params),
+                     rtol=abi.ptr(rtol), atol=abi.ptr(atol), dims=abi.ptr(dims_a, C.c_int32),
+                     family=abi.ptr(fam_a, C.c_int32), t_eval=abi.ptr(te), n_eval=m)
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]), dense=abi.ptr(out["dense"]),
+                      accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
+                      fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
+    rc = lib.degpu_solve_ensemble_host(C.byref(prob), C.byref(method.cfg), C.byref(bi), C.byref(bo))
+    if rc != abi.OK:
+        raise DegpuError(rc, "degpu_solve_ensemble_host")
+    return EnsembleResult(**out)
+
+
+@dataclass
+class Solution:
+    """Result of one solve: the crate's Solution fields (src/solution.rs:30-52) that the GPU
+    produces — the requested output points (or the final point), counters and status."""
+    t: list
+    y: list
+    status: str
+    accepted: int
+    rejected: int
+    fevals: int
+
+
+class IVP:
+    """Single-instance builder with the crate's shape (src/ivp.rs:279, 632, 656, 781-791)."""
+
+    def __init__(self, system: System, t0: float, tf: float, y0):
+        self.system, self.t0, self.tf, self.y0 = system, t0, tf, np.asarray(y0, dtype=np.float64).reshape(-1)
+        self._method: Optional[ExplicitRungeKutta] = None
+        self._t_eval = None
+
+    @classmethod
+    def ode(cls, system: System, t0, tf, y0):
+        return cls(system, t0, tf, y0)
+
+    def method(self, m: ExplicitRungeKutta):
+        self._method = m
+        return self
+
+    def t_eval(self, pts):
+        self._t_eval = list(pts)
+        return self
+
+    def solve(self) -> Solution:
+        m = self._method or ExplicitRungeKutta.dopri5()
+        d = len(self.y0)
+        r = solve_ensemble(self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),
+                           np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m._rtol], [m._atol], m,
+                           t_eval=self._t_eval, dims=[d] if self.system.rhs_id == abi.RHS["FPU_BETA"] else None)
+        st = STATUS_NAMES.get(int(r.status[0]), str(int(r.status[0])))
+        if self._t_eval is not None:
+            order = sorted(range(len(self._t_eval)), key=lambda i: self._t_eval[i],
+                           reverse=self.tf < self.t0)
+            ts = [self._t_eval[i] for i in order if not np.isnan(r.dense[i, 0, 0])]
+            ys = [r.dense[i, :, 0].copy() for i in order if not np.isnan(r.dense[i, 0, 0])]
+        else:
+            ts, ys = [float(r.t_final[0])], [r.y_final[:, 0].copy()]
+        return Solution(ts, ys, st, int(r.accepted[0]), int(r.rejected[0]), int(r.fevals[0]))

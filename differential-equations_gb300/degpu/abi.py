@@ -1,0 +1,123 @@
+"""ctypes mirror of include/degpu.h (the C ABI of the GB300 ensemble ERK integrator).
+
+The structs here are byte-for-byte the C structs; `load()` opens the in-tree libdegpu.so and
+declares every exported entry point.  There is no fallback: if the shared library is missing
+the import of the solver API raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "csrc", "libdegpu.so")
+
+# degpu_status
+OK, BAD_INPUT, OOM, TIMEOUT, CUDA_ERROR, UNSUPPORTED = range(6)
+# degpu_method
+RK4, DOPRI5, DOP853 = 0, 1, 2
+# degpu_precision
+FP64_PARITY, FP64_FAST, MIXED = 0, 1, 2
+# degpu_kernel
+KERNEL_AUTO, KERNEL_THREAD, KERNEL_WARP, KERNEL_PERSISTENT = 0, 1, 2, 3
+# degpu_dense_mode
+DENSE_REFERENCE, DENSE_HAIRER = 0, 1
+# degpu_instance_status
+COMPLETE, ERR_BAD_INPUT, ERR_MAX_STEPS, ERR_STEP_SIZE, ERR_STIFFNESS = range(5)
+# degpu_rhs_id
+RHS = dict(
+    LORENZ=1, VAN_DER_POL=2, PENDULUM=3, FPU_BETA=4, EXP_GROWTH=5, LINEAR=6, HARMONIC=7,
+    LOGISTIC=8, ROBERTSON=9, HIRES=10, BRUSSELATOR=11, CR3BP=12,
+)
+RHS_NVRTC_BASE = 1000
+
+DP = C.POINTER(C.c_double)
+I32P = C.POINTER(C.c_int32)
+I64P = C.POINTER(C.c_int64)
+
+
+class MethodCfg(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32), ("precision", C.c_int32), ("kernel", C.c_int32), ("dense_mode", C.c_int32),
+        ("h0", C.c_double), ("h_min", C.c_double), ("h_max", C.c_double), ("max_steps", C.c_int64),
+        ("safety_factor", C.c_double), ("min_scale", C.c_double), ("max_scale", C.c_double),
+    ]
+
+
+class Problem(C.Structure):
+    _fields_ = [("rhs_id", C.c_int32), ("dim", C.c_int32), ("n_params", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchIn(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64), ("t0", DP), ("tf", DP), ("y0", DP), ("params", DP), ("rtol", DP), ("atol", DP),
+        ("dims", I32P), ("family", I32P), ("t_eval", DP), ("n_eval", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class BatchOut(C.Structure):
+    _fields_ = [
+        ("y_final", DP), ("t_final", DP), ("dense", DP), ("accepted", I64P), ("rejected", I64P),
+        ("fevals", I64P), ("status", I32P),
+    ]
+
+
+class GrayScott(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("dx", C.c_double), ("Du", C.c_double),
+                ("Dv", C.c_double), ("F", C.c_double), ("k", C.c_double)]
+
+
+def default_cfg(method: int) -> MethodCfg:
+    """The crate's defaults (src/methods/erk/mod.rs:112-159)."""
+    return MethodCfg(method=method, precision=FP64_PARITY, kernel=KERNEL_AUTO, dense_mode=DENSE_REFERENCE,
+                     h0=0.0, h_min=0.0, h_max=float("inf"), max_steps=10_000, safety_factor=0.9,
+                     min_scale=0.2, max_scale=10.0)
+
+
+_lib = None
+
+# name -> (restype, argtypes) for every symbol include/degpu.h declares
+SIGNATURES = {
+    "degpu_default_cfg": (None, [C.POINTER(MethodCfg), C.c_int32]),
+    "degpu_rhs_info": (C.c_int, [C.c_int32, I32P, I32P]),
+    "degpu_solve_ensemble": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                       C.POINTER(BatchOut), C.c_void_p]),
+    "degpu_solve_ensemble_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                            C.POINTER(BatchOut)]),
+    "degpu_eval_rhs": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP,
+                                 C.c_void_p]),
+    "degpu_register_rhs_nvrtc": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, I32P, C.c_char_p,
+                                           C.c_size_t]),
+    "degpu_gray_scott_rk4": (C.c_int, [C.POINTER(GrayScott), C.c_int32, C.c_double, C.c_double, C.c_int64,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    "degpu_gray_scott_rhs": (C.c_int, [C.POINTER(GrayScott), DP, DP, DP, DP, C.c_void_p]),
+    "degpu_status_string": (C.c_char_p, [C.c_int]),
+    "degpu_version": (C.c_char_p, []),
+}
+
+
+def load(path: str = LIB_PATH):
+    """Open libdegpu.so and declare its entry points.  Raises if it is not built."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libdegpu.so is not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+def ptr(arr, ctype=C.c_double):
+    """ctypes pointer to a numpy array's data or a torch tensor's data_ptr (None -> NULL)."""
+    if arr is None:
+        return None
+    if hasattr(arr, "data_ptr"):
+        return C.cast(C.c_void_p(arr.data_ptr()), C.POINTER(ctype))
+    return arr.ctypes.data_as(C.POINTER(ctype))

@@ -1,0 +1,212 @@
+/*
+ * degpu.h — C ABI of the GB300 ensemble explicit Runge–Kutta integrator.
+ *
+ * This is the drop-in boundary for the explicit Runge–Kutta path of the Rust crate
+ * `differential-equations` v0.6.1.  One call solves many independent initial value problems
+ * `dy/dt = f(t, y), y(t0) = y0` with RK4, DOPRI5 or DOP853, exactly as
+ *
+ *     IVP::ode(&system, t0, tf, y0)                         (src/ivp.rs:279)
+ *        .method(ExplicitRungeKutta::dopri5().rtol(r).atol(a))  (src/ivp.rs:632, src/methods/erk/mod.rs:165-174)
+ *        .t_eval(points)                                      (src/ivp.rs:656-660)
+ *        .solve()                                             (src/ivp.rs:781-791 -> src/ode/solve_ivp.rs:116)
+ *
+ * would solve each of them, one instance at a time, on the CPU.
+ *
+ * Conventions
+ *  - Plain C: pointers, sizes and POD structs only.  No exceptions cross the ABI.
+ *  - Every array pointer in degpu_batch_in / degpu_batch_out is a DEVICE pointer for
+ *    degpu_solve_ensemble and a HOST pointer for degpu_solve_ensemble_host.
+ *  - State layout is structure-of-arrays: component c of instance i lives at [c * n + i].
+ *    Dense output lives at [(e * d_max + c) * n + i] for evaluation point e.
+ *  - The global return value says whether the call ran; per-instance failures are values in
+ *    `status[i]`, mirroring `Error` (src/error.rs:13-40).  A failed instance never aborts the
+ *    batch, exactly as one failed `solve()` does not affect another.
+ *  - Calls are stream-ordered and asynchronous on `stream` (a cudaStream_t, NULL = default
+ *    stream) unless the function says otherwise.
+ */
+#ifndef DEGPU_H
+#define DEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Global status of a call. */
+typedef enum {
+    DEGPU_OK = 0,
+    DEGPU_BAD_INPUT = 1,   /* a pointer, size or configuration value is invalid                */
+    DEGPU_OOM = 2,         /* device memory could not be obtained                               */
+    DEGPU_TIMEOUT = 3,     /* a bounded device-side wait gave up                                */
+    DEGPU_CUDA_ERROR = 4,  /* a CUDA runtime / driver call failed                               */
+    DEGPU_UNSUPPORTED = 5  /* the (method, family, precision, kernel) combination is not built */
+} degpu_status;
+
+/* Methods: constructors in src/methods/erk/fixed/mod.rs:69-75 (rk4) and
+ * src/methods/erk/dormandprince/mod.rs:45-58 (dop853, dopri5). */
+typedef enum { DEGPU_RK4 = 0, DEGPU_DOPRI5 = 1, DEGPU_DOP853 = 2 } degpu_method;
+
+/* Arithmetic of the solve.
+ *  FP64_PARITY — every operation in the crate's order, no FMA contraction, correctly rounded
+ *                pow/sin/cos: reproduces the crate's step counts and states bit for bit.
+ *  FP64_FAST   — FP64 with FMA contraction and the fast CUDA math library.
+ *  MIXED       — stage right-hand sides and stage combinations in FP32, y_{n+1} accumulated with
+ *                Kahan compensation; t, h, the error norm and the step-size controller in FP64. */
+typedef enum { DEGPU_FP64_PARITY = 0, DEGPU_FP64_FAST = 1, DEGPU_MIXED = 2 } degpu_precision;
+
+/* Kernel layout. AUTO picks by method and dimension. */
+typedef enum {
+    DEGPU_KERNEL_AUTO = 0,
+    DEGPU_KERNEL_THREAD = 1,      /* one system per thread, state and stages in registers          */
+    DEGPU_KERNEL_WARP = 2,        /* one system per warp, lanes own components, stages in smem     */
+    DEGPU_KERNEL_PERSISTENT = 3   /* persistent grid, device work queue, lane refill               */
+} degpu_kernel;
+
+/* DOP853 dense output: the crate's own fold (src/methods/erk/dormandprince/ordinary.rs:310-333)
+ * or the published Hairer–Nørsett–Wanner continuous extension. */
+typedef enum { DEGPU_DENSE_REFERENCE = 0, DEGPU_DENSE_HAIRER = 1 } degpu_dense_mode;
+
+/* Per-instance result status; values mirror `Error` (src/error.rs:13-40). */
+typedef enum {
+    DEGPU_COMPLETE = 0,        /* Ok(Solution) with Status::Complete (src/ode/solve_ivp.rs:268-276) */
+    DEGPU_ERR_BAD_INPUT = 1,   /* Error::BadInput  (src/utils.rs:60-157, src/ode/solve_ivp.rs:139-147) */
+    DEGPU_ERR_MAX_STEPS = 2,   /* Error::MaxSteps  (dormandprince/ordinary.rs:82-92, fixed/ordinary.rs:64-75) */
+    DEGPU_ERR_STEP_SIZE = 3,   /* Error::StepSize  (dormandprince/ordinary.rs:70-80)                   */
+    DEGPU_ERR_STIFFNESS = 4    /* Error::Stiffness (dormandprince/ordinary.rs:176-186)                 */
+} degpu_instance_status;
+
+/* Built-in right-hand sides (CUDA __device__ twins of `ODE::diff`, src/ode/ode.rs:20-44).
+ * Parameters per instance are given in `params` as [p][n]. */
+typedef enum {
+    DEGPU_RHS_LORENZ = 1,       /* d=3, p=[sigma, rho, beta]        tests/ode/systems.rs:85-101   */
+    DEGPU_RHS_VAN_DER_POL = 2,  /* d=2, p=[mu]                      tests/ode/systems.rs:66-78    */
+    DEGPU_RHS_PENDULUM = 3,     /* d=2, p=[gamma, A, Omega]  damped driven pendulum, g/l = 1       */
+    DEGPU_RHS_FPU_BETA = 4,     /* d=2m, p=[beta]  FPU-beta chain with fixed ends, y=[x_1..x_m,p_1..p_m] */
+    DEGPU_RHS_EXP_GROWTH = 5,   /* d=1, p=[k]                       tests/ode/systems.rs:6-17     */
+    DEGPU_RHS_LINEAR = 6,       /* d=1, p=[a, b]                    tests/ode/systems.rs:19-31    */
+    DEGPU_RHS_HARMONIC = 7,     /* d=2, p=[k]                       tests/ode/systems.rs:33-46    */
+    DEGPU_RHS_LOGISTIC = 8,     /* d=1, p=[k, m]                    tests/ode/systems.rs:48-60    */
+    DEGPU_RHS_ROBERTSON = 9,    /* d=3, p=[]                        tests/ode/systems.rs:155-173  */
+    DEGPU_RHS_HIRES = 10,       /* d=8, p=[]                        tests/ode/systems.rs:175-190  */
+    DEGPU_RHS_BRUSSELATOR = 11, /* d=2, p=[a, b]                    tests/ode/systems.rs:103-120  */
+    DEGPU_RHS_CR3BP = 12,       /* d=6, p=[mu]                      tests/ode/systems.rs:122-153  */
+    DEGPU_RHS_NVRTC_BASE = 1000 /* ids >= this were returned by degpu_register_rhs_nvrtc          */
+} degpu_rhs_id;
+
+/* Solver settings: the fields and defaults of ExplicitRungeKutta (src/methods/erk/mod.rs:112-159)
+ * and its builder setters (src/methods/erk/mod.rs:165-228).  `filter` is always the identity. */
+typedef struct {
+    int32_t method;        /* degpu_method                                                  */
+    int32_t precision;     /* degpu_precision                                               */
+    int32_t kernel;        /* degpu_kernel                                                  */
+    int32_t dense_mode;    /* degpu_dense_mode                                              */
+    double h0;             /* initial step; 0 = h_init heuristic (DP) or |tf-t0|/100 (RK4)  */
+    double h_min;          /* default 0                                                     */
+    double h_max;          /* default +inf                                                  */
+    int64_t max_steps;     /* attempted-step cap, default 10 000                            */
+    double safety_factor;  /* default 0.9                                                   */
+    double min_scale;      /* default 0.2                                                   */
+    double max_scale;      /* default 10                                                    */
+} degpu_method_cfg;
+
+/* The system being solved. */
+typedef struct {
+    int32_t rhs_id;    /* degpu_rhs_id for every instance (ignored when batch_in.family != NULL) */
+    int32_t dim;       /* d, or the maximum d when batch_in.dims != NULL                         */
+    int32_t n_params;  /* p                                                                      */
+    int32_t reserved;
+} degpu_problem;
+
+typedef struct {
+    int64_t n;               /* number of instances                                        */
+    const double* t0;        /* [n]                                                          */
+    const double* tf;        /* [n]                                                          */
+    const double* y0;        /* [dim][n]                                                     */
+    const double* params;    /* [n_params][n] (may be NULL when n_params == 0)               */
+    const double* rtol;      /* [n] scalar Tolerance per instance (src/tolerance.rs:11-14)  */
+    const double* atol;      /* [n]                                                          */
+    const int32_t* dims;     /* [n] per-instance d (ragged ensembles) or NULL                */
+    const int32_t* family;   /* [n] per-instance rhs id (mixed ensembles) or NULL            */
+    const double* t_eval;    /* [n_eval] evaluation times shared by all instances, or NULL  */
+    int32_t n_eval;          /* number of evaluation times (0 = no dense output)             */
+    int32_t reserved;
+} degpu_batch_in;
+
+typedef struct {
+    double* y_final;     /* [dim][n] state at the end (or at the error, as Error{t, y} carries) */
+    double* t_final;     /* [n]                                                                  */
+    double* dense;       /* [n_eval][dim][n] or NULL; t_eval points the solve never reached stay NaN */
+    int64_t* accepted;   /* [n] Steps.accepted (src/stats.rs, counted in src/ode/solve_ivp.rs:218-225) */
+    int64_t* rejected;   /* [n] Steps.rejected                                                  */
+    int64_t* fevals;     /* [n] Evals.function                                                  */
+    int32_t* status;     /* [n] degpu_instance_status                                           */
+} degpu_batch_out;
+
+/* Fill `cfg` with the crate's defaults (src/methods/erk/mod.rs:112-159) for `method`. */
+void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method);
+
+/* Dimension and parameter count of a built-in family (dim = -1 for variable-size families).
+ * Returns DEGPU_BAD_INPUT for an unknown id. */
+degpu_status degpu_rhs_info(int32_t rhs_id, int32_t* dim, int32_t* n_params);
+
+/* Solve an ensemble, device pointers, stream-ordered.
+ * Replaces, per instance i, `IVP::ode(&sys_i, t0[i], tf[i], y0_i).method(m).t_eval(t_eval).solve()`
+ * (src/ivp.rs:279-791; src/ode/solve_ivp.rs:116-277).  Host-side validation of the arguments
+ * happens before anything is launched; per-instance BadInput checks
+ * (src/utils.rs:60-157, src/ode/solve_ivp.rs:139-147) are reported in status[i]. */
+degpu_status degpu_solve_ensemble(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                  const degpu_batch_in* in, degpu_batch_out* out, void* stream);
+
+/* Same contract with HOST pointers: copies inputs to the device, solves, copies results back,
+ * synchronizes.  This is the call a crate user's host code makes. */
+degpu_status degpu_solve_ensemble_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                       const degpu_batch_in* in, degpu_batch_out* out);
+
+/* One evaluation of a built-in right-hand side for every instance (`ODE::diff`,
+ * src/ode/ode.rs:20-44), device pointers: dydt[c*n+i] = f_i(t[i], y_i). */
+degpu_status degpu_eval_rhs(int32_t rhs_id, int32_t precision, int64_t n, int32_t dim, int32_t n_params,
+                            const double* t, const double* y, const double* params, double* dydt,
+                            void* stream);
+
+/* Register a right-hand side written as CUDA source and compiled at run time with NVRTC.
+ * `source` must define
+ *     template <class R> __device__ void <name>(R t, const R* y, R* dydt, const double* p);
+ * (the shape of `ODE::diff(&self, t, &y, &mut dydt)`, src/ode/ode.rs:20-44, with the
+ * system's fields passed as p[0..n_params)).  On success *rhs_id receives an id >= 1000
+ * usable in degpu_problem.rhs_id.  Build log (on failure) goes to log[0..log_size). */
+degpu_status degpu_register_rhs_nvrtc(const char* source, const char* name, int32_t dim, int32_t n_params,
+                                      int32_t* rhs_id, char* log, size_t log_size);
+
+/* Method-of-lines: 2-D Gray–Scott reaction–diffusion on a periodic nx*ny grid, advanced with
+ * fixed-step RK4 (src/methods/erk/fixed/ordinary.rs:58-138) whose right-hand side is the
+ * flux-form finite-difference semi-discretisation of src/pde/semi_discrete.rs:250-287 with a
+ * periodic wrap.  u and v are [ny][nx] row-major device arrays, advanced in place by `steps`
+ * steps of size dt.  precision: DEGPU_FP64_PARITY / DEGPU_FP64_FAST use the double arrays,
+ * DEGPU_MIXED uses the float arrays (FP32 throughout). */
+typedef struct {
+    int32_t nx, ny;
+    double dx;        /* grid spacing (both axes)           */
+    double Du, Dv;    /* diffusivities                      */
+    double F, k;      /* feed and kill rates                */
+} degpu_gray_scott;
+
+degpu_status degpu_gray_scott_rk4(const degpu_gray_scott* gs, int32_t precision, double t0, double dt,
+                                  int64_t steps, void* u, void* v, void* stream);
+
+/* One right-hand-side evaluation of the same semi-discretisation (u, v -> du, dv), FP64. */
+degpu_status degpu_gray_scott_rhs(const degpu_gray_scott* gs, const double* u, const double* v,
+                                  double* du, double* dv, void* stream);
+
+/* Human-readable message for a status. */
+const char* degpu_status_string(degpu_status s);
+
+/* Library version string. */
+const char* degpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DEGPU_H */

@@ -1,0 +1,349 @@
+// oracle.cpp — TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline).
+//
+// C ABI of the CPU restatement in oracle.hpp.  The ensemble entry point mirrors
+// degpu_solve_ensemble (include/degpu.h) with HOST pointers and solves one crate-style IVP per
+// instance, statically chunked over `threads` std::threads — the "one crate solve per instance,
+// looped over all host threads" baseline.
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <thread>
+
+#include "oracle.hpp"
+#include "oracle_mol.hpp"
+
+#if defined(__x86_64__) || defined(__i386__)
+#include <quadmath.h>
+typedef __float128 qreal_t;
+static inline qreal_t q_pow(qreal_t x, qreal_t y) { return powq(x, y); }
+static inline qreal_t q_sin(qreal_t x) { return sinq(x); }
+static inline qreal_t q_cos(qreal_t x) { return cosq(x); }
+#else
+static_assert(LDBL_MANT_DIG == 113, "the correctly rounded oracle mode needs binary128 long double");
+typedef long double qreal_t;
+static inline qreal_t q_pow(qreal_t x, qreal_t y) { return powl(x, y); }
+static inline qreal_t q_sin(qreal_t x) { return sinl(x); }
+static inline qreal_t q_cos(qreal_t x) { return cosl(x); }
+#endif
+
+namespace oracle {
+// A binary128 evaluation (113-bit significand, error of a few units in its last place) rounded
+// once to binary64 gives the correctly rounded double except when the exact value lies within
+// ~2^-58 ulp of a rounding boundary.
+double cr_pow(double x, double y) { return (double)q_pow((qreal_t)x, (qreal_t)y); }
+double cr_sin(double x) { return (double)q_sin((qreal_t)x); }
+double cr_cos(double x) { return (double)q_cos((qreal_t)x); }
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+// Scalar math, exposed for tests of the math policy.
+double oracle_cr_pow(double x, double y) { return cr_pow(x, y); }
+double oracle_cr_sin(double x) { return cr_sin(x); }
+double oracle_cr_cos(double x) { return cr_cos(x); }
+double oracle_libm_pow(double x, double y) { return std::pow(x, y); }
+double oracle_libm_sin(double x) { return std::sin(x); }
+double oracle_libm_cos(double x) { return std::cos(x); }
+
+void oracle_cr_pow_batch(const double* x, const double* y, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) out[i] = cr_pow(x[i], y[i]);
+}
+void oracle_cr_sincos_batch(const double* x, double* s, double* c, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        s[i] = cr_sin(x[i]);
+        c[i] = cr_cos(x[i]);
+    }
+}
+void oracle_libm_pow_batch(const double* x, const double* y, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) out[i] = std::pow(x[i], y[i]);
+}
+
+// Solve one instance i of the batch into the outputs.
+static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                           degpu_batch_out* out, int64_t i, const Math& math) {
+    const int64_t n = in->n;
+    int rhs = in->family ? in->family[i] : pb->rhs_id;
+    int d = in->dims ? in->dims[i] : pb->dim;
+    int dmax = pb->dim;
+    State y0(d);
+    for (int c = 0; c < d; ++c) y0[c] = in->y0[(int64_t)c * n + i];
+    std::vector<double> p(pb->n_params);
+    for (int q = 0; q < pb->n_params; ++q) p[q] = in->params[(int64_t)q * n + i];
+    BuiltinOde ode(rhs, d, p, math);
+    Settings set;
+    set.rtol = in->rtol[i];
+    set.atol = in->atol[i];
+    set.h0 = cfg->h0;
+    set.h_min = cfg->h_min;
+    set.h_max = cfg->h_max;
+    set.max_steps = cfg->max_steps;
+    set.safety_factor = cfg->safety_factor;
+    set.min_scale = cfg->min_scale;
+    set.max_scale = cfg->max_scale;
+    std::vector<double> te;
+    const std::vector<double>* tep = nullptr;
+    if (in->n_eval > 0 && in->t_eval) {
+        te.assign(in->t_eval, in->t_eval + in->n_eval);
+        tep = &te;
+    }
+    Result r = solve_one(cfg->method, ode, in->t0[i], in->tf[i], y0, set, math, tep,
+                         cfg->dense_mode == DEGPU_DENSE_HAIRER);
+    for (int c = 0; c < d; ++c) out->y_final[(int64_t)c * n + i] = r.y_final.size() == (size_t)d ? r.y_final[c] : NAN;
+    for (int c = d; c < dmax; ++c) out->y_final[(int64_t)c * n + i] = 0.0;
+    if (out->t_final) out->t_final[i] = r.t_final;
+    if (out->accepted) out->accepted[i] = r.accepted;
+    if (out->rejected) out->rejected[i] = r.rejected;
+    if (out->fevals) out->fevals[i] = r.fevals;
+    if (out->status) out->status[i] = r.outcome.status;
+    if (out->dense && tep) {
+        for (int e = 0; e < in->n_eval; ++e)
+            for (int c = 0; c < dmax; ++c) {
+                double v = (c < d && (size_t)e < r.dense.size()) ? r.dense[e][c] : (c < d ? NAN : 0.0);
+                out->dense[((int64_t)e * dmax + c) * n + i] = v;
+            }
+    }
+}
+
+// Solve instances [0, n) of the batch with `threads` host threads.  math_mode: 0 libm, 1 cr.
+// Returns 0 on success, 1 on bad input.
+int oracle_solve_ensemble(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                          degpu_batch_out* out, int threads, int math_mode) {
+    if (!pb || !cfg || !in || !out || in->n < 0 || !out->y_final) return 1;
+    Math math;
+    math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
+    int64_t n = in->n;
+    if (threads <= 1 || n < 2) {
+        for (int64_t i = 0; i < n; ++i) solve_instance(pb, cfg, in, out, i, math);
+        return 0;
+    }
+    // dynamic chunking: instances differ widely in cost
+    std::atomic<int64_t> next{0};
+    const int64_t chunk = 16;
+    std::vector<std::thread> pool;
+    for (int w = 0; w < threads; ++w)
+        pool.emplace_back([&]() {
+            for (;;) {
+                int64_t s = next.fetch_add(chunk);
+                if (s >= n) break;
+                int64_t e = std::min(n, s + chunk);
+                for (int64_t i = s; i < e; ++i) solve_instance(pb, cfg, in, out, i, math);
+            }
+        });
+    for (auto& t : pool) t.join();
+    return 0;
+}
+
+// One RHS evaluation per instance (same layout as degpu_eval_rhs).
+int oracle_eval_rhs(int32_t rhs_id, int64_t n, int32_t dim, int32_t n_params, const double* t, const double* y,
+                    const double* params, double* dydt, int math_mode) {
+    Math math;
+    math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
+    for (int64_t i = 0; i < n; ++i) {
+        std::vector<double> p(n_params);
+        for (int q = 0; q < n_params; ++q) p[q] = params[(int64_t)q * n + i];
+        BuiltinOde ode(rhs_id, dim, p, math);
+        State yy(dim), dd(dim, 0.0);
+        for (int c = 0; c < dim; ++c) yy[c] = y[(int64_t)c * n + i];
+        ode.diff(t[i], yy, dd);
+        for (int c = 0; c < dim; ++c) dydt[(int64_t)c * n + i] = dd[c];
+    }
+    return 0;
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Method of lines (oracle_mol.hpp)
+// ---------------------------------------------------------------------------------------------
+static Bc make_bc(int kind, const double* val, int L) {
+    Bc b;
+    b.kind = kind == 0 ? BcKind::Dirichlet : kind == 1 ? BcKind::Neumann : BcKind::Periodic;
+    if (val)
+        b.value.assign(val, val + L);
+    else
+        b.value.assign(L, 0.0);
+    return b;
+}
+
+// Threaded evaluation of SemiDiscrete::diff: nodes are independent, so splitting the node loop
+// across threads gives bit-identical results.
+static void mol_diff_threaded(const SemiDiscrete& sd, double t, const State& y, State& dydt, int threads) {
+    if (threads <= 1) {
+        sd.diff(t, y, dydt);
+        return;
+    }
+    size_t N = sd.len();
+    std::vector<std::thread> pool;
+    for (int w = 0; w < threads; ++w)
+        pool.emplace_back([&, w]() {
+            size_t s = N * w / threads, e = N * (w + 1) / threads;
+            for (size_t node = s; node < e; ++node) {
+                // same per-node body as SemiDiscrete::diff
+                const int L = sd.L;
+                if (sd.dirichlet_mask[node]) {
+                    for (int c = 0; c < L; ++c) dydt[node * L + c] = 0.0;
+                    continue;
+                }
+                double x[2];
+                sd.point(node, x);
+                State der(L, 0.0);
+                sd.pde->source(t, x, &y[node * L], der.data(), L);
+                for (int a = 0; a < sd.D; ++a) {
+                    State flo = sd.fd_flux(t, y, node, a, -1);
+                    State fhi = sd.fd_flux(t, y, node, a, +1);
+                    for (int c = 0; c < L; ++c) der[c] = der[c] + (fhi[c] - flo[c]) / sd.dx[a];
+                }
+                for (int c = 0; c < L; ++c) dydt[node * L + c] = der[c];
+            }
+        });
+    for (auto& th : pool) th.join();
+}
+
+struct ThreadedOde : Ode {
+    const SemiDiscrete* sd;
+    int threads;
+    void diff(double t, const State& y, State& dydt) const override { mol_diff_threaded(*sd, t, y, dydt, threads); }
+};
+
+// 1-D heat equation (tests/pde/method_of_lines.rs:3-11) on StructuredGrid::uniform([lo],[hi],[n]).
+// bc kinds: 0 Dirichlet, 1 Neumann.  dydt = SemiDiscretePde::diff(0, y).
+int oracle_heat1d_diff(double alpha, int n, double lo, double hi, int lo_kind, double lo_val, int hi_kind,
+                       double hi_val, const double* y, double* dydt) {
+    HeatPde pde(alpha);
+    SemiDiscrete sd;
+    sd.pde = &pde;
+    sd.D = 1;
+    sd.L = 1;
+    sd.nodes = {n, 1};
+    sd.lower = {lo, 0.0};
+    sd.dx = {(hi - lo) / (double)(n - 1), 1.0};
+    sd.lo_bc[0] = make_bc(lo_kind, &lo_val, 1);
+    sd.hi_bc[0] = make_bc(hi_kind, &hi_val, 1);
+    sd.build_mask();
+    State yy(y, y + n), dd(n, 0.0);
+    sd.diff(0.0, yy, dd);
+    for (int i = 0; i < n; ++i) dydt[i] = dd[i];
+    return 0;
+}
+
+// Coupled diffusion vector field (tests/pde/method_of_lines.rs:13-34,115-140), 1-D, L = 2,
+// y interleaved [node*2 + c].
+int oracle_coupled1d_diff(double d0, double d1, int n, double lo, double hi, const double* lo_val,
+                          const double* hi_val, const double* y, double* dydt) {
+    CoupledDiffusionPde pde;
+    pde.d0 = d0;
+    pde.d1 = d1;
+    SemiDiscrete sd;
+    sd.pde = &pde;
+    sd.D = 1;
+    sd.L = 2;
+    sd.nodes = {n, 1};
+    sd.lower = {lo, 0.0};
+    sd.dx = {(hi - lo) / (double)(n - 1), 1.0};
+    sd.lo_bc[0] = make_bc(0, lo_val, 2);
+    sd.hi_bc[0] = make_bc(0, hi_val, 2);
+    sd.build_mask();
+    State yy(y, y + 2 * n), dd(2 * n, 0.0);
+    sd.diff(0.0, yy, dd);
+    for (int i = 0; i < 2 * n; ++i) dydt[i] = dd[i];
+    return 0;
+}
+
+// Heat equation solved through the full driver with RK4(h) (method_of_lines.rs:36-70).
+// Writes the final state; returns the per-instance status.
+int oracle_heat1d_solve(double alpha, int n, double t0, double tf, double h, const double* u0, double* uf,
+                        int64_t* accepted) {
+    HeatPde pde(alpha);
+    SemiDiscrete sd;
+    sd.pde = &pde;
+    sd.D = 1;
+    sd.L = 1;
+    sd.nodes = {n, 1};
+    sd.lower = {0.0, 0.0};
+    sd.dx = {1.0 / (double)(n - 1), 1.0};
+    double z = 0.0;
+    sd.lo_bc[0] = make_bc(0, &z, 1);
+    sd.hi_bc[0] = make_bc(0, &z, 1);
+    sd.build_mask();
+    Settings set;
+    set.h0 = h;
+    set.max_steps = 10000000;
+    Math math;
+    State y0(u0, u0 + n);
+    Result r = solve_one(DEGPU_RK4, sd, t0, tf, y0, set, math, nullptr);
+    for (int i = 0; i < n; ++i) uf[i] = r.y_final[i];
+    if (accepted) *accepted = r.accepted;
+    return r.outcome.status;
+}
+
+static void gs_setup(SemiDiscrete& sd, GrayScottPde& pde, const degpu_gray_scott* gs) {
+    pde.Du = gs->Du;
+    pde.Dv = gs->Dv;
+    pde.F = gs->F;
+    pde.k = gs->k;
+    sd.pde = &pde;
+    sd.D = 2;
+    sd.L = 2;
+    sd.nodes = {gs->nx, gs->ny};
+    sd.lower = {0.0, 0.0};
+    sd.dx = {gs->dx, gs->dx};
+    for (int a = 0; a < 2; ++a) {
+        sd.lo_bc[a] = make_bc(2, nullptr, 2);
+        sd.hi_bc[a] = make_bc(2, nullptr, 2);
+    }
+    sd.build_mask();
+}
+
+// Gray–Scott periodic semi-discretisation, u/v as [ny][nx] planes (node = ix + nx*iy).
+int oracle_gray_scott_rhs(const degpu_gray_scott* gs, const double* u, const double* v, double* du, double* dv,
+                          int threads) {
+    GrayScottPde pde;
+    SemiDiscrete sd;
+    gs_setup(sd, pde, gs);
+    size_t N = sd.len();
+    State y(2 * N), d(2 * N, 0.0);
+    for (size_t i = 0; i < N; ++i) {
+        y[2 * i] = u[i];
+        y[2 * i + 1] = v[i];
+    }
+    mol_diff_threaded(sd, 0.0, y, d, threads);
+    for (size_t i = 0; i < N; ++i) {
+        du[i] = d[2 * i];
+        dv[i] = d[2 * i + 1];
+    }
+    return 0;
+}
+
+// `steps` calls of the crate's fixed RK4 step (fixed/ordinary.rs:58-138) after init
+// (fixed/ordinary.rs:16-56) with h = dt, on the Gray–Scott system, in place.
+int oracle_gray_scott_rk4(const degpu_gray_scott* gs, double t0, double dt, int64_t steps, double* u, double* v,
+                          int threads) {
+    GrayScottPde pde;
+    SemiDiscrete sd;
+    gs_setup(sd, pde, gs);
+    ThreadedOde ode;
+    ode.sd = &sd;
+    ode.threads = threads;
+    size_t N = sd.len();
+    State y(2 * N);
+    for (size_t i = 0; i < N; ++i) {
+        y[2 * i] = u[i];
+        y[2 * i + 1] = v[i];
+    }
+    FixedRK s;
+    s.tab = tableau_rk4();
+    s.set.h0 = dt;
+    s.set.max_steps = steps + 1;
+    Outcome o;
+    int64_t fe = 0;
+    if (!s.init(ode, t0, t0 + dt * (double)steps, y, fe, o)) return 1;
+    for (int64_t st = 0; st < steps; ++st)
+        if (!s.step(ode, fe, o)) return 2;
+    for (size_t i = 0; i < N; ++i) {
+        u[i] = s.y[2 * i];
+        v[i] = s.y[2 * i + 1];
+    }
+    return 0;
+}
+}  // extern "C"

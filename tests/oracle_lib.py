@@ -1,0 +1,116 @@
+"""Loader for the CPU oracle (oracle/liboracle.so) used as the parity checker by the tests.
+
+The oracle is test infrastructure: it is a C++ restatement of the crate's explicit Runge–Kutta
+path and is never on the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(REPO, "oracle")
+ORACLE_SO = os.path.join(ORACLE_DIR, "liboracle.so")
+sys.path.insert(0, os.path.join(REPO, "differential-equations_gb300"))
+
+from degpu import abi  # noqa: E402  (boundary structs only)
+
+DP = C.POINTER(C.c_double)
+I64P = C.POINTER(C.c_int64)
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(ORACLE_SO)
+        L.oracle_solve_ensemble.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.MethodCfg),
+                                            C.POINTER(abi.BatchIn), C.POINTER(abi.BatchOut), C.c_int, C.c_int]
+        L.oracle_solve_ensemble.restype = C.c_int
+        L.oracle_eval_rhs.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP, C.c_int]
+        for nm in ("oracle_cr_pow", "oracle_libm_pow"):
+            getattr(L, nm).argtypes = [C.c_double, C.c_double]
+            getattr(L, nm).restype = C.c_double
+        for nm in ("oracle_cr_sin", "oracle_cr_cos", "oracle_libm_sin", "oracle_libm_cos"):
+            getattr(L, nm).argtypes = [C.c_double]
+            getattr(L, nm).restype = C.c_double
+        for nm in ("oracle_cr_pow_batch", "oracle_libm_pow_batch"):
+            getattr(L, nm).argtypes = [DP, DP, DP, C.c_int64]
+        L.oracle_cr_sincos_batch.argtypes = [DP, DP, DP, C.c_int64]
+        L.oracle_heat1d_diff.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
+                                         C.c_int, C.c_double, DP, DP]
+        L.oracle_coupled1d_diff.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, DP, DP,
+                                            DP, DP]
+        L.oracle_heat1d_solve.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, DP, DP, I64P]
+        L.oracle_gray_scott_rhs.argtypes = [C.POINTER(abi.GrayScott), DP, DP, DP, DP, C.c_int]
+        L.oracle_gray_scott_rk4.argtypes = [C.POINTER(abi.GrayScott), C.c_double, C.c_double, C.c_int64, DP, DP,
+                                            C.c_int]
+        _lib = L
+    return _lib
+
+
+def p(a):
+    return abi.ptr(a)
+
+
+class Batch:
+    """Host-side batch of IVPs in the ABI's structure-of-arrays layout."""
+
+    def __init__(self, rhs_id, dim, n_params, t0, tf, y0, params, rtol, atol, t_eval=None, dims=None,
+                 family=None):
+        self.n = len(t0)
+        self.problem = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=n_params)
+        self.t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        self.tf = np.ascontiguousarray(tf, dtype=np.float64)
+        self.y0 = np.ascontiguousarray(y0, dtype=np.float64).reshape(dim, self.n)
+        self.params = np.ascontiguousarray(params, dtype=np.float64).reshape(max(n_params, 1), self.n) \
+            if n_params else np.zeros((1, self.n))
+        self.rtol = np.ascontiguousarray(rtol, dtype=np.float64)
+        self.atol = np.ascontiguousarray(atol, dtype=np.float64)
+        self.t_eval = None if t_eval is None else np.ascontiguousarray(t_eval, dtype=np.float64)
+        self.dims = None if dims is None else np.ascontiguousarray(dims, dtype=np.int32)
+        self.family = None if family is None else np.ascontiguousarray(family, dtype=np.int32)
+        self.dim = dim
+
+    def batch_in(self):
+        return abi.BatchIn(
+            n=self.n, t0=p(self.t0), tf=p(self.tf), y0=p(self.y0), params=p(self.params), rtol=p(self.rtol),
+            atol=p(self.atol), dims=abi.ptr(self.dims, C.c_int32), family=abi.ptr(self.family, C.c_int32),
+            t_eval=p(self.t_eval), n_eval=0 if self.t_eval is None else len(self.t_eval))
+
+    def new_outputs(self):
+        m = 0 if self.t_eval is None else len(self.t_eval)
+        return dict(
+            y_final=np.full((self.dim, self.n), np.nan), t_final=np.full(self.n, np.nan),
+            dense=np.full((m, self.dim, self.n), np.nan) if m else None,
+            accepted=np.zeros(self.n, np.int64), rejected=np.zeros(self.n, np.int64),
+            fevals=np.zeros(self.n, np.int64), status=np.full(self.n, -1, np.int32))
+
+    @staticmethod
+    def batch_out(o):
+        return abi.BatchOut(
+            y_final=p(o["y_final"]), t_final=p(o["t_final"]), dense=p(o["dense"]),
+            accepted=abi.ptr(o["accepted"], C.c_int64), rejected=abi.ptr(o["rejected"], C.c_int64),
+            fevals=abi.ptr(o["fevals"], C.c_int64), status=abi.ptr(o["status"], C.c_int32))
+
+
+def solve(batch: Batch, cfg, threads=None, math_mode=1):
+    """Oracle solve of every instance.  math_mode 1 = correctly rounded pow/sin/cos, 0 = host libm."""
+    out = batch.new_outputs()
+    bi = batch.batch_in()
+    bo = Batch.batch_out(out)
+    threads = threads or os.cpu_count() or 1
+    rc = lib().oracle_solve_ensemble(C.byref(batch.problem), C.byref(cfg), C.byref(bi), C.byref(bo), threads,
+                                     math_mode)
+    assert rc == 0
+    return out

@@ -1,0 +1,222 @@
+"""GPU ensemble solves against the CPU oracle, through the C ABI.
+
+Bar (FP64 parity path): every instance's accepted and rejected step counts, function
+evaluations and status equal the oracle's, and the final state agrees within 1e-12 relative
+(in practice bit for bit: both follow the crate's operation order without FMA contraction and
+round pow/sin/cos correctly).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from degpu import abi, workloads as W
+import degpu
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-12  # parity tolerance on final states and dense outputs (FP64 parity path)
+
+
+def oracle_solve(e: W.Ensemble, cfg, t_eval=None):
+    b = O.Batch(e.rhs_id, e.dim, e.n_params, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol,
+                t_eval=t_eval if t_eval is not None else e.t_eval, dims=e.dims, family=e.family)
+    return O.solve(b, cfg, math_mode=1)
+
+
+def gpu_solve(e: W.Ensemble, cfg, t_eval=None):
+    m = degpu.ExplicitRungeKutta(cfg.method)
+    m.cfg = cfg
+    te = t_eval if t_eval is not None else e.t_eval
+    return degpu.solve_ensemble(e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, m, t_eval=te,
+                                dims=e.dims, family=e.family, n_params=e.n_params)
+
+
+def rel_err(a, b):
+    scale = np.maximum(np.abs(b), 1e-300)
+    d = np.abs(a - b)
+    d[np.isnan(a) & np.isnan(b)] = 0.0
+    return d / scale
+
+
+def assert_parity(g, o, dense=False, tol=REL_TOL):
+    np.testing.assert_array_equal(g.status, o["status"])
+    ok = o["status"] == abi.COMPLETE
+    np.testing.assert_array_equal(g.accepted[ok], o["accepted"][ok])
+    np.testing.assert_array_equal(g.rejected[ok], o["rejected"][ok])
+    np.testing.assert_array_equal(g.fevals[ok], o["fevals"][ok])
+    r = rel_err(g.y_final, o["y_final"])
+    assert np.nanmax(np.where(np.abs(o["y_final"]) < 1e-300, 0, r)) <= tol, np.nanmax(r)
+    if dense:
+        r = rel_err(g.dense, o["dense"])
+        assert np.all(np.isnan(g.dense) == np.isnan(o["dense"]))
+        assert np.nanmax(np.where(np.abs(o["dense"]) < 1e-300, 0, r)) <= tol
+
+
+def cfg_for(method, precision=abi.FP64_PARITY, kernel=abi.KERNEL_THREAD, max_steps=10_000_000, h0=0.0):
+    c = abi.default_cfg(method)
+    c.precision, c.kernel, c.max_steps, c.h0 = precision, kernel, max_steps, h0
+    return c
+
+
+def test_lorenz_dopri5_4096_parity():
+    """4096 Lorenz IVPs, DOPRI5 rtol=1e-8 atol=1e-10 on [0, 20] (the plain small configuration)."""
+    e = W.config0()
+    cfg = cfg_for(abi.DOPRI5)
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    assert_parity(g, o)
+    # bit-for-bit in practice
+    assert np.array_equal(g.y_final, o["y_final"])
+
+
+@pytest.mark.parametrize("kernel", [abi.KERNEL_THREAD, abi.KERNEL_PERSISTENT])
+def test_uneven_ensemble_parity(kernel):
+    """A slice of the uneven ensemble (Van der Pol / pendulum / Lorenz, mixed horizons and
+    tolerances) in one call, per-family work lists, thread and persistent kernels."""
+    e = W.config1(n=3 * 700)
+    e.tf = np.minimum(e.tf, 12.0)  # bounded oracle time
+    cfg = cfg_for(abi.DOPRI5, kernel=kernel)
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    assert_parity(g, o)
+
+
+@pytest.mark.parametrize("method", [abi.DOPRI5, abi.DOP853])
+def test_dense_output_parity(method):
+    e = W.config1(n=3 * 200)
+    e.tf = np.minimum(e.tf, 8.0)
+    te = np.array([0.0, 0.37, 1.0, 2.5, 2.5, 5.0, 7.9, 8.0, 11.0])  # unsorted duplicates, beyond tf
+    te = te[[3, 0, 5, 1, 2, 4, 8, 6, 7]]
+    cfg = cfg_for(method)
+    o = oracle_solve(e, cfg, t_eval=te)
+    g = gpu_solve(e, cfg, t_eval=te)
+    assert_parity(g, o, dense=True)
+
+
+def test_dop853_hairer_dense_mode_parity():
+    e = W.config0(n=256)
+    e.tf[:] = 3.0
+    te = np.linspace(0.0, 3.0, 17)
+    cfg = cfg_for(abi.DOP853)
+    cfg.dense_mode = abi.DENSE_HAIRER
+    o = oracle_solve(e, cfg, t_eval=te)
+    g = gpu_solve(e, cfg, t_eval=te)
+    assert_parity(g, o, dense=True)
+
+
+def test_rk4_parity_with_dense():
+    e = W.config1(n=3 * 100)
+    e.tf = np.minimum(e.tf, 5.0)
+    te = np.linspace(0.0, 5.0, 11)
+    cfg = cfg_for(abi.RK4, h0=1e-3)
+    o = oracle_solve(e, cfg, t_eval=te)
+    g = gpu_solve(e, cfg, t_eval=te)
+    assert_parity(g, o, dense=True)
+
+
+SYSTEMS = [
+    # (name, rhs, params, y0, t0, tf)  tests/ode/systems.rs + accuracy.rs setups
+    ("exp+", "EXP_GROWTH", [1.0], [1.0], 0.0, 10.0),
+    ("exp-", "EXP_GROWTH", [1.0], [22026.46579479], 0.0, -10.0),
+    ("linear", "LINEAR", [1.0, 1.0], [1.0], 0.0, 10.0),
+    ("harmonic", "HARMONIC", [1.0], [1.0, 0.0], 0.0, 10.0),
+    ("logistic", "LOGISTIC", [1.0, 10.0], [0.1], 0.0, 10.0),
+    ("robertson", "ROBERTSON", [], [1.0, 0.0, 0.0], 0.0, 0.4),
+    ("hires", "HIRES", [], [1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0057], 0.0, 5.0),
+    ("brusselator", "BRUSSELATOR", [1.0, 3.0], [1.5, 3.0], 0.0, 10.0),
+    ("cr3bp", "CR3BP", [0.012277471], [0.994, 0.0, 0.0, 0.0, -2.00158510637908, 0.0], 0.0, 5.0),
+]
+
+
+@pytest.mark.parametrize("method,h0", [(abi.DOPRI5, 0.0), (abi.DOP853, 0.0), (abi.RK4, 0.01)])
+@pytest.mark.parametrize("sysdef", SYSTEMS, ids=[s[0] for s in SYSTEMS])
+def test_crate_test_systems_parity(sysdef, method, h0):
+    name, rhs, p, y0, t0, tf = sysdef
+    d = len(y0)
+    n = 64
+    rng = np.random.default_rng(7)
+    y0s = np.array(y0, dtype=float)[:, None] * (1.0 + 1e-3 * rng.standard_normal((d, n)))
+    rtol = np.exp(rng.uniform(np.log(1e-10), np.log(1e-5), n))
+    params = np.array(p, dtype=float).reshape(-1, 1).repeat(n, axis=1) if p else np.zeros((0, n))
+    e = W.Ensemble(name, method, n, d, len(p), np.full(n, t0), np.full(n, tf), y0s, params if p else np.zeros((1, n)),
+                   rtol, 1e-2 * rtol, rhs_id=abi.RHS[rhs])
+    cfg = cfg_for(method, h0=h0 if tf > t0 else -h0, max_steps=200_000)
+    o = oracle_solve(e, cfg, t_eval=np.linspace(t0, tf, 5))
+    g = gpu_solve(e, cfg, t_eval=np.linspace(t0, tf, 5))
+    assert_parity(g, o, dense=True)
+
+
+def test_error_statuses_parity():
+    """MaxSteps, BadInput (h0 beyond the interval, tf == t0) per instance, batch not aborted."""
+    e = W.config0(n=8)
+    e.tf[2] = e.t0[2]              # tf == t0 -> BadInput
+    cfg = cfg_for(abi.DOPRI5, max_steps=300)  # most instances hit MaxSteps
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    assert_parity(g, o)
+    assert g.status[2] == abi.ERR_BAD_INPUT
+    assert (g.status == abi.ERR_MAX_STEPS).sum() >= 5
+    cfg = cfg_for(abi.DOPRI5, h0=100.0)  # h0 > |tf - t0| -> BadInput everywhere
+    g = gpu_solve(e, cfg)
+    assert np.all(g.status == abi.ERR_BAD_INPUT)
+
+
+def test_device_pointer_entry_point():
+    """degpu_solve_ensemble with device pointers (torch CUDA tensors) on a stream equals the
+    host entry point."""
+    torch = pytest.importorskip("torch")
+    e = W.config0(n=512)
+    cfg = cfg_for(abi.DOPRI5, kernel=abi.KERNEL_PERSISTENT)
+    g = gpu_solve(e, cfg)
+    dev = torch.device("cuda:0")
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    t0, tf, y0, p, rt, at = T(e.t0), T(e.tf), T(e.y0), T(e.params), T(e.rtol), T(e.atol)
+    yf = torch.empty((3, e.n), dtype=torch.float64, device=dev)
+    acc = torch.empty(e.n, dtype=torch.int64, device=dev)
+    rej = torch.empty_like(acc)
+    fe = torch.empty_like(acc)
+    st = torch.empty(e.n, dtype=torch.int32, device=dev)
+    lib = abi.load()
+    prob = abi.Problem(rhs_id=e.rhs_id, dim=3, n_params=3)
+    bi = abi.BatchIn(n=e.n, t0=abi.ptr(t0), tf=abi.ptr(tf), y0=abi.ptr(y0), params=abi.ptr(p), rtol=abi.ptr(rt),
+                     atol=abi.ptr(at), n_eval=0)
+    bo = abi.BatchOut(y_final=abi.ptr(yf), accepted=abi.ptr(acc, C.c_int64), rejected=abi.ptr(rej, C.c_int64),
+                      fevals=abi.ptr(fe, C.c_int64), status=abi.ptr(st, C.c_int32))
+    s = torch.cuda.Stream()
+    rc = lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), C.c_void_p(s.cuda_stream))
+    assert rc == abi.OK
+    s.synchronize()
+    assert np.array_equal(yf.cpu().numpy(), g.y_final)
+    assert np.array_equal(acc.cpu().numpy(), g.accepted)
+
+
+def test_fast_fp64_accuracy():
+    """FMA-contracted FP64 with the CUDA math library: same method, results differ only by
+    rounding; compared on non-chaotic instances (Van der Pol / pendulum slice) at final time."""
+    e = W.config1(n=3 * 300)
+    keep = e.family != abi.RHS["LORENZ"]
+    e = e.subset(np.nonzero(keep)[0])
+    e.tf = np.minimum(e.tf, 10.0)
+    o = oracle_solve(e, cfg_for(abi.DOPRI5))
+    g = gpu_solve(e, cfg_for(abi.DOPRI5, precision=abi.FP64_FAST))
+    assert np.all(g.status == abi.COMPLETE)
+    err = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.maximum(1.0, np.max(np.abs(o["y_final"]), axis=0))
+    assert np.median(err) < 1e-9
+
+
+def test_mixed_precision_error_vs_oracle():
+    """Mixed form (FP32 stages, Kahan-compensated y, FP64 controller): error against the FP64
+    oracle at tolerances the FP32 stages can meet."""
+    e = W.config1(n=3 * 300)
+    keep = e.family == abi.RHS["VAN_DER_POL"]
+    e = e.subset(np.nonzero(keep)[0])
+    e.tf = np.minimum(e.tf, 10.0)
+    e.rtol[:] = 1e-6
+    e.atol[:] = 1e-8
+    o = oracle_solve(e, cfg_for(abi.DOPRI5))
+    g = gpu_solve(e, cfg_for(abi.DOPRI5, precision=abi.MIXED))
+    assert np.all(g.status == abi.COMPLETE)
+    err = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.maximum(1.0, np.max(np.abs(o["y_final"]), axis=0))
+    assert np.median(err) < 1e-5
