@@ -1,6 +1,5 @@
 #include "wps.cuh"
 namespace degpu {
-degpu_status wps_solve(const degpu_problem*, const degpu_method_cfg*, const EnsArgs&, const int32_t*, cudaStream_t) { return DEGPU_UNSUPPORTED; }
 degpu_status nvrtc_rhs_info(int32_t, int32_t*, int32_t*) { return DEGPU_UNSUPPORTED; }
 degpu_status nvrtc_solve(const degpu_problem*, const degpu_method_cfg*, const degpu_batch_in*, degpu_batch_out*, cudaStream_t) { return DEGPU_UNSUPPORTED; }
 }

@@ -65,7 +65,10 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
                            degpu_batch_out* out, int64_t i, const Math& math) {
     const int64_t n = in->n;
     int rhs = in->family ? in->family[i] : pb->rhs_id;
-    int d = in->dims ? in->dims[i] : pb->dim;
+    // per-instance dimension: given explicitly (ragged batches) or the family's own
+    int fam_dim, fam_np;
+    builtin_info(rhs, fam_dim, fam_np);
+    int d = in->dims ? in->dims[i] : (fam_dim > 0 ? fam_dim : pb->dim);
     int dmax = pb->dim;
     State y0(d);
     for (int c = 0; c < d; ++c) y0[c] = in->y0[(int64_t)c * n + i];

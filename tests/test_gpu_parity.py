@@ -220,3 +220,41 @@ def test_mixed_precision_error_vs_oracle():
     assert np.all(g.status == abi.COMPLETE)
     err = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.maximum(1.0, np.max(np.abs(o["y_final"]), axis=0))
     assert np.median(err) < 1e-5
+
+
+@pytest.mark.parametrize("precision", [abi.FP64_PARITY])
+def test_fpu_chain_group_kernel_parity(precision):
+    """FPU-beta chains of ragged dimension (2..256 components), DOP853 rtol=1e-10 atol=1e-12 with
+    64 dense output times, through the group-per-system kernel; every dimension bucket
+    (8/16/32 lanes per system, 1..8 components per lane) is exercised."""
+    e = W.config2(n=96)
+    # cover each bucket explicitly: masses 2, 4, 8, 16, 30, 64, 100, 128
+    masses = np.array([2, 4, 8, 16, 30, 64, 100, 128] * 12)
+    e.dims = (2 * masses).astype(np.int32)
+    e.tf[:] = 10.0
+    e.t_eval = 10.0 * np.arange(64) / 63.0
+    cfg = cfg_for(abi.DOP853, precision=precision)
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    assert_parity(g, o, dense=True)
+
+
+def test_fpu_chain_dopri5_parity():
+    e = W.config2(n=64)
+    e.tf[:] = 5.0
+    cfg = cfg_for(abi.DOPRI5)
+    o = oracle_solve(e, cfg, t_eval=np.linspace(0.0, 5.0, 9))
+    g = gpu_solve(e, cfg, t_eval=np.linspace(0.0, 5.0, 9))
+    assert_parity(g, o, dense=True)
+
+
+def test_fpu_chain_fast_and_mixed_accuracy():
+    e = W.config2(n=128)
+    e.tf[:] = 10.0
+    e.t_eval = None
+    o = oracle_solve(e, cfg_for(abi.DOP853))
+    for prec, tol in ((abi.FP64_FAST, 1e-8), (abi.MIXED, 1e-4)):
+        g = gpu_solve(e, cfg_for(abi.DOP853, precision=prec))
+        assert np.all(g.status == abi.COMPLETE)
+        err = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.max(np.abs(o["y_final"]), axis=0)
+        assert np.median(err) < tol, (prec, np.median(err))
