@@ -25,8 +25,10 @@
 // without FMA contraction on the parity path, so host and device builds agree.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <math.h>
 #include <stdint.h>
+#endif
 
 #if defined(__CUDACC__)
 #define DD_HD __host__ __device__ __forceinline__

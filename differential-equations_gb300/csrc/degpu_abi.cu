@@ -26,6 +26,10 @@ std::map<VariantKey, EnsLaunchFn>& ens_registry() {
     static std::map<VariantKey, EnsLaunchFn> m;
     return m;
 }
+std::map<VariantKey, RoundOps>& round_registry() {
+    static std::map<VariantKey, RoundOps> m;
+    return m;
+}
 std::map<std::pair<int, int>, RhsLaunchFn>& rhs_registry() {
     static std::map<std::pair<int, int>, RhsLaunchFn> m;
     return m;
@@ -38,13 +42,15 @@ int device_sm_count() {
     return sms > 0 ? sms : 1;
 }
 
-static void ensure_registered() {
+void ensure_registered() {
     static std::once_flag once;
     std::call_once(once, []() {
         register_parity_main();
         register_parity_tests();
         register_fast();
         register_mixed();
+        register_parity_multi();
+        register_multi_fast_mixed();
     });
 }
 
@@ -156,6 +162,41 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
     // ragged (per-instance dimension) problems go to the warp-per-system kernel
     if (pb->rhs_id == DEGPU_RHS_FPU_BETA) {
         return wps_solve(pb, cfg, a, in->dims, s);
+    }
+
+    int kernel_sel = cfg->kernel;
+    if (kernel_sel == DEGPU_KERNEL_AUTO)
+        kernel_sel = (cfg->method != DEGPU_RK4 && n >= 32768) ? DEGPU_KERNEL_PERSISTENT : DEGPU_KERNEL_THREAD;
+
+    // persistent solves of the production families (Van der Pol, pendulum, Lorenz): one
+    // multi-family launch over longest-first work lists
+    if (kernel_sel == DEGPU_KERNEL_PERSISTENT) {
+        auto prod = [](int id) {
+            return id == DEGPU_RHS_VAN_DER_POL || id == DEGPU_RHS_PENDULUM || id == DEGPU_RHS_LORENZ;
+        };
+        bool seen[3] = {false, false, false};
+        bool ok = true;
+        auto note = [&](int id) {
+            if (!prod(id)) ok = false;
+            else seen[id == DEGPU_RHS_VAN_DER_POL ? 0 : id == DEGPU_RHS_PENDULUM ? 1 : 2] = true;
+        };
+        if (family_host) {
+            for (int64_t i = 0; i < n && ok; ++i) note(family_host[i]);
+        } else {
+            note(pb->rhs_id);
+        }
+        const int ids[3] = {DEGPU_RHS_VAN_DER_POL, DEGPU_RHS_PENDULUM, DEGPU_RHS_LORENZ};
+        for (int f = 0; f < 3 && ok; ++f) {
+            if (!seen[f]) continue;
+            int dim, np;
+            builtin_info(ids[f], dim, np);
+            if (dim > pb->dim || np > pb->n_params) return DEGPU_BAD_INPUT;
+        }
+        if (ok) {
+            EnsArgs ma = a;
+            ma.count = n;
+            return multi_solve(cfg, ma, family_host ? in->family : nullptr, pb->rhs_id, dense, s);
+        }
     }
 
     // work lists per family

@@ -23,7 +23,9 @@
 // counters equal the crate's.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <stdint.h>
+#endif
 
 #include "rhs.cuh"
 #include "tableau.cuh"
@@ -91,10 +93,17 @@ struct Lane {
     __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const { Rhs::template diff<P>(tt, yy, dd, p); }
 
     __device__ __forceinline__ double norm_term(S e, S yv, S ynv) const {
-        // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407), in FP64
-        double sk = atol + rtol * fmax(fabs((double)yv), fabs((double)ynv));
-        double q = (double)e / sk;
-        return q * q;
+        // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
+        if constexpr (P::KAHAN) {
+            // mixed: the quotient of FP32 stage data in FP32, accumulated by the caller in FP64
+            float sk = (float)atol + (float)rtol * fmaxf(fabsf(yv), fabsf(ynv));
+            float q = __fdividef(e, sk);
+            return (double)(q * q);
+        } else {
+            double sk = atol + rtol * fmax(fabs((double)yv), fabs((double)ynv));
+            double q = (double)e / sk;
+            return q * q;
+        }
     }
 
     // ----- h_init: src/methods/h_init.rs:45-136 --------------------------------------------
@@ -388,11 +397,20 @@ struct Lane {
         }
         double deno = Tab::HAS_BH ? err + 0.01 * err2 : err;
         if (deno <= 0.0) deno = 1.0;
-        err = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
-
-        double error_exponent = 1.0 / (double)O;
-        double scale = a.safety * P::pow(err, -error_exponent);
-        scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+        double scale;
+        if constexpr (P::KAHAN) {
+            // mixed: the normalisation and the controller's power in FP32; the decision err <= 1,
+            // h and t stay FP64
+            float ef = (float)err * sqrtf(1.0f / ((float)deno * (float)D));
+            err = fabs(h) * (double)ef;
+            float pw = exp2f(__log2f((float)err) * (float)(-1.0 / (double)O));
+            scale = (double)fminf(fmaxf((float)a.safety * pw, (float)a.min_scale), (float)a.max_scale);
+        } else {
+            err = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
+            double error_exponent = 1.0 / (double)O;
+            scale = a.safety * P::pow(err, -error_exponent);
+            scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+        }
 
         int result;
         if (err <= 1.0) {
@@ -617,6 +635,142 @@ struct Lane {
         if (a.status) a.status[inst] = status;
     }
 };
+
+// ---------------------------------------------------------------------------------------------
+// Multi-family persistent kernel with longest-first work lists.
+//
+// The host-side plan (plan kernels in degpu_abi.cu) sorts every instance into the work list of
+// its family, in descending order of estimated cost |tf - t0| * rtol^(-1/order), so that the
+// longest solves start first and the end of each list holds the shortest ones.  Each warp works
+// on one family at a time (the family switch is warp-uniform, so it costs no divergence); a lane
+// whose instance finishes takes the next item of that family's list; when the list is empty and
+// every lane of the warp is idle, the warp moves to another family that still has work.
+// ---------------------------------------------------------------------------------------------
+struct MultiQueue {
+    const int64_t* items;         // work lists of the three families, concatenated
+    const int64_t* start;         // [3] first item of each family's list
+    const int64_t* count;         // [3] length of each family's list
+    unsigned long long* head;     // [3] per-family list heads
+};
+
+template <class Tab, class P, bool DENSE, class R0, class R1, class R2>
+struct MultiLane {
+    union {
+        Lane<Tab, R0, P, DENSE> l0;
+        Lane<Tab, R1, P, DENSE> l1;
+        Lane<Tab, R2, P, DENSE> l2;
+    };
+    __device__ MultiLane() {}
+};
+
+template <class Tab, class P, bool DENSE, class R0, class R1, class R2>
+__global__ void __launch_bounds__(128) erk_multi_kernel(EnsArgs a, MultiQueue q) {
+    MultiLane<Tab, P, DENSE, R0, R1, R2> M;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    const int64_t cnt[3] = {q.count[0], q.count[1], q.count[2]};
+    const int64_t st[3] = {q.start[0], q.start[1], q.start[2]};
+    // initial family: warps split in proportion to the list lengths
+    int64_t total = cnt[0] + cnt[1] + cnt[2];
+    int fam = 0;
+    {
+        int64_t pos = total > 0 ? (int64_t)warp * total / (nwarps > 0 ? nwarps : 1) : 0;
+        fam = pos < cnt[0] ? 0 : (pos < cnt[0] + cnt[1] ? 1 : 2);
+    }
+    bool active = false, exhausted = false;
+    for (;;) {
+        if (!active && !exhausted) {
+            unsigned long long w = atomicAdd(&q.head[fam], 1ULL);
+            if (w < (unsigned long long)cnt[fam]) {
+                int64_t inst = q.items[st[fam] + (int64_t)w];
+                if (fam == 0) {
+                    M.l0.begin(inst, a);
+                    if (M.l0.done) M.l0.finish(a); else active = true;
+                } else if (fam == 1) {
+                    M.l1.begin(inst, a);
+                    if (M.l1.done) M.l1.finish(a); else active = true;
+                } else {
+                    M.l2.begin(inst, a);
+                    if (M.l2.done) M.l2.finish(a); else active = true;
+                }
+            } else {
+                exhausted = true;
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) {
+            if (!__any_sync(0xffffffffu, !exhausted)) {
+                // the whole warp is idle and its list is empty: find a family with work left
+                int nf = -1;
+                if ((threadIdx.x & 31) == 0) {
+                    for (int f = 0; f < 3; ++f) {
+                        int g = (fam + 1 + f) % 3;
+                        if (atomicAdd(&q.head[g], 0ULL) < (unsigned long long)cnt[g]) {
+                            nf = g;
+                            break;
+                        }
+                    }
+                }
+                nf = __shfl_sync(0xffffffffu, nf, 0);
+                if (nf < 0) break;
+                fam = nf;
+                exhausted = false;
+            }
+            continue;
+        }
+        if (active) {
+            if (fam == 0) {
+                M.l0.iterate(a);
+                if (M.l0.done) { M.l0.finish(a); active = false; }
+            } else if (fam == 1) {
+                M.l1.iterate(a);
+                if (M.l1.done) { M.l1.finish(a); active = false; }
+            } else {
+                M.l2.iterate(a);
+                if (M.l2.done) { M.l2.finish(a); active = false; }
+            }
+        }
+    }
+}
+
+// Resident per-instance solver state of the serving path: a Lane parked between rounds.
+// `phase`: 0 not started, 1 in progress, 2 finished.
+template <class LaneT>
+struct Parked {
+    int32_t phase;
+    int32_t pad;
+    LaneT lane;
+};
+
+// Resumable persistent form used by the server: every instance is visited once per round; a
+// visit resumes the parked state (or starts the instance), advances it by at most `budget`
+// driver iterations, then parks it again or finishes it.  `done_count` counts finished
+// instances across rounds.
+template <class Tab, class Rhs, class P, bool DENSE>
+__global__ void __launch_bounds__(128) erk_round_kernel(EnsArgs a, Parked<Lane<Tab, Rhs, P, DENSE>>* park,
+                                                        int budget, unsigned long long* done_count) {
+    for (;;) {
+        unsigned long long w = atomicAdd(a.ticket, 1ULL);
+        if (w >= (unsigned long long)a.count) break;
+        Parked<Lane<Tab, Rhs, P, DENSE>>& slot = park[w];
+        int phase = slot.phase;
+        if (phase == 2) continue;
+        Lane<Tab, Rhs, P, DENSE> L;
+        if (phase == 0) {
+            L.begin((int64_t)w, a);
+        } else {
+            L = slot.lane;
+        }
+        for (int it = 0; it < budget && !L.done; ++it) L.iterate(a);
+        if (L.done) {
+            L.finish(a);
+            slot.phase = 2;
+            atomicAdd(done_count, 1ULL);
+        } else {
+            slot.lane = L;
+            slot.phase = 1;
+        }
+    }
+}
 
 // One instance per thread, run to completion.
 template <class Tab, class Rhs, class P, bool DENSE>

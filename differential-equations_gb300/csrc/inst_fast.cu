@@ -12,6 +12,9 @@ void register_fast() {
     register_variant<TabRK4, RhsLorenz, PrecFast>();
     register_variant<TabRK4, RhsVanDerPol, PrecFast>();
     register_variant<TabRK4, RhsPendulum, PrecFast>();
+    register_round_all_methods<RhsLorenz, PrecFast>();
+    register_round_all_methods<RhsVanDerPol, PrecFast>();
+    register_round_all_methods<RhsPendulum, PrecFast>();
     register_rhs<RhsLorenz, PrecFast>();
     register_rhs<RhsVanDerPol, PrecFast>();
     register_rhs<RhsPendulum, PrecFast>();

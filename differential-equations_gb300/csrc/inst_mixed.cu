@@ -12,6 +12,9 @@ void register_mixed() {
     register_variant<TabRK4, RhsLorenz, PrecMixed>();
     register_variant<TabRK4, RhsVanDerPol, PrecMixed>();
     register_variant<TabRK4, RhsPendulum, PrecMixed>();
+    register_round_all_methods<RhsLorenz, PrecMixed>();
+    register_round_all_methods<RhsVanDerPol, PrecMixed>();
+    register_round_all_methods<RhsPendulum, PrecMixed>();
     register_rhs<RhsLorenz, PrecMixed>();
     register_rhs<RhsVanDerPol, PrecMixed>();
     register_rhs<RhsPendulum, PrecMixed>();

@@ -17,6 +17,9 @@ void register_parity_main() {
     register_variant<TabRK4, RhsLorenz, PrecParity>();
     register_variant<TabRK4, RhsVanDerPol, PrecParity>();
     register_variant<TabRK4, RhsPendulum, PrecParity>();
+    register_round_all_methods<RhsLorenz, PrecParity>();
+    register_round_all_methods<RhsVanDerPol, PrecParity>();
+    register_round_all_methods<RhsPendulum, PrecParity>();
     register_rhs<RhsLorenz, PrecParity>();
     register_rhs<RhsVanDerPol, PrecParity>();
     register_rhs<RhsPendulum, PrecParity>();

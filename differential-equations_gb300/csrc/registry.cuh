@@ -60,11 +60,86 @@ void register_variant() {
     ens_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 1}] = &launch_ens<Tab, Rhs, P, true>;
 }
 
+// Resumable round kernels of the serving path (no dense output).
+struct RoundOps {
+    size_t park_bytes;  // resident state per instance
+    cudaError_t (*launch)(const EnsArgs& a, void* park, int budget, unsigned long long* done, int max_blocks,
+                          cudaStream_t s);
+};
+std::map<VariantKey, RoundOps>& round_registry();
+
+template <class Tab, class Rhs, class P>
+cudaError_t launch_round(const EnsArgs& a, void* park, int budget, unsigned long long* done, int max_blocks,
+                         cudaStream_t s) {
+    using L = Lane<Tab, Rhs, P, false>;
+    if (a.count <= 0) return cudaSuccess;
+    static int blocks_per_sm = -1;
+    if (blocks_per_sm < 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm,
+                                                                      erk_round_kernel<Tab, Rhs, P, false>, 128, 0);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    long long grid = (long long)blocks_per_sm * device_sm_count();
+    long long need = (a.count + 127) / 128;
+    if (grid > need) grid = need;
+    if (max_blocks > 0 && grid > max_blocks) grid = max_blocks;
+    erk_round_kernel<Tab, Rhs, P, false><<<(unsigned)grid, 128, 0, s>>>(a, (Parked<L>*)park, budget, done);
+    return cudaGetLastError();
+}
+
+template <class Tab, class Rhs, class P>
+void register_round() {
+    round_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 0}] =
+        RoundOps{sizeof(Parked<Lane<Tab, Rhs, P, false>>), &launch_round<Tab, Rhs, P>};
+}
+
+template <class Rhs, class P>
+void register_round_all_methods() {
+    register_round<TabRK4, Rhs, P>();
+    register_round<TabDopri5, Rhs, P>();
+    register_round<TabDop853, Rhs, P>();
+}
+
+// Multi-family persistent kernels: families Van der Pol (slot 0), pendulum (1), Lorenz (2).
+using MultiLaunchFn = cudaError_t (*)(const EnsArgs& a, const MultiQueue& q, int64_t total, cudaStream_t s);
+std::map<std::tuple<int, int, int>, MultiLaunchFn>& multi_registry();
+
+template <class Tab, class P, bool DENSE>
+cudaError_t launch_multi(const EnsArgs& a, const MultiQueue& q, int64_t total, cudaStream_t s) {
+    auto kern = erk_multi_kernel<Tab, P, DENSE, RhsVanDerPol, RhsPendulum, RhsLorenz>;
+    static int blocks_per_sm = -1;
+    if (blocks_per_sm < 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, 128, 0);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    long long grid = (long long)blocks_per_sm * device_sm_count();
+    long long need = (total + 127) / 128;
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    kern<<<(unsigned)grid, 128, 0, s>>>(a, q);
+    return cudaGetLastError();
+}
+
+template <class Tab, class P>
+void register_multi() {
+    multi_registry()[{method_id<Tab>(), P::ID, 0}] = &launch_multi<Tab, P, false>;
+    multi_registry()[{method_id<Tab>(), P::ID, 1}] = &launch_multi<Tab, P, true>;
+}
+
 // Per-translation-unit registration hooks (called once by the ABI).
 void register_parity_main();
 void register_parity_tests();
 void register_fast();
 void register_mixed();
+void register_parity_multi();
+void register_multi_fast_mixed();
+void ensure_registered();
+
+// Longest-first planning + one multi-family persistent launch (plan.cu).
+degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
+                         bool dense, cudaStream_t s);
 
 // Right-hand-side evaluation kernels (degpu_eval_rhs)
 using RhsLaunchFn = cudaError_t (*)(int64_t n, const double* t, const double* y, const double* p, double* dydt,

@@ -27,8 +27,10 @@
 #ifndef DEGPU_H
 #define DEGPU_H
 
+#if !defined(__CUDACC_RTC__)
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {

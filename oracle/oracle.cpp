@@ -103,7 +103,8 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
     if (out->dense && tep) {
         for (int e = 0; e < in->n_eval; ++e)
             for (int c = 0; c < dmax; ++c) {
-                double v = (c < d && (size_t)e < r.dense.size()) ? r.dense[e][c] : (c < d ? NAN : 0.0);
+                // rows beyond the instance's dimension are never written: they keep the NaN fill
+                double v = (c < d && (size_t)e < r.dense.size()) ? r.dense[e][c] : NAN;
                 out->dense[((int64_t)e * dmax + c) * n + i] = v;
             }
     }
