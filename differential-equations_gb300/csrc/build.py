@@ -72,7 +72,7 @@ def build(jobs=None, verbose=False):
     with cf.ThreadPoolExecutor(jobs) as ex:
         objs = [f.result()[0] for f in [ex.submit(compile_one, s, verbose) for s in srcs]]
     if not os.path.exists(OUT) or any(os.path.getmtime(o) > os.path.getmtime(OUT) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart", "-lnvrtc", "-lcuda"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart", "-lnvrtc"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -6,7 +6,7 @@
 // system's fields in p[0..n_params).  Registration compiles the integrator headers plus that
 // source with NVRTC for this GPU twice — once with -fmad=false (the parity variants) and once
 // with contraction (FP64_FAST / MIXED) — and loads the kernels through the driver API.
-#include <cuda.h>
+
 #include <cuda_runtime.h>
 #include <dlfcn.h>
 #include <nvrtc.h>
@@ -27,9 +27,9 @@ namespace degpu {
 
 struct NvrtcRhs {
     int dim, n_params;
-    CUmodule mod[2] = {nullptr, nullptr};  // [0] parity build, [1] contracted build
+    cudaLibrary_t mod[2] = {nullptr, nullptr};  // [0] parity build, [1] contracted build
     // [method][prec][dense][kernel: 0 thread, 1 persistent]
-    CUfunction fn[3][3][2][2] = {};
+    cudaKernel_t fn[3][3][2][2] = {};
 };
 
 static std::mutex g_mu;
@@ -92,8 +92,8 @@ static degpu_status compile_module(const std::string& src, bool parity, NvrtcRhs
     nvrtcGetCUBINSize(prog, &cs);
     std::vector<char> cubin(cs);
     nvrtcGetCUBIN(prog, cubin.data());
-    CUmodule mod;
-    if (cuModuleLoadData(&mod, cubin.data()) != CUDA_SUCCESS) {
+    cudaLibrary_t mod;
+    if (cudaLibraryLoadData(&mod, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess) {
         nvrtcDestroyProgram(&prog);
         return DEGPU_CUDA_ERROR;
     }
@@ -106,7 +106,7 @@ static degpu_status compile_module(const std::string& src, bool parity, NvrtcRhs
                     std::string nm = kernel_name(m, p, d, k);
                     const char* lowered = nullptr;
                     if (nvrtcGetLoweredName(prog, nm.c_str(), &lowered) != NVRTC_SUCCESS ||
-                        cuModuleGetFunction(&r->fn[m][p][d][k], mod, lowered) != CUDA_SUCCESS) {
+                        cudaLibraryGetKernel(&r->fn[m][p][d][k], mod, lowered) != cudaSuccess) {
                         nvrtcDestroyProgram(&prog);
                         return DEGPU_CUDA_ERROR;
                     }
@@ -163,7 +163,7 @@ degpu_status nvrtc_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     a.n_params = pb->n_params;
     if (in->n_eval > 0) return DEGPU_UNSUPPORTED;  // dense output for run-time systems: not built
     const int persistent = cfg->kernel == DEGPU_KERNEL_PERSISTENT ? 1 : 0;
-    CUfunction f = r->fn[cfg->method][cfg->precision][0][persistent];
+    cudaKernel_t f = r->fn[cfg->method][cfg->precision][0][persistent];
     if (!f) return DEGPU_UNSUPPORTED;
     unsigned long long* tk = nullptr;
     if (persistent) {
@@ -175,16 +175,16 @@ degpu_status nvrtc_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     unsigned grid;
     if (persistent) {
         int bps = 0;
-        cuOccupancyMaxActiveBlocksPerMultiprocessor(&bps, f, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)f, 128, 0);
         long long g = (long long)(bps > 0 ? bps : 1) * device_sm_count();
         long long need = (n + 127) / 128;
         grid = (unsigned)(g < need ? g : need);
     } else {
         grid = (unsigned)((n + 127) / 128);
     }
-    CUresult cr = cuLaunchKernel(f, grid, 1, 1, 128, 1, 1, 0, (CUstream)s, args, nullptr);
+    cudaError_t cr = cudaLaunchKernel((const void*)f, dim3(grid), dim3(128), args, 0, s);
     if (tk) cudaFreeAsync(tk, s);
-    return cr == CUDA_SUCCESS ? DEGPU_OK : DEGPU_CUDA_ERROR;
+    return cr == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
 }
 
 }  // namespace degpu
@@ -215,8 +215,8 @@ extern "C" degpu_status degpu_register_rhs_nvrtc(const char* source, const char*
         log[k] = 0;
     }
     if (st != DEGPU_OK) {
-        for (CUmodule m : r->mod)
-            if (m) cuModuleUnload(m);
+        for (cudaLibrary_t m : r->mod)
+            if (m) cudaLibraryUnload(m);
         delete r;
         return st;
     }
