@@ -68,6 +68,10 @@ class GrayScott(C.Structure):
                 ("Dv", C.c_double), ("F", C.c_double), ("k", C.c_double)]
 
 
+class ServerCfg(C.Structure):
+    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_active", C.c_int32), ("round_budget", C.c_int32)]
+
+
 def default_cfg(method: int) -> MethodCfg:
     """The crate's defaults (src/methods/erk/mod.rs:112-159)."""
     return MethodCfg(method=method, precision=FP64_PARITY, kernel=KERNEL_AUTO, dense_mode=DENSE_REFERENCE,
@@ -92,6 +96,12 @@ SIGNATURES = {
     "degpu_gray_scott_rk4": (C.c_int, [C.POINTER(GrayScott), C.c_int32, C.c_double, C.c_double, C.c_int64,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
     "degpu_gray_scott_rhs": (C.c_int, [C.POINTER(GrayScott), DP, DP, DP, DP, C.c_void_p]),
+    "degpu_server_create": (C.c_int, [C.POINTER(ServerCfg), C.POINTER(C.c_void_p)]),
+    "degpu_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                      C.POINTER(BatchOut), C.POINTER(C.c_uint64)]),
+    "degpu_server_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "degpu_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
+    "degpu_server_destroy": (C.c_int, [C.c_void_p]),
     "degpu_status_string": (C.c_char_p, [C.c_int]),
     "degpu_version": (C.c_char_p, []),
 }

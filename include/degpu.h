@@ -30,6 +30,12 @@
 #if !defined(__CUDACC_RTC__)
 #include <stddef.h>
 #include <stdint.h>
+#else
+/* run-time compilation (NVRTC) has no C library headers */
+typedef int int32_t;
+typedef long long int64_t;
+typedef unsigned int uint32_t;
+typedef unsigned long long uint64_t;
 #endif
 
 #ifdef __cplusplus
@@ -200,6 +206,43 @@ degpu_status degpu_gray_scott_rk4(const degpu_gray_scott* gs, int32_t precision,
 /* One right-hand-side evaluation of the same semi-discretisation (u, v -> du, dv), FP64. */
 degpu_status degpu_gray_scott_rhs(const degpu_gray_scott* gs, const double* u, const double* v,
                                   double* du, double* dv, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Serving: continuous batching of ensemble solves.
+ *
+ * The crate solves one IVP per call, synchronously (src/ivp.rs:781-791); a server built on it
+ * would queue whole solves.  Here requests (each an ensemble, as degpu_solve_ensemble_host takes
+ * it) are admitted as device memory frees up, under a memory budget, in arrival order; every
+ * admitted request keeps its instances' solver state (t, h, y, derivative, counters, controller
+ * state) resident on the device and advances in bounded rounds of a persistent kernel on its own
+ * stream, so requests that arrive while others run join at the next round and their work overlaps
+ * on the GPU.  A request's results do not depend on what else is in flight.
+ * --------------------------------------------------------------------------------------------- */
+typedef struct degpu_server degpu_server;
+
+typedef struct {
+    uint64_t memory_budget_bytes;  /* device memory admitted requests may hold (0 = 150 GB)          */
+    int32_t max_active;            /* requests resident at once (0 = 64)                             */
+    int32_t round_budget;          /* driver iterations per instance per round (0 = 512)             */
+} degpu_server_cfg;
+
+/* Start a server (a scheduler thread on the current device). */
+degpu_status degpu_server_create(const degpu_server_cfg* cfg, degpu_server** server);
+
+/* Queue a request.  `in` and `out` are HOST pointers that must stay valid until the request is
+ * done; the call copies nothing yet and returns at once with the request's id. */
+degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                 const degpu_batch_in* in, degpu_batch_out* out, uint64_t* request_id);
+
+/* Non-blocking: *done = 1 once the outputs are in `out`; *latency_ms = submit-to-done time.
+ * The return value is the request's own status (DEGPU_OK, or why it failed) once done. */
+degpu_status degpu_server_poll(degpu_server* server, uint64_t request_id, int32_t* done, double* latency_ms);
+
+/* Block until the request is done. */
+degpu_status degpu_server_wait(degpu_server* server, uint64_t request_id, double* latency_ms);
+
+/* Drain every queued and running request, stop the scheduler and release the device memory. */
+degpu_status degpu_server_destroy(degpu_server* server);
 
 /* Human-readable message for a status. */
 const char* degpu_status_string(degpu_status s);

@@ -1,0 +1,204 @@
+// degpu.hpp — C++17 host API over the C ABI (degpu.h), with the crate's builder shape.
+//
+//   auto m   = degpu::ExplicitRungeKutta::dopri5().rtol(1e-8).atol(1e-10);   // src/methods/erk/mod.rs:165-174
+//   auto sol = degpu::IVP::ode(degpu::System::lorenz(10, 28, 8.0 / 3), 0.0, 20.0, {1, 1, 1})  // src/ivp.rs:279
+//                  .method(m)                                                 // src/ivp.rs:632
+//                  .t_eval({0.5, 1.0})                                        // src/ivp.rs:656-660
+//                  .solve();                                                  // src/ivp.rs:781-791
+//   if (sol.ok()) ... sol.value().y.back() ... else sol.error().kind == degpu::ErrorKind::MaxSteps
+//
+// and solve_ensemble() for n instances in one call.  Errors are values, as in the crate
+// (`Result<Solution, Error>`, src/error.rs:13-40): BadInput carries a message starting with
+// "Invalid input"; MaxSteps / StepSize / Stiffness carry the (t, y) where the solve stopped.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "degpu.h"
+
+namespace degpu {
+
+enum class ErrorKind { BadInput, MaxSteps, StepSize, Stiffness, Device };
+
+struct Error {
+    ErrorKind kind;
+    std::string msg;
+    double t = 0.0;
+    std::vector<double> y;
+};
+
+// Solution fields the GPU produces (src/solution.rs:30-52, src/stats.rs).
+struct Solution {
+    std::vector<double> t;
+    std::vector<std::vector<double>> y;
+    std::size_t evals = 0;      // Evals.function
+    std::size_t accepted = 0;   // Steps.accepted
+    std::size_t rejected = 0;   // Steps.rejected
+};
+
+template <class T>
+class Result {
+   public:
+    static Result ok_value(T v) { Result r; r.ok_ = true; r.v_ = std::move(v); return r; }
+    static Result err(Error e) { Result r; r.ok_ = false; r.e_ = std::move(e); return r; }
+    bool ok() const { return ok_; }
+    const T& value() const { if (!ok_) throw std::runtime_error(e_.msg); return v_; }
+    const Error& error() const { return e_; }
+   private:
+    bool ok_ = false;
+    T v_{};
+    Error e_{};
+};
+
+class ExplicitRungeKutta {
+   public:
+    static ExplicitRungeKutta rk4(double h0) { ExplicitRungeKutta m(DEGPU_RK4); m.cfg_.h0 = h0; return m; }
+    static ExplicitRungeKutta dopri5() { return ExplicitRungeKutta(DEGPU_DOPRI5); }
+    static ExplicitRungeKutta dop853() { return ExplicitRungeKutta(DEGPU_DOP853); }
+    ExplicitRungeKutta& rtol(double v) { rtol_ = v; return *this; }
+    ExplicitRungeKutta& atol(double v) { atol_ = v; return *this; }
+    ExplicitRungeKutta& h0(double v) { cfg_.h0 = v; return *this; }
+    ExplicitRungeKutta& h_min(double v) { cfg_.h_min = v; return *this; }
+    ExplicitRungeKutta& h_max(double v) { cfg_.h_max = v; return *this; }
+    ExplicitRungeKutta& max_steps(int64_t v) { cfg_.max_steps = v; return *this; }
+    ExplicitRungeKutta& safety_factor(double v) { cfg_.safety_factor = v; return *this; }
+    ExplicitRungeKutta& min_scale(double v) { cfg_.min_scale = v; return *this; }
+    ExplicitRungeKutta& max_scale(double v) { cfg_.max_scale = v; return *this; }
+    // GPU knobs
+    ExplicitRungeKutta& precision(degpu_precision p) { cfg_.precision = p; return *this; }
+    ExplicitRungeKutta& kernel(degpu_kernel k) { cfg_.kernel = k; return *this; }
+    const degpu_method_cfg& cfg() const { return cfg_; }
+    double rtol() const { return rtol_; }
+    double atol() const { return atol_; }
+
+   private:
+    explicit ExplicitRungeKutta(int method) { degpu_default_cfg(&cfg_, method); }
+    degpu_method_cfg cfg_{};
+    double rtol_ = 1e-6, atol_ = 1e-6;  // src/methods/erk/mod.rs:135-136
+};
+
+// A right-hand side with a device twin: a built-in family or an id from degpu_register_rhs_nvrtc.
+struct System {
+    int32_t rhs_id;
+    std::vector<double> params;
+    static System lorenz(double sigma, double rho, double beta) { return {DEGPU_RHS_LORENZ, {sigma, rho, beta}}; }
+    static System van_der_pol(double mu) { return {DEGPU_RHS_VAN_DER_POL, {mu}}; }
+    static System pendulum(double gamma, double a, double omega) { return {DEGPU_RHS_PENDULUM, {gamma, a, omega}}; }
+    static System exponential_growth(double k) { return {DEGPU_RHS_EXP_GROWTH, {k}}; }
+    static System harmonic(double k) { return {DEGPU_RHS_HARMONIC, {k}}; }
+    static System fpu_beta(double beta) { return {DEGPU_RHS_FPU_BETA, {beta}}; }
+};
+
+// Results of an ensemble solve, structure of arrays (layout of degpu.h).
+struct EnsembleResult {
+    int64_t n = 0;
+    int32_t dim = 0;
+    std::vector<double> y_final, t_final, dense;
+    std::vector<int64_t> accepted, rejected, fevals;
+    std::vector<int32_t> status;
+};
+
+inline EnsembleResult solve_ensemble(int32_t rhs_id, int32_t dim, int32_t n_params, const std::vector<double>& t0,
+                                     const std::vector<double>& tf, const std::vector<double>& y0,
+                                     const std::vector<double>& params, const std::vector<double>& rtol,
+                                     const std::vector<double>& atol, const ExplicitRungeKutta& m,
+                                     const std::vector<double>& t_eval = {},
+                                     const std::vector<int32_t>& dims = {}) {
+    EnsembleResult r;
+    r.n = (int64_t)t0.size();
+    r.dim = dim;
+    const size_t n = (size_t)r.n;
+    r.y_final.resize((size_t)dim * n);
+    r.t_final.resize(n);
+    r.dense.resize(t_eval.size() * (size_t)dim * n);
+    r.accepted.resize(n);
+    r.rejected.resize(n);
+    r.fevals.resize(n);
+    r.status.resize(n);
+    degpu_problem pb{rhs_id, dim, n_params, 0};
+    degpu_batch_in in{};
+    in.n = r.n;
+    in.t0 = t0.data();
+    in.tf = tf.data();
+    in.y0 = y0.data();
+    in.params = params.empty() ? nullptr : params.data();
+    in.rtol = rtol.data();
+    in.atol = atol.data();
+    in.dims = dims.empty() ? nullptr : dims.data();
+    in.t_eval = t_eval.empty() ? nullptr : t_eval.data();
+    in.n_eval = (int32_t)t_eval.size();
+    degpu_batch_out out{r.y_final.data(), r.t_final.data(), t_eval.empty() ? nullptr : r.dense.data(),
+                        r.accepted.data(), r.rejected.data(), r.fevals.data(), r.status.data()};
+    degpu_status st = degpu_solve_ensemble_host(&pb, &m.cfg(), &in, &out);
+    if (st != DEGPU_OK) throw std::runtime_error(std::string("degpu_solve_ensemble_host: ") + degpu_status_string(st));
+    return r;
+}
+
+class IVP {
+   public:
+    static IVP ode(System sys, double t0, double tf, std::vector<double> y0) {
+        IVP p;
+        p.sys_ = std::move(sys);
+        p.t0_ = t0;
+        p.tf_ = tf;
+        p.y0_ = std::move(y0);
+        return p;
+    }
+    IVP& method(const ExplicitRungeKutta& m) { m_ = m; return *this; }
+    IVP& t_eval(std::vector<double> pts) { te_ = std::move(pts); return *this; }
+
+    Result<Solution> solve() const {
+        const int32_t d = (int32_t)y0_.size();
+        EnsembleResult r;
+        try {
+            r = solve_ensemble(sys_.rhs_id, d, (int32_t)sys_.params.size(), {t0_}, {tf_}, y0_, sys_.params,
+                               {m_.rtol()}, {m_.atol()}, m_, te_,
+                               sys_.rhs_id == DEGPU_RHS_FPU_BETA ? std::vector<int32_t>{d} : std::vector<int32_t>{});
+        } catch (const std::exception& ex) {
+            return Result<Solution>::err(Error{ErrorKind::Device, ex.what()});
+        }
+        std::vector<double> yf(r.y_final.begin(), r.y_final.begin() + d);
+        switch (r.status[0]) {
+            case DEGPU_ERR_BAD_INPUT:
+                return Result<Solution>::err(Error{ErrorKind::BadInput, "Invalid input: step size or interval"});
+            case DEGPU_ERR_MAX_STEPS: return Result<Solution>::err(Error{ErrorKind::MaxSteps, "MaxSteps", r.t_final[0], yf});
+            case DEGPU_ERR_STEP_SIZE: return Result<Solution>::err(Error{ErrorKind::StepSize, "StepSize", r.t_final[0], yf});
+            case DEGPU_ERR_STIFFNESS: return Result<Solution>::err(Error{ErrorKind::Stiffness, "Stiffness", r.t_final[0], yf});
+            default: break;
+        }
+        Solution s;
+        s.evals = (size_t)r.fevals[0];
+        s.accepted = (size_t)r.accepted[0];
+        s.rejected = (size_t)r.rejected[0];
+        if (te_.empty()) {
+            s.t.push_back(r.t_final[0]);
+            s.y.push_back(yf);
+        } else {
+            // requested points in integration order (TEvalSolout sorts by direction)
+            std::vector<size_t> idx(te_.size());
+            for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+            const bool fwd = tf_ >= t0_;
+            std::stable_sort(idx.begin(), idx.end(),
+                             [&](size_t a, size_t b) { return fwd ? te_[a] < te_[b] : te_[a] > te_[b]; });
+            for (size_t e : idx) {
+                if (std::isnan(r.dense[e * (size_t)d])) continue;
+                s.t.push_back(te_[e]);
+                s.y.emplace_back(r.dense.begin() + e * d, r.dense.begin() + (e + 1) * d);
+            }
+        }
+        return Result<Solution>::ok_value(std::move(s));
+    }
+
+   private:
+    System sys_{};
+    double t0_ = 0, tf_ = 0;
+    std::vector<double> y0_, te_;
+    ExplicitRungeKutta m_ = ExplicitRungeKutta::dopri5();
+};
+
+}  // namespace degpu

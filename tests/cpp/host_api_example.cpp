@@ -1,0 +1,35 @@
+// C++ host API (include/degpu.hpp) used the way the crate's tests use the crate:
+// exp growth to t=10 with DOP853 rtol=atol=1e-12 (tests/ode/accuracy.rs:70-79) and a t_eval
+// interpolation (tests/ode/interpolation.rs:14-87), plus an ensemble call.  Prints "ok" or fails.
+#include <cmath>
+#include <cstdio>
+
+#include "degpu.hpp"
+
+int main() {
+    using namespace degpu;
+    auto sol = IVP::ode(System::exponential_growth(1.0), 0.0, 10.0, {1.0})
+                   .method(ExplicitRungeKutta::dop853().rtol(1e-12).atol(1e-12))
+                   .solve();
+    if (!sol.ok()) { std::printf("solve failed: %s\n", sol.error().msg.c_str()); return 1; }
+    double y = sol.value().y.back()[0];
+    if (std::fabs(y - 22026.46579479) >= 1e-3) { std::printf("accuracy %f\n", y); return 2; }
+    auto s2 = IVP::ode(System::exponential_growth(1.0), 0.0, 2.0, {1.0})
+                  .method(ExplicitRungeKutta::dopri5())
+                  .t_eval({1.69, 0.5, 1.0})
+                  .solve();
+    if (!s2.ok() || s2.value().t.size() != 3 || s2.value().t[0] != 0.5) { std::printf("t_eval\n"); return 3; }
+    if (std::fabs(s2.value().y[0][0] - std::exp(0.5)) >= 1e-3) { std::printf("interp\n"); return 4; }
+    auto bad = IVP::ode(System::exponential_growth(1.0), 0.0, 1.0, {1.0})
+                   .method(ExplicitRungeKutta::dopri5().h0(10.0))
+                   .solve();
+    if (bad.ok() || bad.error().kind != ErrorKind::BadInput || bad.error().msg.rfind("Invalid input", 0) != 0) {
+        std::printf("bad input\n");
+        return 5;
+    }
+    auto er = solve_ensemble(DEGPU_RHS_HARMONIC, 2, 1, {0.0, 0.0}, {10.0, 5.0}, {1.0, 1.0, 0.0, 0.0}, {1.0, 1.0},
+                             {1e-10, 1e-10}, {1e-12, 1e-12}, ExplicitRungeKutta::dop853());
+    if (er.status[0] != DEGPU_COMPLETE || std::fabs(er.y_final[0] - std::cos(10.0)) > 1e-8) { std::printf("ens\n"); return 6; }
+    std::printf("ok\n");
+    return 0;
+}
