@@ -308,7 +308,7 @@ def main():
     e2e = n * world / (float(np.mean(e2e_ms)) * 1e-3)
 
     extra = {}
-    for v in [x for x in args.compare.split(",") if x and x != args.variant]:
+    for v in [x for x in args.compare.split(",") if x in VARIANTS and x != args.variant]:
         t, _ = timed(cfg_of(v), 1, 1)
         extra[v] = {"solves_per_s": n * world / (t * 1e-3), "ms": t}
 

@@ -328,8 +328,8 @@ struct Lane {
         static_for<1, NS>([&](auto i) {
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = y[c];
-            static_for<0, i>([&](auto j) {
-                constexpr double aij = Tab::a(i, j);
+            static_for<0, decltype(i)::value>([&](auto j) {
+                constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                 if constexpr (aij != 0.0) {
                     S ah = stage_coef(aij);
 #pragma unroll
@@ -343,7 +343,7 @@ struct Lane {
 #pragma unroll
         for (int c = 0; c < D; ++c) yseg[c] = (S)0;
         static_for<0, NS>([&](auto i) {
-            constexpr double bi_ = Tab::b(i);
+            constexpr double bi_ = Tab::b(decltype(i)::value);
             if constexpr (bi_ != 0.0) {
 #pragma unroll
                 for (int c = 0; c < D; ++c) yseg[c] = yseg[c] + (S)bi_ * k[i][c];
@@ -372,7 +372,7 @@ struct Lane {
 #pragma unroll
             for (int c = 0; c < D; ++c) es[c] = (S)0;
             static_for<0, NS>([&](auto j) {
-                constexpr double e_ = Tab::er(j);
+                constexpr double e_ = Tab::er(decltype(j)::value);
                 if constexpr (e_ != 0.0) {
 #pragma unroll
                     for (int c = 0; c < D; ++c) es[c] = es[c] + (S)e_ * k[j][c];
@@ -386,7 +386,7 @@ struct Lane {
 #pragma unroll
             for (int c = 0; c < D; ++c) es[c] = yseg[c];
             static_for<0, NS>([&](auto j) {
-                constexpr double bh_ = Tab::bh(j);
+                constexpr double bh_ = Tab::bh(decltype(j)::value);
                 if constexpr (bh_ != 0.0) {
 #pragma unroll
                     for (int c = 0; c < D; ++c) es[c] = es[c] + (S)(-bh_) * k[j][c];
@@ -504,8 +504,8 @@ struct Lane {
                 static_for<NS + 1, I>([&](auto i) {
 #pragma unroll
                     for (int c = 0; c < D; ++c) ys[c] = y[c];
-                    static_for<0, i>([&](auto j) {
-                        constexpr double aij = Tab::a(i, j);
+                    static_for<0, decltype(i)::value>([&](auto j) {
+                        constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                         if constexpr (aij != 0.0) {
                             S ah = stage_coef(aij);
 #pragma unroll
@@ -521,7 +521,7 @@ struct Lane {
                 for (int c = 0; c < D; ++c) {
                     S s = (S)0;
                     static_for<0, I>([&](auto j) {
-                        constexpr double v = Tab::bi(i, j);
+                        constexpr double v = Tab::bi(decltype(i)::value, decltype(j)::value);
                         if constexpr (v != 0.0) s = s + (S)v * k[j][c];
                     });
                     cont[i][c] = s * hs;
@@ -544,8 +544,8 @@ struct Lane {
         static_for<1, NS>([&](auto i) {
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = y[c];
-            static_for<0, i>([&](auto j) {
-                constexpr double aij = Tab::a(i, j);
+            static_for<0, decltype(i)::value>([&](auto j) {
+                constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                 if constexpr (aij != 0.0) {
                     S ah = stage_coef(aij);
 #pragma unroll

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol():
     lib = abi.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert set(declared_functions()) <= set(abi.SIGNATURES) | {"degpu_solve_ensemble_noalloc"}
+    assert set(declared_functions()) <= set(abi.SIGNATURES)
 
 
 def test_defaults_match_crate():
