@@ -1,0 +1,193 @@
+// noalloc.cu — degpu_solve_ensemble_noalloc: the persistent multi-family ensemble solve whose
+// work lists live in a fixed device array of this library instead of memory allocated per call.
+//
+// Who needs it: callers that must not allocate device memory while they run.  Examples are an
+// application that reserves the whole device memory pool for itself at start-up and forbids any
+// later cudaMalloc (to keep its footprint fixed and avoid fragmentation), and a latency-critical
+// loop that cannot afford an allocator call in its step (cudaMalloc/cudaFree may synchronise the
+// device).  Such a caller still provides the inputs and outputs; the few megabytes of work-list
+// space the solve needs come from `noalloc_scratch` below.
+//
+// The array is held by every GPU that loads the library until the process exits.  All calls
+// share it and it keeps the previous call's contents, so each call first clears the part that
+// must start at zero; two calls whose work overlaps on the GPU (different streams, or different
+// host threads) race on it and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "registry.cuh"
+
+namespace degpu {
+
+namespace {
+
+constexpr int NA_NB = 128;  // cost buckets per family
+constexpr int64_t NA_MAX = DEGPU_NOALLOC_MAX_INSTANCES;
+
+// layout of the scratch array (bytes)
+constexpr size_t NA_CELLS = 0;                                   // int[3 * NA_NB]
+constexpr size_t NA_START = NA_CELLS + 3 * NA_NB * 4;            // int64[3]
+constexpr size_t NA_COUNT = NA_START + 3 * 8;                    // int64[3]
+constexpr size_t NA_HEAD = NA_COUNT + 3 * 8;                     // u64[3]
+constexpr size_t NA_ZERO_END = NA_HEAD + 3 * 8;                  // cleared by every call
+constexpr size_t NA_ITEMS = (NA_ZERO_END + 255) / 256 * 256;     // int64[NA_MAX]
+constexpr size_t NA_POS = NA_ITEMS + (size_t)NA_MAX * 8;         // int[NA_MAX]
+constexpr size_t NA_KEY = NA_POS + (size_t)NA_MAX * 4;           // int[NA_MAX]
+constexpr size_t NA_BYTES = NA_KEY + (size_t)NA_MAX * 4;
+
+static __device__ __align__(256) unsigned char noalloc_scratch[NA_BYTES];
+
+std::mutex na_mu;
+void* na_ptr[64] = {};  // device address of noalloc_scratch, per device
+
+// The array's device address, looked up once per device with that device current.
+degpu_status scratch_address(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEGPU_CUDA_ERROR;
+    std::lock_guard<std::mutex> g(na_mu);
+    if (!na_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress((void**)&p, noalloc_scratch) != cudaSuccess || !p) return DEGPU_CUDA_ERROR;
+        na_ptr[dev] = p;
+    }
+    *out = na_ptr[dev];
+    return DEGPU_OK;
+}
+
+__device__ __forceinline__ int na_slot(int id) {
+    return id == DEGPU_RHS_VAN_DER_POL ? 0 : id == DEGPU_RHS_PENDULUM ? 1 : id == DEGPU_RHS_LORENZ ? 2 : -1;
+}
+
+// Cost key and (family, bucket) position; an instance of another family is reported as BadInput
+// and left out of the lists.
+__global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, const double* rtol,
+                                const int32_t* family, int fam_const, double inv_order, double h0,
+                                unsigned char* scratch, int32_t* status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int* cells = (int*)(scratch + NA_CELLS);
+    int* pos = (int*)(scratch + NA_POS);
+    int* key = (int*)(scratch + NA_KEY);
+    int f = na_slot(family ? family[i] : fam_const);
+    if (f < 0) {
+        if (status) status[i] = DEGPU_ERR_BAD_INPUT;
+        key[i] = -1;
+        return;
+    }
+    double span = fabs(tf[i] - t0[i]);
+    double c = inv_order > 0.0 ? log2(span) - inv_order * log2(rtol[i]) : log2(span / fabs(h0));
+    if (!isfinite(c)) c = 0.0;
+    int b = (int)floor((c + 24.0) * 1.5);
+    b = b < 0 ? 0 : (b > NA_NB - 1 ? NA_NB - 1 : b);
+    int k = f * NA_NB + (NA_NB - 1 - b);
+    pos[i] = atomicAdd(&cells[k], 1);
+    key[i] = k;
+}
+
+__global__ void na_scan_kernel(unsigned char* scratch) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int* cells = (int*)(scratch + NA_CELLS);
+    int64_t* start = (int64_t*)(scratch + NA_START);
+    int64_t* count = (int64_t*)(scratch + NA_COUNT);
+    int64_t run = 0;
+    for (int f = 0; f < 3; ++f) {
+        start[f] = run;
+        for (int b = 0; b < NA_NB; ++b) {
+            int c = cells[f * NA_NB + b];
+            cells[f * NA_NB + b] = (int)run;
+            run += c;
+        }
+        count[f] = run - start[f];
+    }
+}
+
+__global__ void na_scatter_kernel(int64_t n, unsigned char* scratch) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int* key = (const int*)(scratch + NA_KEY);
+    int k = key[i];
+    if (k < 0) return;
+    const int* cells = (const int*)(scratch + NA_CELLS);
+    const int* pos = (const int*)(scratch + NA_POS);
+    int64_t* items = (int64_t*)(scratch + NA_ITEMS);
+    items[cells[k] + pos[i]] = i;
+}
+
+}  // namespace
+}  // namespace degpu
+
+using namespace degpu;
+
+extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                                     const degpu_batch_in* in, degpu_batch_out* out, void* stream) {
+    if (!pb || !cfg || !in || !out) return DEGPU_BAD_INPUT;
+    if (in->n < 0) return DEGPU_BAD_INPUT;
+    if (in->n > NA_MAX) return DEGPU_BAD_INPUT;  // beyond DEGPU_NOALLOC_MAX_INSTANCES
+    if (in->n == 0) return DEGPU_OK;
+    if (cfg->method != DEGPU_RK4 && cfg->method != DEGPU_DOPRI5 && cfg->method != DEGPU_DOP853) return DEGPU_BAD_INPUT;
+    if (cfg->precision < DEGPU_FP64_PARITY || cfg->precision > DEGPU_MIXED || cfg->max_steps < 0) return DEGPU_BAD_INPUT;
+    if (!in->t0 || !in->tf || !in->y0 || !in->rtol || !in->atol || !out->y_final) return DEGPU_BAD_INPUT;
+    if (in->n_eval > 0 || in->dims) return DEGPU_UNSUPPORTED;
+    if (in->family) {
+        // the family map is on the device: the rows must have room for every family
+        if (pb->dim < 3 || pb->n_params < 3 || !in->params) return DEGPU_BAD_INPUT;
+    } else {
+        const int id = pb->rhs_id;
+        const int need_d = id == DEGPU_RHS_LORENZ ? 3 : (id == DEGPU_RHS_VAN_DER_POL || id == DEGPU_RHS_PENDULUM) ? 2 : 0;
+        const int need_p = id == DEGPU_RHS_VAN_DER_POL ? 1 : 3;
+        if (need_d == 0) return DEGPU_UNSUPPORTED;
+        if (pb->dim < need_d || pb->n_params < need_p || !in->params) return DEGPU_BAD_INPUT;
+    }
+    ensure_registered();
+    auto it = multi_registry().find({cfg->method, cfg->precision, 0});
+    if (it == multi_registry().end()) return DEGPU_UNSUPPORTED;
+    void* base = nullptr;
+    degpu_status st = scratch_address(&base);
+    if (st != DEGPU_OK) return st;
+    unsigned char* scratch = (unsigned char*)base;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t n = in->n;
+
+    // the lists, counts and heads from the previous call are still in the array: clear them
+    if (cudaMemsetAsync(scratch, 0, NA_ZERO_END, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    na_count_kernel<<<blocks, 256, 0, s>>>(n, in->t0, in->tf, in->rtol, in->family, pb->rhs_id, inv_order,
+                                           cfg->h0 != 0.0 ? cfg->h0 : 1.0, scratch, out->status);
+    na_scan_kernel<<<1, 32, 0, s>>>(scratch);
+    na_scatter_kernel<<<blocks, 256, 0, s>>>(n, scratch);
+    if (cudaGetLastError() != cudaSuccess) return DEGPU_CUDA_ERROR;
+
+    EnsArgs a{};
+    a.n = n;
+    a.count = n;
+    a.t0 = in->t0;
+    a.tf = in->tf;
+    a.y0 = in->y0;
+    a.params = in->params;
+    a.rtol = in->rtol;
+    a.atol = in->atol;
+    a.dmax = pb->dim;
+    a.y_final = out->y_final;
+    a.t_final = out->t_final;
+    a.accepted = out->accepted;
+    a.rejected = out->rejected;
+    a.fevals = out->fevals;
+    a.status = out->status;
+    a.h0 = cfg->h0;
+    a.h_min = cfg->h_min;
+    a.h_max = cfg->h_max;
+    a.max_steps = cfg->max_steps;
+    a.safety = cfg->safety_factor;
+    a.min_scale = cfg->min_scale;
+    a.max_scale = cfg->max_scale;
+    a.dense_mode = cfg->dense_mode;
+    a.n_params = pb->n_params;
+    MultiQueue q;
+    q.items = (const int64_t*)(scratch + NA_ITEMS);
+    q.start = (const int64_t*)(scratch + NA_START);
+    q.count = (const int64_t*)(scratch + NA_COUNT);
+    q.head = (unsigned long long*)(scratch + NA_HEAD);
+    return it->second(a, q, n, s) == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
+}

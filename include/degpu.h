@@ -167,6 +167,28 @@ degpu_status degpu_rhs_info(int32_t rhs_id, int32_t* dim, int32_t* n_params);
 degpu_status degpu_solve_ensemble(const degpu_problem* problem, const degpu_method_cfg* cfg,
                                   const degpu_batch_in* in, degpu_batch_out* out, void* stream);
 
+/* Largest batch degpu_solve_ensemble_noalloc accepts. */
+#define DEGPU_NOALLOC_MAX_INSTANCES 262144
+
+/* degpu_solve_ensemble without any device memory allocation.  It has no counterpart in the
+ * reference (the crate solves one problem per call on the CPU); it exists for callers that must
+ * not allocate device memory while they run, such as an application that reserves the whole
+ * device pool for itself at start-up or a latency-critical loop that cannot afford an allocator
+ * call (cudaMalloc/cudaFree may synchronise the device).  The caller passes device inputs and
+ * outputs as for degpu_solve_ensemble; the solve's work lists live in a fixed array of about
+ * 4.2 MB inside the library (held by every GPU that loads it, until the process exits).
+ *  - n must be <= DEGPU_NOALLOC_MAX_INSTANCES, otherwise DEGPU_BAD_INPUT and nothing runs.
+ *  - Only the persistent solve of the Van der Pol, pendulum and Lorenz families, without dense
+ *    output or per-instance dimensions (DEGPU_UNSUPPORTED otherwise).  With a device family map,
+ *    dim and n_params must be >= 3; an instance of another family gets status BadInput and no
+ *    other output.
+ *  - The first call on a device looks up the array's address on that device; make that first
+ *    call before starting any stream capture.
+ *  - Every call reuses the same array: calls that overlap on the GPU (other streams, other host
+ *    threads) race and must be serialised by the caller. */
+degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                          const degpu_batch_in* in, degpu_batch_out* out, void* stream);
+
 /* Same contract with HOST pointers: copies inputs to the device, solves, copies results back,
  * synchronizes.  This is the call a crate user's host code makes. */
 degpu_status degpu_solve_ensemble_host(const degpu_problem* problem, const degpu_method_cfg* cfg,

@@ -1,0 +1,94 @@
+"""degpu_solve_ensemble_noalloc against degpu_solve_ensemble.
+
+The no-allocation entry point serves callers that must not allocate device memory while they
+run, e.g. an application that has reserved the device memory pool for itself, or a loop whose
+step cannot absorb an allocator call that may synchronise the device.  It must give the same
+results as the ordinary entry point.  Two calls run back to back, the second on a different,
+smaller batch, because the fixed work-list array keeps the previous call's contents.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from degpu import abi, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-12  # same bar as the parity tests
+
+
+def device_batch(torch, e, dev):
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    ins = dict(t0=T(e.t0), tf=T(e.tf), y0=T(e.y0), params=T(e.params), rtol=T(e.rtol), atol=T(e.atol),
+               family=T(e.family, torch.int32))
+    bi = abi.BatchIn(n=e.n, t0=abi.ptr(ins["t0"]), tf=abi.ptr(ins["tf"]), y0=abi.ptr(ins["y0"]),
+                     params=abi.ptr(ins["params"]), rtol=abi.ptr(ins["rtol"]), atol=abi.ptr(ins["atol"]),
+                     family=abi.ptr(ins["family"], C.c_int32), n_eval=0)
+    return ins, bi
+
+
+def device_outputs(torch, n, dev):
+    o = dict(y_final=torch.full((3, n), float("nan"), dtype=torch.float64, device=dev),
+             t_final=torch.empty(n, dtype=torch.float64, device=dev),
+             accepted=torch.empty(n, dtype=torch.int64, device=dev),
+             rejected=torch.empty(n, dtype=torch.int64, device=dev),
+             fevals=torch.empty(n, dtype=torch.int64, device=dev),
+             status=torch.full((n,), -1, dtype=torch.int32, device=dev))
+    bo = abi.BatchOut(y_final=abi.ptr(o["y_final"]), t_final=abi.ptr(o["t_final"]),
+                      accepted=abi.ptr(o["accepted"], C.c_int64), rejected=abi.ptr(o["rejected"], C.c_int64),
+                      fevals=abi.ptr(o["fevals"], C.c_int64), status=abi.ptr(o["status"], C.c_int32))
+    return o, bo
+
+
+def solve_both(torch, lib, e, precision, stream):
+    dev = torch.device("cuda:0")
+    cfg = abi.default_cfg(abi.DOPRI5)
+    cfg.precision, cfg.kernel, cfg.max_steps = precision, abi.KERNEL_PERSISTENT, 10_000_000
+    prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
+    ins, bi = device_batch(torch, e, dev)
+    ref, bo_ref = device_outputs(torch, e.n, dev)
+    got, bo_got = device_outputs(torch, e.n, dev)
+    h = C.c_void_p(stream.cuda_stream)
+    assert lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo_ref), h) == abi.OK
+    assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo_got), h) == abi.OK
+    stream.synchronize()
+    return {k: v.cpu().numpy() for k, v in ref.items()}, {k: v.cpu().numpy() for k, v in got.items()}
+
+
+def assert_same(ref, got):
+    for k in ("status", "accepted", "rejected", "fevals"):
+        assert np.array_equal(ref[k], got[k]), k
+    scale = np.maximum(np.abs(ref["y_final"]), 1e-300)
+    assert np.max(np.abs(got["y_final"] - ref["y_final"]) / scale) <= REL_TOL
+    assert np.array_equal(ref["t_final"], got["t_final"])
+
+
+@pytest.mark.parametrize("precision", [abi.FP64_PARITY, abi.MIXED])
+def test_noalloc_matches_ordinary_entry_point_twice(precision):
+    torch = pytest.importorskip("torch")
+    lib = abi.load()
+    stream = torch.cuda.Stream()
+    first = W.config1(n=3 * 2000)
+    first.tf = np.minimum(first.tf, 8.0)
+    second = W.config1(n=3 * 500, first=50_000)  # different and smaller: stale lists must not leak
+    second.tf = np.minimum(second.tf, 8.0)
+    for e in (first, second):
+        ref, got = solve_both(torch, lib, e, precision, stream)
+        assert np.all(ref["status"] == abi.COMPLETE)
+        assert_same(ref, got)
+
+
+def test_noalloc_rejects_batches_beyond_its_maximum():
+    torch = pytest.importorskip("torch")
+    lib = abi.load()
+    e = W.config1(n=30)
+    dev = torch.device("cuda:0")
+    ins, bi = device_batch(torch, e, dev)
+    out, bo = device_outputs(torch, e.n, dev)
+    bi.n = abi_max = 262144 + 1  # DEGPU_NOALLOC_MAX_INSTANCES + 1: refused before anything runs
+    cfg = abi.default_cfg(abi.DOPRI5)
+    prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
+    assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), None) == \
+        abi.BAD_INPUT
+    assert abi_max > 262144
