@@ -131,6 +131,66 @@ def cpu_baseline(e: W.Ensemble, sample: int, threads: int):
     return sample / dt, dt
 
 
+def accuracy_report(e: W.Ensemble, y_gpu: np.ndarray, per_family: int = 1000, threads: int = 0):
+    """Final-state error of the GPU result against (a) the FP64 oracle at the same tolerances
+    (the crate's CPU solver, restated) and (b) an FP64 oracle run at rtol = atol = 1e-13
+    (DOP853), on `per_family` instances of each family.  Relative error = max_c |a_c - b_c| /
+    max_c |b_c|.  Lorenz instances with rho > ~24.7 are chaotic over these horizons, so their
+    errors against any other trajectory grow to O(1); the table reports them as measured."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib as O
+
+    threads = threads or (os.cpu_count() or 1)
+    idx = np.concatenate([np.nonzero(e.family == f)[0][:per_family] for f in W.FAMILIES_C1])
+    s = e.subset(idx)
+    b = O.Batch(0, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, s.rtol, s.atol, family=s.family)
+    cfg = abi.default_cfg(abi.DOPRI5)
+    cfg.max_steps = s.max_steps
+    same = O.solve(b, cfg, threads=threads, math_mode=1)["y_final"]
+    bt = O.Batch(0, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, np.full(s.n, 1e-13), np.full(s.n, 1e-13),
+                 family=s.family)
+    cfg8 = abi.default_cfg(abi.DOP853)
+    cfg8.max_steps = 50_000_000
+    tight = O.solve(bt, cfg8, threads=threads, math_mode=1)["y_final"]
+    g = y_gpu[:, idx]
+
+    def rel(a, ref):
+        return np.max(np.abs(a - ref), axis=0) / np.maximum(np.max(np.abs(ref), axis=0), 1e-300)
+
+    out = {}
+    names = {abi.RHS["VAN_DER_POL"]: "van_der_pol", abi.RHS["PENDULUM"]: "pendulum", abi.RHS["LORENZ"]: "lorenz"}
+    for f in W.FAMILIES_C1:
+        m = s.family == f
+        r_same = rel(g[:, m], same[:, m])
+        r_tight = rel(g[:, m], tight[:, m])
+        r_fp64_tight = rel(same[:, m], tight[:, m])
+        q = lambda v: {"median": float(np.median(v)), "p90": float(np.percentile(v, 90)), "max": float(np.max(v))}
+        out[names[f]] = {"vs_fp64_oracle": q(r_same), "frac_le_1e-6_vs_fp64_oracle": float(np.mean(r_same <= 1e-6)),
+                         "vs_tight_oracle": q(r_tight), "fp64_oracle_vs_tight": q(r_fp64_tight)}
+        if f == abi.RHS["LORENZ"]:
+            nc = s.params[1, m] < 24.0  # non-chaotic Lorenz (rho below the chaotic onset)
+            out[names[f]]["nonchaotic_vs_fp64_oracle"] = q(r_same[nc]) if nc.any() else None
+    out["sample"] = f"first {per_family} instances of each family; tight oracle = DOP853 rtol=atol=1e-13"
+    return out
+
+
+def run_profile_case(args):
+    """A small case of the same workload for profiler captures: the first N instances (all three
+    families), solved --steps times with the chosen variant through degpu_solve_ensemble_host."""
+    import degpu
+
+    e = W.config1(n=args.profile_case)
+    prec, kern = VARIANTS[args.variant]
+    m = degpu.ExplicitRungeKutta(abi.DOPRI5)
+    m.cfg.precision, m.cfg.kernel, m.cfg.max_steps = prec, kern, e.max_steps
+    for _ in range(max(1, args.steps)):
+        t = time.perf_counter()
+        g = degpu.solve_ensemble(0, 3, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, m, family=e.family, n_params=3)
+        print(json.dumps({"profile_case": e.n, "variant": args.variant, "wall_s": time.perf_counter() - t,
+                          "step_attempts": int((g.accepted + g.rejected).sum()),
+                          "complete": int((g.status == abi.COMPLETE).sum())}))
+
+
 def run_reference(args):
     """--impl reference: the crate's CPU path (oracle restatement) on this host's cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -170,9 +230,14 @@ def main():
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--cpu-sample", type=int, default=12000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0,
+                    help="solve only the first N instances once per --steps (a small case for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return run_profile_case(args)
 
     import torch
 
@@ -307,6 +372,10 @@ def main():
         assert rc == abi.OK
     e2e = n * world / (float(np.mean(e2e_ms)) * 1e-3)
 
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        accuracy = accuracy_report(e, d_out["y_final"].cpu().numpy())
+
     extra = {}
     for v in [x for x in args.compare.split(",") if x in VARIANTS and x != args.variant]:
         t, _ = timed(cfg_of(v), 1, 1)
@@ -339,6 +408,7 @@ def main():
         "gpu_launches": launches,
         "clocks": ck,
         "variants": extra,
+        "accuracy": accuracy,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -266,6 +266,12 @@ static degpu_status validate(const degpu_problem* pb, const degpu_method_cfg* cf
     if (!in->family) {
         int dim, np;
         builtin_info(pb->rhs_id, dim, np);
+        if (np < 0 && pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) {
+            int32_t d32 = 0, p32 = 0;
+            if (nvrtc_rhs_info(pb->rhs_id, &d32, &p32) != DEGPU_OK) return DEGPU_BAD_INPUT;
+            dim = d32;
+            np = p32;
+        }
         if (np < 0) return DEGPU_BAD_INPUT;
         if (dim > 0 && dim != pb->dim) return DEGPU_BAD_INPUT;
         if (np > pb->n_params) return DEGPU_BAD_INPUT;

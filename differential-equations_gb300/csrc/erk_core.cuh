@@ -78,6 +78,8 @@ struct Lane {
 
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
+    double rem;    // tf - t (mixed form)
+    bool bounded;  // h_min / h_max differ from the defaults 0 / +inf
     double p[NPP];
     S y[D];
     S yc[D];  // Kahan compensation of y (mixed precision only)
@@ -92,13 +94,16 @@ struct Lane {
 
     __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const { Rhs::template diff<P>(tt, yy, dd, p); }
 
-    __device__ __forceinline__ double norm_term(S e, S yv, S ynv) const {
+    // Type of the per-component error terms and their sum: FP64 except in the mixed form, whose
+    // terms come from FP32 stage data (and whose sum therefore gains nothing from FP64).
+    using NormT = typename Select<P::KAHAN, float, double>::type;
+
+    __device__ __forceinline__ NormT norm_term(S e, S yv, S ynv) const {
         // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
         if constexpr (P::KAHAN) {
-            // mixed: the quotient of FP32 stage data in FP32, accumulated by the caller in FP64
             float sk = (float)atol + (float)rtol * fmaxf(fabsf(yv), fabsf(ynv));
             float q = __fdividef(e, sk);
-            return (double)(q * q);
+            return q * q;
         } else {
             double sk = atol + rtol * fmax(fabs((double)yv), fabs((double)ynv));
             double q = (double)e / sk;
@@ -271,6 +276,8 @@ struct Lane {
         t = t0;
         t_prev = t0;
         h_prev = 0.0;
+        rem = tf - t0;
+        bounded = !(a.h_min == 0.0 && isinf(a.h_max) && a.h_max > 0.0);
         steps = acc = rej = fev = 0;
         stiff = nonstiff = 0;
         next_eval = 0;
@@ -366,7 +373,7 @@ struct Lane {
         double t_new = t + h;
         fev += NS - 1;
 
-        double err = 0.0, err2 = 0.0;
+        NormT err = (NormT)0, err2 = (NormT)0;
         {
             S es[D];
 #pragma unroll
@@ -395,25 +402,25 @@ struct Lane {
 #pragma unroll
             for (int c = 0; c < D; ++c) err2 = err2 + norm_term(es[c], y[c], ynew[c]);
         }
-        double deno = Tab::HAS_BH ? err + 0.01 * err2 : err;
-        if (deno <= 0.0) deno = 1.0;
-        double scale;
+        NormT deno = Tab::HAS_BH ? err + (NormT)0.01 * err2 : err;
+        if (deno <= (NormT)0) deno = (NormT)1;
+        double scale, errd;
         if constexpr (P::KAHAN) {
-            // mixed: the normalisation and the controller's power in FP32; the decision err <= 1,
-            // h and t stay FP64
-            float ef = (float)err * sqrtf(1.0f / ((float)deno * (float)D));
-            err = fabs(h) * (double)ef;
-            float pw = exp2f(__log2f((float)err) * (float)(-1.0 / (double)O));
+            // mixed: the normalisation and the controller's power in FP32; the accept/reject
+            // decision on the FP64 value, and h and t in FP64
+            float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf((float)h);
+            errd = (double)ef;
+            float pw = exp2f(__log2f(ef) * (float)(-1.0 / (double)O));
             scale = (double)fminf(fmaxf((float)a.safety * pw, (float)a.min_scale), (float)a.max_scale);
         } else {
-            err = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
+            errd = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
             double error_exponent = 1.0 / (double)O;
-            scale = a.safety * P::pow(err, -error_exponent);
+            scale = a.safety * P::pow(errd, -error_exponent);
             scale = fmin(fmax(scale, a.min_scale), a.max_scale);
         }
 
         int result;
-        if (err <= 1.0) {
+        if (errd <= 1.0) {
             S dydt[D];
             rhs(t_new, ynew, dydt);
             fev += 1;
@@ -466,11 +473,13 @@ struct Lane {
             result = 2;
         }
         h = h * scale;
-        // constrain_step_size, utils.rs:22-33
-        if (fabs(h) < a.h_min)
-            h = rs_signum(h) * a.h_min;
-        else if (fabs(h) > a.h_max)
-            h = rs_signum(h) * a.h_max;
+        // constrain_step_size, utils.rs:22-33 (a no-op for the default bounds 0 and +inf)
+        if (bounded) {
+            if (fabs(h) < a.h_min)
+                h = rs_signum(h) * a.h_min;
+            else if (fabs(h) > a.h_max)
+                h = rs_signum(h) * a.h_max;
+        }
         return result;
     }
 
@@ -601,7 +610,17 @@ struct Lane {
     // ----- one iteration of the driver loop: solve_ivp.rs:191-266 ----------------------------
     __device__ __forceinline__ void iterate(const EnsArgs& a) {
         const double eps10 = 2.220446049250313e-16 * 10.0;
-        if ((t + h - tf) * dir > 0.0) {
+        if constexpr (P::KAHAN) {
+            // mixed form: the remaining interval tf - t is kept (updated on acceptance), so the
+            // overshoot test is one comparison
+            if (dir > 0.0 ? h > rem : h < rem) {
+                if (fabs(rem) < eps10) {
+                    done = true;
+                    return;
+                }
+                h = rem;
+            }
+        } else if ((t + h - tf) * dir > 0.0) {
             double h_new = tf - t;
             if (fabs(h_new) < eps10) {
                 done = true;
@@ -620,7 +639,12 @@ struct Lane {
         }
         acc += 1;
         solout(a);
-        if (fabs(tf - t) <= eps10) done = true;
+        if constexpr (P::KAHAN) {
+            rem = tf - t;
+            if (fabs(rem) <= eps10) done = true;
+        } else {
+            if (fabs(tf - t) <= eps10) done = true;
+        }
     }
 
     __device__ void finish(const EnsArgs& a) const {

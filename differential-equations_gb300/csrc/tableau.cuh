@@ -131,6 +131,16 @@ struct TabDop853 {
     __host__ __device__ static constexpr double bi(int i, int j) { return BI[i][j]; }
 };
 
+// Type selection (std::conditional without <type_traits>, which run-time compilation lacks).
+template <bool B, class T, class F>
+struct Select {
+    using type = T;
+};
+template <class T, class F>
+struct Select<false, T, F> {
+    using type = F;
+};
+
 // Compile-time loop: f(std::integral_constant<int, k>) for k in [Begin, End).
 template <int V>
 struct IC {
