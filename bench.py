@@ -15,6 +15,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import subprocess
 import sys
@@ -174,6 +175,293 @@ def accuracy_report(e: W.Ensemble, y_gpu: np.ndarray, per_family: int = 1000, th
     return out
 
 
+def _clock_ms(fn, stream, torch, reps):
+    """Mean CUDA-event time of fn() on `stream` over `reps` calls (after one warm-up)."""
+    fn()
+    stream.synchronize()
+    ms = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    return float(np.mean(ms))
+
+
+def _device_batch(torch, e, dev, dims=None):
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    keep = dict(t0=T(e.t0), tf=T(e.tf), y0=T(e.y0), params=T(e.params), rtol=T(e.rtol), atol=T(e.atol))
+    if e.family is not None:
+        keep["family"] = T(e.family, torch.int32)
+    if dims is not None:
+        keep["dims"] = T(dims, torch.int32)
+    if e.t_eval is not None:
+        keep["t_eval"] = T(e.t_eval)
+    bi = abi.BatchIn(n=e.n, t0=abi.ptr(keep["t0"]), tf=abi.ptr(keep["tf"]), y0=abi.ptr(keep["y0"]),
+                     params=abi.ptr(keep["params"]), rtol=abi.ptr(keep["rtol"]), atol=abi.ptr(keep["atol"]),
+                     family=abi.ptr(keep.get("family"), C.c_int32), dims=abi.ptr(keep.get("dims"), C.c_int32),
+                     t_eval=abi.ptr(keep.get("t_eval")), n_eval=0 if e.t_eval is None else len(e.t_eval))
+    out = dict(y_final=torch.empty((e.dim, e.n), dtype=torch.float64, device=dev),
+               t_final=torch.empty(e.n, dtype=torch.float64, device=dev),
+               accepted=torch.empty(e.n, dtype=torch.int64, device=dev),
+               rejected=torch.empty(e.n, dtype=torch.int64, device=dev),
+               fevals=torch.empty(e.n, dtype=torch.int64, device=dev),
+               status=torch.empty(e.n, dtype=torch.int32, device=dev))
+    if e.t_eval is not None:
+        out["dense"] = torch.empty((len(e.t_eval), e.dim, e.n), dtype=torch.float64, device=dev)
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
+                      dense=abi.ptr(out.get("dense")), accepted=abi.ptr(out["accepted"], C.c_int64),
+                      rejected=abi.ptr(out["rejected"], C.c_int64), fevals=abi.ptr(out["fevals"], C.c_int64),
+                      status=abi.ptr(out["status"], C.c_int32))
+    return keep, bi, out, bo
+
+
+def _oracle_solve(e, method, threads, math_mode=0):
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib as O
+
+    b = O.Batch(e.rhs_id, e.dim, e.n_params, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, t_eval=e.t_eval,
+                dims=e.dims, family=e.family)
+    cfg = abi.default_cfg(method)
+    cfg.max_steps = e.max_steps
+    t = time.perf_counter()
+    o = O.solve(b, cfg, threads=threads, math_mode=math_mode)
+    return o, time.perf_counter() - t
+
+
+def run_lorenz4096(args, torch, dev, lib):
+    """4096 Lorenz IVPs (d=3), DOPRI5 rtol=1e-8 atol=1e-10 on [0, 20]: plain FP64 parity kernel,
+    persistent parity kernel, and the CPU oracle with every host thread."""
+    e = W.config0()
+    stream = torch.cuda.Stream(device=dev)
+    keep, bi, out, bo = _device_batch(torch, e, dev)
+    prob = abi.Problem(rhs_id=e.rhs_id, dim=3, n_params=3)
+    res = {}
+    for name, (prec, kern) in (("fp64-plain", (abi.FP64_PARITY, abi.KERNEL_THREAD)),
+                               ("fp64-persistent", (abi.FP64_PARITY, abi.KERNEL_PERSISTENT)),
+                               ("mixed-persistent", (abi.MIXED, abi.KERNEL_PERSISTENT))):
+        cfg = abi.default_cfg(abi.DOPRI5)
+        cfg.precision, cfg.kernel, cfg.max_steps = prec, kern, e.max_steps
+        f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
+                                             C.c_void_p(stream.cuda_stream))
+        ms = _clock_ms(f, stream, torch, max(1, args.steps))
+        res[name] = {"solves_per_s": e.n / (ms * 1e-3), "ms": ms}
+    threads = os.cpu_count() or 1
+    o, dt = _oracle_solve(e, abi.DOPRI5, threads)
+    line = {"metric": "IVP solves/sec (4096 Lorenz, DOPRI5 rtol=1e-8 atol=1e-10, t in [0,20])",
+            "value": res["fp64-plain"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": "lorenz-4096"}, "variants": res,
+            "step_attempts": int((o["accepted"] + o["rejected"]).sum()),
+            "cpu_baseline": {"value": e.n / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": "all 4096 instances (host libm)"}}
+    print(json.dumps(line))
+
+
+def fpu_energy(torch, y, dims, beta):
+    """H = sum p^2/2 + sum_{i=0..m} (D_i^2/2 + beta D_i^4/4) per chain, y [dmax, n] on the device."""
+    n = y.shape[1]
+    m = (dims // 2).long()
+    rows = torch.arange(y.shape[0], device=y.device)[:, None]
+    x = torch.where(rows < m[None, :], y, torch.zeros_like(y))
+    pidx = (rows + m[None, :]).clamp(max=y.shape[0] - 1)
+    p = torch.where(rows < m[None, :], torch.gather(y, 0, pidx), torch.zeros_like(y))
+    xp = torch.cat([torch.zeros((1, n), dtype=y.dtype, device=y.device), x], 0)  # x_0 = 0
+    xn = torch.cat([x, torch.zeros((1, n), dtype=y.dtype, device=y.device)], 0)  # x_{m+1} = 0
+    dlt = (xn - xp)  # D_0 .. D_dmax; entries beyond m+1 are 0 - 0
+    return (p * p).sum(0) / 2 + (dlt * dlt / 2 + beta[None, :] * dlt ** 4 / 4).sum(0)
+
+
+def run_fpu(args, torch, dev, lib):
+    """131,072 FPU-beta chains (2..128 masses), DOP853 rtol=1e-10 atol=1e-12 on [0,100] with 64
+    output times: group-per-system kernel, FP64 parity and mixed; energy drift from the dense
+    output; CPU oracle on a sample."""
+    n = args.fpu_n
+    e = W.config2(n=n)
+    stream = torch.cuda.Stream(device=dev)
+    keep, bi, out, bo = _device_batch(torch, e, dev, dims=e.dims)
+    prob = abi.Problem(rhs_id=e.rhs_id, dim=e.dim, n_params=1)
+    res = {}
+    dims_t = keep["dims"]
+    beta_t = keep["params"][0]
+    for name, prec in (("fp64", abi.FP64_PARITY), ("mixed", abi.MIXED)):
+        cfg = abi.default_cfg(abi.DOP853)
+        cfg.precision, cfg.max_steps = prec, e.max_steps
+        f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
+                                             C.c_void_p(stream.cuda_stream))
+        ms = _clock_ms(f, stream, torch, max(1, args.steps))
+        h0 = fpu_energy(torch, out["dense"][0], dims_t, beta_t)
+        h1 = fpu_energy(torch, out["dense"][-1], dims_t, beta_t)
+        drift = ((h1 - h0).abs() / h0.abs()).cpu().numpy()
+        res[name] = {"solves_per_s": n / (ms * 1e-3), "ms": ms,
+                     "energy_drift_rel": {"median": float(np.median(drift)), "p99": float(np.percentile(drift, 99)),
+                                          "max": float(np.max(drift))},
+                     "step_attempts": int((out["accepted"] + out["rejected"]).sum().item()),
+                     "complete": int((out["status"] == 0).sum().item())}
+        if name == "fp64":
+            y64 = out["dense"][-1].clone()
+        else:
+            d = (out["dense"][-1] - y64).abs().amax(0) / y64.abs().amax(0).clamp_min(1e-300)
+            res[name]["vs_fp64_final"] = {"median": float(d.median().item()), "max": float(d.max().item())}
+    threads = os.cpu_count() or 1
+    s = e.subset(np.arange(args.fpu_cpu_sample))
+    s.dim = e.dim
+    o, dt = _oracle_solve(s, abi.DOP853, threads)
+    line = {"metric": "IVP solves/sec (FPU-beta chains, DOP853 + 64 dense outputs)",
+            "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": True, "dtype": "f32-stage/f64-control", "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": f"fpu-beta {n} chains, masses int-logU[2,128], t in [0,100]"}, "variants": res,
+            "cpu_baseline": {"value": args.fpu_cpu_sample / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"first {args.fpu_cpu_sample} chains (host libm)"}}
+    print(json.dumps(line))
+
+
+def run_gray_scott(args, torch, dev, lib):
+    """2-D Gray-Scott, 4096 x 4096 periodic, RK4 dt = 0.2 dx^2/Du, 1000 steps, FP64 and FP32:
+    time per step and algorithmic HBM bandwidth (240 / 120 B per node per step) vs the measured
+    copy bandwidth."""
+    nx = ny = args.gs_n
+    dx = 1.0 / 4096
+    p = W.GRAY_SCOTT
+    gs = abi.GrayScott(nx=nx, ny=ny, dx=dx, Du=p["Du"], Dv=p["Dv"], F=p["F"], k=p["k"])
+    dt = 0.2 * dx * dx / p["Du"]
+    u0, v0 = W.gray_scott_init(nx, ny)
+    stream = torch.cuda.Stream(device=dev)
+    peak = None
+    mp = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(mp):
+        peak = json.load(open(mp)).get("hbm_gbs")
+    res = {}
+    steps = args.gs_steps
+    for name, prec, tdt, bpn in (("fp32", abi.MIXED, torch.float32, 120), ("fp64", abi.FP64_FAST, torch.float64, 240),
+                                 ("fp64-parity", abi.FP64_PARITY, torch.float64, 240)):
+        u = torch.as_tensor(u0, dtype=tdt, device=dev)
+        v = torch.as_tensor(v0, dtype=tdt, device=dev)
+        f = lambda: lib.degpu_gray_scott_rk4(C.byref(gs), prec, 0.0, dt, steps, C.c_void_p(u.data_ptr()),
+                                             C.c_void_p(v.data_ptr()), C.c_void_p(stream.cuda_stream))
+        ms = _clock_ms(f, stream, torch, 1)
+        per_step = ms / steps
+        gbs = bpn * nx * ny / (per_step * 1e-3) / 1e9
+        res[name] = {"ms_per_step": per_step, "algorithmic_GBps": gbs,
+                     "frac_of_measured_hbm": (gbs / peak) if peak else None,
+                     "node_steps_per_s": nx * ny / (per_step * 1e-3)}
+    # CPU baseline: the oracle's restatement of SemiDiscretePde::diff on a 256x256 grid, 4 steps
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib as O
+
+    cn = 256
+    cg = abi.GrayScott(nx=cn, ny=cn, dx=dx, Du=p["Du"], Dv=p["Dv"], F=p["F"], k=p["k"])
+    cu, cv = W.gray_scott_init(cn, cn, squares=4)
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    O.lib().oracle_gray_scott_rk4(C.byref(cg), 0.0, dt, 4, O.p(cu), O.p(cv), threads)
+    cdt = time.perf_counter() - t
+    line = {"metric": "Gray-Scott 4096^2 RK4 node-steps/s and HBM GB/s", "value": res["fp32"]["node_steps_per_s"],
+            "unit": "node-steps/s", "n_gpus": 1, "steps": steps, "higher_is_better": True,
+            "dtype": "f32 (fp64 reported beside)", "data": "synthetic (seeded squares)",
+            "config": {"workload": f"gray-scott {nx}x{ny} periodic, dt=0.2dx^2/Du, {steps} RK4 steps"},
+            "variants": res, "hbm_peak_GBps": peak,
+            "cpu_baseline": {"value": cn * cn * 4 / cdt, "unit": "node-steps/s", "cores": threads, "kind": "port",
+                             "sample": "256x256 grid, 4 RK4 steps, FP64 (restated SemiDiscretePde::diff)"}}
+    print(json.dumps(line))
+
+
+def serving_requests(count, seed_base=7_000_000):
+    """Requests of the serving configuration, from the seed: ensemble size ~ int logU[1,65536],
+    family uniform over {Van der Pol, pendulum, Lorenz, FPU-beta chain with <= 64 masses},
+    method uniform over {RK4 h=1e-3, DOPRI5, DOP853} (DOPRI5/DOP853 for chains),
+    rtol ~ logU[1e-10,1e-5], atol = 1e-2 rtol.  Horizons are t_end ~ U[1,10] (shorter than the
+    ensemble benchmark's so that a sweep of arrival rates fits in minutes)."""
+    r = np.arange(count)
+    size = np.floor(np.exp(W.U(4, r, 0, 0.0, math.log(65537.0)))).astype(np.int64).clip(1, 65536)
+    fam = np.floor(W.U(4, r, 1, 0.0, 4.0)).astype(int).clip(0, 3)
+    meth = np.floor(W.U(4, r, 2, 0.0, 3.0)).astype(int).clip(0, 2)
+    rtol = W.logU(4, r, 3, 1e-10, 1e-5)
+    reqs = []
+    for k in range(count):
+        n = int(size[k])
+        if fam[k] < 3:
+            fid = W.FAMILIES_C1[fam[k]]
+            base = W.config1(n=3 * n, first=seed_base + 3 * 65536 * k)
+            e = base.subset(np.nonzero(base.family == fid)[0][:n])
+            e.rhs_id = fid
+            e.family = None
+            e.dim = 3 if fid == abi.RHS["LORENZ"] else 2
+            e.y0 = np.ascontiguousarray(e.y0[:e.dim])
+            m = [abi.RK4, abi.DOPRI5, abi.DOP853][meth[k]]
+        else:
+            e = W.config2(n=n, first=seed_base + 65536 * k)
+            masses = np.minimum(e.dims // 2, 64)
+            e.dims = (2 * masses).astype(np.int32)
+            e.dim = 128
+            y = np.zeros((128, n))
+            rows = min(128, e.y0.shape[0])
+            mask = np.arange(rows)[:, None] < masses[None, :]
+            y[:rows] = np.where(mask, e.y0[:rows], 0.0)
+            e.y0 = y
+            e.t_eval = None
+            m = [abi.DOPRI5, abi.DOP853, abi.DOP853][meth[k]]
+        e.n = len(e.t0)
+        e.tf = W.U(4, np.arange(e.n) + 1000 * k, 5, 1.0, 10.0)
+        e.rtol = np.full(e.n, rtol[k])
+        e.atol = 1e-2 * e.rtol
+        reqs.append((e, m))
+    return reqs
+
+
+def run_serving(args, torch, dev, lib):
+    """Continuous-batching server under Poisson arrivals: saturated capacity first, then a sweep of
+    arrival rates (fractions of capacity); p50/p99 latency and solves/s, mixed vs FP64."""
+    import degpu
+    from degpu.serving import Server
+
+    reqs = serving_requests(args.requests)
+    total_inst = sum(e.n for e, _ in reqs)
+    out = {}
+    for prec_name, prec in (("mixed", abi.MIXED), ("fp64", abi.FP64_PARITY)):
+        def run(rate):
+            srv = Server(memory_budget_gb=150.0, max_active=64, round_budget=512)
+            rng = np.random.default_rng(11)
+            gaps = rng.exponential(1.0 / rate, len(reqs)) if rate > 0 else np.zeros(len(reqs))
+            ids = []
+            t0 = time.perf_counter()
+            next_t = t0
+            for (e, m), g in zip(reqs, gaps):
+                next_t += g
+                while time.perf_counter() < next_t:
+                    time.sleep(min(0.0005, max(0.0, next_t - time.perf_counter())))
+                meth = degpu.ExplicitRungeKutta(m, h0=1e-3 if m == abi.RK4 else 0.0)
+                meth.cfg.precision, meth.cfg.max_steps = prec, 10_000_000
+                ids.append(srv.submit(e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, meth,
+                                      dims=e.dims))
+            lats = [srv.wait(i)[1] for i in ids]
+            wall = time.perf_counter() - t0
+            srv.close()
+            lats = np.array(lats)
+            return {"rate_req_per_s": rate, "p50_ms": float(np.percentile(lats, 50)),
+                    "p99_ms": float(np.percentile(lats, 99)), "solves_per_s": total_inst / wall,
+                    "requests_per_s": len(reqs) / wall}
+
+        sat = run(0.0)
+        cap = sat["requests_per_s"]
+        fracs = (0.25, 0.5, 0.75, 0.9) if prec == abi.MIXED else (0.5, 0.9)
+        sweep = [run(f * cap) for f in fracs]
+        # highest swept rate whose p99 stays within 3x the lightest load's p99
+        ok = [s for s in sweep if s["p99_ms"] <= 3.0 * sweep[0]["p99_ms"]]
+        out[prec_name] = {"saturated": sat, "sweep": sweep, "sustainable": ok[-1] if ok else sweep[0]}
+    line = {"metric": "serving p50/p99 latency and solves/s (continuous batching)",
+            "value": out["mixed"]["sustainable"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32-stage/f64-control (fp64 beside)",
+            "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": f"{len(reqs)} requests, size int-logU[1,65536] ({total_inst} instances), "
+                                   f"VdP/pendulum/Lorenz/FPU(<=64 masses), RK4 h=1e-3 / DOPRI5 / DOP853, "
+                                   f"rtol logU[1e-10,1e-5], t_end U[1,10], 150 GB budget"},
+            "results": out}
+    print(json.dumps(line))
+
+
 def run_profile_case(args):
     """A small case of the same workload for profiler captures: the first N instances (all three
     families), solved --steps times with the chosen variant through degpu_solve_ensemble_host."""
@@ -231,6 +519,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=12000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--workload", default="uneven", choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving"],
+                    help="uneven = the headline 1M-instance ensemble; the others print their own line")
+    ap.add_argument("--fpu-n", type=int, default=131072)
+    ap.add_argument("--fpu-cpu-sample", type=int, default=200)
+    ap.add_argument("--gs-n", type=int, default=4096)
+    ap.add_argument("--gs-steps", type=int, default=1000)
+    ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--profile-case", type=int, default=0,
                     help="solve only the first N instances once per --steps (a small case for ncu captures)")
     args = ap.parse_args()
@@ -251,6 +546,11 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     lib = abi.load()
+    if args.workload != "uneven":
+        if rank == 0:
+            {"lorenz4096": run_lorenz4096, "fpu": run_fpu, "gray-scott": run_gray_scott,
+             "serving": run_serving}[args.workload](args, torch, dev, lib)
+        return
 
     # each rank solves its own slice of instances (weak scaling: instances are independent)
     e = W.config1(n=args.n, first=rank * args.n)
