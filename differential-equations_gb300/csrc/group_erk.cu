@@ -19,12 +19,16 @@ void register_group_fast() {
     reg_group<TabDop853, PrecFast, 8, 1>();
     reg_group<TabDop853, PrecFast, 16, 1>();
     reg_group<TabDop853, PrecFast, 32, 1>();
+    reg_group<TabDop853, PrecFast, 16, 2>();
+    reg_group<TabDop853, PrecFast, 16, 4>();
     reg_group<TabDop853, PrecFast, 32, 2>();
     reg_group<TabDop853, PrecFast, 32, 4>();
     reg_group<TabDop853, PrecFast, 32, 8>();
     reg_group<TabDop853, PrecMixed, 8, 1>();
     reg_group<TabDop853, PrecMixed, 16, 1>();
     reg_group<TabDop853, PrecMixed, 32, 1>();
+    reg_group<TabDop853, PrecMixed, 16, 2>();
+    reg_group<TabDop853, PrecMixed, 16, 4>();
     reg_group<TabDop853, PrecMixed, 32, 2>();
     reg_group<TabDop853, PrecMixed, 32, 4>();
     reg_group<TabDop853, PrecMixed, 32, 8>();
@@ -106,6 +110,9 @@ degpu_status wps_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, con
         if (c.dmax < 0) return DEGPU_UNSUPPORTED;
         buckets[{c.g, c.cpl}].push_back(i);
     }
+    // longest first inside a bucket: the largest systems start first, the tail holds small ones
+    for (auto& b : buckets)
+        std::stable_sort(b.second.begin(), b.second.end(), [&](int64_t x, int64_t y) { return hd[x] > hd[y]; });
     std::vector<void*> to_free;
     degpu_status st = DEGPU_OK;
     for (auto& b : buckets) {

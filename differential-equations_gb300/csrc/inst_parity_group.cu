@@ -11,6 +11,8 @@ void register_group_parity() {
     reg_group<TabDop853, PrecParity, 8, 1>();
     reg_group<TabDop853, PrecParity, 16, 1>();
     reg_group<TabDop853, PrecParity, 32, 1>();
+    reg_group<TabDop853, PrecParity, 16, 2>();
+    reg_group<TabDop853, PrecParity, 16, 4>();
     reg_group<TabDop853, PrecParity, 32, 2>();
     reg_group<TabDop853, PrecParity, 32, 4>();
     reg_group<TabDop853, PrecParity, 32, 8>();

@@ -116,6 +116,10 @@ def load(path: str = LIB_PATH):
         return _lib
     if not os.path.exists(path):
         raise RuntimeError(f"libdegpu.so is not built ({path}); run __graft_entry__.build()")
+    # group-kernel layouts chosen by the autotuner (degpu/autotune.py), read at the first ragged solve
+    tuned = os.path.join(_HERE, "group_tune.txt")
+    if os.path.exists(tuned):
+        os.environ.setdefault("DEGPU_TUNE_FILE", tuned)
     lib = C.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
