@@ -553,7 +553,8 @@ def main():
         return
 
     # each rank solves its own slice of instances (weak scaling: instances are independent)
-    e = W.config1(n=args.n, first=rank * args.n)
+    first, count = W.rank_slice(args.n, rank)
+    e = W.config1(n=count, first=first)
     n = e.n
     T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
     d_in = dict(t0=T(e.t0), tf=T(e.tf), y0=T(e.y0), params=T(e.params), rtol=T(e.rtol), atol=T(e.atol),

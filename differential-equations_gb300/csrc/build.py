@@ -38,6 +38,8 @@ def sources():
 def flags_for(src):
     name = os.path.basename(src)
     f = list(ARCH) + list(COMMON)
+    # extra nvcc flags for tuning experiments, e.g. DEGPU_NVCC_EXTRA="-DDEGPU_MIXED_MIN_BLOCKS=8"
+    f += os.environ.get("DEGPU_NVCC_EXTRA", "").split()
     if name.startswith("inst_parity"):
         f += PARITY
     return f

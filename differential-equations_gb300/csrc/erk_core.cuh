@@ -688,7 +688,7 @@ struct MultiLane {
 };
 
 template <class Tab, class P, bool DENSE, class R0, class R1, class R2>
-__global__ void __launch_bounds__(128) erk_multi_kernel(EnsArgs a, MultiQueue q) {
+__global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(EnsArgs a, MultiQueue q) {
     MultiLane<Tab, P, DENSE, R0, R1, R2> M;
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);

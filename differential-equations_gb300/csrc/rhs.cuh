@@ -15,10 +15,17 @@ namespace degpu {
 // Precision policies --------------------------------------------------------------------------
 // Parity: FP64, crate operation order, correctly rounded pow/sin/cos, no FMA contraction (the
 // translation units that instantiate it are compiled with -fmad=false).
+// Minimum resident blocks per SM requested for the mixed form's persistent kernel (a register
+// cap: 65536 / (128 * blocks) registers per thread); 1 leaves the compiler's choice.
+#ifndef DEGPU_MIXED_MIN_BLOCKS
+#define DEGPU_MIXED_MIN_BLOCKS 1
+#endif
+
 struct PrecParity {
     using S = double;
     static constexpr int ID = 0;
     static constexpr bool KAHAN = false;
+    static constexpr int MULTI_MIN_BLOCKS = 1;
     __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl(x, y); }
     __device__ static __forceinline__ double sin(double x) { return ddm::sin_cr(x); }
     __device__ static __forceinline__ double cos(double x) { return ddm::cos_cr(x); }
@@ -29,6 +36,7 @@ struct PrecFast {
     using S = double;
     static constexpr int ID = 1;
     static constexpr bool KAHAN = false;
+    static constexpr int MULTI_MIN_BLOCKS = 1;
     __device__ static __forceinline__ double pow(double x, double y) { return ::pow(x, y); }
     __device__ static __forceinline__ double sin(double x) { return ::sin(x); }
     __device__ static __forceinline__ double cos(double x) { return ::cos(x); }
@@ -39,6 +47,7 @@ struct PrecMixed {
     using S = float;
     static constexpr int ID = 2;
     static constexpr bool KAHAN = true;
+    static constexpr int MULTI_MIN_BLOCKS = DEGPU_MIXED_MIN_BLOCKS;
     // x^(-1/order) of the controller: FP64 result from an FP32 log2/exp2 estimate refined by
     // one FP64 Newton step on r^q = x^-1 (q = 5 or 8); general y falls back to FP64 pow.
     __device__ static __forceinline__ double pow(double x, double y) {

@@ -174,3 +174,9 @@ def gray_scott_init(nx: int = 4096, ny: int = 4096, squares: int = 64, size: int
 
 
 GRAY_SCOTT = dict(F=0.037, k=0.06, Du=2e-5, Dv=1e-5)
+
+
+def rank_slice(n_per_rank: int, rank: int):
+    """Instances [rank * n, (rank + 1) * n) of a workload: the replica partition used with several
+    GPUs (instances are independent, so ranks share nothing but the timing reduction)."""
+    return rank * n_per_rank, n_per_rank
