@@ -175,9 +175,10 @@ def accuracy_report(e: W.Ensemble, y_gpu: np.ndarray, per_family: int = 1000, th
     return out
 
 
-def _clock_ms(fn, stream, torch, reps):
-    """Mean CUDA-event time of fn() on `stream` over `reps` calls (after one warm-up)."""
-    fn()
+def _clock_ms(fn, stream, torch, reps, warmup=True):
+    """Mean CUDA-event time of fn() on `stream` over `reps` calls (after one warm-up call)."""
+    if warmup:
+        fn()
     stream.synchronize()
     ms = []
     for _ in range(reps):
@@ -288,23 +289,30 @@ def run_fpu(args, torch, dev, lib):
     beta_t = keep["params"][0]
     for name, prec in (("fp64", abi.FP64_PARITY), ("mixed", abi.MIXED)):
         cfg = abi.default_cfg(abi.DOP853)
-        cfg.precision, cfg.max_steps = prec, e.max_steps
+        # FP32 stages cannot reach rtol 1e-10: cap the attempted steps of the mixed form so that
+        # instances whose error estimate sits on the FP32 noise floor end (as MaxSteps) in bounded time
+        cfg.precision, cfg.max_steps = prec, e.max_steps if prec != abi.MIXED else args.fpu_mixed_max_steps
         f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
                                              C.c_void_p(stream.cuda_stream))
-        ms = _clock_ms(f, stream, torch, max(1, args.steps))
+        ms = _clock_ms(f, stream, torch, max(1, args.steps), warmup=False)
         h0 = fpu_energy(torch, out["dense"][0], dims_t, beta_t)
         h1 = fpu_energy(torch, out["dense"][-1], dims_t, beta_t)
-        drift = ((h1 - h0).abs() / h0.abs()).cpu().numpy()
+        ok = (out["status"] == 0).cpu().numpy()
+        drift = ((h1 - h0).abs() / h0.abs()).cpu().numpy()[ok]
+        st = out["status"].cpu().numpy()
         res[name] = {"solves_per_s": n / (ms * 1e-3), "ms": ms,
                      "energy_drift_rel": {"median": float(np.median(drift)), "p99": float(np.percentile(drift, 99)),
-                                          "max": float(np.max(drift))},
+                                          "max": float(np.max(drift))} if ok.any() else None,
                      "step_attempts": int((out["accepted"] + out["rejected"]).sum().item()),
-                     "complete": int((out["status"] == 0).sum().item())}
+                     "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}}
+        print(json.dumps({"fpu_variant": name, **res[name]}), flush=True)
         if name == "fp64":
             y64 = out["dense"][-1].clone()
         else:
             d = (out["dense"][-1] - y64).abs().amax(0) / y64.abs().amax(0).clamp_min(1e-300)
-            res[name]["vs_fp64_final"] = {"median": float(d.median().item()), "max": float(d.max().item())}
+            d = d[~torch.isnan(d)]
+            res[name]["vs_fp64_final"] = ({"median": float(d.median().item()), "max": float(d.max().item())}
+                                          if d.numel() else None)
     threads = os.cpu_count() or 1
     s = e.subset(np.arange(args.fpu_cpu_sample))
     s.dim = e.dim
@@ -523,6 +531,7 @@ def main():
                     help="uneven = the headline 1M-instance ensemble; the others print their own line")
     ap.add_argument("--fpu-n", type=int, default=131072)
     ap.add_argument("--fpu-cpu-sample", type=int, default=200)
+    ap.add_argument("--fpu-mixed-max-steps", type=int, default=200_000)
     ap.add_argument("--gs-n", type=int, default=4096)
     ap.add_argument("--gs-steps", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=200)

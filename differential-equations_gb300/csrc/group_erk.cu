@@ -32,6 +32,14 @@ void register_group_fast() {
     reg_group<TabDop853, PrecMixed, 32, 2>();
     reg_group<TabDop853, PrecMixed, 32, 4>();
     reg_group<TabDop853, PrecMixed, 32, 8>();
+    reg_group<TabDopri5, PrecFast, 8, 1>();
+    reg_group<TabDopri5, PrecFast, 16, 1>();
+    reg_group<TabDopri5, PrecMixed, 8, 1>();
+    reg_group<TabDopri5, PrecMixed, 16, 1>();
+    reg_group<TabDopri5, PrecMixed, 32, 1>();
+    reg_group<TabDopri5, PrecMixed, 32, 2>();
+    reg_group<TabDopri5, PrecMixed, 32, 4>();
+    reg_group<TabDopri5, PrecMixed, 32, 8>();
     reg_group<TabDopri5, PrecFast, 32, 1>();
     reg_group<TabDopri5, PrecFast, 32, 2>();
     reg_group<TabDopri5, PrecFast, 32, 4>();

@@ -148,10 +148,206 @@ __global__ void __launch_bounds__(256) gs_pass_kernel(GsPlanes P, GsParams<T> p)
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Register-blocked form: each thread owns a 4 x 4 block of nodes (4 along x in one 16-byte
+// vector for FP32, two for FP64; 4 rows).  A warp covers 128 consecutive x; its lanes hand the
+// stage state of their edge columns to their neighbours by shuffles, and only lanes 0 and 31
+// load the columns beyond the warp (with the periodic wrap).  Rows j0-1 .. j0+4 are loaded once
+// and shared by the four output rows.  Per node the arithmetic is gs_rhs_at's, in the same order.
+// Requires nx % 128 == 0 and ny % 16 == 0 (the block is 32 x 4 threads = 128 x 16 nodes).
+// ---------------------------------------------------------------------------------------------
+template <class T>
+struct Vec4 {
+    T v[4];
+};
+
+template <class T>
+__device__ __forceinline__ Vec4<T> ld4(const T* p) {
+    Vec4<T> r;
+    if constexpr (sizeof(T) == 4) {
+        float4 q = __ldg((const float4*)p);
+        r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+    } else {
+        double2 a = __ldg((const double2*)p), b = __ldg((const double2*)p + 1);
+        r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
+    }
+    return r;
+}
+template <class T>
+__device__ __forceinline__ void st4(T* p, const Vec4<T>& r) {
+    if constexpr (sizeof(T) == 4) {
+        *(float4*)p = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+    } else {
+        ((double2*)p)[0] = make_double2(r.v[0], r.v[1]);
+        ((double2*)p)[1] = make_double2(r.v[2], r.v[3]);
+    }
+}
+
+// one node's f from its stage state and its four neighbours (gs_rhs_at's operation order)
+template <class T, bool POW2>
+__device__ __forceinline__ void gs_node(const GsParams<T>& p, T u, T v, T ul, T vl, T ur, T vr, T ud, T vd, T uu,
+                                        T vu, T& du, T& dv) {
+    T uvv = u * v * v;
+    T a_u = -uvv + p.F * ((T)1 - u);
+    T a_v = uvv - (p.F + p.k) * v;
+    {
+        T flo_u = p.Du * gs_ddx<T, POW2>(u - ul, p);
+        T fhi_u = p.Du * gs_ddx<T, POW2>(ur - u, p);
+        a_u = a_u + gs_ddx<T, POW2>(fhi_u - flo_u, p);
+        T flo_v = p.Dv * gs_ddx<T, POW2>(v - vl, p);
+        T fhi_v = p.Dv * gs_ddx<T, POW2>(vr - v, p);
+        a_v = a_v + gs_ddx<T, POW2>(fhi_v - flo_v, p);
+    }
+    {
+        T flo_u = p.Du * gs_ddx<T, POW2>(u - ud, p);
+        T fhi_u = p.Du * gs_ddx<T, POW2>(uu - u, p);
+        a_u = a_u + gs_ddx<T, POW2>(fhi_u - flo_u, p);
+        T flo_v = p.Dv * gs_ddx<T, POW2>(v - vd, p);
+        T fhi_v = p.Dv * gs_ddx<T, POW2>(vu - v, p);
+        a_v = a_v + gs_ddx<T, POW2>(fhi_v - flo_v, p);
+    }
+    du = a_u;
+    dv = a_v;
+}
+
+template <class T, bool POW2, int PASS>
+__global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T> p) {
+    constexpr int R = 4;  // rows per thread
+    const int lane = threadIdx.x & 31;
+    const int wy = threadIdx.x >> 5;  // warp within block: 4 warps stacked in y
+    const int xb = blockIdx.x * 128;
+    const int x0 = xb + lane * 4;
+    const int j0 = (blockIdx.y * 4 + wy) * R;
+    const int64_t nx = p.nx;
+    const int ny = p.ny;
+    const T* yu = (const T*)P.yu;
+    const T* yv = (const T*)P.yv;
+    const T* ku = (const T*)P.ku;
+    const T* kv = (const T*)P.kv;
+    const bool has_k = PASS != 4;
+    const T ah = p.ah;
+    // stage state of rows j0-1 .. j0+R (R+2 rows) at this lane's 4 columns
+    T su[R + 2][4], sv[R + 2][4];
+#pragma unroll
+    for (int r = 0; r < R + 2; ++r) {
+        int j = j0 - 1 + r;
+        j = j < 0 ? j + ny : (j >= ny ? j - ny : j);
+        const int64_t o = (int64_t)j * nx + x0;
+        Vec4<T> a = ld4(yu + o), b = ld4(yv + o);
+        if (has_k) {
+            Vec4<T> c = ld4(ku + o), d = ld4(kv + o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                su[r][q] = a.v[q] + ah * c.v[q];
+                sv[r][q] = b.v[q] + ah * d.v[q];
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                su[r][q] = a.v[q];
+                sv[r][q] = b.v[q];
+            }
+        }
+    }
+    // columns x0-1 and x0+4 of the output rows: from the neighbouring lanes, or loaded at the warp
+    // edges (periodic wrap)
+    const int xl = xb == 0 ? (int)nx - 1 : xb - 1;
+    const int xr = xb + 128 == (int)nx ? 0 : xb + 128;
+    T lu[R], lv[R], ru[R], rv[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        lu[r] = __shfl_up_sync(0xffffffffu, su[r + 1][3], 1);
+        lv[r] = __shfl_up_sync(0xffffffffu, sv[r + 1][3], 1);
+        ru[r] = __shfl_down_sync(0xffffffffu, su[r + 1][0], 1);
+        rv[r] = __shfl_down_sync(0xffffffffu, sv[r + 1][0], 1);
+    }
+    if (lane == 0 || lane == 31) {
+        const int xe = lane == 0 ? xl : xr;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int64_t o = (int64_t)(j0 + r) * nx + xe;
+            T eu = __ldg(yu + o), ev = __ldg(yv + o);
+            if (has_k) {
+                eu = eu + ah * __ldg(ku + o);
+                ev = ev + ah * __ldg(kv + o);
+            }
+            if (lane == 0) {
+                lu[r] = eu;
+                lv[r] = ev;
+            } else {
+                ru[r] = eu;
+                rv[r] = ev;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = j0 + r;
+        const int64_t o = (int64_t)j * nx + x0;
+        Vec4<T> du, dv;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            T ul = q == 0 ? lu[r] : su[r + 1][q - 1];
+            T vl = q == 0 ? lv[r] : sv[r + 1][q - 1];
+            T ur = q == 3 ? ru[r] : su[r + 1][q + 1];
+            T vr = q == 3 ? rv[r] : sv[r + 1][q + 1];
+            gs_node<T, POW2>(p, su[r + 1][q], sv[r + 1][q], ul, vl, ur, vr, su[r][q], sv[r][q], su[r + 2][q],
+                             sv[r + 2][q], du.v[q], dv.v[q]);
+        }
+        if constexpr (PASS == 4) {
+            st4((T*)P.ou + o, du);
+            st4((T*)P.ov + o, dv);
+        } else if constexpr (PASS == 1) {
+            Vec4<T> y_u = ld4(yu + o), y_v = ld4(yv + o), k_u = ld4((const T*)P.k0u + o), k_v = ld4((const T*)P.k0v + o);
+            Vec4<T> au, av;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                au.v[q] = (y_u.v[q] + p.bh0 * k_u.v[q]) + p.bh1 * du.v[q];
+                av.v[q] = (y_v.v[q] + p.bh0 * k_v.v[q]) + p.bh1 * dv.v[q];
+            }
+            st4((T*)P.accu + o, au);
+            st4((T*)P.accv + o, av);
+            st4((T*)P.ou + o, du);
+            st4((T*)P.ov + o, dv);
+        } else if constexpr (PASS == 2) {
+            Vec4<T> au = ld4((const T*)P.accu + o), av = ld4((const T*)P.accv + o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                au.v[q] = au.v[q] + p.bh0 * du.v[q];
+                av.v[q] = av.v[q] + p.bh0 * dv.v[q];
+            }
+            st4((T*)P.accu + o, au);
+            st4((T*)P.accv + o, av);
+            st4((T*)P.ou + o, du);
+            st4((T*)P.ov + o, dv);
+        } else {
+            Vec4<T> au = ld4((const T*)P.accu + o), av = ld4((const T*)P.accv + o);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                au.v[q] = au.v[q] + p.bh0 * du.v[q];
+                av.v[q] = av.v[q] + p.bh0 * dv.v[q];
+            }
+            st4((T*)P.ynu + o, au);
+            st4((T*)P.ynv + o, av);
+        }
+    }
+}
+
 // Launchers for one precision (instantiated in stencil.cu and, for the parity build, in
 // inst_parity_stencil.cu with -fmad=false).
 template <class T, bool POW2>
 cudaError_t gs_launch_pass(int pass, const GsPlanes& P, const GsParams<T>& p, cudaStream_t s) {
+    if (p.nx % 128 == 0 && p.ny % 16 == 0) {
+        dim3 blk(128);
+        dim3 grd(p.nx / 128, p.ny / 16);
+        switch (pass) {
+            case 1: gs_pass_vec_kernel<T, POW2, 1><<<grd, blk, 0, s>>>(P, p); break;
+            case 2: gs_pass_vec_kernel<T, POW2, 2><<<grd, blk, 0, s>>>(P, p); break;
+            case 3: gs_pass_vec_kernel<T, POW2, 3><<<grd, blk, 0, s>>>(P, p); break;
+            default: gs_pass_vec_kernel<T, POW2, 4><<<grd, blk, 0, s>>>(P, p); break;
+        }
+        return cudaGetLastError();
+    }
     dim3 blk(64, 4);
     dim3 grd((p.nx + blk.x - 1) / blk.x, (p.ny + blk.y - 1) / blk.y);
     switch (pass) {

@@ -35,10 +35,12 @@ def gpu_rk4(gs, prec, dt, steps, u, v):
     return tu.double().cpu().numpy(), tv.double().cpu().numpy()
 
 
+# (64, 48): one node per thread; (256, 128): the register-blocked 4 x 4 kernel (nx % 128, ny % 16)
+@pytest.mark.parametrize("shape", [(64, 48), (256, 128)])
 @pytest.mark.parametrize("dx", [1.0 / 64, 0.013])  # power of two (exact reciprocal) and not
-def test_gray_scott_rhs_parity(dx):
+def test_gray_scott_rhs_parity(dx, shape):
     torch = pytest.importorskip("torch")
-    nx, ny = 64, 48
+    nx, ny = shape
     gs = gs_struct(nx, ny, dx)
     u, v = small_state(nx, ny)
     du, dv = np.zeros_like(u), np.zeros_like(v)
@@ -51,9 +53,10 @@ def test_gray_scott_rhs_parity(dx):
     assert np.array_equal(gu.cpu().numpy(), du) and np.array_equal(gv.cpu().numpy(), dv)
 
 
+@pytest.mark.parametrize("shape", [(64, 64), (256, 128)])
 @pytest.mark.parametrize("steps", [1, 2, 5])
-def test_gray_scott_rk4_parity(steps):
-    nx, ny = 64, 64
+def test_gray_scott_rk4_parity(steps, shape):
+    nx, ny = shape
     dx = 1.0 / 64
     gs = gs_struct(nx, ny, dx)
     dt = 0.2 * dx * dx / W.GRAY_SCOTT["Du"]
