@@ -124,6 +124,32 @@ DD_HD dd fifth_root_dd(double x, double r0) {
     return fast_two_sum(r0, -c);
 }
 
+// x^(-1/q) as a double-double for q in {5, 8} and finite x in [2^-800, 2^800], without division:
+// an FP32 estimate (about 2^-21), two FP64 Newton steps on s^-q = x,
+//     s <- s ((q+1) - x s^q) / q          (error ~ (q+1)/2 e^2, so 2^-21 -> 2^-40 -> FP64 rounding),
+// then one Newton step whose residual 1 - x s^q is formed in double-double (error ~ 2^-100).
+DD_HD dd inv_root_dd(double xs, int q) {
+    int ex = 0;
+    double m = frexp(xs, &ex);  // xs = m 2^ex, m in [0.5, 1)
+    float t = -((float)ex + log2f((float)m)) / (float)q;
+    float kf = floorf(t);
+    double s = ldexp((double)exp2f(t - kf), (int)kf);
+    const double qd = (double)q, q1 = (double)(q + 1), iq = q == 5 ? 0.2 : 0.125;
+    for (int it = 0; it < 2; ++it) {
+        double s2 = s * s;
+        double s4 = s2 * s2;
+        double sq = q == 5 ? s4 * s : s4 * s4;
+        s = s * (q1 - xs * sq) * iq;
+    }
+    (void)qd;
+    dd s2 = two_prod(s, s);
+    dd s4 = dd_mul(s2, s2);
+    dd sq = q == 5 ? dd_mul_d(s4, s) : dd_mul(s4, s4);
+    dd xsq = dd_mul_d(sq, xs);
+    double e = (1.0 - xsq.hi) - xsq.lo;  // 1 - xsq.hi is exact: xsq.hi is within 2^-50 of 1
+    return fast_two_sum(s, s * e * iq);
+}
+
 // pow(x, y) for the exponents of the crate's controller and initial-step heuristic:
 // y in {0.2, -0.2, 0.125, -0.125} (binary64 values of ±1/5 and ±1/8).  Other y fall back to the
 // platform pow and are not guaranteed to be correctly rounded.
@@ -146,15 +172,15 @@ DD_HD double pow_ctrl(double x, double y) {
         post = ldexp(1.0, fifth ? 160 : 100);
     }
     dd r;
-    if (fifth) {
+    if (y < 0.0) {
+        // the controller's exponents: x^(-1/q) directly
+        r = inv_root_dd(xs, fifth ? 5 : 8);
+        post = 1.0 / post;  // exact: power of two
+    } else if (fifth) {
         double r0 = pow(xs, 0.2);  // starting value, a few ulp from x^(1/5)
         r = fifth_root_dd(xs, r0);
     } else {
         r = dd_sqrt(dd_sqrt(dd_sqrt(dd{xs, 0.0})));
-    }
-    if (y < 0.0) {
-        r = dd_recip(r);
-        post = 1.0 / post;  // exact: power of two
     }
     if (fifth) {
         // binary64 0.2 = (1/5)(1 + 2^-54): multiply by exp(+-2^-54 ln(x) / 5)
