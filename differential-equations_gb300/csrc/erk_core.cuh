@@ -79,6 +79,7 @@ struct Lane {
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
     double rem;    // tf - t (mixed form)
+    float h_lim;   // 1e-14 |h_prev| in FP32 (mixed form's step-size guard)
     bool bounded;  // h_min / h_max differ from the defaults 0 / +inf
     double p[NPP];
     S y[D];
@@ -277,6 +278,7 @@ struct Lane {
         t_prev = t0;
         h_prev = 0.0;
         rem = tf - t0;
+        h_lim = 0.0f;
         bounded = !(a.h_min == 0.0 && isinf(a.h_max) && a.h_max > 0.0);
         steps = acc = rej = fev = 0;
         stiff = nonstiff = 0;
@@ -319,7 +321,13 @@ struct Lane {
     // ----- one Dormand–Prince step attempt: ordinary.rs:63-268 -------------------------------
     // returns 1 accepted, 2 rejected, 3 error
     __device__ int step_dp(const EnsArgs& a) {
-        if (fabs(h) < fabs(h_prev) * 1e-14) {
+        if constexpr (P::KAHAN) {
+            // mixed: the step-size guard on FP32 copies (h_lim = 1e-14 |h_prev|, set on acceptance)
+            if (fabsf((float)h) < h_lim) {
+                status = DEGPU_ERR_STEP_SIZE;
+                return 3;
+            }
+        } else if (fabs(h) < fabs(h_prev) * 1e-14) {
             status = DEGPU_ERR_STEP_SIZE;
             return 3;
         }
@@ -370,7 +378,6 @@ struct Lane {
                 ycn[c] = (S)0;
             }
         }
-        double t_new = t + h;
         fev += NS - 1;
 
         NormT err = (NormT)0, err2 = (NormT)0;
@@ -404,12 +411,13 @@ struct Lane {
         }
         NormT deno = Tab::HAS_BH ? err + (NormT)0.01 * err2 : err;
         if (deno <= (NormT)0) deno = (NormT)1;
-        double scale, errd;
+        double scale, errd = 0.0;
+        float errf = 0.0f;
         if constexpr (P::KAHAN) {
-            // mixed: the normalisation and the controller's power in FP32; the accept/reject
-            // decision on the FP64 value, and h and t in FP64
+            // mixed: the normalisation and the controller's power in FP32 (the error terms are
+            // FP32 data); h, t and the step-size update stay FP64
             float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf((float)h);
-            errd = (double)ef;
+            errf = ef;
             float pw = exp2f(__log2f(ef) * (float)(-1.0 / (double)O));
             scale = (double)fminf(fmaxf((float)a.safety * pw, (float)a.min_scale), (float)a.max_scale);
         } else {
@@ -420,7 +428,14 @@ struct Lane {
         }
 
         int result;
-        if (errd <= 1.0) {
+        // mixed: comparing the FP32 error with 1 is the same decision as after widening it
+        bool accept;
+        if constexpr (P::KAHAN)
+            accept = errf <= 1.0f;
+        else
+            accept = errd <= 1.0;
+        if (accept) {
+            const double t_new = t + h;
             S dydt[D];
             rhs(t_new, ynew, dydt);
             fev += 1;
@@ -456,6 +471,7 @@ struct Lane {
             }
             t_prev = t;
             h_prev = h;
+            if constexpr (P::KAHAN) h_lim = fabsf((float)h) * 1e-14f;
             t = t_new;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
