@@ -36,7 +36,10 @@ VARIANTS = {
     "fp64-plain": (abi.FP64_PARITY, abi.KERNEL_THREAD),
     "fp64fast-persistent": (abi.FP64_FAST, abi.KERNEL_PERSISTENT),
     "mixed-thread": (abi.MIXED, abi.KERNEL_THREAD),
+    # FP32 stages for every instance: the mixed-precision bound switched off for this variant
+    "mixed-persistent-nosplit": (abi.MIXED, abi.KERNEL_PERSISTENT),
 }
+NOSPLIT = {"mixed-persistent-nosplit"}
 
 # Algorithmic FP operations of one attempted DOPRI5 step of a d-dimensional system whose
 # right-hand side costs F operations (mul/add/div/sqrt = 1, pow/sin/cos not counted):
@@ -60,12 +63,13 @@ def flops_of(family, accepted, rejected):
 
 
 def fp64_ops_mixed(family, accepted, rejected):
-    """FP64 operations of the mixed form per attempted step: the norm accumulation (d adds), t and
-    h bookkeeping (~10); the pendulum adds its FP64 stage times and drive phases (6*2 + 7*3)."""
+    """FP64 operations of the mixed form per attempted step: t and h bookkeeping (~8: h * scale,
+    the remaining span, t + h, the step-size guard); the pendulum adds its FP64 stage times and
+    drive phases (6*2 + 7*3)."""
     tot = 0.0
     for rid, (d, _F) in RHS_FLOPS.items():
         m = family == rid
-        per = d + 10 + (33 if rid == abi.RHS["PENDULUM"] else 0)
+        per = 8 + (33 if rid == abi.RHS["PENDULUM"] else 0)
         tot += per * float((accepted[m] + rejected[m]).sum())
     return tot
 
@@ -287,11 +291,16 @@ def run_fpu(args, torch, dev, lib):
     res = {}
     dims_t = keep["dims"]
     beta_t = keep["params"][0]
-    for name, prec in (("fp64", abi.FP64_PARITY), ("mixed", abi.MIXED)):
+    bound = lib.degpu_mixed_min_rtol(abi.DOP853)
+    # "mixed": the library's mixed form, whose precision bound sends every chain (rtol 1e-10) to
+    # FP64; "mixed-nosplit": FP32 stages forced on every chain, which cannot reach rtol 1e-10 —
+    # its attempted steps are capped so that chains whose error estimate sits on the FP32 noise
+    # floor end (as MaxSteps) in bounded time
+    for name, prec in (("fp64", abi.FP64_PARITY), ("mixed", abi.MIXED), ("mixed-nosplit", abi.MIXED)):
         cfg = abi.default_cfg(abi.DOP853)
-        # FP32 stages cannot reach rtol 1e-10: cap the attempted steps of the mixed form so that
-        # instances whose error estimate sits on the FP32 noise floor end (as MaxSteps) in bounded time
-        cfg.precision, cfg.max_steps = prec, e.max_steps if prec != abi.MIXED else args.fpu_mixed_max_steps
+        nosplit = name == "mixed-nosplit"
+        lib.degpu_set_mixed_min_rtol(abi.DOP853, 0.0 if nosplit else bound)
+        cfg.precision, cfg.max_steps = prec, e.max_steps if not nosplit else args.fpu_mixed_max_steps
         f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
                                              C.c_void_p(stream.cuda_stream))
         ms = _clock_ms(f, stream, torch, max(1, args.steps), warmup=False)
@@ -305,6 +314,7 @@ def run_fpu(args, torch, dev, lib):
                                           "max": float(np.max(drift))} if ok.any() else None,
                      "step_attempts": int((out["accepted"] + out["rejected"]).sum().item()),
                      "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}}
+        res[name]["fp64_chains"] = int((e.rtol < (0.0 if nosplit else bound)).sum()) if prec == abi.MIXED else n
         print(json.dumps({"fpu_variant": name, **res[name]}), flush=True)
         if name == "fp64":
             y64 = out["dense"][-1].clone()
@@ -313,14 +323,17 @@ def run_fpu(args, torch, dev, lib):
             d = d[~torch.isnan(d)]
             res[name]["vs_fp64_final"] = ({"median": float(d.median().item()), "max": float(d.max().item())}
                                           if d.numel() else None)
+    lib.degpu_set_mixed_min_rtol(abi.DOP853, bound)
     threads = os.cpu_count() or 1
     s = e.subset(np.arange(args.fpu_cpu_sample))
     s.dim = e.dim
     o, dt = _oracle_solve(s, abi.DOP853, threads)
     line = {"metric": "IVP solves/sec (FPU-beta chains, DOP853 + 64 dense outputs)",
             "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-            "higher_is_better": True, "dtype": "f32-stage/f64-control", "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": f"fpu-beta {n} chains, masses int-logU[2,128], t in [0,100]"}, "variants": res,
+            "higher_is_better": True, "dtype": "f32/f64 mixed (f64 below rtol %g)" % bound,
+            "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": f"fpu-beta {n} chains, masses int-logU[2,128], t in [0,100]",
+                       "mixed_min_rtol": bound}, "variants": res,
             "cpu_baseline": {"value": args.fpu_cpu_sample / dt, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"first {args.fpu_cpu_sample} chains (host libm)"}}
     print(json.dumps(line))
@@ -461,11 +474,13 @@ def run_serving(args, torch, dev, lib):
         out[prec_name] = {"saturated": sat, "sweep": sweep, "sustainable": ok[-1] if ok else sweep[0]}
     line = {"metric": "serving p50/p99 latency and solves/s (continuous batching)",
             "value": out["mixed"]["sustainable"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
-            "higher_is_better": True, "dtype": "f32-stage/f64-control (fp64 beside)",
+            "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 beside)",
             "data": "synthetic (seeded SplitMix64)",
             "config": {"workload": f"{len(reqs)} requests, size int-logU[1,65536] ({total_inst} instances), "
                                    f"VdP/pendulum/Lorenz/FPU(<=64 masses), RK4 h=1e-3 / DOPRI5 / DOP853, "
-                                   f"rtol logU[1e-10,1e-5], t_end U[1,10], 150 GB budget"},
+                                   f"rtol logU[1e-10,1e-5], t_end U[1,10], 150 GB budget",
+                       "mixed_min_rtol": {"dopri5": lib.degpu_mixed_min_rtol(abi.DOPRI5),
+                                          "dop853": lib.degpu_mixed_min_rtol(abi.DOP853)}},
             "results": out}
     print(json.dumps(line))
 
@@ -522,7 +537,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", default="mixed-persistent", choices=list(VARIANTS))
-    ap.add_argument("--compare", default="fp64-plain", help="comma list of extra variants timed once each")
+    ap.add_argument("--compare", default="fp64-plain,mixed-persistent-nosplit",
+                    help="comma list of extra variants timed once each")
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--cpu-sample", type=int, default=12000)
     ap.add_argument("--no-cpu", action="store_true")
@@ -596,6 +612,11 @@ def main():
         if rc != abi.OK:
             raise RuntimeError(f"degpu_solve_ensemble failed: {rc}")
 
+    bound = lib.degpu_mixed_min_rtol(abi.DOPRI5)
+
+    def set_split(variant):
+        lib.degpu_set_mixed_min_rtol(abi.DOPRI5, 0.0 if variant in NOSPLIT else bound)
+
     def timed(cfg, steps, warmup, clocks=None):
         for _ in range(warmup):
             solve_dev(cfg)
@@ -624,6 +645,7 @@ def main():
         return t, ck
 
     cfg = cfg_of(args.variant)
+    set_split(args.variant)
     clocks = Clocks()
     ms, ck = timed(cfg, args.steps, args.warmup, clocks)
     status = d_out["status"].cpu().numpy()
@@ -644,8 +666,15 @@ def main():
     lib.degpu_internal_fma_peak(0, C.byref(pk))
     fp32_peak = pk.value
     total_ops = flops_of(fam, acc, rej)
-    fp64_ops = total_ops if prec != abi.MIXED else fp64_ops_mixed(fam, acc, rej)
-    fp32_ops = 0.0 if prec != abi.MIXED else total_ops - fp64_ops
+    if prec != abi.MIXED:
+        fp64_ops, fp32_ops = total_ops, 0.0
+    else:
+        # instances below the mixed-precision bound run every operation in FP64
+        split = 0.0 if args.variant in NOSPLIT else bound
+        lo = e.rtol < split
+        hi = ~lo
+        fp64_ops = flops_of(fam[lo], acc[lo], rej[lo]) + fp64_ops_mixed(fam[hi], acc[hi], rej[hi])
+        fp32_ops = total_ops - fp64_ops
     t_s = ms * 1e-3 / world
     a64 = fp64_ops / t_s / 1e12
     a32 = fp32_ops / t_s / 1e12
@@ -688,8 +717,14 @@ def main():
 
     extra = {}
     for v in [x for x in args.compare.split(",") if x in VARIANTS and x != args.variant]:
+        set_split(v)
         t, _ = timed(cfg_of(v), 1, 1)
-        extra[v] = {"solves_per_s": n * world / (t * 1e-3), "ms": t}
+        extra[v] = {"solves_per_s": n * world / (t * 1e-3), "ms": t,
+                    "status_counts": {str(k): int(c) for k, c in
+                                      zip(*np.unique(d_out["status"].cpu().numpy(), return_counts=True))}}
+        if v in NOSPLIT and rank == 0 and not args.no_accuracy:
+            extra[v]["accuracy"] = accuracy_report(e, d_out["y_final"].cpu().numpy())
+    set_split(args.variant)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -701,15 +736,20 @@ def main():
     # per solve: persistent variants = 3 planning kernels + 1 multi-family ensemble kernel;
     # thread variants = one ensemble kernel per family
     per_solve = 4 if VARIANTS[args.variant][1] == abi.KERNEL_PERSISTENT else 3
+    if prec == abi.MIXED and args.variant not in NOSPLIT and bound > 0.0:
+        per_solve += 1 if VARIANTS[args.variant][1] == abi.KERNEL_PERSISTENT else 3  # FP64 part
     launches = per_solve * args.steps
     line = {
         "metric": "IVP solves/sec (uneven ensemble, DOPRI5)", "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32-stage/f64-control" if prec == abi.MIXED else "f64",
+        "vs_baseline": None, "dtype": "f32/f64 mixed" if prec == abi.MIXED else "f64",
         "data": "synthetic (seeded SplitMix64)",
         "config": {"workload": f"uneven ensemble {n} instances/GPU: 1/3 Van der Pol, 1/3 damped driven pendulum, "
                                f"1/3 Lorenz; t_end~U[5,50], rtol~logU[1e-9,1e-5], DOPRI5",
-                   "variant": args.variant, "l2": "flushed (256 MB write) between timed iterations"},
+                   "variant": args.variant, "l2": "flushed (256 MB write) between timed iterations",
+                   "mixed_min_rtol": (0.0 if args.variant in NOSPLIT else bound) if prec == abi.MIXED else None,
+                   "fp64_instances": int((e.rtol < bound).sum()) if prec == abi.MIXED and args.variant not in NOSPLIT
+                   else (n if prec != abi.MIXED else 0)},
         "steps_per_s": steps_per_s,
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
         "roofline": roof,

@@ -95,13 +95,13 @@ struct Lane {
 
     __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const { Rhs::template diff<P>(tt, yy, dd, p); }
 
-    // Type of the per-component error terms and their sum: FP64 except in the mixed form, whose
-    // terms come from FP32 stage data (and whose sum therefore gains nothing from FP64).
-    using NormT = typename Select<P::KAHAN, float, double>::type;
+    // Type of the per-component error terms and their sum: FP64, except in the mixed form built
+    // with the FP32 controller (P::F32_CTRL), whose terms are FP32 stage data.
+    using NormT = typename Select<P::F32_CTRL, float, double>::type;
 
     __device__ __forceinline__ NormT norm_term(S e, S yv, S ynv) const {
         // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
-        if constexpr (P::KAHAN) {
+        if constexpr (P::F32_CTRL) {
             float sk = (float)atol + (float)rtol * fmaxf(fabsf(yv), fabsf(ynv));
             float q = __fdividef(e, sk);
             return q * q;
@@ -321,7 +321,7 @@ struct Lane {
     // ----- one Dormand–Prince step attempt: ordinary.rs:63-268 -------------------------------
     // returns 1 accepted, 2 rejected, 3 error
     __device__ int step_dp(const EnsArgs& a) {
-        if constexpr (P::KAHAN) {
+        if constexpr (P::F32_CTRL) {
             // mixed: the step-size guard on FP32 copies (h_lim = 1e-14 |h_prev|, set on acceptance)
             if (fabsf((float)h) < h_lim) {
                 status = DEGPU_ERR_STEP_SIZE;
@@ -413,9 +413,9 @@ struct Lane {
         if (deno <= (NormT)0) deno = (NormT)1;
         double scale, errd = 0.0;
         float errf = 0.0f;
-        if constexpr (P::KAHAN) {
-            // mixed: the normalisation and the controller's power in FP32 (the error terms are
-            // FP32 data); h, t and the step-size update stay FP64
+        if constexpr (P::F32_CTRL) {
+            // mixed with the FP32 controller: the normalisation and the controller's power in
+            // FP32 (the error terms are FP32 data); h, t and the step-size update stay FP64
             float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf((float)h);
             errf = ef;
             float pw = exp2f(__log2f(ef) * (float)(-1.0 / (double)O));
@@ -430,7 +430,7 @@ struct Lane {
         int result;
         // mixed: comparing the FP32 error with 1 is the same decision as after widening it
         bool accept;
-        if constexpr (P::KAHAN)
+        if constexpr (P::F32_CTRL)
             accept = errf <= 1.0f;
         else
             accept = errd <= 1.0;
@@ -471,7 +471,7 @@ struct Lane {
             }
             t_prev = t;
             h_prev = h;
-            if constexpr (P::KAHAN) h_lim = fabsf((float)h) * 1e-14f;
+            if constexpr (P::F32_CTRL) h_lim = fabsf((float)h) * 1e-14f;
             t = t_new;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
@@ -784,7 +784,8 @@ struct Parked {
 // Resumable persistent form used by the server: every instance is visited once per round; a
 // visit resumes the parked state (or starts the instance), advances it by at most `budget`
 // driver iterations, then parks it again or finishes it.  `done_count` counts finished
-// instances across rounds.
+// instances across rounds.  Slot w of `park` holds work item w: instance a.index[w] when an
+// index list is given (a request split by precision), else instance w.
 template <class Tab, class Rhs, class P, bool DENSE>
 __global__ void __launch_bounds__(128) erk_round_kernel(EnsArgs a, Parked<Lane<Tab, Rhs, P, DENSE>>* park,
                                                         int budget, unsigned long long* done_count) {
@@ -796,7 +797,7 @@ __global__ void __launch_bounds__(128) erk_round_kernel(EnsArgs a, Parked<Lane<T
         if (phase == 2) continue;
         Lane<Tab, Rhs, P, DENSE> L;
         if (phase == 0) {
-            L.begin((int64_t)w, a);
+            L.begin(a.index ? a.index[w] : (int64_t)w, a);
         } else {
             L = slot.lane;
         }

@@ -4,6 +4,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <tuple>
 #include <vector>
 
 #include "group_erk.cuh"
@@ -109,14 +110,24 @@ degpu_status wps_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, con
         cudaStreamSynchronize(s) != cudaSuccess)
         return DEGPU_CUDA_ERROR;
     const int dense = a.n_eval > 0 ? 1 : 0;
-    // buckets keyed by the chosen (G, CPL)
-    std::map<std::pair<int, int>, std::vector<int64_t>> buckets;
+    // a mixed solve sends instances with rtol below the mixed-precision bound to FP64_FAST
+    const double split = mixed_split(cfg);
+    std::vector<double> rtol_host;
+    if (split > 0.0) {
+        rtol_host.resize(n);
+        if (cudaMemcpyAsync(rtol_host.data(), a.rtol, n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    // buckets keyed by (precision, G, CPL)
+    std::map<std::tuple<int, int, int>, std::vector<int64_t>> buckets;
     for (int64_t i = 0; i < n; ++i) {
         int d = hd[i];
         if (d <= 0 || d > pb->dim || (d & 1)) return DEGPU_BAD_INPUT;
-        GroupChoice c = choose(cfg->method, cfg->precision, dense, d);
+        const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
+        GroupChoice c = choose(cfg->method, prec, dense, d);
         if (c.dmax < 0) return DEGPU_UNSUPPORTED;
-        buckets[{c.g, c.cpl}].push_back(i);
+        buckets[{prec, c.g, c.cpl}].push_back(i);
     }
     // longest first inside a bucket: the largest systems start first, the tail holds small ones
     for (auto& b : buckets)
@@ -124,7 +135,8 @@ degpu_status wps_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, con
     std::vector<void*> to_free;
     degpu_status st = DEGPU_OK;
     for (auto& b : buckets) {
-        auto it = group_registry().find(GroupKey{cfg->method, cfg->precision, dense, b.first.first, b.first.second});
+        const int prec = std::get<0>(b.first);
+        auto it = group_registry().find(GroupKey{cfg->method, prec, dense, std::get<1>(b.first), std::get<2>(b.first)});
         if (it == group_registry().end()) {
             st = DEGPU_UNSUPPORTED;
             break;

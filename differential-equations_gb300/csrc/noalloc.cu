@@ -22,15 +22,16 @@ namespace degpu {
 
 namespace {
 
-constexpr int NA_NB = 128;  // cost buckets per family
+constexpr int NA_NB = 128;    // cost buckets per family
+constexpr int NA_LISTS = 6;   // (precision class, family): class 1 = FP64 part of a mixed solve
 constexpr int64_t NA_MAX = DEGPU_NOALLOC_MAX_INSTANCES;
 
 // layout of the scratch array (bytes)
-constexpr size_t NA_CELLS = 0;                                   // int[3 * NA_NB]
-constexpr size_t NA_START = NA_CELLS + 3 * NA_NB * 4;            // int64[3]
-constexpr size_t NA_COUNT = NA_START + 3 * 8;                    // int64[3]
-constexpr size_t NA_HEAD = NA_COUNT + 3 * 8;                     // u64[3]
-constexpr size_t NA_ZERO_END = NA_HEAD + 3 * 8;                  // cleared by every call
+constexpr size_t NA_CELLS = 0;                                   // int[NA_LISTS * NA_NB]
+constexpr size_t NA_START = NA_CELLS + NA_LISTS * NA_NB * 4;     // int64[NA_LISTS]
+constexpr size_t NA_COUNT = NA_START + NA_LISTS * 8;             // int64[NA_LISTS]
+constexpr size_t NA_HEAD = NA_COUNT + NA_LISTS * 8;              // u64[NA_LISTS]
+constexpr size_t NA_ZERO_END = NA_HEAD + NA_LISTS * 8;           // cleared by every call
 constexpr size_t NA_ITEMS = (NA_ZERO_END + 255) / 256 * 256;     // int64[NA_MAX]
 constexpr size_t NA_POS = NA_ITEMS + (size_t)NA_MAX * 8;         // int[NA_MAX]
 constexpr size_t NA_KEY = NA_POS + (size_t)NA_MAX * 4;           // int[NA_MAX]
@@ -59,10 +60,11 @@ __device__ __forceinline__ int na_slot(int id) {
     return id == DEGPU_RHS_VAN_DER_POL ? 0 : id == DEGPU_RHS_PENDULUM ? 1 : id == DEGPU_RHS_LORENZ ? 2 : -1;
 }
 
-// Cost key and (family, bucket) position; an instance of another family is reported as BadInput
-// and left out of the lists.
+// Precision class (1: rtol below the mixed-precision bound `split`), cost key and (class,
+// family, bucket) position; an instance of another family is reported as BadInput and left out
+// of the lists.
 __global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, const double* rtol,
-                                const int32_t* family, int fam_const, double inv_order, double h0,
+                                const int32_t* family, int fam_const, double inv_order, double h0, double split,
                                 unsigned char* scratch, int32_t* status) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -80,7 +82,8 @@ __global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, c
     if (!isfinite(c)) c = 0.0;
     int b = (int)floor((c + 24.0) * 1.5);
     b = b < 0 ? 0 : (b > NA_NB - 1 ? NA_NB - 1 : b);
-    int k = f * NA_NB + (NA_NB - 1 - b);
+    const int cls = rtol[i] < split ? 1 : 0;
+    int k = (cls * 3 + f) * NA_NB + (NA_NB - 1 - b);
     pos[i] = atomicAdd(&cells[k], 1);
     key[i] = k;
 }
@@ -91,7 +94,7 @@ __global__ void na_scan_kernel(unsigned char* scratch) {
     int64_t* start = (int64_t*)(scratch + NA_START);
     int64_t* count = (int64_t*)(scratch + NA_COUNT);
     int64_t run = 0;
-    for (int f = 0; f < 3; ++f) {
+    for (int f = 0; f < NA_LISTS; ++f) {
         start[f] = run;
         for (int b = 0; b < NA_NB; ++b) {
             int c = cells[f * NA_NB + b];
@@ -142,6 +145,13 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     ensure_registered();
     auto it = multi_registry().find({cfg->method, cfg->precision, 0});
     if (it == multi_registry().end()) return DEGPU_UNSUPPORTED;
+    const double split = mixed_split(cfg);
+    MultiLaunchFn fp64_launch = nullptr;
+    if (split > 0.0) {
+        auto it64 = multi_registry().find({cfg->method, DEGPU_FP64_FAST, 0});
+        if (it64 == multi_registry().end()) return DEGPU_UNSUPPORTED;
+        fp64_launch = it64->second;
+    }
     void* base = nullptr;
     degpu_status st = scratch_address(&base);
     if (st != DEGPU_OK) return st;
@@ -154,7 +164,7 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     na_count_kernel<<<blocks, 256, 0, s>>>(n, in->t0, in->tf, in->rtol, in->family, pb->rhs_id, inv_order,
-                                           cfg->h0 != 0.0 ? cfg->h0 : 1.0, scratch, out->status);
+                                           cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, scratch, out->status);
     na_scan_kernel<<<1, 32, 0, s>>>(scratch);
     na_scatter_kernel<<<blocks, 256, 0, s>>>(n, scratch);
     if (cudaGetLastError() != cudaSuccess) return DEGPU_CUDA_ERROR;
@@ -184,10 +194,15 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     a.max_scale = cfg->max_scale;
     a.dense_mode = cfg->dense_mode;
     a.n_params = pb->n_params;
-    MultiQueue q;
-    q.items = (const int64_t*)(scratch + NA_ITEMS);
-    q.start = (const int64_t*)(scratch + NA_START);
-    q.count = (const int64_t*)(scratch + NA_COUNT);
-    q.head = (unsigned long long*)(scratch + NA_HEAD);
+    const int64_t* items = (const int64_t*)(scratch + NA_ITEMS);
+    const int64_t* start = (const int64_t*)(scratch + NA_START);
+    const int64_t* count = (const int64_t*)(scratch + NA_COUNT);
+    unsigned long long* head = (unsigned long long*)(scratch + NA_HEAD);
+    // the FP64 lists of a mixed solve first (class 1: lists 3..5), then class 0
+    if (fp64_launch) {
+        MultiQueue q64{items, start + 3, count + 3, head + 3};
+        if (fp64_launch(a, q64, n, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    }
+    MultiQueue q{items, start, count, head};
     return it->second(a, q, n, s) == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
 }

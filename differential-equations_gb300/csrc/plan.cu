@@ -1,10 +1,14 @@
 // plan.cu — longest-first work lists for the multi-family persistent kernel.
 //
 // Three small kernels, no host round trip:
-//   count   : each instance gets a cost key |tf - t0| * rtol^(-1/order) (log2 scale, 128 buckets,
-//             descending) and a position inside its (family, bucket) cell by atomic increment;
-//   scan    : exclusive scan over the 3 x 128 cells -> list offsets, list starts and lengths;
+//   count   : each instance gets a precision class (1 when a mixed solve sends it to FP64
+//             because its rtol is below the mixed-precision bound, else 0), a cost key
+//             |tf - t0| * rtol^(-1/order) (log2 scale, 128 buckets, descending) and a position
+//             inside its (class, family, bucket) cell by atomic increment;
+//   scan    : exclusive scan over the 2 x 3 x 128 cells -> list offsets, list starts and lengths;
 //   scatter : items[offset(cell) + position] = instance.
+// Then one persistent launch per class: FP64 first (its instances are the most expensive ones),
+// the mixed kernel after it.
 // Ordering inside a bucket follows the atomics and is not deterministic; every instance's result
 // is independent of the order in which instances are taken, so solutions are deterministic.
 #include <cuda_runtime.h>
@@ -25,9 +29,11 @@ __device__ __forceinline__ int fam_slot(int id) {
     return id == DEGPU_RHS_VAN_DER_POL ? 0 : id == DEGPU_RHS_PENDULUM ? 1 : id == DEGPU_RHS_LORENZ ? 2 : -1;
 }
 
+static constexpr int NLISTS = 6;  // (class, family)
+
 __global__ void plan_count_kernel(int64_t n, const double* t0, const double* tf, const double* rtol,
-                                  const int32_t* family, int fam_const, double inv_order, double h0, int* cells,
-                                  int* pos, int* key, int* bad) {
+                                  const int32_t* family, int fam_const, double inv_order, double h0, double split,
+                                  int* cells, int* pos, int* key, int* bad) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int f = fam_slot(family ? family[i] : fam_const);
@@ -40,7 +46,8 @@ __global__ void plan_count_kernel(int64_t n, const double* t0, const double* tf,
     if (!isfinite(c)) c = 0.0;
     int b = (int)floor((c + 24.0) * 1.5);
     b = b < 0 ? 0 : (b > NB - 1 ? NB - 1 : b);
-    int k = f * NB + (NB - 1 - b);  // descending cost
+    const int cls = rtol[i] < split ? 1 : 0;  // split = 0: every instance in class 0
+    int k = (cls * 3 + f) * NB + (NB - 1 - b);  // descending cost
     pos[i] = atomicAdd(&cells[k], 1);
     key[i] = k;
 }
@@ -48,7 +55,7 @@ __global__ void plan_count_kernel(int64_t n, const double* t0, const double* tf,
 __global__ void plan_scan_kernel(int* cells, int64_t* start, int64_t* count) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int64_t run = 0;
-    for (int f = 0; f < 3; ++f) {
+    for (int f = 0; f < NLISTS; ++f) {
         start[f] = run;
         for (int b = 0; b < NB; ++b) {
             int c = cells[f * NB + b];
@@ -65,43 +72,53 @@ __global__ void plan_scatter_kernel(int64_t n, const int* pos, const int* key, c
     items[cells[key[i]] + pos[i]] = i;
 }
 
-// Plans and launches one multi-family persistent solve.  Returns DEGPU_UNSUPPORTED when a
-// family outside {Van der Pol, pendulum, Lorenz} is present (checked on the host when the family
-// map is known; `family_host` may be NULL for single-family batches).
+// Plans and launches one multi-family persistent solve (two launches when a mixed solve splits
+// by rtol).  Returns DEGPU_UNSUPPORTED when no kernel is registered for the combination.
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
                          bool dense, cudaStream_t s) {
-    auto it = multi_registry().find({cfg->method, cfg->precision, dense ? 1 : 0});
+    const int d = dense ? 1 : 0;
+    auto it = multi_registry().find({cfg->method, cfg->precision, d});
     if (it == multi_registry().end()) return DEGPU_UNSUPPORTED;
+    const double split = mixed_split(cfg);
+    MultiLaunchFn fp64_launch = nullptr;
+    if (split > 0.0) {
+        auto it64 = multi_registry().find({cfg->method, DEGPU_FP64_FAST, d});
+        if (it64 == multi_registry().end()) return DEGPU_UNSUPPORTED;
+        fp64_launch = it64->second;
+    }
     const int64_t n = a.n;
-    // one scratch block: cells, pos, key, items, start, count, head, bad
-    size_t bytes = NB * 3 * 4 + n * 4 + n * 4 + n * 8 + 3 * 8 + 3 * 8 + 3 * 8 + 8 + 64;
+    // one scratch block: cells, start, count, head, bad, items, pos, key
+    const size_t cells_bytes = ((size_t)NB * NLISTS * 4 + 7) / 8 * 8;
+    const size_t head_bytes = cells_bytes + NLISTS * 8 * 3 + 8;
+    size_t bytes = head_bytes + n * 8 + n * 4 + n * 4 + 64;
     char* blk = nullptr;
     if (cudaMallocAsync((void**)&blk, bytes, s) != cudaSuccess) return DEGPU_OOM;
     int* cells = (int*)blk;
-    int64_t* start = (int64_t*)(blk + ((NB * 3 * 4 + 7) / 8) * 8);
-    int64_t* count = start + 3;
-    unsigned long long* head = (unsigned long long*)(count + 3);
-    int* bad = (int*)(head + 3);
-    int64_t* items = (int64_t*)(bad + 2);
+    int64_t* start = (int64_t*)(blk + cells_bytes);
+    int64_t* count = start + NLISTS;
+    unsigned long long* head = (unsigned long long*)(count + NLISTS);
+    int* bad = (int*)(head + NLISTS);
+    int64_t* items = (int64_t*)(blk + head_bytes);
     int* pos = (int*)(items + n);
     int* key = pos + n;
     degpu_status st = DEGPU_OK;
-    if (cudaMemsetAsync(blk, 0, (char*)items - blk, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
+    if (cudaMemsetAsync(blk, 0, head_bytes, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
     const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
     unsigned blocks = (unsigned)((n + 255) / 256);
     if (st == DEGPU_OK) {
         plan_count_kernel<<<blocks, 256, 0, s>>>(n, a.t0, a.tf, a.rtol, family_dev, fam_const, inv_order,
-                                                  cfg->h0 != 0.0 ? cfg->h0 : 1.0, cells, pos, key, bad);
+                                                  cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, cells, pos, key, bad);
         plan_scan_kernel<<<1, 32, 0, s>>>(cells, start, count);
         plan_scatter_kernel<<<blocks, 256, 0, s>>>(n, pos, key, cells, items);
         if (cudaGetLastError() != cudaSuccess) st = DEGPU_CUDA_ERROR;
     }
+    // class 1 (FP64) lists: start/count/head [3..6); class 0: [0..3)
+    if (st == DEGPU_OK && fp64_launch) {
+        MultiQueue q{items, start + 3, count + 3, head + 3};
+        if (fp64_launch(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
+    }
     if (st == DEGPU_OK) {
-        MultiQueue q;
-        q.items = items;
-        q.start = start;
-        q.count = count;
-        q.head = head;
+        MultiQueue q{items, start, count, head};
         if (it->second(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
     }
     cudaFreeAsync(blk, s);

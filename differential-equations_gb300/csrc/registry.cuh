@@ -137,9 +137,14 @@ void register_parity_multi();
 void register_multi_fast_mixed();
 void ensure_registered();
 
-// Longest-first planning + one multi-family persistent launch (plan.cu).
+// Longest-first planning + one multi-family persistent launch per precision class (plan.cu).
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
                          bool dense, cudaStream_t s);
+
+// Mixed-precision split of a solve (degpu_set_mixed_min_rtol): the rtol bound below which an
+// instance of a DEGPU_MIXED solve runs the DEGPU_FP64_FAST variant; 0 when cfg asks for another
+// precision or for RK4.
+double mixed_split(const degpu_method_cfg* cfg);
 
 // Right-hand-side evaluation kernels (degpu_eval_rhs)
 using RhsLaunchFn = cudaError_t (*)(int64_t n, const double* t, const double* y, const double* p, double* dydt,

@@ -43,6 +43,14 @@ struct SrvRequest {
     size_t bytes = 0;
     bool resumable = false;
     RoundOps ops{};
+    // mixed request split by rtol (degpu_set_mixed_min_rtol): idx[0] runs `ops`, idx[1] the
+    // FP64_FAST round kernels `ops64`, each with its own resident state and work ticket
+    bool split = false;
+    std::vector<int64_t> idx[2];
+    RoundOps ops64{};
+    EnsArgs args64{};
+    void* park64 = nullptr;
+    unsigned long long* ticket64 = nullptr;
     // device side
     cudaStream_t stream = nullptr;
     cudaEvent_t ev = nullptr;
@@ -77,7 +85,11 @@ struct ServerImpl {
         const size_t m = (size_t)(r.in.n_eval > 0 ? r.in.n_eval : 0);
         size_t b = align(n * 8) * 6 + align(d * n * 8) * 2 + align(np * n * 8) + align(n * 4) * 3 + align(n * 8) * 3;
         b += align(m * 8) + align(m * d * n * 8);
-        if (r.resumable) b += align(n * r.ops.park_bytes) + 512;
+        if (r.resumable && !r.split) b += align(n * r.ops.park_bytes) + 512;
+        if (r.split) {
+            b += align(r.idx[0].size() * 8) + align(r.idx[1].size() * 8);
+            b += align(r.idx[0].size() * r.ops.park_bytes) + align(r.idx[1].size() * r.ops64.park_bytes) + 1024;
+        }
         return b;
     }
 
@@ -123,10 +135,11 @@ struct ServerImpl {
             }
             return true;
         }
-        r.park = take(n * r.ops.park_bytes);
+        const size_t n0 = r.split ? r.idx[0].size() : n;
+        r.park = take(n0 * r.ops.park_bytes);
         r.ticket = (unsigned long long*)take(16);
         r.done_dev = (unsigned long long*)take(16);
-        cudaMemsetAsync(r.park, 0, n * r.ops.park_bytes, s);  // phase 0: not started
+        cudaMemsetAsync(r.park, 0, n0 * r.ops.park_bytes, s);  // phase 0: not started
         cudaMemsetAsync(r.done_dev, 0, 8, s);
         EnsArgs& a = r.args;
         a = EnsArgs{};
@@ -155,11 +168,27 @@ struct ServerImpl {
         a.dense_mode = r.cfg.dense_mode;
         a.n_params = r.pb.n_params;
         a.ticket = r.ticket;
+        if (r.split) {
+            const size_t n1 = r.idx[1].size();
+            a.index = (const int64_t*)up(r.idx[0].data(), n0 * 8);
+            a.count = (int64_t)n0;
+            r.args64 = a;
+            r.args64.index = (const int64_t*)up(r.idx[1].data(), n1 * 8);
+            r.args64.count = (int64_t)n1;
+            r.park64 = take(n1 * r.ops64.park_bytes);
+            r.ticket64 = (unsigned long long*)take(16);
+            r.args64.ticket = r.ticket64;
+            cudaMemsetAsync(r.park64, 0, n1 * r.ops64.park_bytes, s);
+        }
         return launch_round(r);
     }
 
     bool launch_round(SrvRequest& r) {
         cudaStream_t s = r.stream;
+        if (r.split) {
+            if (cudaMemsetAsync(r.ticket64, 0, 8, s) != cudaSuccess) return false;
+            if (r.ops64.launch(r.args64, r.park64, cfg.round_budget, r.done_dev, 0, s) != cudaSuccess) return false;
+        }
         if (cudaMemsetAsync(r.ticket, 0, 8, s) != cudaSuccess) return false;
         if (r.ops.launch(r.args, r.park, cfg.round_budget, r.done_dev, 0, s) != cudaSuccess) return false;
         cudaMemcpyAsync(r.done_host, r.done_dev, 8, cudaMemcpyDeviceToHost, s);
@@ -315,6 +344,23 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
         if (it != round_registry().end()) {
             r->resumable = true;
             r->ops = it->second;
+        }
+        // a mixed request whose rtol values straddle the mixed-precision bound: the instances
+        // below it run the FP64_FAST round kernels
+        const double bound = mixed_split(cfg);
+        auto it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, DEGPU_FP64_FAST, 0});
+        if (r->resumable && bound > 0.0) {
+            if (it64 == round_registry().end()) return DEGPU_UNSUPPORTED;
+            for (int64_t i = 0; i < in->n; ++i) r->idx[in->rtol[i] < bound ? 1 : 0].push_back(i);
+            if (r->idx[1].empty()) {
+                r->idx[0].clear();
+            } else if (r->idx[0].empty()) {
+                r->ops = it64->second;  // every instance below the bound: a plain FP64_FAST request
+                r->idx[1].clear();
+            } else {
+                r->split = true;
+                r->ops64 = it64->second;
+            }
         }
     }
     r->bytes = I.footprint(*r);

@@ -19,7 +19,7 @@ import numpy as np
 from . import abi
 
 __all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
-           "Solution"]
+           "Solution", "set_mixed_min_rtol", "mixed_min_rtol"]
 
 STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
                 abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness"}
@@ -146,6 +146,18 @@ class EnsembleResult:
     rejected: np.ndarray
     fevals: np.ndarray
     status: np.ndarray
+
+
+def set_mixed_min_rtol(method: int, min_rtol: float) -> None:
+    """Mixed-precision bound of DOPRI5 / DOP853 (degpu_set_mixed_min_rtol): in a MIXED solve an
+    instance with rtol below it runs in FP64_FAST arithmetic; 0 disables the split."""
+    rc = abi.load().degpu_set_mixed_min_rtol(method, float(min_rtol))
+    if rc != abi.OK:
+        raise DegpuError(rc, "degpu_set_mixed_min_rtol")
+
+
+def mixed_min_rtol(method: int) -> float:
+    return abi.load().degpu_mixed_min_rtol(method)
 
 
 def _f64(a, shape=None):

@@ -85,6 +85,8 @@ _lib = None
 SIGNATURES = {
     "degpu_default_cfg": (None, [C.POINTER(MethodCfg), C.c_int32]),
     "degpu_rhs_info": (C.c_int, [C.c_int32, I32P, I32P]),
+    "degpu_set_mixed_min_rtol": (C.c_int, [C.c_int32, C.c_double]),
+    "degpu_mixed_min_rtol": (C.c_double, [C.c_int32]),
     "degpu_solve_ensemble": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
                                        C.POINTER(BatchOut), C.c_void_p]),
     "degpu_solve_ensemble_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),

@@ -22,8 +22,10 @@ import numpy as np
 from . import abi
 from . import workloads as W
 
-CANDIDATES = {8: [(8, 1)], 16: [(16, 1)], 32: [(32, 1), (16, 2)], 64: [(32, 2), (16, 4)], 128: [(32, 4)],
-              256: [(32, 8)]}
+CANDIDATES = {8: [(8, 1), (16, 1), (32, 1)], 16: [(16, 1), (32, 1)], 32: [(32, 1), (16, 2)],
+              64: [(32, 2), (16, 4)], 128: [(32, 4)], 256: [(32, 8)]}
+# DOPRI5 has no (16, CPL > 1) kernels: its buckets of 32 and 64 keep the 32-lane layouts
+DOPRI5_MISSING = {(16, 2), (16, 4)}
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNE_TXT = os.path.join(HERE, "group_tune.txt")
 TUNE_JSON = os.path.join(HERE, "group_tune.json")
@@ -45,6 +47,8 @@ def tune(method=abi.DOP853, precision=abi.FP64_PARITY, dense=True, per_bucket=10
     choices = []
     lo = 0
     for dmax, cands in CANDIDATES.items():
+        if method == abi.DOPRI5:
+            cands = [c for c in cands if c not in DOPRI5_MISSING]
         sel = np.nonzero((pool.dims > lo) & (pool.dims <= dmax))[0][:per_bucket]
         lo = dmax
         if len(sel) == 0:
@@ -52,6 +56,10 @@ def tune(method=abi.DOP853, precision=abi.FP64_PARITY, dense=True, per_bucket=10
             continue
         e = pool.subset(sel)
         e.tf[:] = horizon
+        if precision == abi.MIXED:
+            # the FP32-stage kernels run only above the mixed-precision bound: tune them there
+            e.rtol[:] = max(1e-6, 10.0 * lib.degpu_mixed_min_rtol(method))
+            e.atol = 1e-2 * e.rtol
         te = np.linspace(0.0, horizon, 8) if dense else None
         m = degpu.ExplicitRungeKutta(method)
         m.cfg.precision, m.cfg.max_steps = precision, 10_000_000
@@ -72,8 +80,15 @@ def tune(method=abi.DOP853, precision=abi.FP64_PARITY, dense=True, per_bucket=10
 
 
 def save(results):
+    """Merges `results` into the files: entries of other (method, precision, dense) keys stay."""
+    merged = {}
+    if os.path.exists(TUNE_JSON):
+        with open(TUNE_JSON) as f:
+            for b in json.load(f):
+                merged[(b["method"], b["precision"], b["dense"])] = b["buckets"]
+    merged.update(results)
     lines, blob = [], []
-    for (method, prec, dense), choices in results.items():
+    for (method, prec, dense), choices in sorted(merged.items()):
         for c in choices:
             lines.append(f"{method} {prec} {dense} {c['dmax']} {c['g']} {c['cpl']}")
         blob.append({"method": method, "precision": prec, "dense": dense, "buckets": choices})

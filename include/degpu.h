@@ -61,7 +61,9 @@ typedef enum { DEGPU_RK4 = 0, DEGPU_DOPRI5 = 1, DEGPU_DOP853 = 2 } degpu_method;
  *                pow/sin/cos: reproduces the crate's step counts and states bit for bit.
  *  FP64_FAST   — FP64 with FMA contraction and the fast CUDA math library.
  *  MIXED       — stage right-hand sides and stage combinations in FP32, y_{n+1} accumulated with
- *                Kahan compensation; t, h, the error norm and the step-size controller in FP64. */
+ *                Kahan compensation; t, h, the error norm and the step-size controller in FP64.
+ *                Instances whose rtol is below the method's mixed-precision bound
+ *                (degpu_set_mixed_min_rtol) run in FP64_FAST arithmetic instead. */
 typedef enum { DEGPU_FP64_PARITY = 0, DEGPU_FP64_FAST = 1, DEGPU_MIXED = 2 } degpu_precision;
 
 /* Kernel layout. AUTO picks by method and dimension. */
@@ -154,6 +156,20 @@ typedef struct {
 
 /* Fill `cfg` with the crate's defaults (src/methods/erk/mod.rs:112-159) for `method`. */
 void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method);
+
+/* Mixed-precision bound of an adaptive method (no counterpart in the crate, which is FP64 only).
+ * FP32 stages cannot meet tolerances near their own rounding level: the embedded error estimate
+ * stalls at the FP32 noise floor, the controller keeps rejecting and the instance ends in
+ * MaxSteps.  So in a DEGPU_MIXED solve an instance with rtol < min_rtol runs in DEGPU_FP64_FAST
+ * arithmetic; the choice depends on the instance's own rtol only, so a result does not depend on
+ * the batch it is solved in.  min_rtol = 0 disables the split.  The setting is process-wide and
+ * applies to solves launched after the call; the environment variable DEGPU_MIXED_MIN_RTOL, read
+ * at the first solve, replaces the defaults of both methods.  RK4 (fixed step) has no bound.
+ * Returns DEGPU_BAD_INPUT for RK4, an unknown method, or a negative or non-finite min_rtol. */
+degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol);
+
+/* The bound in force for `method` (0 for RK4 and unknown methods). */
+double degpu_mixed_min_rtol(int32_t method);
 
 /* Dimension and parameter count of a built-in family (dim = -1 for variable-size families).
  * Returns DEGPU_BAD_INPUT for an unknown id. */

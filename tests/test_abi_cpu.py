@@ -68,3 +68,22 @@ def test_bad_input_rejected_before_any_launch():
     assert lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(abi.BatchIn(n=0)), C.byref(bo),
                                     None) == abi.OK
     assert lib.degpu_status_string(abi.BAD_INPUT) == b"bad input"
+
+
+def test_mixed_min_rtol_setting():
+    lib = abi.load()
+    old5, old8 = lib.degpu_mixed_min_rtol(abi.DOPRI5), lib.degpu_mixed_min_rtol(abi.DOP853)
+    assert old5 >= 0.0 and old8 >= 0.0
+    assert lib.degpu_mixed_min_rtol(abi.RK4) == 0.0  # fixed step: no bound
+    try:
+        assert lib.degpu_set_mixed_min_rtol(abi.DOP853, 3e-9) == abi.OK
+        assert lib.degpu_mixed_min_rtol(abi.DOP853) == 3e-9
+        assert lib.degpu_mixed_min_rtol(abi.DOPRI5) == old5
+        assert lib.degpu_set_mixed_min_rtol(abi.DOPRI5, 0.0) == abi.OK  # split off
+        assert lib.degpu_set_mixed_min_rtol(abi.RK4, 1e-9) == abi.BAD_INPUT
+        assert lib.degpu_set_mixed_min_rtol(9, 1e-9) == abi.BAD_INPUT
+        assert lib.degpu_set_mixed_min_rtol(abi.DOPRI5, -1.0) == abi.BAD_INPUT
+        assert lib.degpu_set_mixed_min_rtol(abi.DOPRI5, float("nan")) == abi.BAD_INPUT
+    finally:
+        lib.degpu_set_mixed_min_rtol(abi.DOPRI5, old5)
+        lib.degpu_set_mixed_min_rtol(abi.DOP853, old8)

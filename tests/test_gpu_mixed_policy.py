@@ -1,0 +1,83 @@
+"""Mixed-precision bound (degpu_set_mixed_min_rtol): in a MIXED solve, instances with rtol below
+the bound run the FP64_FAST arithmetic and the others the FP32-stage form.  Each instance's result
+must equal, bit for bit, the same instance solved by the arithmetic its rtol selects, on every
+kernel layout (persistent multi-family, one system per thread, group per system)."""
+import numpy as np
+import pytest
+
+import degpu
+from degpu import abi, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+BOUND = 1e-8
+
+
+@pytest.fixture
+def bound():
+    old = {m: degpu.mixed_min_rtol(m) for m in (abi.DOPRI5, abi.DOP853)}
+    yield
+    for m, v in old.items():
+        degpu.set_mixed_min_rtol(m, v)
+
+
+def straddling(n, first=0):
+    e = W.config1(n=n, first=first)
+    e.tf = np.minimum(e.tf, 8.0)
+    e.rtol = W.logU(7, np.arange(first, first + n), 1, 1e-10, 1e-6)
+    e.atol = 1e-2 * e.rtol
+    return e
+
+
+def run(e, method, prec, kernel, rhs=None, dims=None, t_eval=None):
+    m = degpu.ExplicitRungeKutta(method).precision(prec).kernel(kernel)
+    return degpu.solve_ensemble(rhs if rhs is not None else e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol,
+                                e.atol, m, family=e.family, dims=dims, t_eval=t_eval, n_params=e.params.shape[0])
+
+
+def same(a, b, sel):
+    assert np.array_equal(a.status[sel], b.status[sel])
+    assert np.array_equal(a.accepted[sel], b.accepted[sel])
+    assert np.array_equal(a.rejected[sel], b.rejected[sel])
+    assert np.array_equal(a.fevals[sel], b.fevals[sel])
+    assert np.array_equal(a.y_final[:, sel], b.y_final[:, sel])
+
+
+@pytest.mark.parametrize("method", [abi.DOPRI5, abi.DOP853])
+@pytest.mark.parametrize("kernel", [abi.KERNEL_PERSISTENT, abi.KERNEL_THREAD])
+def test_split_matches_the_selected_arithmetic(bound, method, kernel):
+    e = straddling(6000)
+    tight = e.rtol < BOUND
+    assert 0 < tight.sum() < e.n
+    degpu.set_mixed_min_rtol(method, BOUND)
+    split = run(e, method, abi.MIXED, kernel)
+    fast = run(e, method, abi.FP64_FAST, kernel)
+    degpu.set_mixed_min_rtol(method, 0.0)
+    mixed = run(e, method, abi.MIXED, kernel)
+    same(split, fast, tight)
+    same(split, mixed, ~tight)
+    # the FP32-stage form below the bound is what the split avoids: it needs more steps there
+    steps = lambda r: (r.accepted + r.rejected)[tight].mean()
+    assert steps(mixed) > steps(fast)
+
+
+def test_split_on_ragged_group_kernel(bound):
+    f = W.config2(n=96)
+    f.tf[:] = 4.0
+    f.rtol = W.logU(8, np.arange(f.n), 1, 1e-10, 1e-6)
+    f.atol = 1e-2 * f.rtol
+    tight = f.rtol < BOUND
+    assert 0 < tight.sum() < f.n
+    degpu.set_mixed_min_rtol(abi.DOP853, BOUND)
+    split = run(f, abi.DOP853, abi.MIXED, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
+    fast = run(f, abi.DOP853, abi.FP64_FAST, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
+    degpu.set_mixed_min_rtol(abi.DOP853, 0.0)
+    mixed = run(f, abi.DOP853, abi.MIXED, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
+    same(split, fast, tight)
+    same(split, mixed, ~tight)
+
+
+def test_rk4_has_no_bound(bound):
+    assert degpu.mixed_min_rtol(abi.RK4) == 0.0
+    with pytest.raises(degpu.DegpuError):
+        degpu.set_mixed_min_rtol(abi.RK4, 1e-8)
