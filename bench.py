@@ -63,14 +63,15 @@ def flops_of(family, accepted, rejected):
 
 
 def fp64_ops_mixed(family, accepted, rejected):
-    """FP64 operations of the mixed form per attempted step: t and h bookkeeping (~8: h * scale,
-    the remaining span, t + h, the step-size guard); the pendulum adds its FP64 stage times and
-    drive phases (6*2 + 7*3)."""
+    """FP64 operations of the mixed form: none on a rejected attempt; on an accepted step t + h
+    (a conversion and an add) and the remaining span tf - t (an add and a conversion); the
+    pendulum also reduces its drive phase at the new t (a multiply, a multiply-round, an FMA and
+    a conversion)."""
     tot = 0.0
     for rid, (d, _F) in RHS_FLOPS.items():
         m = family == rid
-        per = 8 + (33 if rid == abi.RHS["PENDULUM"] else 0)
-        tot += per * float((accepted[m] + rejected[m]).sum())
+        per = 4 + (5 if rid == abi.RHS["PENDULUM"] else 0)
+        tot += per * float(accepted[m].sum())
     return tot
 
 

@@ -75,11 +75,22 @@ struct Lane {
     static constexpr int NC = DENSE ? (Tab::ADAPTIVE ? O : 2) : 1;  // RK4 keeps y_prev, dydt_prev
     static constexpr int NPP = Rhs::NP > 0 ? Rhs::NP : 1;
     using S = typename P::S;
+    static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
+    static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
 
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
-    double rem;    // tf - t (mixed form)
+    double rem;    // tf - t (mixed form of RK4)
     float h_lim;   // 1e-14 |h_prev| in FP32 (mixed form's step-size guard)
+    // Mixed form of the adaptive methods (MIX): the step size, the remaining span used by the
+    // overshoot test and the drive phase of time-dependent families are FP32; FP64 is touched
+    // only on acceptance (t += h, tf - t, the phase at the new t).
+    float hf;        // step size
+    float remf;      // tf - t, refreshed on acceptance
+    float ph0;       // families with a drive phase: the reduced phase at t
+    float rtolf, atolf;  // FP32 copies of the tolerances (mixed form's FP32 error terms)
+    bool fwd;        // tf > t0
+    bool last_step;  // this attempt was clamped to end at tf
     bool bounded;  // h_min / h_max differ from the defaults 0 / +inf
     double p[NPP];
     S y[D];
@@ -94,6 +105,14 @@ struct Lane {
     bool done;
 
     __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const { Rhs::template diff<P>(tt, yy, dd, p); }
+    // Right-hand side at t + dt in the mixed form: a family with a drive phase adds Omega dt to
+    // the phase at t in FP32; the others get the stage time t + dt (unused by autonomous ones).
+    __device__ __forceinline__ void rhs_at(float dt, const S* yy, S* dd) const {
+        if constexpr (PHASE)
+            Rhs::template diff_phase<P>(ph0, dt, yy, dd, p);
+        else
+            rhs(t + (double)dt, yy, dd);
+    }
 
     // Type of the per-component error terms and their sum: FP64, except in the mixed form built
     // with the FP32 controller (P::F32_CTRL), whose terms are FP32 stage data.
@@ -102,7 +121,7 @@ struct Lane {
     __device__ __forceinline__ NormT norm_term(S e, S yv, S ynv) const {
         // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
         if constexpr (P::F32_CTRL) {
-            float sk = (float)atol + (float)rtol * fmaxf(fabsf(yv), fabsf(ynv));
+            float sk = atolf + rtolf * fmaxf(fabsf(yv), fabsf(ynv));
             float q = __fdividef(e, sk);
             return q * q;
         } else {
@@ -267,6 +286,10 @@ struct Lane {
         tf = a.tf[inst];
         rtol = a.rtol[inst];
         atol = a.atol[inst];
+        if constexpr (P::F32_CTRL) {
+            rtolf = (float)rtol;
+            atolf = (float)atol;
+        }
 #pragma unroll
         for (int q = 0; q < Rhs::NP; ++q) p[q] = a.params[(int64_t)q * n + inst];
 #pragma unroll
@@ -306,6 +329,13 @@ struct Lane {
             return;
         }
         h = h0;
+        if constexpr (MIX) {
+            hf = (float)h0;
+            remf = (float)rem;
+            fwd = dir > 0.0;
+            last_step = false;
+            if constexpr (PHASE) ph0 = Rhs::phase(t0, p);
+        }
         rhs(t, y, k0);
         fev += 1;
         if constexpr (DENSE && !Tab::ADAPTIVE) {
@@ -321,9 +351,9 @@ struct Lane {
     // ----- one Dormand–Prince step attempt: ordinary.rs:63-268 -------------------------------
     // returns 1 accepted, 2 rejected, 3 error
     __device__ int step_dp(const EnsArgs& a) {
-        if constexpr (P::F32_CTRL) {
-            // mixed: the step-size guard on FP32 copies (h_lim = 1e-14 |h_prev|, set on acceptance)
-            if (fabsf((float)h) < h_lim) {
+        if constexpr (MIX) {
+            // mixed: the step-size guard in FP32 (h_lim = 1e-14 |h_prev|, set on acceptance)
+            if (fabsf(hf) < h_lim) {
                 status = DEGPU_ERR_STEP_SIZE;
                 return 3;
             }
@@ -351,7 +381,10 @@ struct Lane {
                     for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
                 }
             });
-            rhs(t + Tab::c(i) * h, ys, k[i]);
+            if constexpr (MIX)
+                rhs_at((float)Tab::c(i) * hf, ys, k[i]);
+            else
+                rhs(t + Tab::c(i) * h, ys, k[i]);
         });
         // ys now holds the last stage state (ysti, ordinary.rs:107)
         S yseg[D], ynew[D], ycn[D];
@@ -364,7 +397,11 @@ struct Lane {
                 for (int c = 0; c < D; ++c) yseg[c] = yseg[c] + (S)bi_ * k[i][c];
             }
         });
-        S hs = P::from(h);
+        S hs;
+        if constexpr (MIX)
+            hs = hf;
+        else
+            hs = P::from(h);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
             if constexpr (P::KAHAN) {
@@ -411,20 +448,24 @@ struct Lane {
         }
         NormT deno = Tab::HAS_BH ? err + (NormT)0.01 * err2 : err;
         if (deno <= (NormT)0) deno = (NormT)1;
-        double scale, errd = 0.0;
-        float errf = 0.0f;
+        double scale = 1.0, errd = 0.0;
+        float errf = 0.0f, scalef = 1.0f;
         if constexpr (P::F32_CTRL) {
             // mixed with the FP32 controller: the normalisation and the controller's power in
-            // FP32 (the error terms are FP32 data); h, t and the step-size update stay FP64
-            float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf((float)h);
+            // FP32 (the error terms are FP32 data)
+            float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf(hf);
             errf = ef;
             float pw = exp2f(__log2f(ef) * (float)(-1.0 / (double)O));
-            scale = (double)fminf(fmaxf((float)a.safety * pw, (float)a.min_scale), (float)a.max_scale);
+            scalef = fminf(fmaxf((float)a.safety * pw, (float)a.min_scale), (float)a.max_scale);
         } else {
-            errd = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
+            if constexpr (MIX)
+                errd = (double)fabsf(hf) * err * sqrt(1.0 / (deno * (double)D));
+            else
+                errd = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
             double error_exponent = 1.0 / (double)O;
             scale = a.safety * P::pow(errd, -error_exponent);
             scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+            if constexpr (MIX) scalef = (float)scale;
         }
 
         int result;
@@ -435,9 +476,16 @@ struct Lane {
         else
             accept = errd <= 1.0;
         if (accept) {
-            const double t_new = t + h;
+            double t_new;
+            if constexpr (MIX)
+                t_new = last_step ? tf : t + (double)hf;  // a clamped last step ends exactly at tf
+            else
+                t_new = t + h;
             S dydt[D];
-            rhs(t_new, ynew, dydt);
+            if constexpr (PHASE)
+                rhs_at(hf, ynew, dydt);
+            else
+                rhs(t_new, ynew, dydt);
             fev += 1;
             // stiffness detection, ordinary.rs:165-194
             if (steps % 100 == 0) {
@@ -450,7 +498,7 @@ struct Lane {
                     stden = stden + d2 * d2;
                 }
                 if (stden > 0.0) {
-                    double h_lamb = h * sqrt(stdnum / stden);
+                    double h_lamb = (MIX ? (double)hf : h) * sqrt(stdnum / stden);
                     if (h_lamb > 6.1) {
                         nonstiff = 0;
                         stiff += 1;
@@ -470,9 +518,14 @@ struct Lane {
                 fev += I - NS - (I > NS ? 1 : 0);  // DOP853: three dense stages the crate evaluates
             }
             t_prev = t;
-            h_prev = h;
-            if constexpr (P::F32_CTRL) h_lim = fabsf((float)h) * 1e-14f;
+            if constexpr (MIX) {
+                if constexpr (DENSE) h_prev = t_new - t;  // the interpolation's step length
+                h_lim = fabsf(hf) * 1e-14f;
+            } else {
+                h_prev = h;
+            }
             t = t_new;
+            if constexpr (PHASE) ph0 = Rhs::phase(t, p);
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 y[c] = ynew[c];
@@ -481,26 +534,44 @@ struct Lane {
             }
             if (last_rejected) {
                 last_rejected = false;
-                scale = fmin(scale, 1.0);
+                if constexpr (MIX)
+                    scalef = fminf(scalef, 1.0f);
+                else
+                    scale = fmin(scale, 1.0);
             }
             result = 1;
         } else {
             last_rejected = true;
             result = 2;
         }
-        h = h * scale;
-        // constrain_step_size, utils.rs:22-33 (a no-op for the default bounds 0 and +inf)
-        if (bounded) {
-            if (fabs(h) < a.h_min)
-                h = rs_signum(h) * a.h_min;
-            else if (fabs(h) > a.h_max)
-                h = rs_signum(h) * a.h_max;
+        if constexpr (MIX) {
+            hf = hf * scalef;
+            if (bounded) {
+                // constrain_step_size, utils.rs:22-33
+                double hd = (double)hf;
+                if (fabs(hd) < a.h_min)
+                    hd = rs_signum(hd) * a.h_min;
+                else if (fabs(hd) > a.h_max)
+                    hd = rs_signum(hd) * a.h_max;
+                hf = (float)hd;
+            }
+        } else {
+            h = h * scale;
+            // constrain_step_size, utils.rs:22-33 (a no-op for the default bounds 0 and +inf)
+            if (bounded) {
+                if (fabs(h) < a.h_min)
+                    h = rs_signum(h) * a.h_min;
+                else if (fabs(h) > a.h_max)
+                    h = rs_signum(h) * a.h_max;
+            }
         }
         return result;
     }
 
     __device__ __forceinline__ S stage_coef(double aij) const {
-        if constexpr (P::KAHAN)
+        if constexpr (MIX)
+            return (float)aij * hf;
+        else if constexpr (P::KAHAN)
             return (float)aij * (float)h;
         else
             return aij * h;
@@ -509,7 +580,11 @@ struct Lane {
     // dense-output preparation, ordinary.rs:196-235 (k[S..I) computed here for DOP853)
     __device__ void dense_coefficients(S (&k)[I][D], const S* ynew, const S* dydt) {
         if constexpr (DENSE && Tab::ADAPTIVE) {
-            S hs = P::from(h);
+            S hs;
+            if constexpr (MIX)
+                hs = hf;
+            else
+                hs = P::from(h);
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 cont[0][c] = y[c];
@@ -537,7 +612,10 @@ struct Lane {
                             for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
                         }
                     });
-                    rhs(t + Tab::c(i) * h, ys, k[i]);
+                    if constexpr (MIX)
+                        rhs_at((float)Tab::c(i) * hf, ys, k[i]);
+                    else
+                        rhs(t + Tab::c(i) * h, ys, k[i]);
                     fev += 1;
                 });
             }
@@ -626,9 +704,21 @@ struct Lane {
     // ----- one iteration of the driver loop: solve_ivp.rs:191-266 ----------------------------
     __device__ __forceinline__ void iterate(const EnsArgs& a) {
         const double eps10 = 2.220446049250313e-16 * 10.0;
-        if constexpr (P::KAHAN) {
-            // mixed form: the remaining interval tf - t is kept (updated on acceptance), so the
-            // overshoot test is one comparison
+        if constexpr (MIX) {
+            // mixed form: the overshoot test on FP32 copies; an attempt that reaches tf is
+            // clamped to the remaining span and, if accepted, ends exactly at tf
+            last_step = false;
+            if (fwd ? hf >= remf : hf <= remf) {
+                if (fabsf(remf) < (float)eps10) {
+                    done = true;
+                    return;
+                }
+                hf = remf;
+                last_step = true;
+            }
+        } else if constexpr (P::KAHAN) {
+            // mixed form of RK4: the remaining interval tf - t is kept (updated on acceptance),
+            // so the overshoot test is one comparison
             if (dir > 0.0 ? h > rem : h < rem) {
                 if (fabs(rem) < eps10) {
                     done = true;
@@ -655,7 +745,14 @@ struct Lane {
         }
         acc += 1;
         solout(a);
-        if constexpr (P::KAHAN) {
+        if constexpr (MIX) {
+            if (last_step) {
+                done = true;  // t == tf
+            } else {
+                remf = (float)(tf - t);
+                if (fabsf(remf) <= (float)eps10) done = true;
+            }
+        } else if constexpr (P::KAHAN) {
             rem = tf - t;
             if (fabs(rem) <= eps10) done = true;
         } else {

@@ -29,6 +29,17 @@ namespace degpu {
 #define DEGPU_MIXED_F32_CTRL 1
 #endif
 
+// PhaseOf<R>::value: the family declares PHASE (a drive phase the mixed form advances in FP32,
+// with `phase` and `diff_phase`).
+template <class R>
+struct PhaseOf {
+    template <class U>
+    __host__ __device__ static constexpr bool test(decltype(U::PHASE)*) { return U::PHASE; }
+    template <class U>
+    __host__ __device__ static constexpr bool test(...) { return false; }
+    static constexpr bool value = test<R>(nullptr);
+};
+
 // Parity: FP64, crate operation order, correctly rounded pow/sin/cos, no FMA contraction (the
 // translation units that instantiate it are compiled with -fmad=false).
 struct PrecParity {
@@ -116,6 +127,22 @@ struct RhsVanDerPol {
 // (the model of examples/ode/05_damped_pendulum/main.rs:34-40 plus a periodic drive).
 struct RhsPendulum {
     static constexpr int ID = 3, D = 2, NP = 3;
+    // Mixed form: the drive phase Omega t reduced to [-pi, pi] in FP64 once per accepted step;
+    // a stage at t + dt adds Omega dt to it in FP32 (diff_phase), so the stages need no FP64.
+    static constexpr bool PHASE = true;
+    __device__ static __forceinline__ float phase(double t, const double* p) {
+        double ph = p[2] * t;
+        double k = rint(ph * 0.15915494309189535);
+        return (float)fma(-k, 6.283185307179586, ph);
+    }
+    template <class P>
+    __device__ static __forceinline__ void diff_phase(float ph0, float dt, const float* y, float* dydt,
+                                                      const double* p) {
+        float theta = y[0], omega = y[1];
+        float r = ph0 + (float)p[2] * dt;
+        dydt[0] = omega;
+        dydt[1] = -(float)p[0] * omega - P::sin(theta) + (float)p[1] * P::cos(r);
+    }
     template <class P>
     __device__ static __forceinline__ void diff(double t, const typename P::S* y, typename P::S* dydt, const double* p) {
         using S = typename P::S;
