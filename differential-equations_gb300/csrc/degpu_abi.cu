@@ -166,6 +166,9 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
     a.safety = cfg->safety_factor;
     a.min_scale = cfg->min_scale;
     a.max_scale = cfg->max_scale;
+    a.safety_f = (float)a.safety;
+    a.min_scale_f = (float)a.min_scale;
+    a.max_scale_f = (float)a.max_scale;
     a.dense_mode = cfg->dense_mode;
     a.n_params = pb->n_params;
     const bool dense = a.n_eval > 0 && out->dense;

@@ -57,6 +57,7 @@ struct EnsArgs {
     double h0, h_min, h_max;
     int64_t max_steps;
     double safety, min_scale, max_scale;
+    float safety_f, min_scale_f, max_scale_f;  // FP32 copies (mixed form's controller)
     int32_t dense_mode;
     int32_t n_params;
     const int32_t* family;           // per-instance family id (multi-family persistent kernel)
@@ -65,6 +66,33 @@ struct EnsArgs {
 
 // f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
 __device__ __forceinline__ double rs_signum(double x) { return x != x ? x : copysign(1.0, x); }
+
+// Conversions between FP32 and FP64 done with integer operations on the bit patterns, for the
+// mixed form's per-step bookkeeping: a hardware conversion involving FP64 occupies the FP64 pipe,
+// which runs at 1/64 of the FP32 rate on this GPU.
+// widen_f32: exact FP32 -> FP64 (subnormal inputs become signed zero; inf and NaN are kept).
+__device__ __forceinline__ double widen_f32(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xffu;
+    const unsigned int sign = b & 0x80000000u;
+    if (e == 0u) return __hiloint2double((int)sign, 0);
+    const unsigned int ee = e == 0xffu ? 0x7ffu : e + 896u;  // rebias 127 -> 1023
+    const unsigned int hi = sign | (ee << 20) | ((b & 0x7fffffu) >> 3);
+    const unsigned int lo = (b & 0x7u) << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+// narrow_rz: FP64 -> FP32 rounded toward zero (|result| <= |x|); magnitudes below the FP32
+// normal range become signed zero, above it infinity; NaN stays NaN.
+__device__ __forceinline__ float narrow_rz(double x) {
+    const unsigned int hi = (unsigned int)__double2hiint(x);
+    const unsigned int lo = (unsigned int)__double2loint(x);
+    const unsigned int e = (hi >> 20) & 0x7ffu;
+    const unsigned int sign = hi & 0x80000000u;
+    if (e <= 896u) return __uint_as_float(sign);
+    if (e == 0x7ffu && ((hi & 0xfffffu) | lo)) return __uint_as_float(0x7fc00000u);
+    if (e >= 1151u) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
 
 template <class Tab, class Rhs, class P, bool DENSE>
 struct Lane {
@@ -77,6 +105,7 @@ struct Lane {
     using S = typename P::S;
     static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
+    static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
 
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
@@ -93,6 +122,7 @@ struct Lane {
     bool last_step;  // this attempt was clamped to end at tf
     bool bounded;  // h_min / h_max differ from the defaults 0 / +inf
     double p[NPP];
+    float pf[NPP];  // mixed form: FP32 copies of p, made once per instance
     S y[D];
     S yc[D];  // Kahan compensation of y (mixed precision only)
     S k0[D];  // derivative at (t, y): k[0] of the next step
@@ -104,12 +134,17 @@ struct Lane {
     bool last_rejected;
     bool done;
 
-    __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const { Rhs::template diff<P>(tt, yy, dd, p); }
+    __device__ __forceinline__ void rhs(double tt, const S* yy, S* dd) const {
+        if constexpr (PF)
+            Rhs::template diff<P>(tt, yy, dd, pf);
+        else
+            Rhs::template diff<P>(tt, yy, dd, p);
+    }
     // Right-hand side at t + dt in the mixed form: a family with a drive phase adds Omega dt to
     // the phase at t in FP32; the others get the stage time t + dt (unused by autonomous ones).
     __device__ __forceinline__ void rhs_at(float dt, const S* yy, S* dd) const {
         if constexpr (PHASE)
-            Rhs::template diff_phase<P>(ph0, dt, yy, dd, p);
+            Rhs::template diff_phase<P>(ph0, dt, yy, dd, pf);
         else
             rhs(t + (double)dt, yy, dd);
     }
@@ -133,6 +168,7 @@ struct Lane {
 
     // ----- h_init: src/methods/h_init.rs:45-136 --------------------------------------------
     __device__ double initial_step(double t0, const EnsArgs& a) {
+        if constexpr (MIX) return initial_step_f32(t0, a);
         double posneg = rs_signum(tf - t0);
         S f0[D], f1[D], y1[D];
         rhs(t0, y, f0);
@@ -176,6 +212,57 @@ struct Lane {
         double interval = fabs(tf - t0);
         hh = fmin(fmax(fmin(fmin(fabs(hh) * 100.0, h1), a.h_max), a.h_min), interval);
         return hh * posneg;
+    }
+
+    // The same heuristic in FP32 for the mixed form (the stage data are FP32; an FP64 version
+    // would put dozens of FP64 divisions and square roots on every refill of a lane).
+    __device__ double initial_step_f32(double t0, const EnsArgs& a) {
+        const double posneg = rs_signum(tf - t0);
+        const float pn = (float)posneg;
+        S f0[D], f1[D], y1[D];
+        rhs_at(0.0f, y, f0);
+        fev += 1;
+        float dnf = 0.0f, dny = 0.0f;
+        float sk[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            sk[c] = atolf + rtolf * fabsf(y[c]);
+            float q = f0[c] / sk[c];
+            dnf = dnf + q * q;
+            float r = y[c] / sk[c];
+            dny = dny + r * r;
+        }
+        float hh;
+        if (dnf <= 1.0e-10f || dny <= 1.0e-10f)
+            hh = 1.0e-6f;
+        else
+            hh = sqrtf(dny / dnf) * 0.01f;
+        const float hmax = (float)a.h_max;
+        hh = fminf(hh, hmax);
+        hh = hh * pn;
+#pragma unroll
+        for (int c = 0; c < D; ++c) y1[c] = y[c] + hh * f0[c];
+        rhs_at(hh, y1, f1);
+        fev += 1;
+        float der2 = 0.0f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            float q = (f1[c] - f0[c]) / sk[c];
+            der2 = der2 + q * q;
+        }
+        der2 = sqrtf(der2) / fabsf(hh);
+        float der12 = fmaxf(sqrtf(dnf), der2);
+        float h1;
+        if (der12 <= 1.0e-15f)
+            h1 = fabsf(hh) * 1.0e-3f;
+        else
+            h1 = powf(0.01f / der12, 1.0f / (float)O);
+        const float interval = (float)fabs(tf - t0);
+        hh = fminf(fmaxf(fminf(fminf(fabsf(hh) * 100.0f, h1), hmax), (float)a.h_min), interval);
+        // FP32 rounding must not carry the step outside [h_min, |tf - t0|] of the FP64 checks
+        double h = (double)hh;
+        h = fmin(fmax(h, a.h_min), fabs(tf - t0));
+        return h * posneg;
     }
 
     // ----- validate_step_size_parameters: src/utils.rs:60-157 ------------------------------
@@ -286,18 +373,23 @@ struct Lane {
         tf = a.tf[inst];
         rtol = a.rtol[inst];
         atol = a.atol[inst];
-        if constexpr (P::F32_CTRL) {
+        if constexpr (P::KAHAN) {
             rtolf = (float)rtol;
             atolf = (float)atol;
         }
 #pragma unroll
         for (int q = 0; q < Rhs::NP; ++q) p[q] = a.params[(int64_t)q * n + inst];
+        if constexpr (PF) {
+#pragma unroll
+            for (int q = 0; q < Rhs::NP; ++q) pf[q] = (float)p[q];
+        }
 #pragma unroll
         for (int c = 0; c < D; ++c) {
             y[c] = P::from(a.y0[(int64_t)c * n + inst]);
             yc[c] = (S)0;
         }
         t = t0;
+        if constexpr (PHASE) ph0 = Rhs::phase(t0, p);
         t_prev = t0;
         h_prev = 0.0;
         rem = tf - t0;
@@ -331,12 +423,14 @@ struct Lane {
         h = h0;
         if constexpr (MIX) {
             hf = (float)h0;
-            remf = (float)rem;
+            remf = narrow_rz(rem);  // |remf| <= |tf - t|: the overshoot test never lets t pass tf
             fwd = dir > 0.0;
             last_step = false;
-            if constexpr (PHASE) ph0 = Rhs::phase(t0, p);
         }
-        rhs(t, y, k0);
+        if constexpr (PHASE)
+            rhs_at(0.0f, y, k0);
+        else
+            rhs(t, y, k0);
         fev += 1;
         if constexpr (DENSE && !Tab::ADAPTIVE) {
 #pragma unroll
@@ -456,7 +550,7 @@ struct Lane {
             float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf(hf);
             errf = ef;
             float pw = exp2f(__log2f(ef) * (float)(-1.0 / (double)O));
-            scalef = fminf(fmaxf((float)a.safety * pw, (float)a.min_scale), (float)a.max_scale);
+            scalef = fminf(fmaxf(a.safety_f * pw, a.min_scale_f), a.max_scale_f);
         } else {
             if constexpr (MIX)
                 errd = (double)fabsf(hf) * err * sqrt(1.0 / (deno * (double)D));
@@ -478,7 +572,7 @@ struct Lane {
         if (accept) {
             double t_new;
             if constexpr (MIX)
-                t_new = last_step ? tf : t + (double)hf;  // a clamped last step ends exactly at tf
+                t_new = last_step ? tf : t + widen_f32(hf);  // a clamped last step ends exactly at tf
             else
                 t_new = t + h;
             S dydt[D];
@@ -749,7 +843,7 @@ struct Lane {
             if (last_step) {
                 done = true;  // t == tf
             } else {
-                remf = (float)(tf - t);
+                remf = narrow_rz(tf - t);
                 if (fabsf(remf) <= (float)eps10) done = true;
             }
         } else if constexpr (P::KAHAN) {
@@ -776,12 +870,12 @@ struct Lane {
 // ---------------------------------------------------------------------------------------------
 // Multi-family persistent kernel with longest-first work lists.
 //
-// The host-side plan (plan kernels in degpu_abi.cu) sorts every instance into the work list of
-// its family, in descending order of estimated cost |tf - t0| * rtol^(-1/order), so that the
-// longest solves start first and the end of each list holds the shortest ones.  Each warp works
-// on one family at a time (the family switch is warp-uniform, so it costs no divergence); a lane
-// whose instance finishes takes the next item of that family's list; when the list is empty and
-// every lane of the warp is idle, the warp moves to another family that still has work.
+// The plan kernels (plan.cu) sort every instance into the work list of its family, in descending
+// order of estimated cost |tf - t0| * rtol^(-1/order), so that the longest solves start first and
+// the end of each list holds the shortest ones.  Each warp works on one family at a time (the
+// family switch is warp-uniform, so it costs no divergence); a lane whose instance finishes takes
+// the next item of that family's list; when the list is empty and every lane of the warp is idle,
+// the warp moves to the next family that still has work.
 // ---------------------------------------------------------------------------------------------
 struct MultiQueue {
     const int64_t* items;         // work lists of the three families, concatenated
@@ -803,17 +897,12 @@ struct MultiLane {
 template <class Tab, class P, bool DENSE, class R0, class R1, class R2>
 __global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(EnsArgs a, MultiQueue q) {
     MultiLane<Tab, P, DENSE, R0, R1, R2> M;
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
     const int64_t cnt[3] = {q.count[0], q.count[1], q.count[2]};
     const int64_t st[3] = {q.start[0], q.start[1], q.start[2]};
-    // initial family: warps split in proportion to the list lengths
-    int64_t total = cnt[0] + cnt[1] + cnt[2];
-    int fam = 0;
-    {
-        int64_t pos = total > 0 ? (int64_t)warp * total / (nwarps > 0 ? nwarps : 1) : 0;
-        fam = pos < cnt[0] ? 0 : (pos < cnt[0] + cnt[1] ? 1 : 2);
-    }
+    // every warp starts on the longest list and moves on to the next family when it runs dry, so
+    // that most of the time an SM runs one family's code (the three families' step code together
+    // overflow the instruction cache)
+    int fam = cnt[2] >= cnt[1] && cnt[2] >= cnt[0] ? 2 : (cnt[1] >= cnt[0] ? 1 : 0);
     bool active = false, exhausted = false;
     for (;;) {
         if (!active && !exhausted) {

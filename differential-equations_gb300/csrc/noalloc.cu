@@ -192,6 +192,9 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     a.safety = cfg->safety_factor;
     a.min_scale = cfg->min_scale;
     a.max_scale = cfg->max_scale;
+    a.safety_f = (float)a.safety;
+    a.min_scale_f = (float)a.min_scale;
+    a.max_scale_f = (float)a.max_scale;
     a.dense_mode = cfg->dense_mode;
     a.n_params = pb->n_params;
     const int64_t* items = (const int64_t*)(scratch + NA_ITEMS);

@@ -159,6 +159,9 @@ degpu_status nvrtc_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     a.safety = cfg->safety_factor;
     a.min_scale = cfg->min_scale;
     a.max_scale = cfg->max_scale;
+    a.safety_f = (float)a.safety;
+    a.min_scale_f = (float)a.min_scale;
+    a.max_scale_f = (float)a.max_scale;
     a.dense_mode = cfg->dense_mode;
     a.n_params = pb->n_params;
     if (in->n_eval > 0) return DEGPU_UNSUPPORTED;  // dense output for run-time systems: not built

@@ -2,8 +2,9 @@
 // for the built-in families, and the precision policies they are evaluated under.
 //
 // Each family is a struct with the state dimension D, the parameter count NP and
-//     template <class P> static void diff(double t, const typename P::S* y, typename P::S* dydt,
-//                                         const double* p);
+//     template <class P, class PT> static void diff(double t, const typename P::S* y,
+//                                                   typename P::S* dydt, const PT* p);
+// (PT = double, or float for the mixed form's parameter copies).
 // The expressions keep the evaluation order of the crate's test systems (tests/ode/systems.rs),
 // which is what the parity path (compiled without FMA contraction) must reproduce.
 #pragma once
@@ -35,6 +36,16 @@ template <class R>
 struct PhaseOf {
     template <class U>
     __host__ __device__ static constexpr bool test(decltype(U::PHASE)*) { return U::PHASE; }
+    template <class U>
+    __host__ __device__ static constexpr bool test(...) { return false; }
+    static constexpr bool value = test<R>(nullptr);
+};
+
+// FloatParamsOf<R>::value: the family's diff accepts FP32 parameters (BuiltinRhs).
+template <class R>
+struct FloatParamsOf {
+    template <class U>
+    __host__ __device__ static constexpr bool test(decltype(U::FLOAT_PARAMS)*) { return U::FLOAT_PARAMS; }
     template <class U>
     __host__ __device__ static constexpr bool test(...) { return false; }
     static constexpr bool value = test<R>(nullptr);
@@ -96,11 +107,17 @@ struct PrecMixed {
 };
 
 // Families -------------------------------------------------------------------------------------
+// `diff` takes the parameters as FP64 or, in the mixed form, as FP32 copies made once per
+// instance (PT = float), so that no stage converts a parameter.  Built-in families derive from
+// BuiltinRhs to say they accept both; run-time (NVRTC) families take FP64 parameters only.
+struct BuiltinRhs {
+    static constexpr bool FLOAT_PARAMS = true;
+};
 // tests/ode/systems.rs:85-101
-struct RhsLorenz {
+struct RhsLorenz : BuiltinRhs {
     static constexpr int ID = 1, D = 3, NP = 3;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         S sigma = (S)p[0], rho = (S)p[1], beta = (S)p[2];
         S x = y[0], yv = y[1], z = y[2];
@@ -111,10 +128,10 @@ struct RhsLorenz {
 };
 
 // tests/ode/systems.rs:62-78
-struct RhsVanDerPol {
+struct RhsVanDerPol : BuiltinRhs {
     static constexpr int ID = 2, D = 2, NP = 1;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         S mu = (S)p[0];
         S y1 = y[0], y2 = y[1];
@@ -125,7 +142,7 @@ struct RhsVanDerPol {
 
 // Damped driven pendulum, g/l = 1: theta' = omega, omega' = -gamma omega - sin(theta) + A cos(Omega t)
 // (the model of examples/ode/05_damped_pendulum/main.rs:34-40 plus a periodic drive).
-struct RhsPendulum {
+struct RhsPendulum : BuiltinRhs {
     static constexpr int ID = 3, D = 2, NP = 3;
     // Mixed form: the drive phase Omega t reduced to [-pi, pi] in FP64 once per accepted step;
     // a stage at t + dt adds Omega dt to it in FP32 (diff_phase), so the stages need no FP64.
@@ -137,14 +154,14 @@ struct RhsPendulum {
     }
     template <class P>
     __device__ static __forceinline__ void diff_phase(float ph0, float dt, const float* y, float* dydt,
-                                                      const double* p) {
+                                                      const float* pf) {
         float theta = y[0], omega = y[1];
-        float r = ph0 + (float)p[2] * dt;
+        float r = ph0 + pf[2] * dt;
         dydt[0] = omega;
-        dydt[1] = -(float)p[0] * omega - P::sin(theta) + (float)p[1] * P::cos(r);
+        dydt[1] = -pf[0] * omega - P::sin(theta) + pf[1] * P::cos(r);
     }
-    template <class P>
-    __device__ static __forceinline__ void diff(double t, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double t, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         S theta = y[0], omega = y[1];
         dydt[0] = omega;
@@ -163,29 +180,29 @@ struct RhsPendulum {
 };
 
 // tests/ode/systems.rs:6-17
-struct RhsExpGrowth {
+struct RhsExpGrowth : BuiltinRhs {
     static constexpr int ID = 5, D = 1, NP = 1;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         dydt[0] = (typename P::S)p[0] * y[0];
     }
 };
 
 // tests/ode/systems.rs:19-31
-struct RhsLinear {
+struct RhsLinear : BuiltinRhs {
     static constexpr int ID = 6, D = 1, NP = 2;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         dydt[0] = (S)p[0] + (S)p[1] * y[0];
     }
 };
 
 // tests/ode/systems.rs:33-46
-struct RhsHarmonic {
+struct RhsHarmonic : BuiltinRhs {
     static constexpr int ID = 7, D = 2, NP = 1;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         dydt[0] = y[1];
         dydt[1] = -(S)p[0] * y[0];
@@ -193,20 +210,20 @@ struct RhsHarmonic {
 };
 
 // tests/ode/systems.rs:48-60
-struct RhsLogistic {
+struct RhsLogistic : BuiltinRhs {
     static constexpr int ID = 8, D = 1, NP = 2;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         dydt[0] = (S)p[0] * y[0] * ((S)1 - y[0] / (S)p[1]);
     }
 };
 
 // tests/ode/systems.rs:155-173
-struct RhsRobertson {
+struct RhsRobertson : BuiltinRhs {
     static constexpr int ID = 9, D = 3, NP = 0;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double*) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT*) {
         using S = typename P::S;
         S y1 = y[0], y2 = y[1], y3 = y[2];
         dydt[0] = (S)-0.04 * y1 + (S)1.0e4 * y2 * y3;
@@ -216,10 +233,10 @@ struct RhsRobertson {
 };
 
 // tests/ode/systems.rs:175-190
-struct RhsHires {
+struct RhsHires : BuiltinRhs {
     static constexpr int ID = 10, D = 8, NP = 0;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double*) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT*) {
         using S = typename P::S;
         dydt[0] = (S)-1.71 * y[0] + (S)0.43 * y[1] + (S)8.32 * y[2] + (S)0.0007;
         dydt[1] = (S)1.71 * y[0] - (S)8.75 * y[1];
@@ -233,10 +250,10 @@ struct RhsHires {
 };
 
 // tests/ode/systems.rs:103-120
-struct RhsBrusselator {
+struct RhsBrusselator : BuiltinRhs {
     static constexpr int ID = 11, D = 2, NP = 2;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         S a = (S)p[0], b = (S)p[1], y1 = y[0], y2 = y[1];
         dydt[0] = a + y1 * y1 * y2 - (b + (S)1) * y1;
@@ -245,10 +262,10 @@ struct RhsBrusselator {
 };
 
 // tests/ode/systems.rs:122-153; powi(2) -> x*x, powi(3) -> x*(x*x) as LLVM expands them.
-struct RhsCr3bp {
+struct RhsCr3bp : BuiltinRhs {
     static constexpr int ID = 12, D = 6, NP = 1;
-    template <class P>
-    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const double* p) {
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
         using S = typename P::S;
         S mu = (S)p[0];
         S rx = y[0], ry = y[1], rz = y[2], vx = y[3], vy = y[4], vz = y[5];

@@ -165,6 +165,9 @@ struct ServerImpl {
         a.safety = r.cfg.safety_factor;
         a.min_scale = r.cfg.min_scale;
         a.max_scale = r.cfg.max_scale;
+        a.safety_f = (float)a.safety;
+        a.min_scale_f = (float)a.min_scale;
+        a.max_scale_f = (float)a.max_scale;
         a.dense_mode = r.cfg.dense_mode;
         a.n_params = r.pb.n_params;
         a.ticket = r.ticket;
