@@ -210,9 +210,9 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
     if (kernel_sel == DEGPU_KERNEL_AUTO)
         kernel_sel = (cfg->method != DEGPU_RK4 && n >= 32768) ? DEGPU_KERNEL_PERSISTENT : DEGPU_KERNEL_THREAD;
 
-    // persistent solves of the production families (Van der Pol, pendulum, Lorenz): one
-    // multi-family launch over longest-first work lists
-    if (kernel_sel == DEGPU_KERNEL_PERSISTENT) {
+    // solves of the production families (Van der Pol, pendulum, Lorenz) run over longest-first
+    // work lists: one multi-family persistent launch, or one run-to-completion launch per list
+    {
         auto prod = [](int id) {
             return id == DEGPU_RHS_VAN_DER_POL || id == DEGPU_RHS_PENDULUM || id == DEGPU_RHS_LORENZ;
         };
@@ -237,7 +237,9 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
         if (ok) {
             EnsArgs ma = a;
             ma.count = n;
-            return multi_solve(cfg, ma, family_host ? in->family : nullptr, pb->rhs_id, dense, s);
+            const int32_t* fam_dev = family_host ? in->family : nullptr;
+            if (kernel_sel == DEGPU_KERNEL_PERSISTENT) return multi_solve(cfg, ma, fam_dev, pb->rhs_id, dense, s);
+            return sorted_thread_solve(cfg, ma, fam_dev, pb->rhs_id, dense, s);
         }
     }
 

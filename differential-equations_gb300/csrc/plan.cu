@@ -8,7 +8,7 @@
 //   scan    : exclusive scan over the 2 x 3 x 128 cells -> list offsets, list starts and lengths;
 //   scatter : items[offset(cell) + position] = instance.
 // Then one persistent launch per class: FP64 first (its instances are the most expensive ones),
-// the mixed kernel after it.
+// the mixed kernel after it; or, for the run-to-completion layout, one launch per list.
 // Ordering inside a bucket follows the atomics and is not deterministic; every instance's result
 // is independent of the order in which instances are taken, so solutions are deterministic.
 #include <cuda_runtime.h>
@@ -72,6 +72,41 @@ __global__ void plan_scatter_kernel(int64_t n, const int* pos, const int* key, c
     items[cells[key[i]] + pos[i]] = i;
 }
 
+// Scratch of one plan: cells, start, count, head, bad, items, pos, key.
+struct Plan {
+    char* blk = nullptr;
+    int64_t* items = nullptr;
+    int64_t* start = nullptr;  // [NLISTS]
+    int64_t* count = nullptr;  // [NLISTS]
+    unsigned long long* head = nullptr;
+};
+
+// Runs count/scan/scatter into a fresh stream-ordered scratch block (freed by the caller).
+static degpu_status run_plan(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev,
+                             int fam_const, double split, Plan& pl, cudaStream_t s) {
+    const int64_t n = a.n;
+    const size_t cells_bytes = ((size_t)NB * NLISTS * 4 + 7) / 8 * 8;
+    const size_t head_bytes = cells_bytes + NLISTS * 8 * 3 + 8;
+    size_t bytes = head_bytes + n * 8 + n * 4 + n * 4 + 64;
+    if (cudaMallocAsync((void**)&pl.blk, bytes, s) != cudaSuccess) return DEGPU_OOM;
+    int* cells = (int*)pl.blk;
+    pl.start = (int64_t*)(pl.blk + cells_bytes);
+    pl.count = pl.start + NLISTS;
+    pl.head = (unsigned long long*)(pl.count + NLISTS);
+    int* bad = (int*)(pl.head + NLISTS);
+    pl.items = (int64_t*)(pl.blk + head_bytes);
+    int* pos = (int*)(pl.items + n);
+    int* key = pos + n;
+    if (cudaMemsetAsync(pl.blk, 0, head_bytes, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    plan_count_kernel<<<blocks, 256, 0, s>>>(n, a.t0, a.tf, a.rtol, family_dev, fam_const, inv_order,
+                                              cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, cells, pos, key, bad);
+    plan_scan_kernel<<<1, 32, 0, s>>>(cells, pl.start, pl.count);
+    plan_scatter_kernel<<<blocks, 256, 0, s>>>(n, pos, key, cells, pl.items);
+    return cudaGetLastError() == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
+}
+
 // Plans and launches one multi-family persistent solve (two launches when a mixed solve splits
 // by rtol).  Returns DEGPU_UNSUPPORTED when no kernel is registered for the combination.
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
@@ -87,41 +122,50 @@ degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const in
         fp64_launch = it64->second;
     }
     const int64_t n = a.n;
-    // one scratch block: cells, start, count, head, bad, items, pos, key
-    const size_t cells_bytes = ((size_t)NB * NLISTS * 4 + 7) / 8 * 8;
-    const size_t head_bytes = cells_bytes + NLISTS * 8 * 3 + 8;
-    size_t bytes = head_bytes + n * 8 + n * 4 + n * 4 + 64;
-    char* blk = nullptr;
-    if (cudaMallocAsync((void**)&blk, bytes, s) != cudaSuccess) return DEGPU_OOM;
-    int* cells = (int*)blk;
-    int64_t* start = (int64_t*)(blk + cells_bytes);
-    int64_t* count = start + NLISTS;
-    unsigned long long* head = (unsigned long long*)(count + NLISTS);
-    int* bad = (int*)(head + NLISTS);
-    int64_t* items = (int64_t*)(blk + head_bytes);
-    int* pos = (int*)(items + n);
-    int* key = pos + n;
-    degpu_status st = DEGPU_OK;
-    if (cudaMemsetAsync(blk, 0, head_bytes, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
-    const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
-    unsigned blocks = (unsigned)((n + 255) / 256);
-    if (st == DEGPU_OK) {
-        plan_count_kernel<<<blocks, 256, 0, s>>>(n, a.t0, a.tf, a.rtol, family_dev, fam_const, inv_order,
-                                                  cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, cells, pos, key, bad);
-        plan_scan_kernel<<<1, 32, 0, s>>>(cells, start, count);
-        plan_scatter_kernel<<<blocks, 256, 0, s>>>(n, pos, key, cells, items);
-        if (cudaGetLastError() != cudaSuccess) st = DEGPU_CUDA_ERROR;
-    }
+    Plan pl;
+    degpu_status st = run_plan(cfg, a, family_dev, fam_const, split, pl, s);
     // class 1 (FP64) lists: start/count/head [3..6); class 0: [0..3)
     if (st == DEGPU_OK && fp64_launch) {
-        MultiQueue q{items, start + 3, count + 3, head + 3};
+        MultiQueue q{pl.items, pl.start + 3, pl.count + 3, pl.head + 3};
         if (fp64_launch(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
     }
     if (st == DEGPU_OK) {
-        MultiQueue q{items, start, count, head};
+        MultiQueue q{pl.items, pl.start, pl.count, pl.head};
         if (it->second(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
     }
-    cudaFreeAsync(blk, s);
+    if (pl.blk) cudaFreeAsync(pl.blk, s);
+    return st;
+}
+
+// One run-to-completion launch per (precision class, family) of the production families, each
+// over its longest-first work list: the lanes of a warp get instances of similar cost, so a warp
+// is not held by one long instance while its other lanes sit finished.
+degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev,
+                                 int fam_const, bool dense, cudaStream_t s) {
+    const double split = mixed_split(cfg);
+    static const int ids[3] = {DEGPU_RHS_VAN_DER_POL, DEGPU_RHS_PENDULUM, DEGPU_RHS_LORENZ};
+    Plan pl;
+    degpu_status st = run_plan(cfg, a, family_dev, fam_const, split, pl, s);
+    int64_t hs[NLISTS] = {}, hc[NLISTS] = {};
+    if (st == DEGPU_OK &&
+        (cudaMemcpyAsync(hs, pl.start, sizeof(hs), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+         cudaMemcpyAsync(hc, pl.count, sizeof(hc), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+         cudaStreamSynchronize(s) != cudaSuccess))
+        st = DEGPU_CUDA_ERROR;
+    for (int l = NLISTS - 1; l >= 0 && st == DEGPU_OK; --l) {  // FP64 class first
+        if (hc[l] == 0) continue;
+        const int prec = l >= 3 ? DEGPU_FP64_FAST : cfg->precision;
+        auto it = ens_registry().find(VariantKey{cfg->method, ids[l % 3], prec, dense ? 1 : 0});
+        if (it == ens_registry().end()) {
+            st = DEGPU_UNSUPPORTED;
+            break;
+        }
+        EnsArgs ga = a;
+        ga.index = pl.items + hs[l];
+        ga.count = hc[l];
+        if (it->second(ga, DEGPU_KERNEL_THREAD, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
+    }
+    if (pl.blk) cudaFreeAsync(pl.blk, s);
     return st;
 }
 
