@@ -106,6 +106,9 @@ struct Lane {
     static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
     static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
+    // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
+    // itself, and the evaluation the crate repeats at the new point on acceptance is that stage.
+    static constexpr bool FSAL_MIX = MIX && Tab::FSAL;
 
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
@@ -464,7 +467,7 @@ struct Lane {
 #pragma unroll
         for (int c = 0; c < D; ++c) k[0][c] = k0[c];
         S ys[D];
-        static_for<1, NS>([&](auto i) {
+        static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = y[c];
             static_for<0, decltype(i)::value>([&](auto j) {
@@ -508,6 +511,13 @@ struct Lane {
                 ynew[c] = y[c] + hs * yseg[c];
                 ycn[c] = (S)0;
             }
+        }
+        if constexpr (FSAL_MIX) {
+            // the last stage sits at (t + h, y_new): its state is y_new, so it is evaluated there
+            // and doubles as the derivative at the new point on acceptance
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = ynew[c];
+            rhs_at(hf, ynew, k[NS - 1]);
         }
         fev += NS - 1;
 
@@ -576,11 +586,15 @@ struct Lane {
             else
                 t_new = t + h;
             S dydt[D];
-            if constexpr (PHASE)
+            if constexpr (FSAL_MIX) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) dydt[c] = k[NS - 1][c];
+            } else if constexpr (PHASE) {
                 rhs_at(hf, ynew, dydt);
-            else
+            } else {
                 rhs(t_new, ynew, dydt);
-            fev += 1;
+            }
+            fev += 1;  // the crate's evaluation at the new point
             // stiffness detection, ordinary.rs:165-194
             if (steps % 100 == 0) {
                 double stdnum = 0.0, stden = 0.0;

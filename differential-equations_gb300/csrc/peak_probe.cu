@@ -50,3 +50,20 @@ extern "C" int degpu_internal_fma_peak(int fp64, double* tflops) {
     *tflops = flops / (best * 1e-3) / 1e12;
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
+
+// Checks of the mixed form's integer-op conversions (widen_f32, narrow_rz in erk_core.cuh) on
+// device: wide[i] = widen_f32(f[i]), narrow[i] = narrow_rz(d[i]).  Device pointers, n elements.
+#include "erk_core.cuh"
+
+__global__ void conv_check_kernel(int64_t n, const float* f, double* wide, const double* d, float* narrow) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    wide[i] = degpu::widen_f32(f[i]);
+    narrow[i] = degpu::narrow_rz(d[i]);
+}
+
+extern "C" int degpu_internal_conv_check(int64_t n, const float* f, double* wide, const double* d, float* narrow) {
+    if (n <= 0) return 0;
+    conv_check_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, f, wide, d, narrow);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}

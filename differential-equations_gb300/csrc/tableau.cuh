@@ -13,7 +13,7 @@ namespace degpu {
 
 struct TabRK4 {
     static constexpr int S = 4, I = 4, ORDER = 4;
-    static constexpr bool ADAPTIVE = false, HAS_BH = false;
+    static constexpr bool ADAPTIVE = false, HAS_BH = false, FSAL = false;
     static constexpr double C[4] = {0.0, 0.5, 0.5, 1.0};
     static constexpr double A[4][4] = {{0, 0, 0, 0}, {0.5, 0, 0, 0}, {0, 0.5, 0, 0}, {0, 0, 1.0, 0}};
     static constexpr double B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
@@ -30,7 +30,8 @@ struct TabRK4 {
 
 struct TabDopri5 {
     static constexpr int S = 7, I = 7, ORDER = 5;
-    static constexpr bool ADAPTIVE = true, HAS_BH = false;
+    // FSAL: the last row of A equals b and c = 1, so the last stage's state is y_new
+    static constexpr bool ADAPTIVE = true, HAS_BH = false, FSAL = true;
     static constexpr double C[7] = {0.0, 0.2, 0.3, 0.8, 8.0 / 9.0, 1.0, 1.0};
     static constexpr double A[7][7] = {
         {0, 0, 0, 0, 0, 0, 0},
@@ -56,9 +57,19 @@ struct TabDopri5 {
     __host__ __device__ static constexpr double bi(int i, int j) { return BI[i][j]; }
 };
 
+// The FSAL flag is a property of the coefficients: check it.
+template <class Tab>
+__host__ __device__ constexpr bool fsal_holds() {
+    if (Tab::C[Tab::S - 1] != 1.0) return false;
+    for (int j = 0; j < Tab::S; ++j)
+        if (Tab::A[Tab::S - 1][j] != Tab::B[j]) return false;
+    return true;
+}
+static_assert(fsal_holds<TabDopri5>(), "DOPRI5: last row of A must equal b with c = 1");
+
 struct TabDop853 {
     static constexpr int S = 12, I = 16, ORDER = 8;
-    static constexpr bool ADAPTIVE = true, HAS_BH = true;
+    static constexpr bool ADAPTIVE = true, HAS_BH = true, FSAL = false;
     static constexpr double C[16] = {0.0,
                                      5.260015195876773E-2,
                                      7.89002279381516E-2,
