@@ -937,7 +937,8 @@ __global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(Ens
                 exhausted = true;
             }
         }
-        if (__ballot_sync(0xffffffffu, active) == 0u) {
+        const unsigned amask = __ballot_sync(0xffffffffu, active);
+        if (amask == 0u) {
             if (!__any_sync(0xffffffffu, !exhausted)) {
                 // the whole warp is idle and its list is empty: find a family with work left
                 int nf = -1;
@@ -958,15 +959,26 @@ __global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(Ens
             continue;
         }
         if (active) {
+            // the active lanes step together until one of them finishes (it then refills)
+            bool fin;
             if (fam == 0) {
-                M.l0.iterate(a);
-                if (M.l0.done) { M.l0.finish(a); active = false; }
+                do {
+                    M.l0.iterate(a);
+                    fin = M.l0.done;
+                } while (!__any_sync(amask, fin));
+                if (fin) { M.l0.finish(a); active = false; }
             } else if (fam == 1) {
-                M.l1.iterate(a);
-                if (M.l1.done) { M.l1.finish(a); active = false; }
+                do {
+                    M.l1.iterate(a);
+                    fin = M.l1.done;
+                } while (!__any_sync(amask, fin));
+                if (fin) { M.l1.finish(a); active = false; }
             } else {
-                M.l2.iterate(a);
-                if (M.l2.done) { M.l2.finish(a); active = false; }
+                do {
+                    M.l2.iterate(a);
+                    fin = M.l2.done;
+                } while (!__any_sync(amask, fin));
+                if (fin) { M.l2.finish(a); active = false; }
             }
         }
     }
