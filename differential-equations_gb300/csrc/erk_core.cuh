@@ -132,6 +132,7 @@ struct Lane {
     S cont[NC][D];
     int64_t steps, acc, rej, fev;
     int stiff, nonstiff;
+    int mod100;  // steps % 100, kept incrementally (the stiffness test runs every 100th attempt)
     int next_eval;
     int status;
     bool last_rejected;
@@ -399,6 +400,7 @@ struct Lane {
         h_lim = 0.0f;
         bounded = !(a.h_min == 0.0 && isinf(a.h_max) && a.h_max > 0.0);
         steps = acc = rej = fev = 0;
+        mod100 = 0;
         stiff = nonstiff = 0;
         next_eval = 0;
         last_rejected = false;
@@ -463,6 +465,7 @@ struct Lane {
             return 3;
         }
         steps += 1;
+        mod100 = mod100 == 99 ? 0 : mod100 + 1;
         S k[I][D];
 #pragma unroll
         for (int c = 0; c < D; ++c) k[0][c] = k0[c];
@@ -557,9 +560,16 @@ struct Lane {
         if constexpr (P::F32_CTRL) {
             // mixed with the FP32 controller: the normalisation and the controller's power in
             // FP32 (the error terms are FP32 data)
-            float ef = err * sqrtf(1.0f / (deno * (float)D)) * fabsf(hf);
-            errf = ef;
-            float pw = exp2f(__log2f(ef) * (float)(-1.0 / (double)O));
+            // the norm squared, err^2 h^2 / (deno d), decides and feeds the power directly, so
+            // no square root and no IEEE division are needed (DOPRI5: deno = err)
+            const float eh = err * fabsf(hf);
+            float x;
+            if constexpr (Tab::HAS_BH)
+                x = __fdividef(eh * eh, deno * (float)D);
+            else
+                x = eh * fabsf(hf) * (float)(1.0 / (double)D);
+            errf = x;
+            float pw = exp2f(__log2f(x) * (float)(-0.5 / (double)O));
             scalef = fminf(fmaxf(a.safety_f * pw, a.min_scale_f), a.max_scale_f);
         } else {
             if constexpr (MIX)
@@ -573,7 +583,7 @@ struct Lane {
         }
 
         int result;
-        // mixed: comparing the FP32 error with 1 is the same decision as after widening it
+        // mixed: the squared FP32 norm against 1 (the norm itself against 1 in FP64)
         bool accept;
         if constexpr (P::F32_CTRL)
             accept = errf <= 1.0f;
@@ -596,7 +606,7 @@ struct Lane {
             }
             fev += 1;  // the crate's evaluation at the new point
             // stiffness detection, ordinary.rs:165-194
-            if (steps % 100 == 0) {
+            if (mod100 == 0) {
                 double stdnum = 0.0, stden = 0.0;
 #pragma unroll
                 for (int c = 0; c < D; ++c) {
