@@ -607,17 +607,34 @@ struct Lane {
             fev += 1;  // the crate's evaluation at the new point
             // stiffness detection, ordinary.rs:165-194
             if (mod100 == 0) {
-                double stdnum = 0.0, stden = 0.0;
+                bool den_pos, over;
+                if constexpr (MIX) {
+                    // mixed: in FP32, like the stage data it measures (a warp runs this block
+                    // whenever any of its lanes is at a multiple of 100 attempts)
+                    float sn = 0.0f, sd = 0.0f;
 #pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    double d1 = (double)yseg[c] - (double)k[NS - 1][c];
-                    stdnum = stdnum + d1 * d1;
-                    double d2 = (double)dydt[c] - (double)ys[c];
-                    stden = stden + d2 * d2;
+                    for (int c = 0; c < D; ++c) {
+                        float d1 = yseg[c] - k[NS - 1][c];
+                        sn = sn + d1 * d1;
+                        float d2 = dydt[c] - ys[c];
+                        sd = sd + d2 * d2;
+                    }
+                    den_pos = sd > 0.0f;
+                    over = den_pos && hf * sqrtf(sn / sd) > 6.1f;
+                } else {
+                    double stdnum = 0.0, stden = 0.0;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        double d1 = (double)yseg[c] - (double)k[NS - 1][c];
+                        stdnum = stdnum + d1 * d1;
+                        double d2 = (double)dydt[c] - (double)ys[c];
+                        stden = stden + d2 * d2;
+                    }
+                    den_pos = stden > 0.0;
+                    over = den_pos && h * sqrt(stdnum / stden) > 6.1;
                 }
-                if (stden > 0.0) {
-                    double h_lamb = (MIX ? (double)hf : h) * sqrt(stdnum / stden);
-                    if (h_lamb > 6.1) {
+                if (den_pos) {
+                    if (over) {
                         nonstiff = 0;
                         stiff += 1;
                         if (stiff == 15) {
