@@ -492,6 +492,8 @@ def run_profile_case(args):
     import degpu
 
     e = W.config1(n=args.profile_case)
+    if args.profile_family:
+        e = e.subset(np.nonzero(e.family == abi.RHS[args.profile_family])[0])
     prec, kern = VARIANTS[args.variant]
     m = degpu.ExplicitRungeKutta(abi.DOPRI5)
     m.cfg.precision, m.cfg.kernel, m.cfg.max_steps = prec, kern, e.max_steps
@@ -552,6 +554,8 @@ def main():
     ap.add_argument("--gs-n", type=int, default=4096)
     ap.add_argument("--gs-steps", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--profile-family", default="", choices=["", "VAN_DER_POL", "PENDULUM", "LORENZ"],
+                    help="with --profile-case: keep only this family's instances")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="solve only the first N instances once per --steps (a small case for ncu captures)")
     args = ap.parse_args()

@@ -971,7 +971,7 @@ __global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(Ens
                 int nf = -1;
                 if ((threadIdx.x & 31) == 0) {
                     for (int f = 0; f < 3; ++f) {
-                        int g = (fam + 1 + f) % 3;
+                        int g = (fam + 2 + 2 * f) % 3;  // descending: Lorenz, pendulum, Van der Pol
                         if (atomicAdd(&q.head[g], 0ULL) < (unsigned long long)cnt[g]) {
                             nf = g;
                             break;

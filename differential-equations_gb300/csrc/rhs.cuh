@@ -10,6 +10,7 @@
 #pragma once
 
 #include "dd_math.cuh"
+#include "f32_math.cuh"
 
 namespace degpu {
 
@@ -26,6 +27,10 @@ namespace degpu {
 // 1e-5..1e-11): both settings take the same number of steps to within 0.1% in every rtol decade
 // and reach the same error against FP64; with 1 the solve runs 3.3x faster, because every FP64
 // operation costs as much issue time as 64 FP32 operations on this GPU.
+// Mixed form's sin/cos: 0 uses f32_math.cuh, 1 the CUDA library's sinf/cosf.
+#ifndef DEGPU_MIXED_LIBM_TRIG
+#define DEGPU_MIXED_LIBM_TRIG 0
+#endif
 #ifndef DEGPU_MIXED_F32_CTRL
 #define DEGPU_MIXED_F32_CTRL 1
 #endif
@@ -101,8 +106,13 @@ struct PrecMixed {
         }
         return ::pow(x, y);
     }
+#if DEGPU_MIXED_LIBM_TRIG
     __device__ static __forceinline__ float sin(float x) { return ::sinf(x); }
     __device__ static __forceinline__ float cos(float x) { return ::cosf(x); }
+#else
+    __device__ static __forceinline__ float sin(float x) { return f32m::sin_f32(x); }
+    __device__ static __forceinline__ float cos(float x) { return f32m::cos_f32(x); }
+#endif
     __device__ static __forceinline__ S from(double x) { return (float)x; }
 };
 

@@ -17,12 +17,15 @@ SO = os.path.join(CSRC, "libddmath_host.so")
 @pytest.fixture(scope="module")
 def H():
     src = os.path.join(CSRC, "dd_math_host.cpp")
-    deps = [src, os.path.join(CSRC, "dd_math.cuh"), os.path.join(CSRC, "dd_tables.inc")]
+    deps = [src, os.path.join(CSRC, "dd_math.cuh"), os.path.join(CSRC, "dd_tables.inc"),
+            os.path.join(CSRC, "f32_math.cuh")]
     if not os.path.exists(SO) or any(os.path.getmtime(d) > os.path.getmtime(SO) for d in deps):
         subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", SO, src], check=True)
     h = C.CDLL(SO)
     h.degpu_host_pow_ctrl.argtypes = [O.DP, C.c_double, O.DP, C.c_int64]
     h.degpu_host_sincos_cr.argtypes = [O.DP, O.DP, O.DP, C.c_int64]
+    FP = C.POINTER(C.c_float)
+    h.degpu_host_sincos_f32.argtypes = [FP, FP, FP, C.c_int64]
     return h
 
 
@@ -73,3 +76,31 @@ def test_host_libm_is_not_correctly_rounded_everywhere():
     O.lib().oracle_libm_pow_batch(O.p(x), O.p(yy), O.p(b), n)
     frac = np.mean(a != b)
     assert frac < 0.01
+
+
+@pytest.mark.parametrize("lo,hi", [(-1e-3, 1e-3), (-3.2, 3.2), (-200, 200), (-99999, 99999)])
+def test_sincos_f32_mixed_form(H, lo, hi):
+    """The mixed form's FP32 sin/cos (f32_math.cuh): within 2 units of the FP32 spacing of the
+    exact value (a correctly rounded FP32 result measures 1.4 the same way)."""
+    rng = np.random.default_rng(13)
+    n = 400_000
+    x = rng.uniform(lo, hi, n).astype(np.float32)
+    s, c = np.empty_like(x), np.empty_like(x)
+    FP = C.POINTER(C.c_float)
+    H.degpu_host_sincos_f32(x.ctypes.data_as(FP), s.ctypes.data_as(FP), c.ctypes.data_as(FP), n)
+    xd = x.astype(np.float64)
+    for got, ref in ((s, np.sin(xd)), (c, np.cos(xd))):
+        spacing = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+        assert np.max(np.abs(got.astype(np.float64) - ref) / spacing) <= 2.0
+
+
+def test_sincos_f32_falls_back_beyond_its_range(H):
+    x = np.array([1.0e5, -3.0e7, np.inf, np.nan, 0.0, -0.0], dtype=np.float32)
+    s, c = np.empty_like(x), np.empty_like(x)
+    FP = C.POINTER(C.c_float)
+    H.degpu_host_sincos_f32(x.ctypes.data_as(FP), s.ctypes.data_as(FP), c.ctypes.data_as(FP), len(x))
+    assert np.allclose(s[:2], np.sin(x[:2].astype(np.float64)), atol=1e-6)
+    assert np.isnan(s[2]) and np.isnan(s[3]) and np.isnan(c[2]) and np.isnan(c[3])
+    # sin(+-0) is a zero (its sign is not kept); cos(+-0) is 1 within one unit in the last place
+    assert s[4] == 0.0 and s[5] == 0.0
+    assert abs(float(c[4]) - 1.0) <= 2.0 ** -24 and c[5] == c[4]
