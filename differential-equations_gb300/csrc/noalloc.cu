@@ -64,8 +64,9 @@ __device__ __forceinline__ int na_slot(int id) {
 // family, bucket) position; an instance of another family is reported as BadInput and left out
 // of the lists.
 __global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, const double* rtol,
-                                const int32_t* family, int fam_const, double inv_order, double h0, double split,
-                                unsigned char* scratch, int32_t* status) {
+                                const double* params, int n_params, const int32_t* family, int fam_const,
+                                double inv_order, double h0, double split, unsigned char* scratch,
+                                int32_t* status) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int* cells = (int*)(scratch + NA_CELLS);
@@ -78,7 +79,7 @@ __global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, c
         return;
     }
     double span = fabs(tf[i] - t0[i]);
-    double c = inv_order > 0.0 ? log2(span) - inv_order * log2(rtol[i]) : log2(span / fabs(h0));
+    double c = plan_log2_cost(f, span, rtol[i], inv_order, h0, params, n, i, n_params);
     if (!isfinite(c)) c = 0.0;
     int b = (int)floor((c + 24.0) * 1.5);
     b = b < 0 ? 0 : (b > NA_NB - 1 ? NA_NB - 1 : b);
@@ -163,8 +164,9 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     if (cudaMemsetAsync(scratch, 0, NA_ZERO_END, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
     const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    na_count_kernel<<<blocks, 256, 0, s>>>(n, in->t0, in->tf, in->rtol, in->family, pb->rhs_id, inv_order,
-                                           cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, scratch, out->status);
+    na_count_kernel<<<blocks, 256, 0, s>>>(n, in->t0, in->tf, in->rtol, in->params, pb->n_params, in->family,
+                                           pb->rhs_id, inv_order, cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, scratch,
+                                           out->status);
     na_scan_kernel<<<1, 32, 0, s>>>(scratch);
     na_scatter_kernel<<<blocks, 256, 0, s>>>(n, scratch);
     if (cudaGetLastError() != cudaSuccess) return DEGPU_CUDA_ERROR;

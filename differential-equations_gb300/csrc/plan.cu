@@ -3,8 +3,8 @@
 // Three small kernels, no host round trip:
 //   count   : each instance gets a precision class (1 when a mixed solve sends it to FP64
 //             because its rtol is below the mixed-precision bound, else 0), a cost key
-//             |tf - t0| * rtol^(-1/order) (log2 scale, 128 buckets, descending) and a position
-//             inside its (class, family, bucket) cell by atomic increment;
+//             (plan_log2_cost: log2 scale, 128 buckets, descending) and a position inside its
+//             (class, family, bucket) cell by atomic increment;
 //   scan    : exclusive scan over the 2 x 3 x 128 cells -> list offsets, list starts and lengths;
 //   scatter : items[offset(cell) + position] = instance.
 // Then one persistent launch per class: FP64 first (its instances are the most expensive ones),
@@ -32,8 +32,9 @@ __device__ __forceinline__ int fam_slot(int id) {
 static constexpr int NLISTS = 6;  // (class, family)
 
 __global__ void plan_count_kernel(int64_t n, const double* t0, const double* tf, const double* rtol,
-                                  const int32_t* family, int fam_const, double inv_order, double h0, double split,
-                                  int* cells, int* pos, int* key, int* bad) {
+                                  const double* params, int n_params, const int32_t* family, int fam_const,
+                                  double inv_order, double h0, double split, int* cells, int* pos, int* key,
+                                  int* bad) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int f = fam_slot(family ? family[i] : fam_const);
@@ -42,7 +43,7 @@ __global__ void plan_count_kernel(int64_t n, const double* t0, const double* tf,
         f = 0;
     }
     double span = fabs(tf[i] - t0[i]);
-    double c = inv_order > 0.0 ? log2(span) - inv_order * log2(rtol[i]) : log2(span / fabs(h0));
+    double c = plan_log2_cost(f, span, rtol[i], inv_order, h0, params, n, i, n_params);
     if (!isfinite(c)) c = 0.0;
     int b = (int)floor((c + 24.0) * 1.5);
     b = b < 0 ? 0 : (b > NB - 1 ? NB - 1 : b);
@@ -100,8 +101,9 @@ static degpu_status run_plan(const degpu_method_cfg* cfg, const EnsArgs& a, cons
     if (cudaMemsetAsync(pl.blk, 0, head_bytes, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
     const double inv_order = cfg->method == DEGPU_DOPRI5 ? 0.2 : cfg->method == DEGPU_DOP853 ? 0.125 : 0.0;
     unsigned blocks = (unsigned)((n + 255) / 256);
-    plan_count_kernel<<<blocks, 256, 0, s>>>(n, a.t0, a.tf, a.rtol, family_dev, fam_const, inv_order,
-                                              cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, cells, pos, key, bad);
+    plan_count_kernel<<<blocks, 256, 0, s>>>(n, a.t0, a.tf, a.rtol, a.params, a.n_params, family_dev, fam_const,
+                                              inv_order, cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, cells, pos, key,
+                                              bad);
     plan_scan_kernel<<<1, 32, 0, s>>>(cells, pl.start, pl.count);
     plan_scatter_kernel<<<blocks, 256, 0, s>>>(n, pos, key, cells, pl.items);
     return cudaGetLastError() == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
