@@ -727,6 +727,12 @@ def main():
         extra[v] = {"solves_per_s": n * world / (t * 1e-3), "ms": t,
                     "status_counts": {str(k): int(c) for k, c in
                                       zip(*np.unique(d_out["status"].cpu().numpy(), return_counts=True))}}
+        if VARIANTS[v][0] != abi.MIXED:
+            # algorithmic FP64 rate of an FP64 variant against the FP64 FMA peak
+            va, vr = d_out["accepted"].cpu().numpy(), d_out["rejected"].cpu().numpy()
+            a64v = flops_of(fam, va, vr) / (t * 1e-3 / world) / 1e12
+            extra[v]["fp64_algorithmic"] = {"achieved": a64v, "peak": fp64_peak, "unit": "TFLOP/s",
+                                            "frac": a64v / fp64_peak}
         if v in NOSPLIT and rank == 0 and not args.no_accuracy:
             extra[v]["accuracy"] = accuracy_report(e, d_out["y_final"].cpu().numpy())
     set_split(args.variant)

@@ -29,6 +29,10 @@ std::map<VariantKey, EnsLaunchFn>& ens_registry() {
     static std::map<VariantKey, EnsLaunchFn> m;
     return m;
 }
+std::map<VariantKey, EnsLaunchFn>& cross_registry() {
+    static std::map<VariantKey, EnsLaunchFn> m;
+    return m;
+}
 std::map<VariantKey, RoundOps>& round_registry() {
     static std::map<VariantKey, RoundOps> m;
     return m;
@@ -54,6 +58,8 @@ void ensure_registered() {
         register_mixed();
         register_parity_multi();
         register_multi_fast_mixed();
+        register_cross_parity();
+        register_cross_fast_mixed();
     });
 }
 
@@ -132,18 +138,11 @@ static void builtin_info(int id, int& dim, int& np) {
     }
 }
 
-// Core of degpu_solve_ensemble.  `family_host` / `t_eval_host` are host copies of the
-// corresponding device arrays (or NULL when absent).
-static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
-                               degpu_batch_out* out, cudaStream_t s, const int32_t* family_host,
-                               const double* t_eval_host, const int32_t* dims_host) {
-    ensure_registered();
-    const int64_t n = in->n;
-    if (n == 0) return DEGPU_OK;
-    Scratch scratch(s);
-
+// Kernel arguments of a solve: inputs, outputs and settings (no work list yet).
+static EnsArgs make_args(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                         degpu_batch_out* out) {
     EnsArgs a{};
-    a.n = n;
+    a.n = in->n;
     a.t0 = in->t0;
     a.tf = in->tf;
     a.y0 = in->y0;
@@ -171,6 +170,20 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
     a.max_scale_f = (float)a.max_scale;
     a.dense_mode = cfg->dense_mode;
     a.n_params = pb->n_params;
+    return a;
+}
+
+// Core of degpu_solve_ensemble.  `family_host` / `t_eval_host` are host copies of the
+// corresponding device arrays (or NULL when absent).
+static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                               degpu_batch_out* out, cudaStream_t s, const int32_t* family_host,
+                               const double* t_eval_host, const int32_t* dims_host) {
+    ensure_registered();
+    const int64_t n = in->n;
+    if (n == 0) return DEGPU_OK;
+    Scratch scratch(s);
+
+    EnsArgs a = make_args(pb, cfg, in, out);
     const bool dense = a.n_eval > 0 && out->dense;
     if (a.n_eval > 0 && !out->dense) a.n_eval = 0;
 
@@ -343,6 +356,82 @@ static degpu_status validate(const degpu_problem* pb, const degpu_method_cfg* cf
     return DEGPU_OK;
 }
 
+// degpu_solve_ensemble_crossing: one run-to-completion crossing-detection launch per
+// (family, precision) work list.
+static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                  const degpu_crossing* cr, degpu_batch_out* out, degpu_crossing_out* co,
+                                  cudaStream_t s) {
+    const int64_t n = in->n;
+    Scratch scratch(s);
+    std::vector<int32_t> fam_host;
+    if (in->family) {
+        fam_host.resize(n);
+        if (cudaMemcpyAsync(fam_host.data(), in->family, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    const double split = mixed_split(cfg);
+    std::vector<double> rtol_host;
+    if (split > 0.0) {
+        rtol_host.resize(n);
+        if (cudaMemcpyAsync(rtol_host.data(), in->rtol, n * sizeof(double), cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    std::map<std::pair<int, int>, std::vector<int64_t>> lists;
+    for (int64_t i = 0; i < n; ++i) {
+        const int fam = in->family ? fam_host[i] : pb->rhs_id;
+        const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
+        lists[{fam, prec}].push_back(i);
+    }
+    for (auto& kv : lists) {
+        int dim, np;
+        builtin_info(kv.first.first, dim, np);
+        if (np < 0 || dim > pb->dim || np > pb->n_params || cr->component >= dim) return DEGPU_BAD_INPUT;
+        if (cross_registry().find(VariantKey{cfg->method, kv.first.first, kv.first.second, 1}) ==
+            cross_registry().end())
+            return DEGPU_UNSUPPORTED;
+    }
+    EnsArgs a = make_args(pb, cfg, in, out);
+    a.n_eval = 0;
+    a.cross_comp = cr->component;
+    a.cross_dir = cr->direction;
+    a.cross_max = cr->max_points;
+    a.cross_value = cr->threshold;
+    a.cross_t = co->t;
+    a.cross_y = co->y;
+    a.cross_count = co->count;
+    if (cr->max_points > 0) {
+        // 0xFF bytes form a quiet NaN: slots past an instance's count stay NaN
+        const size_t m = (size_t)cr->max_points * n;
+        if (cudaMemsetAsync(co->t, 0xFF, m * sizeof(double), s) != cudaSuccess ||
+            cudaMemsetAsync(co->y, 0xFF, m * pb->dim * sizeof(double), s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    for (auto& kv : lists) {
+        EnsArgs ga = a;
+        if (lists.size() > 1 || in->family) {
+            int64_t* d_idx = scratch.alloc<int64_t>(kv.second.size());
+            if (!d_idx) return DEGPU_OOM;
+            if (cudaMemcpyAsync(d_idx, kv.second.data(), kv.second.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                s) != cudaSuccess)
+                return DEGPU_CUDA_ERROR;
+            ga.index = d_idx;
+            ga.count = (int64_t)kv.second.size();
+        } else {
+            ga.index = nullptr;
+            ga.count = n;
+        }
+        auto it = cross_registry().find(VariantKey{cfg->method, kv.first.first, kv.first.second, 1});
+        if (it->second(ga, DEGPU_KERNEL_THREAD, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    }
+    // the index lists came from host vectors that die with this call
+    if (cudaStreamSynchronize(s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    return DEGPU_OK;
+}
+
 }  // namespace degpu
 
 using namespace degpu;
@@ -410,6 +499,20 @@ degpu_status degpu_solve_ensemble(const degpu_problem* pb, const degpu_method_cf
     if ((in->family || in->n_eval > 0) && cudaStreamSynchronize(s) != cudaSuccess) return DEGPU_CUDA_ERROR;
     return solve_impl(pb, cfg, in, out, s, in->family ? fam.data() : nullptr, in->n_eval > 0 ? te.data() : nullptr,
                       nullptr);
+}
+
+degpu_status degpu_solve_ensemble_crossing(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                           const degpu_batch_in* in, const degpu_crossing* cr, degpu_batch_out* out,
+                                           degpu_crossing_out* co, void* stream) {
+    if (!cr || !co) return DEGPU_BAD_INPUT;
+    degpu_status v = validate(pb, cfg, in, out);
+    if (v != DEGPU_OK || in->n == 0) return v;
+    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
+    if (cr->component < 0 || cr->component >= pb->dim || cr->max_points < 0) return DEGPU_BAD_INPUT;
+    if (cr->direction < -1 || cr->direction > 1) return DEGPU_BAD_INPUT;
+    if (!co->count || (cr->max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
+    ensure_registered();
+    return crossing_impl(pb, cfg, in, cr, out, co, (cudaStream_t)stream);
 }
 
 degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,

@@ -62,6 +62,12 @@ struct EnsArgs {
     int32_t n_params;
     const int32_t* family;           // per-instance family id (multi-family persistent kernel)
     unsigned long long* ticket;      // persistent queue head
+    // crossing detection (erk_cross_kernel): y[cross_comp] - cross_value changes sign
+    int32_t cross_comp, cross_dir, cross_max;  // dir: 0 both, 1 from below, -1 from above
+    double cross_value;
+    double* cross_t;       // [cross_max][n]
+    double* cross_y;       // [cross_max][dmax][n]
+    int32_t* cross_count;  // [n]
 };
 
 // f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
@@ -94,8 +100,10 @@ __device__ __forceinline__ float narrow_rz(double x) {
     return __uint_as_float(sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
 }
 
-template <class Tab, class Rhs, class P, bool DENSE>
+// CROSS: crossing detection instead of output times (needs DENSE for the step's interpolant).
+template <class Tab, class Rhs, class P, bool DENSE, bool CROSS = false>
 struct Lane {
+    static_assert(!CROSS || DENSE, "crossing detection interpolates within the step");
     static constexpr int D = Rhs::D;
     static constexpr int I = Tab::I;
     static constexpr int NS = Tab::S;
@@ -135,6 +143,9 @@ struct Lane {
     int mod100;  // steps % 100, kept incrementally (the stiffness test runs every 100th attempt)
     int next_eval;
     int status;
+    double last_off;     // crossing detection: previous offset y[comp] - value
+    bool have_last_off;
+    int ncross;
     bool last_rejected;
     bool done;
 
@@ -344,7 +355,100 @@ struct Lane {
             }
         }
     }
+    // ----- crossing detection: CrossingSolout, src/solout/crossing.rs:200-330 -------------------
+    __device__ __forceinline__ double comp_value(const S* v, int comp) const {
+        S r = v[0];
+#pragma unroll
+        for (int c = 1; c < D; ++c)
+            if (c == comp) r = v[c];
+        return (double)r;
+    }
+    __device__ __forceinline__ double interp_offset(double te, int comp, double thr, const EnsArgs& a) const {
+        S v[D];
+        interpolate(te, v, a);
+        return comp_value(v, comp) - thr;
+    }
+    // find_crossing_newton (crossing.rs:254-328): Newton on the interpolant with a
+    // finite-difference derivative; false when it does not converge
+    __device__ bool find_crossing_newton(double t_lower, double t_upper, double off_lower, double off_upper,
+                                         double& t_out, const EnsArgs& a) const {
+        const double eps = 2.220446049250313e-16;
+        const int comp = a.cross_comp;
+        const double thr = a.cross_value;
+        double tt = t_lower - off_lower * (t_upper - t_lower) / (off_upper - off_lower);
+        const double tolerance = eps * 100.0;
+        double offset;
+        for (int it = 0; it < 10; ++it) {
+            offset = interp_offset(tt, comp, thr, a);
+            if (fabs(offset) < tolerance) {
+                t_out = tt;
+                return true;
+            }
+            const double delta_t = (t_upper - t_lower) * 1e-6;
+            const double t_plus = tt + delta_t;
+            const double offset_plus = interp_offset(t_plus, comp, thr, a);
+            const double derivative = (offset_plus - offset) / delta_t;
+            if (fabs(derivative) < eps * 10.0) break;
+            const double t_new = tt - offset / derivative;
+            if (t_new < t_lower || t_new > t_upper) {
+                tt = (t_lower + t_upper) / 2.0;
+            } else {
+                const double change = fabs(t_new - tt);
+                if (change < tolerance * 0.1) {
+                    tt = t_new;
+                    break;
+                }
+                tt = t_new;
+            }
+        }
+        offset = interp_offset(tt, comp, thr, a);
+        if (fabs(offset) < tolerance * 10.0) {
+            t_out = tt;
+            return true;
+        }
+        return false;
+    }
+    __device__ void crossing_solout(const EnsArgs& a) {
+        double cur = comp_value(y, a.cross_comp);
+        if constexpr (P::KAHAN) cur = cur - comp_value(yc, a.cross_comp);
+        const double offset = cur - a.cross_value;
+        if (have_last_off) {
+            if (rs_signum(last_off) != rs_signum(offset)) {
+                bool record;
+                if (a.cross_dir > 0)
+                    record = last_off < 0.0 && offset >= 0.0;
+                else if (a.cross_dir < 0)
+                    record = last_off > 0.0 && offset <= 0.0;
+                else
+                    record = true;
+                if (record) {
+                    double tc;
+                    if (!find_crossing_newton(t_prev, t, last_off, offset, tc, a)) {
+                        const double frac = -last_off / (offset - last_off);
+                        tc = t_prev + frac * (t - t_prev);
+                    }
+                    if (ncross < a.cross_max) {
+                        S v[D];
+                        interpolate(tc, v, a);
+                        const int64_t n = a.n;
+                        a.cross_t[(int64_t)ncross * n + inst] = tc;
+                        double* out = a.cross_y + ((int64_t)ncross * a.dmax) * n + inst;
+#pragma unroll
+                        for (int c = 0; c < D; ++c) out[(int64_t)c * n] = (double)v[c];
+                    }
+                    ncross += 1;
+                }
+            }
+        }
+        last_off = offset;
+        have_last_off = true;
+    }
+
     __device__ void solout(const EnsArgs& a) {
+        if constexpr (CROSS) {
+            crossing_solout(a);
+            return;
+        }
         if constexpr (DENSE) {
             int idx = next_eval;
             while (idx < a.n_eval) {
@@ -403,6 +507,11 @@ struct Lane {
         mod100 = 0;
         stiff = nonstiff = 0;
         next_eval = 0;
+        if constexpr (CROSS) {
+            have_last_off = false;
+            last_off = 0.0;
+            ncross = 0;
+        }
         last_rejected = false;
         done = false;
         status = DEGPU_COMPLETE;
@@ -905,6 +1014,7 @@ struct Lane {
         if (a.rejected) a.rejected[inst] = rej;
         if (a.fevals) a.fevals[inst] = fev;
         if (a.status) a.status[inst] = status;
+        if constexpr (CROSS) a.cross_count[inst] = ncross;
     }
 };
 
@@ -1058,6 +1168,17 @@ __global__ void __launch_bounds__(128) erk_thread_kernel(EnsArgs a) {
     int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= a.count) return;
     Lane<Tab, Rhs, P, DENSE> L;
+    L.begin(a.index ? a.index[w] : w, a);
+    while (!L.done) L.iterate(a);
+    L.finish(a);
+}
+
+// One instance per thread with crossing detection (degpu_solve_ensemble_crossing).
+template <class Tab, class Rhs, class P>
+__global__ void __launch_bounds__(128) erk_cross_kernel(EnsArgs a) {
+    int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= a.count) return;
+    Lane<Tab, Rhs, P, true, true> L;
     L.begin(a.index ? a.index[w] : w, a);
     while (!L.done) L.iterate(a);
     L.finish(a);

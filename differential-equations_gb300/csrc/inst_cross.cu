@@ -1,0 +1,21 @@
+// inst_cross.cu — crossing-detection kernels, FP64 fast and mixed arithmetic.
+#include "registry.cuh"
+
+namespace degpu {
+
+void register_cross_fast_mixed() {
+    register_cross_all_methods<RhsVanDerPol, PrecFast>();
+    register_cross_all_methods<RhsPendulum, PrecFast>();
+    register_cross_all_methods<RhsLorenz, PrecFast>();
+    register_cross_all_methods<RhsHarmonic, PrecFast>();
+    register_cross_all_methods<RhsBrusselator, PrecFast>();
+    register_cross_all_methods<RhsCr3bp, PrecFast>();
+    register_cross_all_methods<RhsVanDerPol, PrecMixed>();
+    register_cross_all_methods<RhsPendulum, PrecMixed>();
+    register_cross_all_methods<RhsLorenz, PrecMixed>();
+    register_cross_all_methods<RhsHarmonic, PrecMixed>();
+    register_cross_all_methods<RhsBrusselator, PrecMixed>();
+    register_cross_all_methods<RhsCr3bp, PrecMixed>();
+}
+
+}  // namespace degpu

@@ -60,6 +60,23 @@ void register_variant() {
     ens_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 1}] = &launch_ens<Tab, Rhs, P, true>;
 }
 
+// Crossing-detection kernels (degpu_solve_ensemble_crossing), keyed like ens_registry with dense = 1.
+std::map<VariantKey, EnsLaunchFn>& cross_registry();
+
+template <class Tab, class Rhs, class P>
+cudaError_t launch_cross(const EnsArgs& a, int, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    erk_cross_kernel<Tab, Rhs, P><<<(unsigned)((a.count + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class Rhs, class P>
+void register_cross_all_methods() {
+    cross_registry()[VariantKey{DEGPU_RK4, Rhs::ID, P::ID, 1}] = &launch_cross<TabRK4, Rhs, P>;
+    cross_registry()[VariantKey{DEGPU_DOPRI5, Rhs::ID, P::ID, 1}] = &launch_cross<TabDopri5, Rhs, P>;
+    cross_registry()[VariantKey{DEGPU_DOP853, Rhs::ID, P::ID, 1}] = &launch_cross<TabDop853, Rhs, P>;
+}
+
 // Resumable round kernels of the serving path (no dense output).
 struct RoundOps {
     size_t park_bytes;  // resident state per instance
@@ -135,6 +152,8 @@ void register_fast();
 void register_mixed();
 void register_parity_multi();
 void register_multi_fast_mixed();
+void register_cross_parity();
+void register_cross_fast_mixed();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to

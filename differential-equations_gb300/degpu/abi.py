@@ -63,6 +63,18 @@ class BatchOut(C.Structure):
     ]
 
 
+class Crossing(C.Structure):
+    _fields_ = [("component", C.c_int32), ("direction", C.c_int32), ("max_points", C.c_int32),
+                ("reserved", C.c_int32), ("threshold", C.c_double)]
+
+
+class CrossingOut(C.Structure):
+    _fields_ = [("t", DP), ("y", DP), ("count", I32P)]
+
+
+CROSS_BOTH, CROSS_POSITIVE, CROSS_NEGATIVE = 0, 1, -1
+
+
 class GrayScott(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("dx", C.c_double), ("Du", C.c_double),
                 ("Dv", C.c_double), ("F", C.c_double), ("k", C.c_double)]
@@ -93,6 +105,9 @@ SIGNATURES = {
                                             C.POINTER(BatchOut)]),
     "degpu_solve_ensemble_noalloc": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
                                                C.POINTER(BatchOut), C.c_void_p]),
+    "degpu_solve_ensemble_crossing": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                                C.POINTER(Crossing), C.POINTER(BatchOut), C.POINTER(CrossingOut),
+                                                C.c_void_p]),
     "degpu_eval_rhs": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP,
                                  C.c_void_p]),
     "degpu_register_rhs_nvrtc": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, I32P, C.c_char_p,

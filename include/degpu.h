@@ -210,6 +210,37 @@ degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* problem, const de
 degpu_status degpu_solve_ensemble_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
                                        const degpu_batch_in* in, degpu_batch_out* out);
 
+/* Crossing detection: the crate's `.crossing(component, threshold, direction)` output
+ * (CrossingSolout, src/solout/crossing.rs:200-330; IVP::crossing, src/ivp.rs:682-693).
+ * After every accepted step, the sign of y[component] - threshold is compared with its value
+ * at the previous step (the first value is taken at t0). On a change of sign that matches the
+ * direction, the crossing time is located on the step's interpolant:
+ *  - up to 10 Newton iterations with a finite-difference derivative;
+ *  - the linear estimate between the two steps when those do not converge.
+ * The time and the interpolated state are recorded. */
+typedef enum { DEGPU_CROSS_BOTH = 0, DEGPU_CROSS_POSITIVE = 1, DEGPU_CROSS_NEGATIVE = -1 } degpu_crossing_direction;
+
+typedef struct {
+    int32_t component;   /* index of the monitored state component, 0 <= component < dim      */
+    int32_t direction;   /* degpu_crossing_direction                                           */
+    int32_t max_points;  /* capacity per instance of the outputs below (>= 0)                  */
+    int32_t reserved;
+    double threshold;
+} degpu_crossing;
+
+typedef struct {
+    double* t;       /* [max_points][n] crossing times, in the order found; NaN past the count  */
+    double* y;       /* [max_points][dim][n] interpolated states at those times                */
+    int32_t* count;  /* [n] crossings found; can exceed max_points (the first ones are stored) */
+} degpu_crossing_out;
+
+/* degpu_solve_ensemble with crossing detection instead of output times (in->n_eval must be 0),
+ * device pointers, stream-ordered. Families: Van der Pol, pendulum, Lorenz, harmonic oscillator,
+ * Brusselator and CR3BP (DEGPU_UNSUPPORTED otherwise); every method and precision. */
+degpu_status degpu_solve_ensemble_crossing(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                           const degpu_batch_in* in, const degpu_crossing* crossing,
+                                           degpu_batch_out* out, degpu_crossing_out* crossing_out, void* stream);
+
 /* One evaluation of a built-in right-hand side for every instance (`ODE::diff`,
  * src/ode/ode.rs:20-44), device pointers: dydt[c*n+i] = f_i(t[i], y_i). */
 degpu_status degpu_eval_rhs(int32_t rhs_id, int32_t precision, int64_t n, int32_t dim, int32_t n_params,

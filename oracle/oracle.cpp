@@ -37,6 +37,29 @@ double cr_cos(double x) { return (double)q_cos((qreal_t)x); }
 
 using namespace oracle;
 
+// Runs body(i) for i in [0, n) on `threads` host threads with dynamic chunks (instances differ
+// widely in cost).
+template <class Body>
+static void for_instances(int64_t n, int threads, Body body) {
+    if (threads <= 1 || n < 2) {
+        for (int64_t i = 0; i < n; ++i) body(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    const int64_t chunk = 16;
+    std::vector<std::thread> pool;
+    for (int w = 0; w < threads; ++w)
+        pool.emplace_back([&]() {
+            for (;;) {
+                int64_t s = next.fetch_add(chunk);
+                if (s >= n) break;
+                int64_t e = std::min(n, s + chunk);
+                for (int64_t i = s; i < e; ++i) body(i);
+            }
+        });
+    for (auto& t : pool) t.join();
+}
+
 extern "C" {
 
 // Scalar math, exposed for tests of the math policy.
@@ -62,7 +85,8 @@ void oracle_libm_pow_batch(const double* x, const double* y, double* out, int64_
 
 // Solve one instance i of the batch into the outputs.
 static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
-                           degpu_batch_out* out, int64_t i, const Math& math) {
+                           degpu_batch_out* out, int64_t i, const Math& math, const degpu_crossing* cr = nullptr,
+                           degpu_crossing_out* co = nullptr) {
     const int64_t n = in->n;
     int rhs = in->family ? in->family[i] : pb->rhs_id;
     // per-instance dimension: given explicitly (ragged batches) or the family's own
@@ -91,8 +115,24 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
         te.assign(in->t_eval, in->t_eval + in->n_eval);
         tep = &te;
     }
+    CrossingSolout cs;
+    if (cr) {
+        cs.comp = cr->component;
+        cs.threshold = cr->threshold;
+        cs.direction = cr->direction;
+    }
     Result r = solve_one(cfg->method, ode, in->t0[i], in->tf[i], y0, set, math, tep,
-                         cfg->dense_mode == DEGPU_DENSE_HAIRER);
+                         cfg->dense_mode == DEGPU_DENSE_HAIRER, cr ? &cs : nullptr);
+    if (cr && co) {
+        const int64_t m = cr->max_points;
+        co->count[i] = (int32_t)cs.t.size();
+        for (int64_t k = 0; k < m; ++k) {
+            const bool have = (size_t)k < cs.t.size();
+            co->t[k * n + i] = have ? cs.t[k] : NAN;
+            for (int c = 0; c < dmax; ++c)
+                co->y[(k * dmax + c) * n + i] = (have && c < d) ? cs.y[k][c] : NAN;
+        }
+    }
     for (int c = 0; c < d; ++c) out->y_final[(int64_t)c * n + i] = r.y_final.size() == (size_t)d ? r.y_final[c] : NAN;
     for (int c = d; c < dmax; ++c) out->y_final[(int64_t)c * n + i] = 0.0;
     if (out->t_final) out->t_final[i] = r.t_final;
@@ -108,6 +148,19 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
                 out->dense[((int64_t)e * dmax + c) * n + i] = v;
             }
     }
+}
+
+// Crossing detection (CrossingSolout) for every instance; outputs laid out as
+// degpu_solve_ensemble_crossing's.  Returns 0 on success, 1 on bad input.
+int oracle_solve_ensemble_crossing(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                   const degpu_crossing* cr, degpu_batch_out* out, degpu_crossing_out* co,
+                                   int threads, int math_mode) {
+    if (!pb || !cfg || !in || !out || !cr || !co || in->n < 0 || !out->y_final || in->n_eval > 0) return 1;
+    if (cr->component < 0 || cr->component >= pb->dim || cr->max_points < 0) return 1;
+    Math math;
+    math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
+    for_instances(in->n, threads, [&](int64_t i) { solve_instance(pb, cfg, in, out, i, math, cr, co); });
+    return 0;
 }
 
 // Solve instances [0, n) of the batch with `threads` host threads.  math_mode: 0 libm, 1 cr.

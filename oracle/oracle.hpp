@@ -12,6 +12,7 @@
 //   State algebra ................... src/traits.rs:316-410
 //   cubic Hermite ................... src/interpolate.rs:40-60
 //   TEvalSolout ..................... src/solout/t_eval.rs:82-171
+//   CrossingSolout .................. src/solout/crossing.rs:200-330
 //   tableaus ........................ src/tableau/runge_kutta.rs:39-70, src/tableau/dorman_prince.rs:37-381
 //
 // Compile with -ffp-contract=off: Rust never contracts a*b+c into an FMA, so neither may this.
@@ -637,6 +638,88 @@ struct TEvalSolout {
 };
 
 // ---------------------------------------------------------------------------------------------
+// Crossing detection: CrossingSolout (src/solout/crossing.rs:200-330). After each call (at t0 and
+// after every accepted step) the offset y[comp] - threshold is compared in sign with the previous
+// one; a crossing in the requested direction is located by find_crossing_newton on the step's
+// interpolant, or by the linear estimate when that does not converge.
+// ---------------------------------------------------------------------------------------------
+struct CrossingSolout {
+    int comp = 0;
+    double threshold = 0.0;
+    int direction = 0;  // 0 both, 1 positive (from below), -1 negative
+    bool have_last = false;
+    double last_offset = 0.0;
+    std::vector<double> t;  // crossings in the order found
+    std::vector<State> y;
+
+    void solout(double t_curr, double t_prev, const State& y_curr, Interpolator& interp) {
+        const double offset = y_curr[comp] - threshold;
+        if (have_last) {
+            const bool is_crossing = rust_signum(last_offset) != rust_signum(offset);  // crossing.rs:210
+            if (is_crossing) {
+                bool record;  // crossing.rs:214-218
+                if (direction > 0)
+                    record = last_offset < 0.0 && offset >= 0.0;
+                else if (direction < 0)
+                    record = last_offset > 0.0 && offset <= 0.0;
+                else
+                    record = true;
+                if (record) {
+                    double tc;
+                    if (!find_crossing_newton(interp, t_prev, t_curr, last_offset, offset, tc)) {
+                        // crossing.rs:234-238: linear estimate
+                        const double frac = -last_offset / (offset - last_offset);
+                        tc = t_prev + frac * (t_curr - t_prev);
+                    }
+                    t.push_back(tc);
+                    y.push_back(interp.interpolate(tc));
+                }
+            }
+        }
+        last_offset = offset;
+        have_last = true;
+    }
+
+    // crossing.rs:254-328
+    bool find_crossing_newton(Interpolator& interp, double t_lower, double t_upper, double offset_lower,
+                              double offset_upper, double& t_out) const {
+        const double eps = std::numeric_limits<double>::epsilon();
+        double t = t_lower - offset_lower * (t_upper - t_lower) / (offset_upper - offset_lower);
+        const double tolerance = eps * 100.0;
+        double offset;
+        for (int it = 0; it < 10; ++it) {
+            offset = interp.interpolate(t)[comp] - threshold;
+            if (std::fabs(offset) < tolerance) {
+                t_out = t;
+                return true;
+            }
+            const double delta_t = (t_upper - t_lower) * 1e-6;
+            const double t_plus = t + delta_t;
+            const double offset_plus = interp.interpolate(t_plus)[comp] - threshold;
+            const double derivative = (offset_plus - offset) / delta_t;
+            if (std::fabs(derivative) < eps * 10.0) break;
+            const double t_new = t - offset / derivative;
+            if (t_new < t_lower || t_new > t_upper) {
+                t = (t_lower + t_upper) / 2.0;
+            } else {
+                const double change = std::fabs(t_new - t);
+                if (change < tolerance * 0.1) {
+                    t = t_new;
+                    break;
+                }
+                t = t_new;
+            }
+        }
+        offset = interp.interpolate(t)[comp] - threshold;
+        if (std::fabs(offset) < tolerance * 10.0) {
+            t_out = t;
+            return true;
+        }
+        return false;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
 // Numerical methods
 // ---------------------------------------------------------------------------------------------
 enum class Status { Uninitialized, Initialized, Solving, RejectedStep, Complete, Error };
@@ -941,7 +1024,7 @@ struct Result {
 
 template <class Solver>
 Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const State& y0,
-                 const std::vector<double>* t_eval) {
+                 const std::vector<double>* t_eval, CrossingSolout* cross = nullptr) {
     Result r;
     double integration_direction;
     {
@@ -968,6 +1051,7 @@ Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const Sta
     TEvalSolout te_obj(t_eval ? *t_eval : std::vector<double>{}, t0, tf, &r.dense);
     if (t_eval) te = &te_obj;
     if (te) te->solout(solver.t, solver.t_prev, solver.y, solver);
+    if (cross) cross->solout(solver.t, solver.t_prev, solver.y, solver);
     solver.status = Status::Solving;
 
     const double eps10 = std::numeric_limits<double>::epsilon() * 10.0;
@@ -991,6 +1075,7 @@ Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const Sta
         }
         r.accepted += 1;
         if (te) te->solout(solver.t, solver.t_prev, solver.y, solver);
+        if (cross) cross->solout(solver.t, solver.t_prev, solver.y, solver);
         if (std::fabs(tf - solver.t) <= eps10) break;
     }
     r.outcome.status = DEGPU_COMPLETE;
@@ -1001,19 +1086,20 @@ Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const Sta
 
 // One IVP solve with one of the three methods.
 inline Result solve_one(int method, const Ode& ode, double t0, double tf, const State& y0, const Settings& set,
-                        const Math& math, const std::vector<double>* t_eval, bool hairer_dense = false) {
+                        const Math& math, const std::vector<double>* t_eval, bool hairer_dense = false,
+                        CrossingSolout* cross = nullptr) {
     if (method == DEGPU_RK4) {
         FixedRK s;
         s.tab = tableau_rk4();
         s.set = set;
-        return solve_ode(s, ode, t0, tf, y0, t_eval);
+        return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
     }
     DormandPrince s;
     s.tab = method == DEGPU_DOP853 ? tableau_dop853() : tableau_dopri5();
     s.set = set;
     s.math = math;
     s.hairer_dense = hairer_dense;
-    return solve_ode(s, ode, t0, tf, y0, t_eval);
+    return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
 }
 
 }  // namespace oracle

@@ -37,6 +37,11 @@ def lib():
         L.oracle_solve_ensemble.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.MethodCfg),
                                             C.POINTER(abi.BatchIn), C.POINTER(abi.BatchOut), C.c_int, C.c_int]
         L.oracle_solve_ensemble.restype = C.c_int
+        L.oracle_solve_ensemble_crossing.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.MethodCfg),
+                                                     C.POINTER(abi.BatchIn), C.POINTER(abi.Crossing),
+                                                     C.POINTER(abi.BatchOut), C.POINTER(abi.CrossingOut), C.c_int,
+                                                     C.c_int]
+        L.oracle_solve_ensemble_crossing.restype = C.c_int
         L.oracle_eval_rhs.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP, C.c_int]
         for nm in ("oracle_cr_pow", "oracle_libm_pow"):
             getattr(L, nm).argtypes = [C.c_double, C.c_double]
@@ -113,4 +118,23 @@ def solve(batch: Batch, cfg, threads=None, math_mode=1):
     rc = lib().oracle_solve_ensemble(C.byref(batch.problem), C.byref(cfg), C.byref(bi), C.byref(bo), threads,
                                      math_mode)
     assert rc == 0
+    return out
+
+
+def solve_crossing(batch: Batch, cfg, component, threshold, direction=0, max_points=16, threads=None, math_mode=1):
+    """Oracle solve with crossing detection (CrossingSolout): returns the ordinary outputs plus
+    cross_t [max_points, n], cross_y [max_points, dim, n] and cross_count [n]."""
+    out = batch.new_outputs()
+    n, dim = batch.n, batch.problem.dim
+    ct = np.empty((max_points, n))
+    cy = np.empty((max_points, dim, n))
+    cc = np.empty(n, np.int32)
+    cr = abi.Crossing(component=component, direction=direction, max_points=max_points, threshold=threshold)
+    co = abi.CrossingOut(t=p(ct), y=p(cy), count=abi.ptr(cc, C.c_int32))
+    threads = threads or os.cpu_count() or 1
+    rc = lib().oracle_solve_ensemble_crossing(C.byref(batch.problem), C.byref(cfg), C.byref(batch.batch_in()),
+                                              C.byref(cr), C.byref(Batch.batch_out(out)), C.byref(co), threads,
+                                              math_mode)
+    assert rc == 0
+    out.update(cross_t=ct, cross_y=cy, cross_count=cc)
     return out
