@@ -237,6 +237,63 @@ def _oracle_solve(e, method, threads, math_mode=0):
     return o, time.perf_counter() - t
 
 
+def run_crossing(args, torch, dev, lib):
+    """Crossing detection on the uneven ensemble (1,048,576 instances, DOPRI5): the crate's
+    `.crossing(0, 0.0, Both)` output (first state component through zero), up to 8 points kept per
+    instance; FP64 parity and mixed; CPU baseline = the oracle's CrossingSolout on a sample."""
+    n = args.n
+    e = W.config1(n=n)
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    keep = dict(t0=T(e.t0), tf=T(e.tf), y0=T(e.y0), params=T(e.params), rtol=T(e.rtol), atol=T(e.atol),
+                family=T(e.family, torch.int32))
+    bi = abi.BatchIn(n=n, t0=abi.ptr(keep["t0"]), tf=abi.ptr(keep["tf"]), y0=abi.ptr(keep["y0"]),
+                     params=abi.ptr(keep["params"]), rtol=abi.ptr(keep["rtol"]), atol=abi.ptr(keep["atol"]),
+                     family=abi.ptr(keep["family"], C.c_int32), n_eval=0)
+    mp = 8
+    E = lambda *shape, dt=torch.float64: torch.empty(shape, dtype=dt, device=dev)
+    out = dict(y_final=E(3, n), t_final=E(n), accepted=E(n, dt=torch.int64), rejected=E(n, dt=torch.int64),
+               fevals=E(n, dt=torch.int64), status=E(n, dt=torch.int32), ct=E(mp, n), cy=E(mp, 3, n),
+               cc=E(n, dt=torch.int32))
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
+                      accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
+                      fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
+    cr = abi.Crossing(component=0, direction=abi.CROSS_BOTH, max_points=mp, threshold=0.0)
+    co = abi.CrossingOut(t=abi.ptr(out["ct"]), y=abi.ptr(out["cy"]), count=abi.ptr(out["cc"], C.c_int32))
+    prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
+    stream = torch.cuda.Stream(device=dev)
+    res = {}
+    for name, prec in (("mixed", abi.MIXED), ("fp64-parity", abi.FP64_PARITY)):
+        cfg = abi.default_cfg(abi.DOPRI5)
+        cfg.precision, cfg.max_steps = prec, e.max_steps
+        f = lambda: lib.degpu_solve_ensemble_crossing(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(cr),
+                                                      C.byref(bo), C.byref(co), C.c_void_p(stream.cuda_stream))
+        ms = _clock_ms(f, stream, torch, max(1, args.steps))
+        cnt = out["cc"].cpu().numpy()
+        res[name] = {"solves_per_s": n / (ms * 1e-3), "ms": ms, "crossings": int(cnt.sum()),
+                     "crossings_per_s": float(cnt.sum()) / (ms * 1e-3)}
+        print(json.dumps({"crossing_variant": name, **res[name]}), flush=True)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib as O
+
+    s_n = args.cpu_sample
+    s = e.subset(np.arange(s_n))
+    b = O.Batch(s.rhs_id, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, s.rtol, s.atol, family=s.family)
+    cfg = abi.default_cfg(abi.DOPRI5)
+    cfg.max_steps = e.max_steps
+    t = time.perf_counter()
+    O.solve_crossing(b, cfg, 0, 0.0, abi.CROSS_BOTH, mp, threads=threads, math_mode=0)
+    dt = time.perf_counter() - t
+    line = {"metric": "IVP solves/sec with crossing detection (uneven ensemble, DOPRI5)",
+            "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 parity beside)", "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": f"uneven ensemble {n} instances, crossing(0, 0.0, Both), {mp} points kept"},
+            "variants": res,
+            "cpu_baseline": {"value": s_n / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"first {s_n} instances (host libm)"}}
+    print(json.dumps(line))
+
+
 def run_lorenz4096(args, torch, dev, lib):
     """4096 Lorenz IVPs (d=3), DOPRI5 rtol=1e-8 atol=1e-10 on [0, 20]: plain FP64 parity kernel,
     persistent parity kernel, and the CPU oracle with every host thread."""
@@ -546,7 +603,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=12000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--workload", default="uneven", choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving"],
+    ap.add_argument("--workload", default="uneven",
+                    choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing"],
                     help="uneven = the headline 1M-instance ensemble; the others print their own line")
     ap.add_argument("--fpu-n", type=int, default=131072)
     ap.add_argument("--fpu-cpu-sample", type=int, default=200)
@@ -579,7 +637,7 @@ def main():
     if args.workload != "uneven":
         if rank == 0:
             {"lorenz4096": run_lorenz4096, "fpu": run_fpu, "gray-scott": run_gray_scott,
-             "serving": run_serving}[args.workload](args, torch, dev, lib)
+             "serving": run_serving, "crossing": run_crossing}[args.workload](args, torch, dev, lib)
         return
 
     # each rank solves its own slice of instances (weak scaling: instances are independent)

@@ -515,6 +515,76 @@ degpu_status degpu_solve_ensemble_crossing(const degpu_problem* pb, const degpu_
     return crossing_impl(pb, cfg, in, cr, out, co, (cudaStream_t)stream);
 }
 
+degpu_status degpu_solve_ensemble_crossing_host(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                                const degpu_batch_in* in, const degpu_crossing* cr,
+                                                degpu_batch_out* out, degpu_crossing_out* co) {
+    if (!cr || !co) return DEGPU_BAD_INPUT;
+    degpu_status v = validate(pb, cfg, in, out);
+    if (v != DEGPU_OK || in->n == 0) return v;
+    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
+    if (cr->component < 0 || cr->component >= pb->dim || cr->max_points < 0) return DEGPU_BAD_INPUT;
+    if (cr->direction < -1 || cr->direction > 1) return DEGPU_BAD_INPUT;
+    if (!co->count || (cr->max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
+    ensure_registered();
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    degpu_status st = DEGPU_OK;
+    {
+        const int64_t n = in->n;
+        const size_t d = (size_t)pb->dim, np = (size_t)pb->n_params, m = (size_t)cr->max_points;
+        Scratch sc(s);
+        degpu_batch_in din = *in;
+        degpu_batch_out dout{};
+        degpu_crossing_out dco{};
+        auto up = [&](const void* src, size_t bytes) -> void* {
+            if (!src) return nullptr;
+            void* p = sc.alloc<char>(bytes);
+            if (p) cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, s);
+            return p;
+        };
+        din.t0 = (const double*)up(in->t0, n * 8);
+        din.tf = (const double*)up(in->tf, n * 8);
+        din.y0 = (const double*)up(in->y0, d * n * 8);
+        din.params = np > 0 ? (const double*)up(in->params, np * n * 8) : nullptr;
+        din.rtol = (const double*)up(in->rtol, n * 8);
+        din.atol = (const double*)up(in->atol, n * 8);
+        din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
+        dout.y_final = sc.alloc<double>(d * n);
+        dout.t_final = out->t_final ? sc.alloc<double>(n) : nullptr;
+        dout.accepted = out->accepted ? sc.alloc<int64_t>(n) : nullptr;
+        dout.rejected = out->rejected ? sc.alloc<int64_t>(n) : nullptr;
+        dout.fevals = out->fevals ? sc.alloc<int64_t>(n) : nullptr;
+        dout.status = out->status ? sc.alloc<int32_t>(n) : nullptr;
+        dco.t = m > 0 ? sc.alloc<double>(m * n) : nullptr;
+        dco.y = m > 0 ? sc.alloc<double>(m * d * n) : nullptr;
+        dco.count = sc.alloc<int32_t>(n);
+        if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final || !dco.count ||
+            (m > 0 && (!dco.t || !dco.y))) {
+            st = DEGPU_OOM;
+        } else {
+            st = crossing_impl(pb, cfg, &din, cr, &dout, &dco, s);
+        }
+        if (st == DEGPU_OK) {
+            auto down = [&](void* dst, const void* src, size_t bytes) {
+                if (dst && src) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+            };
+            down(out->y_final, dout.y_final, d * n * 8);
+            down(out->t_final, dout.t_final, n * 8);
+            down(out->accepted, dout.accepted, n * 8);
+            down(out->rejected, dout.rejected, n * 8);
+            down(out->fevals, dout.fevals, n * 8);
+            down(out->status, dout.status, n * 4);
+            down(co->t, dco.t, m * n * 8);
+            down(co->y, dco.y, m * d * n * 8);
+            down(co->count, dco.count, n * 4);
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess && st == DEGPU_OK) st = DEGPU_CUDA_ERROR;
+    }
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return st;
+}
+
 degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                                        degpu_batch_out* out) {
     degpu_status v = validate(pb, cfg, in, out);

@@ -19,7 +19,7 @@ import numpy as np
 from . import abi
 
 __all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
-           "Solution", "set_mixed_min_rtol", "mixed_min_rtol"]
+           "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing"]
 
 STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
                 abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness"}
@@ -148,6 +148,40 @@ class EnsembleResult:
     status: np.ndarray
 
 
+def solve_ensemble_crossing(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
+                            component: int, threshold: float, direction: int = abi.CROSS_BOTH,
+                            max_points: int = 16, family=None, n_params: Optional[int] = None):
+    """Solve n IVPs (host arrays) with crossing detection (degpu_solve_ensemble_crossing_host):
+    the crate's `.crossing(component, threshold, direction)` output.  Returns the EnsembleResult
+    and (t [max_points, n], y [max_points, dim, n], count [n])."""
+    lib = abi.load()
+    y0 = np.asarray(y0, dtype=np.float64)
+    n = y0.shape[1]
+    bc = lambda v: _f64(np.broadcast_to(np.asarray(v, dtype=np.float64), (n,)).copy())
+    t0, tf, rtol, atol = bc(t0), bc(tf), bc(rtol), bc(atol)
+    y0 = _f64(y0)
+    params = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, n)) if params is not None \
+        and np.size(params) else np.zeros((1, n))
+    np_ = n_params if n_params is not None else params.shape[0]
+    fam_a = None if family is None else np.ascontiguousarray(family, dtype=np.int32)
+    out = dict(y_final=np.empty((dim, n)), t_final=np.empty(n), dense=None, accepted=np.empty(n, np.int64),
+               rejected=np.empty(n, np.int64), fevals=np.empty(n, np.int64), status=np.empty(n, np.int32))
+    ct, cy, cc = np.empty((max_points, n)), np.empty((max_points, dim, n)), np.empty(n, np.int32)
+    prob = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=np_)
+    bi = abi.BatchIn(n=n, t0=abi.ptr(t0), tf=abi.ptr(tf), y0=abi.ptr(y0), params=abi.ptr(params),
+                     rtol=abi.ptr(rtol), atol=abi.ptr(atol), family=abi.ptr(fam_a, C.c_int32), n_eval=0)
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
+                      accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
+                      fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
+    cr = abi.Crossing(component=component, direction=direction, max_points=max_points, threshold=threshold)
+    co = abi.CrossingOut(t=abi.ptr(ct), y=abi.ptr(cy), count=abi.ptr(cc, C.c_int32))
+    rc = lib.degpu_solve_ensemble_crossing_host(C.byref(prob), C.byref(method.cfg), C.byref(bi), C.byref(cr),
+                                                C.byref(bo), C.byref(co))
+    if rc != abi.OK:
+        raise DegpuError(rc, "degpu_solve_ensemble_crossing_host")
+    return EnsembleResult(**out), (ct, cy, cc)
+
+
 def set_mixed_min_rtol(method: int, min_rtol: float) -> None:
     """Mixed-precision bound of DOPRI5 / DOP853 (degpu_set_mixed_min_rtol): in a MIXED solve an
     instance with rtol below it runs in FP64_FAST arithmetic; 0 disables the split."""
@@ -220,6 +254,7 @@ class IVP:
         self.system, self.t0, self.tf, self.y0 = system, t0, tf, np.asarray(y0, dtype=np.float64).reshape(-1)
         self._method: Optional[ExplicitRungeKutta] = None
         self._t_eval = None
+        self._crossing = None
 
     @classmethod
     def ode(cls, system: System, t0, tf, y0):
@@ -231,11 +266,29 @@ class IVP:
 
     def t_eval(self, pts):
         self._t_eval = list(pts)
+        self._crossing = None
+        return self
+
+    def crossing(self, component: int, threshold: float, direction: int = abi.CROSS_BOTH, max_points: int = 1024):
+        """The crate's IVP::crossing (src/ivp.rs:682-693): the solution holds the points where
+        y[component] crosses `threshold` in `direction` (replaces t_eval)."""
+        self._crossing = (component, threshold, direction, max_points)
+        self._t_eval = None
         return self
 
     def solve(self) -> Solution:
         m = self._method or ExplicitRungeKutta.dopri5()
         d = len(self.y0)
+        if self._crossing is not None:
+            comp, thr, direction, cap = self._crossing
+            r, (ct, cy, cc) = solve_ensemble_crossing(
+                self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),
+                np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m._rtol], [m._atol], m,
+                comp, thr, direction, cap)
+            k = min(int(cc[0]), cap)
+            st = STATUS_NAMES.get(int(r.status[0]), str(int(r.status[0])))
+            return Solution([float(v) for v in ct[:k, 0]], [cy[j, :, 0].copy() for j in range(k)], st,
+                            int(r.accepted[0]), int(r.rejected[0]), int(r.fevals[0]))
         r = solve_ensemble(self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),
                            np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m._rtol], [m._atol], m,
                            t_eval=self._t_eval, dims=[d] if self.system.rhs_id == abi.RHS["FPU_BETA"] else None)

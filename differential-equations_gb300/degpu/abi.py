@@ -108,6 +108,8 @@ SIGNATURES = {
     "degpu_solve_ensemble_crossing": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
                                                 C.POINTER(Crossing), C.POINTER(BatchOut), C.POINTER(CrossingOut),
                                                 C.c_void_p]),
+    "degpu_solve_ensemble_crossing_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                                     C.POINTER(Crossing), C.POINTER(BatchOut), C.POINTER(CrossingOut)]),
     "degpu_eval_rhs": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP,
                                  C.c_void_p]),
     "degpu_register_rhs_nvrtc": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, I32P, C.c_char_p,

@@ -60,8 +60,9 @@ typedef enum { DEGPU_RK4 = 0, DEGPU_DOPRI5 = 1, DEGPU_DOP853 = 2 } degpu_method;
  *  FP64_PARITY — every operation in the crate's order, no FMA contraction, correctly rounded
  *                pow/sin/cos: reproduces the crate's step counts and states bit for bit.
  *  FP64_FAST   — FP64 with FMA contraction and the fast CUDA math library.
- *  MIXED       — stage right-hand sides and stage combinations in FP32, y_{n+1} accumulated with
- *                Kahan compensation; t, h, the error norm and the step-size controller in FP64.
+ *  MIXED       — stage right-hand sides, stage combinations, the error norm, the step-size
+ *                controller and the step size in FP32; y_{n+1} accumulated with Kahan
+ *                compensation; t in FP64 (RK4: t and h in FP64).
  *                Instances whose rtol is below the method's mixed-precision bound
  *                (degpu_set_mixed_min_rtol) run in FP64_FAST arithmetic instead. */
 typedef enum { DEGPU_FP64_PARITY = 0, DEGPU_FP64_FAST = 1, DEGPU_MIXED = 2 } degpu_precision;
@@ -240,6 +241,11 @@ typedef struct {
 degpu_status degpu_solve_ensemble_crossing(const degpu_problem* problem, const degpu_method_cfg* cfg,
                                            const degpu_batch_in* in, const degpu_crossing* crossing,
                                            degpu_batch_out* out, degpu_crossing_out* crossing_out, void* stream);
+
+/* Same with HOST pointers, synchronous (as degpu_solve_ensemble_host). */
+degpu_status degpu_solve_ensemble_crossing_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                                const degpu_batch_in* in, const degpu_crossing* crossing,
+                                                degpu_batch_out* out, degpu_crossing_out* crossing_out);
 
 /* One evaluation of a built-in right-hand side for every instance (`ODE::diff`,
  * src/ode/ode.rs:20-44), device pointers: dydt[c*n+i] = f_i(t[i], y_i). */

@@ -132,3 +132,28 @@ def test_crossing_bad_input():
                                              C.byref(co), None) == abi.BAD_INPUT
     assert lib.degpu_solve_ensemble_crossing(C.byref(prob), C.byref(cfg), C.byref(bi), None, C.byref(bo),
                                              C.byref(co), None) == abi.BAD_INPUT
+
+
+def test_ivp_builder_crossing_and_host_entry():
+    """IVP::ode(..).method(..).crossing(0, 0.0, Both).solve() on the harmonic oscillator: zeros of
+    cos t on [0, 10]; the host entry point returns what the device entry point returns."""
+    import math
+
+    import degpu
+
+    m = degpu.ExplicitRungeKutta.dop853().rtol(1e-11).atol(1e-11).dense_mode(abi.DENSE_HAIRER)
+    sol = degpu.IVP.ode(degpu.System.harmonic(1.0), 0.0, 10.0, [1.0, 0.0]).method(m).crossing(0, 0.0).solve()
+    assert sol.status == "Complete"
+    assert np.allclose(sol.t, [math.pi / 2 + j * math.pi for j in range(3)], rtol=0, atol=1e-9)
+    assert np.allclose([y[0] for y in sol.y], 0.0, atol=1e-9)
+
+    e = family_ensemble("PENDULUM", 300, first=777)
+    cfg = cfg_for(abi.DOPRI5)
+    g = gpu_crossing(e, cfg, 1, 0.0, abi.CROSS_BOTH, 5)
+    meth = degpu.ExplicitRungeKutta(abi.DOPRI5)
+    meth.cfg = cfg
+    r, (ct, cy, cc) = degpu.solve_ensemble_crossing(e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol,
+                                                    meth, 1, 0.0, abi.CROSS_BOTH, 5)
+    assert np.array_equal(cc, g["cross_count"])
+    assert np.array_equal(ct, g["cross_t"], equal_nan=True) and np.array_equal(cy, g["cross_y"], equal_nan=True)
+    assert np.array_equal(r.accepted, g["accepted"]) and np.array_equal(r.y_final, g["y_final"])
