@@ -410,6 +410,18 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
             cudaMemsetAsync(co->y, 0xFF, m * pb->dim * sizeof(double), s) != cudaSuccess)
             return DEGPU_CUDA_ERROR;
     }
+    // the production families go through the longest-first plan lists (lanes of a warp get
+    // instances of similar cost); others through host-built lists
+    bool prod = true;
+    for (auto& kv : lists) {
+        const int f = kv.first.first;
+        prod = prod && (f == DEGPU_RHS_VAN_DER_POL || f == DEGPU_RHS_PENDULUM || f == DEGPU_RHS_LORENZ);
+    }
+    if (prod) {
+        EnsArgs ma = a;
+        ma.count = n;
+        return sorted_thread_solve(cfg, ma, in->family, pb->rhs_id, true, s, true);
+    }
     for (auto& kv : lists) {
         EnsArgs ga = a;
         if (lists.size() > 1 || in->family) {

@@ -355,6 +355,43 @@ struct Lane {
             }
         }
     }
+    // The interpolant at the normalised position sg in the step ([0, 1] from t_prev to t), in the
+    // stage arithmetic S: the mixed form's crossing search runs in this coordinate in FP32.
+    __device__ void interpolate_sigma(S ss, S* out, const EnsArgs& a) const {
+        if constexpr (DENSE) {
+            if constexpr (Tab::ADAPTIVE) {
+                const S ss1 = (S)1 - ss;
+                const bool hairer = a.dense_mode == DEGPU_DENSE_HAIRER;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    S accv = cont[O - 1][c];
+#pragma unroll
+                    for (int i = O - 2; i >= 1; --i) {
+                        S f;
+                        if (i >= 4) {
+                            bool odd = ((O - 1 - i) % 2) == 1;
+                            if (hairer) odd = !odd;
+                            f = odd ? ss1 : ss;
+                        } else {
+                            f = (i % 2 == 1) ? ss1 : ss;
+                        }
+                        accv = accv * f;
+                        accv = accv + cont[i][c];
+                    }
+                    out[c] = cont[0][c] + ss * accv;
+                }
+            } else {
+                const S hh = P::from(t - t_prev);
+                const S s2 = ss * ss, s3 = s2 * ss;
+                const S c00 = (S)2 * s3 - (S)3 * s2 + (S)1, c10 = (s3 - (S)2 * s2 + ss) * hh;
+                const S c01 = (S)-2 * s3 + (S)3 * s2, c11 = (s3 - s2) * hh;
+#pragma unroll
+                for (int c = 0; c < D; ++c)
+                    out[c] = c00 * cont[0][c] + c10 * cont[1][c] + c01 * y[c] + c11 * k0[c];
+            }
+        }
+    }
+
     // ----- crossing detection: CrossingSolout, src/solout/crossing.rs:200-330 -------------------
     __device__ __forceinline__ double comp_value(const S* v, int comp) const {
         S r = v[0];
@@ -408,6 +445,39 @@ struct Lane {
         }
         return false;
     }
+    // Mixed form: find_crossing_newton's iteration on sg in [0, 1] in FP32, with tolerances scaled
+    // to FP32 (100 units of FP32 rounding of the threshold's magnitude); the linear estimate when
+    // it does not converge.
+    __device__ float find_crossing_sigma(float off_l, float off_u, const EnsArgs& a) const {
+        const int comp = a.cross_comp;
+        const float thr = (float)a.cross_value;
+        const float tol = 100.0f * 1.1920929e-7f * fmaxf(1.0f, fabsf(thr));
+        const float lin = -off_l / (off_u - off_l);
+        auto off_at = [&](float sg) {
+            S v[D];
+            interpolate_sigma(sg, v, a);
+            return (float)comp_value(v, comp) - thr;
+        };
+        float sg = lin, offset;
+        for (int it = 0; it < 10; ++it) {
+            offset = off_at(sg);
+            if (fabsf(offset) < tol) return sg;
+            const float ds = 1e-6f;
+            const float derivative = (off_at(sg + ds) - offset) / ds;
+            if (fabsf(derivative) < 10.0f * 1.1920929e-7f) break;
+            const float s_new = sg - offset / derivative;
+            if (s_new < 0.0f || s_new > 1.0f) {
+                sg = 0.5f;
+            } else {
+                const float change = fabsf(s_new - sg);
+                sg = s_new;
+                if (change < tol * 0.1f) break;
+            }
+        }
+        offset = off_at(sg);
+        return fabsf(offset) < tol * 10.0f ? sg : lin;
+    }
+
     __device__ void crossing_solout(const EnsArgs& a) {
         double cur = comp_value(y, a.cross_comp);
         if constexpr (P::KAHAN) cur = cur - comp_value(yc, a.cross_comp);
@@ -423,13 +493,20 @@ struct Lane {
                     record = true;
                 if (record) {
                     double tc;
-                    if (!find_crossing_newton(t_prev, t, last_off, offset, tc, a)) {
-                        const double frac = -last_off / (offset - last_off);
-                        tc = t_prev + frac * (t - t_prev);
+                    S v[D];
+                    if constexpr (P::KAHAN) {
+                        // mixed: the same search in the step's normalised coordinate, in FP32
+                        const float sg = find_crossing_sigma((float)last_off, (float)offset, a);
+                        tc = t_prev + (double)sg * (t - t_prev);
+                        if (ncross < a.cross_max) interpolate_sigma(sg, v, a);
+                    } else {
+                        if (!find_crossing_newton(t_prev, t, last_off, offset, tc, a)) {
+                            const double frac = -last_off / (offset - last_off);
+                            tc = t_prev + frac * (t - t_prev);
+                        }
+                        if (ncross < a.cross_max) interpolate(tc, v, a);
                     }
                     if (ncross < a.cross_max) {
-                        S v[D];
-                        interpolate(tc, v, a);
                         const int64_t n = a.n;
                         a.cross_t[(int64_t)ncross * n + inst] = tc;
                         double* out = a.cross_y + ((int64_t)ncross * a.dmax) * n + inst;

@@ -143,7 +143,8 @@ degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const in
 // over its longest-first work list: the lanes of a warp get instances of similar cost, so a warp
 // is not held by one long instance while its other lanes sit finished.
 degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev,
-                                 int fam_const, bool dense, cudaStream_t s) {
+                                 int fam_const, bool dense, cudaStream_t s, bool crossing) {
+    auto& reg = crossing ? cross_registry() : ens_registry();
     const double split = mixed_split(cfg);
     static const int ids[3] = {DEGPU_RHS_VAN_DER_POL, DEGPU_RHS_PENDULUM, DEGPU_RHS_LORENZ};
     Plan pl;
@@ -157,8 +158,8 @@ degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, 
     for (int l = NLISTS - 1; l >= 0 && st == DEGPU_OK; --l) {  // FP64 class first
         if (hc[l] == 0) continue;
         const int prec = l >= 3 ? DEGPU_FP64_FAST : cfg->precision;
-        auto it = ens_registry().find(VariantKey{cfg->method, ids[l % 3], prec, dense ? 1 : 0});
-        if (it == ens_registry().end()) {
+        auto it = reg.find(VariantKey{cfg->method, ids[l % 3], prec, dense ? 1 : 0});
+        if (it == reg.end()) {
             st = DEGPU_UNSUPPORTED;
             break;
         }

@@ -184,9 +184,10 @@ __device__ __forceinline__ double plan_log2_cost(int slot, double span, double r
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
                          bool dense, cudaStream_t s);
 
-// One run-to-completion launch per (precision class, family) over the same longest-first lists.
+// One run-to-completion launch per (precision class, family) over the same longest-first lists;
+// `crossing` launches the crossing-detection kernels (dense = 1) instead.
 degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev,
-                                 int fam_const, bool dense, cudaStream_t s);
+                                 int fam_const, bool dense, cudaStream_t s, bool crossing = false);
 
 // Mixed-precision split of a solve (degpu_set_mixed_min_rtol): the rtol bound below which an
 // instance of a DEGPU_MIXED solve runs the DEGPU_FP64_FAST variant; 0 when cfg asks for another
