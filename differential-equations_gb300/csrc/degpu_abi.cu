@@ -60,6 +60,8 @@ void ensure_registered() {
         register_multi_fast_mixed();
         register_cross_parity();
         register_cross_fast_mixed();
+        register_embedded_parity();
+        register_embedded_fast_mixed();
     });
 }
 
@@ -81,7 +83,9 @@ struct Scratch {
     }
 };
 
-static bool valid_method(int m) { return m == DEGPU_RK4 || m == DEGPU_DOPRI5 || m == DEGPU_DOP853; }
+static bool valid_method(int m) {
+    return m == DEGPU_RK4 || m == DEGPU_DOPRI5 || m == DEGPU_DOP853 || m == DEGPU_RKF45 || m == DEGPU_CASH_KARP;
+}
 
 // Mixed-precision bounds of DOPRI5 [0] and DOP853 [1]: the rtol below which an instance of a
 // mixed solve runs in FP64.  Below the FP32 rounding level of the stage states the error
@@ -113,9 +117,9 @@ static std::atomic<double>& mixed_bound(int m) {
 }
 
 double mixed_split(const degpu_method_cfg* cfg) {
-    if (cfg->precision != DEGPU_MIXED) return 0.0;
-    if (cfg->method != DEGPU_DOPRI5 && cfg->method != DEGPU_DOP853) return 0.0;
-    return mixed_bound(cfg->method).load();
+    if (cfg->precision != DEGPU_MIXED || cfg->method == DEGPU_RK4) return 0.0;
+    // the order-5 embedded pairs (RKF45, Cash-Karp) share DOPRI5's bound
+    return mixed_bound(cfg->method == DEGPU_DOP853 ? DEGPU_DOP853 : DEGPU_DOPRI5).load();
 }
 
 static bool valid_prec(int p) { return p == DEGPU_FP64_PARITY || p == DEGPU_FP64_FAST || p == DEGPU_MIXED; }
@@ -251,7 +255,8 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
             EnsArgs ma = a;
             ma.count = n;
             const int32_t* fam_dev = family_host ? in->family : nullptr;
-            if (kernel_sel == DEGPU_KERNEL_PERSISTENT) return multi_solve(cfg, ma, fam_dev, pb->rhs_id, dense, s);
+            if (kernel_sel == DEGPU_KERNEL_PERSISTENT && multi_registry().count({cfg->method, cfg->precision, dense ? 1 : 0}))
+                return multi_solve(cfg, ma, fam_dev, pb->rhs_id, dense, s);
             return sorted_thread_solve(cfg, ma, fam_dev, pb->rhs_id, dense, s);
         }
     }
@@ -473,6 +478,7 @@ degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol) {
 }
 
 double degpu_mixed_min_rtol(int32_t method) {
+    if (method == DEGPU_RKF45 || method == DEGPU_CASH_KARP) method = DEGPU_DOPRI5;
     if (method != DEGPU_DOPRI5 && method != DEGPU_DOP853) return 0.0;
     return mixed_bound(method).load();
 }

@@ -108,10 +108,10 @@ struct Lane {
     static constexpr int I = Tab::I;
     static constexpr int NS = Tab::S;
     static constexpr int O = Tab::ORDER;
-    static constexpr int NC = DENSE ? (Tab::ADAPTIVE ? O : 2) : 1;  // RK4 keeps y_prev, dydt_prev
+    static constexpr int NC = DENSE ? (Tab::DP ? O : 2) : 1;  // Hermite keeps y_prev, dydt_prev
     static constexpr int NPP = Rhs::NP > 0 ? Rhs::NP : 1;
     using S = typename P::S;
-    static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
+    static constexpr bool MIX = P::KAHAN && Tab::DP;
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
     static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
@@ -307,7 +307,7 @@ struct Lane {
     }
     __device__ void interpolate(double te, S* out, const EnsArgs& a) const {
         if constexpr (DENSE) {
-            if constexpr (Tab::ADAPTIVE) {
+            if constexpr (Tab::DP) {
                 // ordinary.rs:312-333
                 double s = (te - t_prev) / h_prev;
                 double s1 = 1.0 - s;
@@ -359,7 +359,7 @@ struct Lane {
     // stage arithmetic S: the mixed form's crossing search runs in this coordinate in FP32.
     __device__ void interpolate_sigma(S ss, S* out, const EnsArgs& a) const {
         if constexpr (DENSE) {
-            if constexpr (Tab::ADAPTIVE) {
+            if constexpr (Tab::DP) {
                 const S ss1 = (S)1 - ss;
                 const bool hairer = a.dense_mode == DEGPU_DENSE_HAIRER;
 #pragma unroll
@@ -602,7 +602,10 @@ struct Lane {
         dir = sg;
         double h0 = a.h0;
         if constexpr (Tab::ADAPTIVE) {
-            if (h0 == 0.0) h0 = initial_step(t0, a);
+            if (h0 == 0.0) {
+                h0 = initial_step(t0, a);
+                if constexpr (!Tab::DP) fev += 2;  // adaptive/ordinary.rs:28 counts them a second time
+            }
         } else {
             if (h0 == 0.0) h0 = fabs(tf - t0) / 100.0;
         }
@@ -623,7 +626,7 @@ struct Lane {
         else
             rhs(t, y, k0);
         fev += 1;
-        if constexpr (DENSE && !Tab::ADAPTIVE) {
+        if constexpr (DENSE && !Tab::DP) {
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 cont[0][c] = y[c];
@@ -900,7 +903,7 @@ struct Lane {
 
     // dense-output preparation, ordinary.rs:196-235 (k[S..I) computed here for DOP853)
     __device__ void dense_coefficients(S (&k)[I][D], const S* ynew, const S* dydt) {
-        if constexpr (DENSE && Tab::ADAPTIVE) {
+        if constexpr (DENSE && Tab::DP) {
             S hs;
             if constexpr (MIX)
                 hs = hf;
@@ -952,6 +955,145 @@ struct Lane {
                 }
             });
         }
+    }
+
+    // ----- one step of the Adaptive family (RKF45, Cash-Karp): adaptive/ordinary.rs:63-212 -----
+    // returns 1 accepted, 2 rejected, 3 error.  `stiff` counts consecutive rejections here.
+    __device__ int step_embedded(const EnsArgs& a) {
+        if (fabs(h) < fabs(h_prev) * 1e-14) {
+            status = DEGPU_ERR_STEP_SIZE;
+            return 3;
+        }
+        if (steps >= a.max_steps) {
+            status = DEGPU_ERR_MAX_STEPS;
+            return 3;
+        }
+        steps += 1;
+        S k[NS][D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) k[0][c] = k0[c];
+        S ys[D];
+        static_for<1, NS>([&](auto i) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = y[c];
+            static_for<0, decltype(i)::value>([&](auto j) {
+                constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
+                if constexpr (aij != 0.0) {
+                    S ah = stage_coef(aij);
+#pragma unroll
+                    for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                }
+            });
+            rhs(t + Tab::c(i) * h, ys, k[i]);
+        });
+        fev += NS - 1;
+        // y_high = y + sum (b_i h) k_i and y_low = y + sum (bl_i h) k_i, each accumulated in order
+        // (add_scaled, traits.rs:316-320); their difference is the error estimate
+        S yh[D], ycn[D], err[D];
+        if constexpr (P::KAHAN) {
+            // mixed: the increments in FP32, y_high added to y with Kahan compensation
+            S inc[D], es[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) inc[c] = es[c] = (S)0;
+            static_for<0, NS>([&](auto i) {
+                constexpr double bv = Tab::b(decltype(i)::value), lv = Tab::bl(decltype(i)::value);
+                if constexpr (bv != 0.0) {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) inc[c] = inc[c] + (S)bv * k[i][c];
+                }
+                if constexpr (bv - lv != 0.0) {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) es[c] = es[c] + (S)(bv - lv) * k[i][c];
+                }
+            });
+            const S hs = P::from(h);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                S d = hs * inc[c];
+                S yk = d - yc[c];
+                S ts = y[c] + yk;
+                ycn[c] = (ts - y[c]) - yk;
+                yh[c] = ts;
+                err[c] = hs * es[c];
+            }
+        } else {
+            S yl[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                yh[c] = y[c];
+                yl[c] = y[c];
+                ycn[c] = (S)0;
+            }
+            static_for<0, NS>([&](auto i) {
+                constexpr double bv = Tab::b(decltype(i)::value);
+                if constexpr (bv != 0.0) {
+                    const S bh_ = bv * h;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) yh[c] = yh[c] + bh_ * k[i][c];
+                }
+            });
+            static_for<0, NS>([&](auto i) {
+                constexpr double lv = Tab::bl(decltype(i)::value);
+                if constexpr (lv != 0.0) {
+                    const S bl_ = lv * h;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) yl[c] = yl[c] + bl_ * k[i][c];
+                }
+            });
+#pragma unroll
+            for (int c = 0; c < D; ++c) err[c] = yh[c] - yl[c];
+        }
+        // error_norm_inf (traits.rs:413-433): max |err / sk|, fmax keeping the non-NaN operand
+        double norm = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const double sk = atol + rtol * fmax(fabs((double)y[c]), fabs((double)yh[c]));
+            norm = fmax(norm, fabs((double)err[c] / sk));
+        }
+        double scale = a.safety * P::pow(norm, -(1.0 / (double)O));
+        scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+        int result;
+        if (norm <= 1.0) {
+            if constexpr (DENSE) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    cont[0][c] = y[c];
+                    cont[1][c] = k[0][c];
+                }
+            }
+            t_prev = t;
+            h_prev = h;
+            if (last_rejected) {
+                last_rejected = false;
+                stiff = 0;
+                scale = fmin(scale, 1.0);
+            }
+            t = t + h;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                y[c] = yh[c];
+                yc[c] = ycn[c];
+            }
+            rhs(t, y, k0);  // FSAL is off for both tableaus
+            fev += 1;
+            result = 1;
+        } else {
+            last_rejected = true;
+            stiff += 1;
+            if (stiff >= 100) {  // max_rejects default, src/methods/erk/mod.rs:140
+                status = DEGPU_ERR_STIFFNESS;
+                return 3;
+            }
+            result = 2;
+        }
+        h = h * scale;
+        if (bounded) {
+            if (fabs(h) < a.h_min)
+                h = rs_signum(h) * a.h_min;
+            else if (fabs(h) > a.h_max)
+                h = rs_signum(h) * a.h_max;
+        }
+        return result;
     }
 
     // ----- one fixed RK4 step: fixed/ordinary.rs:58-138 -----------------------------------------
@@ -1055,7 +1197,13 @@ struct Lane {
             }
             h = h_new;
         }
-        int r = Tab::ADAPTIVE ? step_dp(a) : step_fixed(a);
+        int r;
+        if constexpr (Tab::DP)
+            r = step_dp(a);
+        else if constexpr (Tab::ADAPTIVE)
+            r = step_embedded(a);
+        else
+            r = step_fixed(a);
         if (r == 3) {
             done = true;
             return;

@@ -27,7 +27,11 @@ std::map<VariantKey, EnsLaunchFn>& ens_registry();
 
 template <class Tab>
 constexpr int method_id() {
-    return std::is_same<Tab, TabRK4>::value ? DEGPU_RK4 : std::is_same<Tab, TabDopri5>::value ? DEGPU_DOPRI5 : DEGPU_DOP853;
+    return std::is_same<Tab, TabRK4>::value        ? DEGPU_RK4
+           : std::is_same<Tab, TabDopri5>::value   ? DEGPU_DOPRI5
+           : std::is_same<Tab, TabDop853>::value   ? DEGPU_DOP853
+           : std::is_same<Tab, TabRKF45>::value    ? DEGPU_RKF45
+                                                   : DEGPU_CASH_KARP;
 }
 
 int device_sm_count();
@@ -52,6 +56,20 @@ cudaError_t launch_ens(const EnsArgs& a, int kernel, cudaStream_t s) {
         erk_thread_kernel<Tab, Rhs, P, DENSE><<<(unsigned)blocks, 128, 0, s>>>(a);
     }
     return cudaGetLastError();
+}
+
+// Run-to-completion kernels only (a persistent request runs them too).
+template <class Tab, class Rhs, class P, bool DENSE>
+cudaError_t launch_thread_only(const EnsArgs& a, int, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    erk_thread_kernel<Tab, Rhs, P, DENSE><<<(unsigned)((a.count + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class Tab, class Rhs, class P>
+void register_thread_variant() {
+    ens_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 0}] = &launch_thread_only<Tab, Rhs, P, false>;
+    ens_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 1}] = &launch_thread_only<Tab, Rhs, P, true>;
 }
 
 template <class Tab, class Rhs, class P>
@@ -154,6 +172,8 @@ void register_parity_multi();
 void register_multi_fast_mixed();
 void register_cross_parity();
 void register_cross_fast_mixed();
+void register_embedded_parity();
+void register_embedded_fast_mixed();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to

@@ -1,7 +1,7 @@
-// tableau.cuh — Butcher tableaus of the three methods, as compile-time constants.
+// tableau.cuh — Butcher tableaus of the methods, as compile-time constants.
 //
-// Values are the crate's (src/tableau/runge_kutta.rs:39-70, src/tableau/dorman_prince.rs:37-118
-// and :155-381); every coefficient is a binary64 constant evaluated exactly as the crate's
+// Values are the crate's (src/tableau/runge_kutta.rs:39-70 and :335-480,
+// src/tableau/dorman_prince.rs:37-118 and :155-381); every coefficient is a binary64 constant evaluated exactly as the crate's
 // `T::from_f64(x)` of the same literal or quotient.  Being constexpr, each coefficient is an
 // immediate operand after unrolling, and terms whose coefficient is zero are removed at compile
 // time (`if constexpr`).  Removing a term `acc + 0*k` leaves every finite result unchanged bit for
@@ -13,7 +13,7 @@ namespace degpu {
 
 struct TabRK4 {
     static constexpr int S = 4, I = 4, ORDER = 4;
-    static constexpr bool ADAPTIVE = false, HAS_BH = false, FSAL = false;
+    static constexpr bool ADAPTIVE = false, DP = false, HAS_BH = false, FSAL = false;
     static constexpr double C[4] = {0.0, 0.5, 0.5, 1.0};
     static constexpr double A[4][4] = {{0, 0, 0, 0}, {0.5, 0, 0, 0}, {0, 0.5, 0, 0}, {0, 0, 1.0, 0}};
     static constexpr double B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
@@ -31,7 +31,7 @@ struct TabRK4 {
 struct TabDopri5 {
     static constexpr int S = 7, I = 7, ORDER = 5;
     // FSAL: the last row of A equals b and c = 1, so the last stage's state is y_new
-    static constexpr bool ADAPTIVE = true, HAS_BH = false, FSAL = true;
+    static constexpr bool ADAPTIVE = true, DP = true, HAS_BH = false, FSAL = true;
     static constexpr double C[7] = {0.0, 0.2, 0.3, 0.8, 8.0 / 9.0, 1.0, 1.0};
     static constexpr double A[7][7] = {
         {0, 0, 0, 0, 0, 0, 0},
@@ -69,7 +69,7 @@ static_assert(fsal_holds<TabDopri5>(), "DOPRI5: last row of A must equal b with 
 
 struct TabDop853 {
     static constexpr int S = 12, I = 16, ORDER = 8;
-    static constexpr bool ADAPTIVE = true, HAS_BH = true, FSAL = false;
+    static constexpr bool ADAPTIVE = true, DP = true, HAS_BH = true, FSAL = false;
     static constexpr double C[16] = {0.0,
                                      5.260015195876773E-2,
                                      7.89002279381516E-2,
@@ -165,5 +165,58 @@ __host__ __device__ __forceinline__ void static_for(F&& f) {
         static_for<Begin + 1, End>(f);
     }
 }
+
+// Embedded pairs of the crate's Adaptive ERK family (src/methods/erk/adaptive/mod.rs:43-58,
+// ordinary.rs:63-212): y_high from b, y_low from BL (the crate's `bh`), an infinity norm of their
+// difference, cubic Hermite dense output; order 5 in the controller for both.
+struct TabRKF45 {  // src/tableau/runge_kutta.rs:335-406 (Fehlberg 1969)
+    static constexpr int S = 6, I = 6, ORDER = 5;
+    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = false;
+    static constexpr double C[6] = {0.0, 1.0 / 4.0, 3.0 / 8.0, 12.0 / 13.0, 1.0, 1.0 / 2.0};
+    static constexpr double A[6][6] = {{0, 0, 0, 0, 0, 0},
+                                       {1.0 / 4.0, 0, 0, 0, 0, 0},
+                                       {3.0 / 32.0, 9.0 / 32.0, 0, 0, 0, 0},
+                                       {1932.0 / 2197.0, -7200.0 / 2197.0, 7296.0 / 2197.0, 0, 0, 0},
+                                       {439.0 / 216.0, -8.0, 3680.0 / 513.0, -845.0 / 4104.0, 0, 0},
+                                       {-8.0 / 27.0, 2.0, -3544.0 / 2565.0, 1859.0 / 4104.0, -11.0 / 40.0, 0}};
+    static constexpr double B[6] = {16.0 / 135.0, 0.0, 6656.0 / 12825.0, 28561.0 / 56430.0, -9.0 / 50.0, 2.0 / 55.0};
+    static constexpr double BL[6] = {25.0 / 216.0, 0.0, 1408.0 / 2565.0, 2197.0 / 4104.0, -1.0 / 5.0, 0.0};
+    static constexpr double BH[6] = {0, 0, 0, 0, 0, 0};
+    static constexpr double ER[6] = {0, 0, 0, 0, 0, 0};
+    static constexpr double BI[6][6] = {};
+    __host__ __device__ static constexpr double c(int i) { return C[i]; }
+    __host__ __device__ static constexpr double a(int i, int j) { return A[i][j]; }
+    __host__ __device__ static constexpr double b(int i) { return B[i]; }
+    __host__ __device__ static constexpr double bl(int i) { return BL[i]; }
+    __host__ __device__ static constexpr double bh(int i) { return BH[i]; }
+    __host__ __device__ static constexpr double er(int i) { return ER[i]; }
+    __host__ __device__ static constexpr double bi(int i, int j) { return BI[i][j]; }
+};
+
+struct TabCashKarp {  // src/tableau/runge_kutta.rs:420-480 (Cash and Karp 1990)
+    static constexpr int S = 6, I = 6, ORDER = 5;
+    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = false;
+    static constexpr double C[6] = {0.0, 1.0 / 5.0, 3.0 / 10.0, 3.0 / 5.0, 1.0, 7.0 / 8.0};
+    static constexpr double A[6][6] = {
+        {0, 0, 0, 0, 0, 0},
+        {1.0 / 5.0, 0, 0, 0, 0, 0},
+        {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+        {3.0 / 10.0, -9.0 / 10.0, 6.0 / 5.0, 0, 0, 0},
+        {-11.0 / 54.0, 5.0 / 2.0, -70.0 / 27.0, 35.0 / 27.0, 0, 0},
+        {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0, 0}};
+    static constexpr double B[6] = {37.0 / 378.0, 0.0, 250.0 / 621.0, 125.0 / 594.0, 0.0, 512.0 / 1771.0};
+    static constexpr double BL[6] = {2825.0 / 27648.0, 0.0, 18575.0 / 48384.0, 13525.0 / 55296.0, 277.0 / 14336.0,
+                                     1.0 / 4.0};
+    static constexpr double BH[6] = {0, 0, 0, 0, 0, 0};
+    static constexpr double ER[6] = {0, 0, 0, 0, 0, 0};
+    static constexpr double BI[6][6] = {};
+    __host__ __device__ static constexpr double c(int i) { return C[i]; }
+    __host__ __device__ static constexpr double a(int i, int j) { return A[i][j]; }
+    __host__ __device__ static constexpr double b(int i) { return B[i]; }
+    __host__ __device__ static constexpr double bl(int i) { return BL[i]; }
+    __host__ __device__ static constexpr double bh(int i) { return BH[i]; }
+    __host__ __device__ static constexpr double er(int i) { return ER[i]; }
+    __host__ __device__ static constexpr double bi(int i, int j) { return BI[i][j]; }
+};
 
 }  // namespace degpu

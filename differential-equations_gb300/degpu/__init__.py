@@ -55,6 +55,14 @@ class ExplicitRungeKutta:
     def dop853(cls):
         return cls(abi.DOP853)
 
+    @classmethod
+    def rkf45(cls):  # src/methods/erk/adaptive/mod.rs:43-50
+        return cls(abi.RKF45)
+
+    @classmethod
+    def cash_karp(cls):  # src/methods/erk/adaptive/mod.rs:51-58
+        return cls(abi.CASH_KARP)
+
     def rtol(self, v):
         self._rtol = v
         return self

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(PKG_ROOT, "csrc", "libdegpu.so")
 # degpu_status
 OK, BAD_INPUT, OOM, TIMEOUT, CUDA_ERROR, UNSUPPORTED = range(6)
 # degpu_method
-RK4, DOPRI5, DOP853 = 0, 1, 2
+RK4, DOPRI5, DOP853, RKF45, CASH_KARP = 0, 1, 2, 3, 4
 # degpu_precision
 FP64_PARITY, FP64_FAST, MIXED = 0, 1, 2
 # degpu_kernel

@@ -52,9 +52,17 @@ typedef enum {
     DEGPU_UNSUPPORTED = 5  /* the (method, family, precision, kernel) combination is not built */
 } degpu_status;
 
-/* Methods: constructors in src/methods/erk/fixed/mod.rs:69-75 (rk4) and
- * src/methods/erk/dormandprince/mod.rs:45-58 (dop853, dopri5). */
-typedef enum { DEGPU_RK4 = 0, DEGPU_DOPRI5 = 1, DEGPU_DOP853 = 2 } degpu_method;
+/* Methods: constructors in src/methods/erk/fixed/mod.rs:69-75 (rk4),
+ * src/methods/erk/dormandprince/mod.rs:45-58 (dop853, dopri5) and
+ * src/methods/erk/adaptive/mod.rs:43-58 (rkf45, cash_karp: embedded pair, infinity-norm error,
+ * Stiffness after 100 consecutive rejections, cubic Hermite dense output). */
+typedef enum {
+    DEGPU_RK4 = 0,
+    DEGPU_DOPRI5 = 1,
+    DEGPU_DOP853 = 2,
+    DEGPU_RKF45 = 3,
+    DEGPU_CASH_KARP = 4
+} degpu_method;
 
 /* Arithmetic of the solve.
  *  FP64_PARITY — every operation in the crate's order, no FMA contraction, correctly rounded
@@ -169,7 +177,8 @@ void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method);
  * Returns DEGPU_BAD_INPUT for RK4, an unknown method, or a negative or non-finite min_rtol. */
 degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol);
 
-/* The bound in force for `method` (0 for RK4 and unknown methods). */
+/* The bound in force for `method` (0 for RK4 and unknown methods).  RKF45 and Cash-Karp (order-5
+ * pairs) use DOPRI5's bound. */
 double degpu_mixed_min_rtol(int32_t method);
 
 /* Dimension and parameter count of a built-in family (dim = -1 for variable-size families).

@@ -60,6 +60,8 @@ class ExplicitRungeKutta {
     static ExplicitRungeKutta rk4(double h0) { ExplicitRungeKutta m(DEGPU_RK4); m.cfg_.h0 = h0; return m; }
     static ExplicitRungeKutta dopri5() { return ExplicitRungeKutta(DEGPU_DOPRI5); }
     static ExplicitRungeKutta dop853() { return ExplicitRungeKutta(DEGPU_DOP853); }
+    static ExplicitRungeKutta rkf45() { return ExplicitRungeKutta(DEGPU_RKF45); }        // adaptive/mod.rs:43-50
+    static ExplicitRungeKutta cash_karp() { return ExplicitRungeKutta(DEGPU_CASH_KARP); }  // adaptive/mod.rs:51-58
     ExplicitRungeKutta& rtol(double v) { rtol_ = v; return *this; }
     ExplicitRungeKutta& atol(double v) { atol_ = v; return *this; }
     ExplicitRungeKutta& h0(double v) { cfg_.h0 = v; return *this; }

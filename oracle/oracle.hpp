@@ -11,6 +11,7 @@
 //   constrain / validate ............ src/utils.rs:22-157
 //   State algebra ................... src/traits.rs:316-410
 //   cubic Hermite ................... src/interpolate.rs:40-60
+//   Adaptive ERK (RKF45, Cash-Karp)  src/methods/erk/adaptive/ordinary.rs:16-290
 //   TEvalSolout ..................... src/solout/t_eval.rs:82-171
 //   CrossingSolout .................. src/solout/crossing.rs:200-330
 //   tableaus ........................ src/tableau/runge_kutta.rs:39-70, src/tableau/dorman_prince.rs:37-381
@@ -79,6 +80,44 @@ inline Tableau tableau_rk4() {
     t.a[2][1] = 0.5;
     t.a[3][2] = 1.0;
     t.b[0] = 1.0 / 6.0; t.b[1] = 1.0 / 3.0; t.b[2] = 1.0 / 3.0; t.b[3] = 1.0 / 6.0;
+    return t;
+}
+
+// src/tableau/runge_kutta.rs:335-406; constructor adaptive/mod.rs:43-50 (O=5, S=I=6).
+inline Tableau tableau_rkf45() {
+    Tableau t;
+    t.S = 6; t.I = 6; t.order = 5;
+    t.c[0] = 0.0; t.c[1] = 1.0 / 4.0; t.c[2] = 3.0 / 8.0; t.c[3] = 12.0 / 13.0; t.c[4] = 1.0; t.c[5] = 1.0 / 2.0;
+    t.a[1][0] = 1.0 / 4.0;
+    t.a[2][0] = 3.0 / 32.0; t.a[2][1] = 9.0 / 32.0;
+    t.a[3][0] = 1932.0 / 2197.0; t.a[3][1] = -7200.0 / 2197.0; t.a[3][2] = 7296.0 / 2197.0;
+    t.a[4][0] = 439.0 / 216.0; t.a[4][1] = -8.0; t.a[4][2] = 3680.0 / 513.0; t.a[4][3] = -845.0 / 4104.0;
+    t.a[5][0] = -8.0 / 27.0; t.a[5][1] = 2.0; t.a[5][2] = -3544.0 / 2565.0; t.a[5][3] = 1859.0 / 4104.0;
+    t.a[5][4] = -11.0 / 40.0;
+    t.b[0] = 16.0 / 135.0; t.b[1] = 0.0; t.b[2] = 6656.0 / 12825.0; t.b[3] = 28561.0 / 56430.0;
+    t.b[4] = -9.0 / 50.0; t.b[5] = 2.0 / 55.0;
+    t.bh[0] = 25.0 / 216.0; t.bh[1] = 0.0; t.bh[2] = 1408.0 / 2565.0; t.bh[3] = 2197.0 / 4104.0;
+    t.bh[4] = -1.0 / 5.0; t.bh[5] = 0.0;
+    t.has_bh = true;
+    return t;
+}
+
+// src/tableau/runge_kutta.rs:420-480; constructor adaptive/mod.rs:51-58 (O=5, S=I=6).
+inline Tableau tableau_cash_karp() {
+    Tableau t;
+    t.S = 6; t.I = 6; t.order = 5;
+    t.c[0] = 0.0; t.c[1] = 1.0 / 5.0; t.c[2] = 3.0 / 10.0; t.c[3] = 3.0 / 5.0; t.c[4] = 1.0; t.c[5] = 7.0 / 8.0;
+    t.a[1][0] = 1.0 / 5.0;
+    t.a[2][0] = 3.0 / 40.0; t.a[2][1] = 9.0 / 40.0;
+    t.a[3][0] = 3.0 / 10.0; t.a[3][1] = -9.0 / 10.0; t.a[3][2] = 6.0 / 5.0;
+    t.a[4][0] = -11.0 / 54.0; t.a[4][1] = 5.0 / 2.0; t.a[4][2] = -70.0 / 27.0; t.a[4][3] = 35.0 / 27.0;
+    t.a[5][0] = 1631.0 / 55296.0; t.a[5][1] = 175.0 / 512.0; t.a[5][2] = 575.0 / 13824.0;
+    t.a[5][3] = 44275.0 / 110592.0; t.a[5][4] = 253.0 / 4096.0;
+    t.b[0] = 37.0 / 378.0; t.b[1] = 0.0; t.b[2] = 250.0 / 621.0; t.b[3] = 125.0 / 594.0; t.b[4] = 0.0;
+    t.b[5] = 512.0 / 1771.0;
+    t.bh[0] = 2825.0 / 27648.0; t.bh[1] = 0.0; t.bh[2] = 18575.0 / 48384.0; t.bh[3] = 13525.0 / 55296.0;
+    t.bh[4] = 277.0 / 14336.0; t.bh[5] = 1.0 / 4.0;
+    t.has_bh = true;
     return t;
 }
 
@@ -916,6 +955,137 @@ struct DormandPrince : Interpolator {
     void set_h(double hn) { h = hn; }
 };
 
+// Adaptive family (RKF45, Cash-Karp): src/methods/erk/adaptive/ordinary.rs.  FSAL is false for
+// both (adaptive/mod.rs:43-58); no `bi`, so dense output is cubic Hermite.
+struct AdaptiveRK : Interpolator {
+    Tableau tab;
+    Settings set;
+    Math math;
+    int64_t max_rejects = 100;  // src/methods/erk/mod.rs:140
+
+    double h = 0.0, t = 0.0, h_prev = 0.0, t_prev = 0.0;
+    State y, dydt, y_prev, dydt_prev;
+    std::vector<State> k;
+    int64_t stiffness_counter = 0, steps = 0;
+    Status status = Status::Uninitialized;
+
+    // adaptive/ordinary.rs:16-58
+    bool init(const Ode& ode, double t0, double tf, const State& y0, int64_t& fevals, Outcome& o) {
+        if (set.h0 == 0.0) {
+            set.h0 = h_init(ode, t0, tf, y0, tab.order, set.rtol, set.atol, set.h_min, set.h_max, fevals, math);
+            fevals += 2;  // ordinary.rs:28: counted again on top of the two inside compute
+        }
+        double h0v;
+        if (!validate_step_size_parameters(set.h0, set.h_min, set.h_max, t0, tf, h0v, o)) return false;
+        h = h0v;
+        stiffness_counter = 0;
+        t = t0;
+        y = y0;
+        size_t n = y0.size();
+        dydt.assign(n, 0.0);
+        y_prev = y0;
+        dydt_prev.assign(n, 0.0);
+        k.assign(tab.I, State(n, 0.0));
+        ode.diff(t, y, dydt);
+        fevals += 1;
+        t_prev = t;
+        y_prev = y;
+        dydt_prev = dydt;
+        status = Status::Initialized;
+        return true;
+    }
+
+    // adaptive/ordinary.rs:63-212.  Returns false with `o` filled on an error.
+    bool step(const Ode& ode, int64_t& fevals, Outcome& o) {
+        if (std::fabs(h) < std::fabs(h_prev) * 1e-14) {
+            status = Status::Error;
+            o.status = DEGPU_ERR_STEP_SIZE;
+            o.t = t;
+            o.y = y;
+            return false;
+        }
+        if (steps >= set.max_steps) {
+            status = Status::Error;
+            o.status = DEGPU_ERR_MAX_STEPS;
+            o.t = t;
+            o.y = y;
+            return false;
+        }
+        steps += 1;
+        k[0] = dydt;
+        const int S = tab.S;
+        for (int i = 1; i < S; ++i) {
+            State ys = y;
+            for (int j = 0; j < i; ++j) add_scaled(ys, tab.a[i][j] * h, k[j]);
+            ode.diff(t + tab.c[i] * h, ys, k[i]);
+        }
+        fevals += S - 1;
+        State y_high = y;
+        for (int i = 0; i < S; ++i) add_scaled(y_high, tab.b[i] * h, k[i]);
+        State y_low = y;
+        for (int i = 0; i < S; ++i) add_scaled(y_low, tab.bh[i] * h, k[i]);
+        State err = minus(y_high, y_low);
+        // error_norm_inf, traits.rs:413-433 (f64::max keeps the non-NaN operand)
+        double err_norm = 0.0;
+        for (size_t i = 0; i < y.size(); ++i) {
+            double sk = set.atol + set.rtol * std::fmax(std::fabs(y[i]), std::fabs(y_high[i]));
+            err_norm = std::fmax(err_norm, std::fabs(err[i] / sk));
+        }
+        double error_exponent = 1.0 / (double)tab.order;
+        double scale = set.safety_factor * math.pow(err_norm, -error_exponent);
+        scale = std::fmin(std::fmax(scale, set.min_scale), set.max_scale);
+        if (err_norm <= 1.0) {
+            t_prev = t;
+            y_prev = y;
+            dydt_prev = k[0];
+            h_prev = h;
+            if (status == Status::RejectedStep) {
+                stiffness_counter = 0;
+                status = Status::Solving;
+                scale = std::fmin(scale, 1.0);
+            }
+            t += h;
+            y = y_high;
+            ode.diff(t, y, dydt);
+            fevals += 1;
+        } else {
+            status = Status::RejectedStep;
+            stiffness_counter += 1;
+            if (stiffness_counter >= max_rejects) {
+                status = Status::Error;
+                o.status = DEGPU_ERR_STIFFNESS;
+                o.t = t;
+                o.y = y;
+                return false;
+            }
+        }
+        h *= scale;
+        h = constrain_step_size(h, set.h_min, set.h_max);
+        return true;
+    }
+
+    // adaptive/ordinary.rs:236-290 without `bi` -> cubic Hermite (src/interpolate.rs:40-60)
+    State interpolate(double t_interp) override {
+        double t0 = t_prev, t1 = t;
+        double hh = t1 - t0;
+        double s = (t_interp - t0) / hh;
+        double s2 = s * s;
+        double s3 = s2 * s;
+        double h00 = 2.0 * s3 - 3.0 * s2 + 1.0;
+        double h10 = s3 - 2.0 * s2 + s;
+        double h01 = -2.0 * s3 + 3.0 * s2;
+        double h11 = s3 - s2;
+        State out(y.size(), 0.0);
+        add_scaled(out, h00, y_prev);
+        add_scaled(out, h10 * hh, dydt_prev);
+        add_scaled(out, h01, y);
+        add_scaled(out, h11 * hh, dydt);
+        return out;
+    }
+
+    void set_h(double hn) { h = hn; }
+};
+
 // Fixed family (RK4): src/methods/erk/fixed/ordinary.rs.
 struct FixedRK : Interpolator {
     Tableau tab;
@@ -1092,6 +1262,13 @@ inline Result solve_one(int method, const Ode& ode, double t0, double tf, const 
         FixedRK s;
         s.tab = tableau_rk4();
         s.set = set;
+        return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
+    }
+    if (method == DEGPU_RKF45 || method == DEGPU_CASH_KARP) {
+        AdaptiveRK s;
+        s.tab = method == DEGPU_RKF45 ? tableau_rkf45() : tableau_cash_karp();
+        s.set = set;
+        s.math = math;
         return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
     }
     DormandPrince s;

@@ -25,15 +25,20 @@ def solve1(rhs, dim, params, t0, tf, y0, method, rtol=1e-6, atol=1e-6, h0=0.0, t
 # tests/ode/accuracy.rs: (system, t0, tf, y0, expected, [(method, rtol, atol, h0, tol)])
 CASES = [
     ("exp+", R["EXP_GROWTH"], [1.0], 0.0, 10.0, [1.0], [22026.46579479],          # accuracy.rs:70-94
-     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e1), (abi.RK4, 1e-6, 1e-6, 0.01, 1e3)]),
+     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e1), (abi.RK4, 1e-6, 1e-6, 0.01, 1e3),
+      (abi.RKF45, 1e-6, 1e-6, 0.0, 1e3), (abi.CASH_KARP, 1e-6, 1e-6, 0.0, 1e3)]),
     ("exp-", R["EXP_GROWTH"], [1.0], 0.0, -10.0, [22026.46579479], [1.0],          # accuracy.rs:177-204
-     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e-2), (abi.RK4, 1e-6, 1e-6, -0.01, 1e-2)]),
+     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e-2), (abi.RK4, 1e-6, 1e-6, -0.01, 1e-2),
+      (abi.RKF45, 1e-6, 1e-6, 0.0, 1e-2), (abi.CASH_KARP, 1e-6, 1e-6, 0.0, 1e-2)]),
     ("linear", R["LINEAR"], [1.0, 1.0], 0.0, 10.0, [1.0], [44051.93158958],        # accuracy.rs:286-313
-     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e1), (abi.RK4, 1e-6, 1e-6, 0.01, 1e3)]),
+     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e1), (abi.RK4, 1e-6, 1e-6, 0.01, 1e3),
+      (abi.RKF45, 1e-6, 1e-6, 0.0, 1e3), (abi.CASH_KARP, 1e-6, 1e-6, 0.0, 1e3)]),
     ("harmonic", R["HARMONIC"], [1.0], 0.0, 10.0, [1.0, 0.0], [-0.83907153, 0.54402111],  # accuracy.rs:395-422
-     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e-2), (abi.RK4, 1e-6, 1e-6, 0.01, 1e-1)]),
+     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e-2), (abi.RK4, 1e-6, 1e-6, 0.01, 1e-1),
+      (abi.RKF45, 1e-6, 1e-6, 0.0, 1e-3), (abi.CASH_KARP, 1e-6, 1e-6, 0.0, 1e-3)]),
     ("logistic", R["LOGISTIC"], [1.0, 10.0], 0.0, 10.0, [0.1], [9.95525518],       # accuracy.rs:504-531
-     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e-3), (abi.RK4, 1e-6, 1e-6, 0.01, 1e3)]),
+     [(abi.DOP853, 1e-12, 1e-12, 0.0, 1e-3), (abi.DOPRI5, 1e-6, 1e-6, 0.0, 1e-3), (abi.RK4, 1e-6, 1e-6, 0.01, 1e3),
+      (abi.RKF45, 1e-6, 1e-6, 0.0, 1e-2), (abi.CASH_KARP, 1e-6, 1e-6, 0.0, 1e-2)]),
     ("robertson", R["ROBERTSON"], [], 0.0, 0.4, [1.0, 0.0, 0.0],                    # accuracy.rs:622-671
      [0.9851721139, 3.3863953790e-05, 0.0147940222],
      [(abi.DOP853, 1e-10, 1e-12, 0.0, 1e-1), (abi.DOPRI5, 1e-8, 1e-10, 0.0, 5e-1)]),
@@ -51,7 +56,8 @@ def test_accuracy_known_answers(case, math_mode):
             assert abs(o["y_final"][c, 0] - e) < tol, (name, method, c, o["y_final"][c, 0], e)
 
 
-@pytest.mark.parametrize("method,h0", [(abi.DOP853, 0.0), (abi.DOPRI5, 0.0), (abi.RK4, 0.01)])
+@pytest.mark.parametrize("method,h0", [(abi.DOP853, 0.0), (abi.DOPRI5, 0.0), (abi.RK4, 0.01), (abi.RKF45, 0.0),
+                                       (abi.CASH_KARP, 0.0)])
 def test_interpolation_known_answer(method, h0):
     # tests/ode/interpolation.rs:14-87: t_eval [0.5, 1.0, 1.69] on exp growth, |y(0.5) - e^0.5| < 1e-3
     o = solve1(R["EXP_GROWTH"], 1, [1.0], 0.0, 2.0, [1.0], method, h0=h0, t_eval=[0.5, 1.0, 1.69])
