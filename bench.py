@@ -294,6 +294,42 @@ def run_crossing(args, torch, dev, lib):
     print(json.dumps(line))
 
 
+def run_adaptive(args, torch, dev, lib):
+    """The crate's Adaptive ERK family (RKF45, Cash-Karp) on the uneven ensemble (--n instances,
+    rtol ~ logU[1e-9,1e-5]): FP64 parity and mixed, one run-to-completion launch per family over
+    the longest-first lists; CPU baseline = the oracle on a sample."""
+    n = args.n
+    e = W.config1(n=n)
+    keep, bi, out, bo = _device_batch(torch, e, dev)
+    prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
+    stream = torch.cuda.Stream(device=dev)
+    res = {}
+    threads = os.cpu_count() or 1
+    for mname, method in (("rkf45", abi.RKF45), ("cash_karp", abi.CASH_KARP)):
+        for pname, prec in (("mixed", abi.MIXED), ("fp64-parity", abi.FP64_PARITY)):
+            cfg = abi.default_cfg(method)
+            cfg.precision, cfg.max_steps = prec, e.max_steps
+            f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
+                                                 C.c_void_p(stream.cuda_stream))
+            ms = _clock_ms(f, stream, torch, max(1, args.steps))
+            st = out["status"].cpu().numpy()
+            res[f"{mname}-{pname}"] = {"solves_per_s": n / (ms * 1e-3), "ms": ms,
+                                       "status_counts": {str(k): int(v) for k, v in
+                                                         zip(*np.unique(st, return_counts=True))}}
+            print(json.dumps({"adaptive_variant": f"{mname}-{pname}", **res[f"{mname}-{pname}"]}), flush=True)
+        s_e = e.subset(np.arange(args.cpu_sample // 2))
+        _, dt = _oracle_solve(s_e, method, threads)
+        res[f"{mname}-cpu"] = {"solves_per_s": s_e.n / dt, "cores": threads, "sample": s_e.n}
+    line = {"metric": "IVP solves/sec (uneven ensemble, RKF45 and Cash-Karp)",
+            "value": res["rkf45-mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 parity beside)", "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": f"uneven ensemble {n} instances, rtol~logU[1e-9,1e-5], RKF45 / Cash-Karp"},
+            "variants": res,
+            "cpu_baseline": {"value": res["rkf45-cpu"]["solves_per_s"], "unit": "solves/s", "cores": threads,
+                             "kind": "port", "sample": f"first {args.cpu_sample // 2} instances, RKF45 (host libm)"}}
+    print(json.dumps(line))
+
+
 def run_lorenz4096(args, torch, dev, lib):
     """4096 Lorenz IVPs (d=3), DOPRI5 rtol=1e-8 atol=1e-10 on [0, 20]: plain FP64 parity kernel,
     persistent parity kernel, and the CPU oracle with every host thread."""
@@ -604,7 +640,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--workload", default="uneven",
-                    choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing"],
+                    choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing", "adaptive"],
                     help="uneven = the headline 1M-instance ensemble; the others print their own line")
     ap.add_argument("--fpu-n", type=int, default=131072)
     ap.add_argument("--fpu-cpu-sample", type=int, default=200)
@@ -637,7 +673,8 @@ def main():
     if args.workload != "uneven":
         if rank == 0:
             {"lorenz4096": run_lorenz4096, "fpu": run_fpu, "gray-scott": run_gray_scott,
-             "serving": run_serving, "crossing": run_crossing}[args.workload](args, torch, dev, lib)
+             "serving": run_serving, "crossing": run_crossing,
+             "adaptive": run_adaptive}[args.workload](args, torch, dev, lib)
         return
 
     # each rank solves its own slice of instances (weak scaling: instances are independent)
