@@ -111,7 +111,7 @@ struct Lane {
     static constexpr int NC = DENSE ? (Tab::DP ? O : 2) : 1;  // Hermite keeps y_prev, dydt_prev
     static constexpr int NPP = Rhs::NP > 0 ? Rhs::NP : 1;
     using S = typename P::S;
-    static constexpr bool MIX = P::KAHAN && Tab::DP;
+    static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
     static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
@@ -960,7 +960,12 @@ struct Lane {
     // ----- one step of the Adaptive family (RKF45, Cash-Karp): adaptive/ordinary.rs:63-212 -----
     // returns 1 accepted, 2 rejected, 3 error.  `stiff` counts consecutive rejections here.
     __device__ int step_embedded(const EnsArgs& a) {
-        if (fabs(h) < fabs(h_prev) * 1e-14) {
+        if constexpr (MIX) {
+            if (fabsf(hf) < h_lim) {
+                status = DEGPU_ERR_STEP_SIZE;
+                return 3;
+            }
+        } else if (fabs(h) < fabs(h_prev) * 1e-14) {
             status = DEGPU_ERR_STEP_SIZE;
             return 3;
         }
@@ -984,7 +989,10 @@ struct Lane {
                     for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
                 }
             });
-            rhs(t + Tab::c(i) * h, ys, k[i]);
+            if constexpr (MIX)
+                rhs_at((float)Tab::c(i) * hf, ys, k[i]);
+            else
+                rhs(t + Tab::c(i) * h, ys, k[i]);
         });
         fev += NS - 1;
         // y_high = y + sum (b_i h) k_i and y_low = y + sum (bl_i h) k_i, each accumulated in order
@@ -1006,7 +1014,11 @@ struct Lane {
                     for (int c = 0; c < D; ++c) es[c] = es[c] + (S)(bv - lv) * k[i][c];
                 }
             });
-            const S hs = P::from(h);
+            S hs;
+            if constexpr (MIX)
+                hs = hf;
+            else
+                hs = P::from(h);
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 S d = hs * inc[c];
@@ -1044,16 +1056,33 @@ struct Lane {
             for (int c = 0; c < D; ++c) err[c] = yh[c] - yl[c];
         }
         // error_norm_inf (traits.rs:413-433): max |err / sk|, fmax keeping the non-NaN operand
-        double norm = 0.0;
+        bool accept;
+        double scale = 1.0;
+        float scalef = 1.0f;
+        if constexpr (MIX) {
+            // mixed: the norm, the controller's power and the decision in FP32
+            float norm = 0.0f;
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-            const double sk = atol + rtol * fmax(fabs((double)y[c]), fabs((double)yh[c]));
-            norm = fmax(norm, fabs((double)err[c] / sk));
+            for (int c = 0; c < D; ++c) {
+                const float sk = atolf + rtolf * fmaxf(fabsf(y[c]), fabsf(yh[c]));
+                norm = fmaxf(norm, fabsf(__fdividef(err[c], sk)));
+            }
+            const float pw = exp2f(__log2f(norm) * (float)(-1.0 / (double)O));
+            scalef = fminf(fmaxf(a.safety_f * pw, a.min_scale_f), a.max_scale_f);
+            accept = norm <= 1.0f;
+        } else {
+            double norm = 0.0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const double sk = atol + rtol * fmax(fabs((double)y[c]), fabs((double)yh[c]));
+                norm = fmax(norm, fabs((double)err[c] / sk));
+            }
+            scale = a.safety * P::pow(norm, -(1.0 / (double)O));
+            scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+            accept = norm <= 1.0;
         }
-        double scale = a.safety * P::pow(norm, -(1.0 / (double)O));
-        scale = fmin(fmax(scale, a.min_scale), a.max_scale);
         int result;
-        if (norm <= 1.0) {
+        if (accept) {
             if constexpr (DENSE) {
 #pragma unroll
                 for (int c = 0; c < D; ++c) {
@@ -1062,19 +1091,34 @@ struct Lane {
                 }
             }
             t_prev = t;
-            h_prev = h;
+            if constexpr (MIX) {
+                h_lim = fabsf(hf) * 1e-14f;
+            } else {
+                h_prev = h;
+            }
             if (last_rejected) {
                 last_rejected = false;
                 stiff = 0;
-                scale = fmin(scale, 1.0);
+                if constexpr (MIX)
+                    scalef = fminf(scalef, 1.0f);
+                else
+                    scale = fmin(scale, 1.0);
             }
-            t = t + h;
+            if constexpr (MIX) {
+                t = last_step ? tf : t + widen_f32(hf);  // a clamped last step ends exactly at tf
+                if constexpr (PHASE) ph0 = Rhs::phase(t, p);
+            } else {
+                t = t + h;
+            }
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 y[c] = yh[c];
                 yc[c] = ycn[c];
             }
-            rhs(t, y, k0);  // FSAL is off for both tableaus
+            if constexpr (PHASE)
+                rhs_at(0.0f, y, k0);  // FSAL is off for both tableaus
+            else
+                rhs(t, y, k0);
             fev += 1;
             result = 1;
         } else {
@@ -1086,12 +1130,24 @@ struct Lane {
             }
             result = 2;
         }
-        h = h * scale;
-        if (bounded) {
-            if (fabs(h) < a.h_min)
-                h = rs_signum(h) * a.h_min;
-            else if (fabs(h) > a.h_max)
-                h = rs_signum(h) * a.h_max;
+        if constexpr (MIX) {
+            hf = hf * scalef;
+            if (bounded) {
+                double hd = (double)hf;
+                if (fabs(hd) < a.h_min)
+                    hd = rs_signum(hd) * a.h_min;
+                else if (fabs(hd) > a.h_max)
+                    hd = rs_signum(hd) * a.h_max;
+                hf = (float)hd;
+            }
+        } else {
+            h = h * scale;
+            if (bounded) {
+                if (fabs(h) < a.h_min)
+                    h = rs_signum(h) * a.h_min;
+                else if (fabs(h) > a.h_max)
+                    h = rs_signum(h) * a.h_max;
+            }
         }
         return result;
     }
