@@ -19,7 +19,8 @@ import numpy as np
 from . import abi
 
 __all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
-           "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing"]
+           "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing", "write_csv",
+           "rust_debug_f64"]
 
 STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
                 abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness"}
@@ -253,6 +254,43 @@ class Solution:
     accepted: int
     rejected: int
     fevals: int
+
+    def to_csv(self, filename: str) -> None:
+        """The crate's Solution::to_csv (src/solution.rs:190-226): header t,y0,..,yN-1, one row per
+        point, numbers in Rust's Debug format."""
+        write_csv(filename, self.t, self.y)
+
+
+def rust_debug_f64(x: float) -> str:
+    """`format!("{:?}", x)` for an f64: the shortest digits that round-trip, in decimal notation
+    for 1e-4 <= |x| < 1e16 (always with a fractional part) and in exponential notation otherwise
+    ("1e-5", "1.5e16"); "NaN", "inf", "-inf"."""
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return "inf" if x > 0 else "-inf"
+    r = repr(x)  # Python switches to exponential form at the same thresholds
+    if "e" in r:
+        mant, exp = r.split("e")
+        return f"{mant}e{int(exp)}"
+    return r
+
+
+def write_csv(filename: str, t, y) -> None:
+    """Write points (t[k], y[k]) in the crate's CSV format (src/solution.rs:190-226); the parent
+    directory is created when missing."""
+    import os
+
+    parent = os.path.dirname(filename)
+    if parent and not os.path.exists(parent):
+        os.makedirs(parent)
+    ys = [np.asarray(v, dtype=np.float64).reshape(-1) for v in y]
+    n = len(ys[0]) if ys else 0
+    with open(filename, "w") as f:
+        f.write("t" + "".join(f",y{i}" for i in range(n)) + "\n")
+        for tk, yk in zip(t, ys):
+            f.write(rust_debug_f64(tk) + "".join("," + rust_debug_f64(v) for v in yk) + "\n")
 
 
 class IVP:

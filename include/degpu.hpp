@@ -13,7 +13,10 @@
 #pragma once
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
+#include <cstdio>
+#include <filesystem>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -32,6 +35,40 @@ struct Error {
     std::vector<double> y;
 };
 
+// Rust's `format!("{:?}", x)` for an f64: the shortest digits that round-trip, in decimal
+// notation for 1e-4 <= |x| < 1e16 (always with a fractional part) and in exponential notation
+// otherwise ("1e-5", "1.5e16"); "NaN", "inf", "-inf".
+inline std::string rust_debug_f64(double x) {
+    if (std::isnan(x)) return "NaN";
+    if (std::isinf(x)) return x > 0 ? "inf" : "-inf";
+    if (x == 0.0) return std::signbit(x) ? "-0.0" : "0.0";
+    char buf[64];
+    auto r = std::to_chars(buf, buf + sizeof(buf), x, std::chars_format::scientific);  // shortest digits
+    std::string sci(buf, r.ptr);
+    const bool neg = sci[0] == '-';
+    if (neg) sci.erase(0, 1);
+    const std::size_t epos = sci.find('e');
+    std::string digits = sci.substr(0, epos);
+    digits.erase(std::remove(digits.begin(), digits.end(), '.'), digits.end());
+    const int e10 = std::stoi(sci.substr(epos + 1));
+    const double ax = std::fabs(x);
+    std::string out;
+    if (ax >= 1e-4 && ax < 1e16) {
+        const int point = e10 + 1;  // digits before the decimal point
+        if (point <= 0)
+            out = "0." + std::string((std::size_t)(-point), '0') + digits;
+        else if (point >= (int)digits.size())
+            out = digits + std::string((std::size_t)point - digits.size(), '0') + ".0";
+        else
+            out = digits.substr(0, (std::size_t)point) + "." + digits.substr((std::size_t)point);
+    } else {
+        out = digits.substr(0, 1);
+        if (digits.size() > 1) out += "." + digits.substr(1);
+        out += "e" + std::to_string(e10);
+    }
+    return neg ? "-" + out : out;
+}
+
 // Solution fields the GPU produces (src/solution.rs:30-52, src/stats.rs).
 struct Solution {
     std::vector<double> t;
@@ -39,6 +76,27 @@ struct Solution {
     std::size_t evals = 0;      // Evals.function
     std::size_t accepted = 0;   // Steps.accepted
     std::size_t rejected = 0;   // Steps.rejected
+
+    // Solution::to_csv (src/solution.rs:190-226): header t,y0,..,yN-1 and one row per point, numbers
+    // in Rust's Debug format; the parent directory is created when missing.  False on an I/O error.
+    bool to_csv(const std::string& filename) const {
+        const std::filesystem::path path(filename);
+        std::error_code ec;
+        if (path.has_parent_path() && !std::filesystem::exists(path.parent_path()))
+            std::filesystem::create_directories(path.parent_path(), ec);
+        std::FILE* f = std::fopen(filename.c_str(), "w");
+        if (!f) return false;
+        const std::size_t n = y.empty() ? 0 : y[0].size();
+        std::string line = "t";
+        for (std::size_t i = 0; i < n; ++i) line += ",y" + std::to_string(i);
+        std::fprintf(f, "%s\n", line.c_str());
+        for (std::size_t k = 0; k < t.size(); ++k) {
+            line = rust_debug_f64(t[k]);
+            for (std::size_t i = 0; i < n; ++i) line += "," + rust_debug_f64(y[k][i]);
+            std::fprintf(f, "%s\n", line.c_str());
+        }
+        return std::fclose(f) == 0;
+    }
 };
 
 template <class T>
