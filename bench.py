@@ -237,10 +237,17 @@ def _oracle_solve(e, method, threads, math_mode=0):
     return o, time.perf_counter() - t
 
 
+# the hyperplane workload's plane: pos = (y0, y1) through (0.1, -0.2) with normal (1, 1)
+PLANE = ([0, 1], [0.1, -0.2], [1.0, 1.0])
+
+
 def run_crossing(args, torch, dev, lib):
     """Crossing detection on the uneven ensemble (1,048,576 instances, DOPRI5): the crate's
-    `.crossing(0, 0.0, Both)` output (first state component through zero), up to 8 points kept per
-    instance; FP64 parity and mixed; CPU baseline = the oracle's CrossingSolout on a sample."""
+    `.crossing(0, 0.0, Both)` output (first state component through zero), or with
+    `--workload hyperplane` its `.hyperplane_crossing(point, normal, extractor, Both)` output
+    (the plane of PLANE); up to 8 points kept per instance; FP64 parity and mixed; CPU baseline =
+    the oracle's CrossingSolout on a sample."""
+    plane = args.workload == "hyperplane"
     n = args.n
     e = W.config1(n=n)
     T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
@@ -257,7 +264,12 @@ def run_crossing(args, torch, dev, lib):
     bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
                       accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
                       fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
-    cr = abi.Crossing(component=0, direction=abi.CROSS_BOTH, max_points=mp, threshold=0.0)
+    if plane:
+        cr = abi.make_hyperplane(*PLANE, abi.CROSS_BOTH, mp)
+        fn = lib.degpu_solve_ensemble_hyperplane
+    else:
+        cr = abi.Crossing(component=0, direction=abi.CROSS_BOTH, max_points=mp, threshold=0.0)
+        fn = lib.degpu_solve_ensemble_crossing
     co = abi.CrossingOut(t=abi.ptr(out["ct"]), y=abi.ptr(out["cy"]), count=abi.ptr(out["cc"], C.c_int32))
     prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
     stream = torch.cuda.Stream(device=dev)
@@ -265,8 +277,8 @@ def run_crossing(args, torch, dev, lib):
     for name, prec in (("mixed", abi.MIXED), ("fp64-parity", abi.FP64_PARITY)):
         cfg = abi.default_cfg(abi.DOPRI5)
         cfg.precision, cfg.max_steps = prec, e.max_steps
-        f = lambda: lib.degpu_solve_ensemble_crossing(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(cr),
-                                                      C.byref(bo), C.byref(co), C.c_void_p(stream.cuda_stream))
+        f = lambda: fn(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(cr), C.byref(bo), C.byref(co),
+                       C.c_void_p(stream.cuda_stream))
         ms = _clock_ms(f, stream, torch, max(1, args.steps))
         cnt = out["cc"].cpu().numpy()
         res[name] = {"solves_per_s": n / (ms * 1e-3), "ms": ms, "crossings": int(cnt.sum()),
@@ -282,12 +294,17 @@ def run_crossing(args, torch, dev, lib):
     cfg = abi.default_cfg(abi.DOPRI5)
     cfg.max_steps = e.max_steps
     t = time.perf_counter()
-    O.solve_crossing(b, cfg, 0, 0.0, abi.CROSS_BOTH, mp, threads=threads, math_mode=0)
+    if plane:
+        O.solve_hyperplane(b, cfg, *PLANE, abi.CROSS_BOTH, mp, threads=threads, math_mode=0)
+    else:
+        O.solve_crossing(b, cfg, 0, 0.0, abi.CROSS_BOTH, mp, threads=threads, math_mode=0)
     dt = time.perf_counter() - t
-    line = {"metric": "IVP solves/sec with crossing detection (uneven ensemble, DOPRI5)",
+    what = (f"hyperplane_crossing(point {PLANE[1]}, normal {PLANE[2]}, components {PLANE[0]}, Both)" if plane
+            else "crossing(0, 0.0, Both)")
+    line = {"metric": f"IVP solves/sec with {'hyperplane ' if plane else ''}crossing detection (uneven ensemble, DOPRI5)",
             "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
             "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 parity beside)", "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": f"uneven ensemble {n} instances, crossing(0, 0.0, Both), {mp} points kept"},
+            "config": {"workload": f"uneven ensemble {n} instances, {what}, {mp} points kept"},
             "variants": res,
             "cpu_baseline": {"value": s_n / dt, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"first {s_n} instances (host libm)"}}
@@ -640,7 +657,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--workload", default="uneven",
-                    choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing", "adaptive"],
+                    choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing", "hyperplane",
+                             "adaptive"],
                     help="uneven = the headline 1M-instance ensemble; the others print their own line")
     ap.add_argument("--fpu-n", type=int, default=131072)
     ap.add_argument("--fpu-cpu-sample", type=int, default=200)
@@ -673,7 +691,7 @@ def main():
     if args.workload != "uneven":
         if rank == 0:
             {"lorenz4096": run_lorenz4096, "fpu": run_fpu, "gray-scott": run_gray_scott,
-             "serving": run_serving, "crossing": run_crossing,
+             "serving": run_serving, "crossing": run_crossing, "hyperplane": run_crossing,
              "adaptive": run_adaptive}[args.workload](args, torch, dev, lib)
         return
 

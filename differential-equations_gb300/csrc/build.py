@@ -15,7 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "libdegpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no multiply-add contraction (gcc contracts by default on aarch64), so host-side FP64
+# arithmetic such as the hyperplane normal's scaling rounds as the crate's does
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+          "-Xcompiler", "-ffp-contract=off",
           "-diag-suppress", "20091", "-I", os.path.join(HERE, "..", "..", "include")]
 PARITY = ["-fmad=false", "-DDEGPU_NO_FMAD"]
 

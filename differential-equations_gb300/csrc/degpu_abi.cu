@@ -60,6 +60,8 @@ void ensure_registered() {
         register_multi_fast_mixed();
         register_cross_parity();
         register_cross_fast_mixed();
+        register_cross_embedded_parity();
+        register_cross_embedded_fast_mixed();
         register_embedded_parity();
         register_embedded_fast_mixed();
     });
@@ -361,10 +363,63 @@ static degpu_status validate(const degpu_problem* pb, const degpu_method_cfg* cf
     return DEGPU_OK;
 }
 
-// degpu_solve_ensemble_crossing: one run-to-completion crossing-detection launch per
-// (family, precision) work list.
+// What a crossing-detection solve monitors: a component against a threshold
+// (degpu_crossing) or the signed distance to a hyperplane (degpu_hyperplane).
+struct CrossSpec {
+    int32_t plane = 0, comp = 0, dir = 0, max_points = 0;
+    double value = 0.0;  // threshold; for a plane, sum |point_j normal_j|
+    int32_t dim = 0;
+    int32_t comps[DEGPU_HYPERPLANE_MAX_DIM] = {};
+    double point[DEGPU_HYPERPLANE_MAX_DIM] = {}, normal[DEGPU_HYPERPLANE_MAX_DIM] = {};
+    int32_t max_comp = 0;  // largest state index read
+};
+
+static bool make_spec(const degpu_crossing* cr, int32_t dim, CrossSpec& sp) {
+    if (cr->component < 0 || cr->component >= dim || cr->max_points < 0) return false;
+    if (cr->direction < -1 || cr->direction > 1) return false;
+    sp.comp = sp.max_comp = cr->component;
+    sp.dir = cr->direction;
+    sp.max_points = cr->max_points;
+    sp.value = cr->threshold;
+    return true;
+}
+
+// HyperplaneCrossingSolout::new (src/solout/hyperplane.rs): the normal is scaled by 1/|normal|
+// when |normal| exceeds the FP64 epsilon, |normal|^2 folded from zero in component order
+// (src/traits.rs:574-576). Host code is compiled without multiply-add contraction, so the scaled
+// normal is the crate's to the bit.
+static bool make_spec(const degpu_hyperplane* hp, int32_t dim, CrossSpec& sp) {
+    if (hp->dim < 1 || hp->dim > DEGPU_HYPERPLANE_MAX_DIM || hp->max_points < 0) return false;
+    if (hp->direction < -1 || hp->direction > 1) return false;
+    sp.plane = 1;
+    sp.dir = hp->direction;
+    sp.max_points = hp->max_points;
+    sp.dim = hp->dim;
+    double nn = 0.0;
+    for (int j = 0; j < hp->dim; ++j) {
+        if (hp->components[j] < 0 || hp->components[j] >= dim) return false;
+        sp.comps[j] = hp->components[j];
+        sp.max_comp = std::max(sp.max_comp, hp->components[j]);
+        sp.point[j] = hp->point[j];
+        sp.normal[j] = hp->normal[j];
+        const double sq = hp->normal[j] * hp->normal[j];
+        nn = nn + sq;
+    }
+    const double norm = std::sqrt(nn);
+    if (norm > 2.220446049250313e-16) {
+        const double inv = 1.0 / norm;
+        for (int j = 0; j < hp->dim; ++j) sp.normal[j] = sp.normal[j] * inv;
+    }
+    double scale = 0.0;
+    for (int j = 0; j < hp->dim; ++j) scale += std::fabs(sp.point[j] * sp.normal[j]);
+    sp.value = scale;
+    return true;
+}
+
+// degpu_solve_ensemble_crossing / _hyperplane: one run-to-completion crossing-detection launch
+// per (family, precision) work list.
 static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
-                                  const degpu_crossing* cr, degpu_batch_out* out, degpu_crossing_out* co,
+                                  const CrossSpec& cr, degpu_batch_out* out, degpu_crossing_out* co,
                                   cudaStream_t s) {
     const int64_t n = in->n;
     Scratch scratch(s);
@@ -394,23 +449,30 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
     for (auto& kv : lists) {
         int dim, np;
         builtin_info(kv.first.first, dim, np);
-        if (np < 0 || dim > pb->dim || np > pb->n_params || cr->component >= dim) return DEGPU_BAD_INPUT;
+        if (np < 0 || dim > pb->dim || np > pb->n_params || cr.max_comp >= dim) return DEGPU_BAD_INPUT;
         if (cross_registry().find(VariantKey{cfg->method, kv.first.first, kv.first.second, 1}) ==
             cross_registry().end())
             return DEGPU_UNSUPPORTED;
     }
     EnsArgs a = make_args(pb, cfg, in, out);
     a.n_eval = 0;
-    a.cross_comp = cr->component;
-    a.cross_dir = cr->direction;
-    a.cross_max = cr->max_points;
-    a.cross_value = cr->threshold;
+    a.cross_comp = cr.comp;
+    a.cross_dir = cr.dir;
+    a.cross_max = cr.max_points;
+    a.cross_value = cr.value;
     a.cross_t = co->t;
     a.cross_y = co->y;
     a.cross_count = co->count;
-    if (cr->max_points > 0) {
+    a.cross_plane = cr.plane;
+    a.plane_dim = cr.dim;
+    for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j) {
+        a.plane_comp[j] = cr.comps[j];
+        a.plane_point[j] = cr.point[j];
+        a.plane_normal[j] = cr.normal[j];
+    }
+    if (cr.max_points > 0) {
         // 0xFF bytes form a quiet NaN: slots past an instance's count stay NaN
-        const size_t m = (size_t)cr->max_points * n;
+        const size_t m = (size_t)cr.max_points * n;
         if (cudaMemsetAsync(co->t, 0xFF, m * sizeof(double), s) != cudaSuccess ||
             cudaMemsetAsync(co->y, 0xFF, m * pb->dim * sizeof(double), s) != cudaSuccess)
             return DEGPU_CUDA_ERROR;
@@ -447,6 +509,93 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
     // the index lists came from host vectors that die with this call
     if (cudaStreamSynchronize(s) != cudaSuccess) return DEGPU_CUDA_ERROR;
     return DEGPU_OK;
+}
+
+// Shared body of the device-pointer crossing entry points.
+template <class Spec>
+static degpu_status crossing_entry(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                   const Spec* sd, degpu_batch_out* out, degpu_crossing_out* co, cudaStream_t s) {
+    if (!sd || !co) return DEGPU_BAD_INPUT;
+    degpu_status v = validate(pb, cfg, in, out);
+    if (v != DEGPU_OK || in->n == 0) return v;
+    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
+    CrossSpec cr;
+    if (!make_spec(sd, pb->dim, cr)) return DEGPU_BAD_INPUT;
+    if (!co->count || (cr.max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
+    ensure_registered();
+    return crossing_impl(pb, cfg, in, cr, out, co, s);
+}
+
+// Shared body of the host-pointer crossing entry points: copies in, solves, copies back.
+template <class Spec>
+static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                        const degpu_batch_in* in, const Spec* sd, degpu_batch_out* out,
+                                        degpu_crossing_out* co) {
+    if (!sd || !co) return DEGPU_BAD_INPUT;
+    degpu_status v = validate(pb, cfg, in, out);
+    if (v != DEGPU_OK || in->n == 0) return v;
+    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
+    CrossSpec cr;
+    if (!make_spec(sd, pb->dim, cr)) return DEGPU_BAD_INPUT;
+    if (!co->count || (cr.max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
+    ensure_registered();
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    degpu_status st = DEGPU_OK;
+    {
+        const int64_t n = in->n;
+        const size_t d = (size_t)pb->dim, np = (size_t)pb->n_params, m = (size_t)cr.max_points;
+        Scratch sc(s);
+        degpu_batch_in din = *in;
+        degpu_batch_out dout{};
+        degpu_crossing_out dco{};
+        auto up = [&](const void* src, size_t bytes) -> void* {
+            if (!src) return nullptr;
+            void* p = sc.alloc<char>(bytes);
+            if (p) cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, s);
+            return p;
+        };
+        din.t0 = (const double*)up(in->t0, n * 8);
+        din.tf = (const double*)up(in->tf, n * 8);
+        din.y0 = (const double*)up(in->y0, d * n * 8);
+        din.params = np > 0 ? (const double*)up(in->params, np * n * 8) : nullptr;
+        din.rtol = (const double*)up(in->rtol, n * 8);
+        din.atol = (const double*)up(in->atol, n * 8);
+        din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
+        dout.y_final = sc.alloc<double>(d * n);
+        dout.t_final = out->t_final ? sc.alloc<double>(n) : nullptr;
+        dout.accepted = out->accepted ? sc.alloc<int64_t>(n) : nullptr;
+        dout.rejected = out->rejected ? sc.alloc<int64_t>(n) : nullptr;
+        dout.fevals = out->fevals ? sc.alloc<int64_t>(n) : nullptr;
+        dout.status = out->status ? sc.alloc<int32_t>(n) : nullptr;
+        dco.t = m > 0 ? sc.alloc<double>(m * n) : nullptr;
+        dco.y = m > 0 ? sc.alloc<double>(m * d * n) : nullptr;
+        dco.count = sc.alloc<int32_t>(n);
+        if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final || !dco.count ||
+            (m > 0 && (!dco.t || !dco.y))) {
+            st = DEGPU_OOM;
+        } else {
+            st = crossing_impl(pb, cfg, &din, cr, &dout, &dco, s);
+        }
+        if (st == DEGPU_OK) {
+            auto down = [&](void* dst, const void* src, size_t bytes) {
+                if (dst && src) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+            };
+            down(out->y_final, dout.y_final, d * n * 8);
+            down(out->t_final, dout.t_final, n * 8);
+            down(out->accepted, dout.accepted, n * 8);
+            down(out->rejected, dout.rejected, n * 8);
+            down(out->fevals, dout.fevals, n * 8);
+            down(out->status, dout.status, n * 4);
+            down(co->t, dco.t, m * n * 8);
+            down(co->y, dco.y, m * d * n * 8);
+            down(co->count, dco.count, n * 4);
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess && st == DEGPU_OK) st = DEGPU_CUDA_ERROR;
+    }
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return st;
 }
 
 }  // namespace degpu
@@ -522,85 +671,25 @@ degpu_status degpu_solve_ensemble(const degpu_problem* pb, const degpu_method_cf
 degpu_status degpu_solve_ensemble_crossing(const degpu_problem* pb, const degpu_method_cfg* cfg,
                                            const degpu_batch_in* in, const degpu_crossing* cr, degpu_batch_out* out,
                                            degpu_crossing_out* co, void* stream) {
-    if (!cr || !co) return DEGPU_BAD_INPUT;
-    degpu_status v = validate(pb, cfg, in, out);
-    if (v != DEGPU_OK || in->n == 0) return v;
-    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
-    if (cr->component < 0 || cr->component >= pb->dim || cr->max_points < 0) return DEGPU_BAD_INPUT;
-    if (cr->direction < -1 || cr->direction > 1) return DEGPU_BAD_INPUT;
-    if (!co->count || (cr->max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
-    ensure_registered();
-    return crossing_impl(pb, cfg, in, cr, out, co, (cudaStream_t)stream);
+    return crossing_entry(pb, cfg, in, cr, out, co, (cudaStream_t)stream);
 }
 
 degpu_status degpu_solve_ensemble_crossing_host(const degpu_problem* pb, const degpu_method_cfg* cfg,
                                                 const degpu_batch_in* in, const degpu_crossing* cr,
                                                 degpu_batch_out* out, degpu_crossing_out* co) {
-    if (!cr || !co) return DEGPU_BAD_INPUT;
-    degpu_status v = validate(pb, cfg, in, out);
-    if (v != DEGPU_OK || in->n == 0) return v;
-    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
-    if (cr->component < 0 || cr->component >= pb->dim || cr->max_points < 0) return DEGPU_BAD_INPUT;
-    if (cr->direction < -1 || cr->direction > 1) return DEGPU_BAD_INPUT;
-    if (!co->count || (cr->max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
-    ensure_registered();
-    cudaStream_t s;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return DEGPU_CUDA_ERROR;
-    degpu_status st = DEGPU_OK;
-    {
-        const int64_t n = in->n;
-        const size_t d = (size_t)pb->dim, np = (size_t)pb->n_params, m = (size_t)cr->max_points;
-        Scratch sc(s);
-        degpu_batch_in din = *in;
-        degpu_batch_out dout{};
-        degpu_crossing_out dco{};
-        auto up = [&](const void* src, size_t bytes) -> void* {
-            if (!src) return nullptr;
-            void* p = sc.alloc<char>(bytes);
-            if (p) cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, s);
-            return p;
-        };
-        din.t0 = (const double*)up(in->t0, n * 8);
-        din.tf = (const double*)up(in->tf, n * 8);
-        din.y0 = (const double*)up(in->y0, d * n * 8);
-        din.params = np > 0 ? (const double*)up(in->params, np * n * 8) : nullptr;
-        din.rtol = (const double*)up(in->rtol, n * 8);
-        din.atol = (const double*)up(in->atol, n * 8);
-        din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
-        dout.y_final = sc.alloc<double>(d * n);
-        dout.t_final = out->t_final ? sc.alloc<double>(n) : nullptr;
-        dout.accepted = out->accepted ? sc.alloc<int64_t>(n) : nullptr;
-        dout.rejected = out->rejected ? sc.alloc<int64_t>(n) : nullptr;
-        dout.fevals = out->fevals ? sc.alloc<int64_t>(n) : nullptr;
-        dout.status = out->status ? sc.alloc<int32_t>(n) : nullptr;
-        dco.t = m > 0 ? sc.alloc<double>(m * n) : nullptr;
-        dco.y = m > 0 ? sc.alloc<double>(m * d * n) : nullptr;
-        dco.count = sc.alloc<int32_t>(n);
-        if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final || !dco.count ||
-            (m > 0 && (!dco.t || !dco.y))) {
-            st = DEGPU_OOM;
-        } else {
-            st = crossing_impl(pb, cfg, &din, cr, &dout, &dco, s);
-        }
-        if (st == DEGPU_OK) {
-            auto down = [&](void* dst, const void* src, size_t bytes) {
-                if (dst && src) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
-            };
-            down(out->y_final, dout.y_final, d * n * 8);
-            down(out->t_final, dout.t_final, n * 8);
-            down(out->accepted, dout.accepted, n * 8);
-            down(out->rejected, dout.rejected, n * 8);
-            down(out->fevals, dout.fevals, n * 8);
-            down(out->status, dout.status, n * 4);
-            down(co->t, dco.t, m * n * 8);
-            down(co->y, dco.y, m * d * n * 8);
-            down(co->count, dco.count, n * 4);
-        }
-        if (cudaStreamSynchronize(s) != cudaSuccess && st == DEGPU_OK) st = DEGPU_CUDA_ERROR;
-    }
-    cudaStreamSynchronize(s);
-    cudaStreamDestroy(s);
-    return st;
+    return crossing_host_entry(pb, cfg, in, cr, out, co);
+}
+
+degpu_status degpu_solve_ensemble_hyperplane(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                             const degpu_batch_in* in, const degpu_hyperplane* hp,
+                                             degpu_batch_out* out, degpu_crossing_out* co, void* stream) {
+    return crossing_entry(pb, cfg, in, hp, out, co, (cudaStream_t)stream);
+}
+
+degpu_status degpu_solve_ensemble_hyperplane_host(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                                  const degpu_batch_in* in, const degpu_hyperplane* hp,
+                                                  degpu_batch_out* out, degpu_crossing_out* co) {
+    return crossing_host_entry(pb, cfg, in, hp, out, co);
 }
 
 degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,

@@ -68,6 +68,13 @@ struct EnsArgs {
     double* cross_t;       // [cross_max][n]
     double* cross_y;       // [cross_max][dmax][n]
     int32_t* cross_count;  // [n]
+    // hyperplane crossings (cross_plane != 0): the offset is (pos - point) . normal with
+    // pos[j] = y[plane_comp[j]], the normal already of unit length; cross_value then holds
+    // sum |point_j normal_j|, the scale of the mixed form's FP32 search tolerance
+    int32_t cross_plane, plane_dim;
+    int32_t plane_comp[DEGPU_HYPERPLANE_MAX_DIM];
+    double plane_point[DEGPU_HYPERPLANE_MAX_DIM];
+    double plane_normal[DEGPU_HYPERPLANE_MAX_DIM];
 };
 
 // f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
@@ -392,7 +399,8 @@ struct Lane {
         }
     }
 
-    // ----- crossing detection: CrossingSolout, src/solout/crossing.rs:200-330 -------------------
+    // ----- crossing detection: CrossingSolout (src/solout/crossing.rs:200-330) and
+    // HyperplaneCrossingSolout (src/solout/hyperplane.rs) ------------------------------------
     __device__ __forceinline__ double comp_value(const S* v, int comp) const {
         S r = v[0];
 #pragma unroll
@@ -400,45 +408,61 @@ struct Lane {
             if (c == comp) r = v[c];
         return (double)r;
     }
-    __device__ __forceinline__ double interp_offset(double te, int comp, double thr, const EnsArgs& a) const {
+    // The monitored offset of a state given component by component: y[comp] - threshold
+    // (crossing.rs:207), or the hyperplane's signed distance (pos - point) . normal
+    // (hyperplane.rs signed_distance), the dot product folded from zero in component order
+    // (src/traits.rs:551-555).
+    template <class Get>
+    __device__ __forceinline__ double offset_by(Get get, const EnsArgs& a) const {
+        if (!a.cross_plane) return get(a.cross_comp) - a.cross_value;
+        double sum = 0.0;
+#pragma unroll
+        for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
+            if (j < a.plane_dim) {
+                const double d = get(a.plane_comp[j]) - a.plane_point[j];
+                sum = sum + d * a.plane_normal[j];
+            }
+        return sum;
+    }
+    __device__ __forceinline__ double interp_offset(double te, const EnsArgs& a) const {
         S v[D];
         interpolate(te, v, a);
-        return comp_value(v, comp) - thr;
+        return offset_by([&](int c) { return comp_value(v, c); }, a);
     }
-    // find_crossing_newton (crossing.rs:254-328): Newton on the interpolant with a
-    // finite-difference derivative; false when it does not converge
+    // find_crossing_newton (crossing.rs:254-328, hyperplane.rs find_crossing_newton): Newton on
+    // the interpolant with a finite-difference derivative; false when it does not converge. The
+    // hyperplane form stops on a derivative below eps (not 10 eps) and has no step-change test.
     __device__ bool find_crossing_newton(double t_lower, double t_upper, double off_lower, double off_upper,
                                          double& t_out, const EnsArgs& a) const {
         const double eps = 2.220446049250313e-16;
-        const int comp = a.cross_comp;
-        const double thr = a.cross_value;
+        const bool plane = a.cross_plane != 0;
         double tt = t_lower - off_lower * (t_upper - t_lower) / (off_upper - off_lower);
         const double tolerance = eps * 100.0;
         double offset;
         for (int it = 0; it < 10; ++it) {
-            offset = interp_offset(tt, comp, thr, a);
+            offset = interp_offset(tt, a);
             if (fabs(offset) < tolerance) {
                 t_out = tt;
                 return true;
             }
             const double delta_t = (t_upper - t_lower) * 1e-6;
             const double t_plus = tt + delta_t;
-            const double offset_plus = interp_offset(t_plus, comp, thr, a);
+            const double offset_plus = interp_offset(t_plus, a);
             const double derivative = (offset_plus - offset) / delta_t;
-            if (fabs(derivative) < eps * 10.0) break;
+            if (fabs(derivative) < (plane ? eps : eps * 10.0)) break;
             const double t_new = tt - offset / derivative;
             if (t_new < t_lower || t_new > t_upper) {
                 tt = (t_lower + t_upper) / 2.0;
             } else {
                 const double change = fabs(t_new - tt);
-                if (change < tolerance * 0.1) {
+                if (!plane && change < tolerance * 0.1) {
                     tt = t_new;
                     break;
                 }
                 tt = t_new;
             }
         }
-        offset = interp_offset(tt, comp, thr, a);
+        offset = interp_offset(tt, a);
         if (fabs(offset) < tolerance * 10.0) {
             t_out = tt;
             return true;
@@ -446,17 +470,24 @@ struct Lane {
         return false;
     }
     // Mixed form: find_crossing_newton's iteration on sg in [0, 1] in FP32, with tolerances scaled
-    // to FP32 (100 units of FP32 rounding of the threshold's magnitude); the linear estimate when
-    // it does not converge.
+    // to FP32 (100 units of FP32 rounding of the monitored quantity's scale: |threshold|, or
+    // sum |point_j normal_j| for a hyperplane); the linear estimate when it does not converge.
     __device__ float find_crossing_sigma(float off_l, float off_u, const EnsArgs& a) const {
-        const int comp = a.cross_comp;
+        const bool plane = a.cross_plane != 0;
         const float thr = (float)a.cross_value;
         const float tol = 100.0f * 1.1920929e-7f * fmaxf(1.0f, fabsf(thr));
         const float lin = -off_l / (off_u - off_l);
         auto off_at = [&](float sg) {
             S v[D];
             interpolate_sigma(sg, v, a);
-            return (float)comp_value(v, comp) - thr;
+            if (!plane) return (float)comp_value(v, a.cross_comp) - thr;
+            float sum = 0.0f;
+#pragma unroll
+            for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
+                if (j < a.plane_dim)
+                    sum += ((float)comp_value(v, a.plane_comp[j]) - (float)a.plane_point[j]) *
+                           (float)a.plane_normal[j];
+            return sum;
         };
         float sg = lin, offset;
         for (int it = 0; it < 10; ++it) {
@@ -464,14 +495,14 @@ struct Lane {
             if (fabsf(offset) < tol) return sg;
             const float ds = 1e-6f;
             const float derivative = (off_at(sg + ds) - offset) / ds;
-            if (fabsf(derivative) < 10.0f * 1.1920929e-7f) break;
+            if (fabsf(derivative) < (plane ? 1.0f : 10.0f) * 1.1920929e-7f) break;
             const float s_new = sg - offset / derivative;
             if (s_new < 0.0f || s_new > 1.0f) {
                 sg = 0.5f;
             } else {
                 const float change = fabsf(s_new - sg);
                 sg = s_new;
-                if (change < tol * 0.1f) break;
+                if (!plane && change < tol * 0.1f) break;
             }
         }
         offset = off_at(sg);
@@ -479,11 +510,19 @@ struct Lane {
     }
 
     __device__ void crossing_solout(const EnsArgs& a) {
-        double cur = comp_value(y, a.cross_comp);
-        if constexpr (P::KAHAN) cur = cur - comp_value(yc, a.cross_comp);
-        const double offset = cur - a.cross_value;
+        const double offset = offset_by(
+            [&](int c) {
+                double v = comp_value(y, c);
+                if constexpr (P::KAHAN) v = v - comp_value(yc, c);
+                return v;
+            },
+            a);
         if (have_last_off) {
-            if (rs_signum(last_off) != rs_signum(offset)) {
+            bool is_crossing = rs_signum(last_off) != rs_signum(offset);
+            // hyperplane.rs: leaving or reaching the plane exactly also counts
+            if (a.cross_plane)
+                is_crossing = is_crossing || (last_off == 0.0 && offset != 0.0) || (last_off != 0.0 && offset == 0.0);
+            if (is_crossing) {
                 bool record;
                 if (a.cross_dir > 0)
                     record = last_off < 0.0 && offset >= 0.0;

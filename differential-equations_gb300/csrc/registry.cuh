@@ -94,6 +94,12 @@ void register_cross_all_methods() {
     cross_registry()[VariantKey{DEGPU_DOPRI5, Rhs::ID, P::ID, 1}] = &launch_cross<TabDopri5, Rhs, P>;
     cross_registry()[VariantKey{DEGPU_DOP853, Rhs::ID, P::ID, 1}] = &launch_cross<TabDop853, Rhs, P>;
 }
+// The adaptive (embedded-pair) methods, in their own translation units.
+template <class Rhs, class P>
+void register_cross_embedded_methods() {
+    cross_registry()[VariantKey{DEGPU_RKF45, Rhs::ID, P::ID, 1}] = &launch_cross<TabRKF45, Rhs, P>;
+    cross_registry()[VariantKey{DEGPU_CASH_KARP, Rhs::ID, P::ID, 1}] = &launch_cross<TabCashKarp, Rhs, P>;
+}
 
 // Resumable round kernels of the serving path (no dense output).
 struct RoundOps {
@@ -172,6 +178,8 @@ void register_parity_multi();
 void register_multi_fast_mixed();
 void register_cross_parity();
 void register_cross_fast_mixed();
+void register_cross_embedded_parity();
+void register_cross_embedded_fast_mixed();
 void register_embedded_parity();
 void register_embedded_fast_mixed();
 void ensure_registered();

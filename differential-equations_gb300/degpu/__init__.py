@@ -19,8 +19,8 @@ import numpy as np
 from . import abi
 
 __all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
-           "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing", "write_csv",
-           "rust_debug_f64"]
+           "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing", "solve_ensemble_hyperplane",
+           "write_csv", "rust_debug_f64"]
 
 STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
                 abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness"}
@@ -145,6 +145,15 @@ class System:
     def fpu_beta(beta, masses):
         return System(abi.RHS["FPU_BETA"], [beta], 2 * masses)
 
+    @staticmethod
+    def brusselator(a, b):
+        return System(abi.RHS["BRUSSELATOR"], [a, b], 2)
+
+    @staticmethod
+    def cr3bp(mu):
+        """Circular restricted three-body problem, state (x, y, z, vx, vy, vz)."""
+        return System(abi.RHS["CR3BP"], [mu], 6)
+
 
 @dataclass
 class EnsembleResult:
@@ -157,12 +166,8 @@ class EnsembleResult:
     status: np.ndarray
 
 
-def solve_ensemble_crossing(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
-                            component: int, threshold: float, direction: int = abi.CROSS_BOTH,
-                            max_points: int = 16, family=None, n_params: Optional[int] = None):
-    """Solve n IVPs (host arrays) with crossing detection (degpu_solve_ensemble_crossing_host):
-    the crate's `.crossing(component, threshold, direction)` output.  Returns the EnsembleResult
-    and (t [max_points, n], y [max_points, dim, n], count [n])."""
+def _solve_crossing_host(fn, name, spec, rhs_id, dim, t0, tf, y0, params, rtol, atol, method, max_points, family,
+                         n_params):
     lib = abi.load()
     y0 = np.asarray(y0, dtype=np.float64)
     n = y0.shape[1]
@@ -182,13 +187,34 @@ def solve_ensemble_crossing(rhs_id: int, dim: int, t0, tf, y0, params, rtol, ato
     bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
                       accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
                       fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
-    cr = abi.Crossing(component=component, direction=direction, max_points=max_points, threshold=threshold)
     co = abi.CrossingOut(t=abi.ptr(ct), y=abi.ptr(cy), count=abi.ptr(cc, C.c_int32))
-    rc = lib.degpu_solve_ensemble_crossing_host(C.byref(prob), C.byref(method.cfg), C.byref(bi), C.byref(cr),
-                                                C.byref(bo), C.byref(co))
+    rc = getattr(lib, fn)(C.byref(prob), C.byref(method.cfg), C.byref(bi), C.byref(spec), C.byref(bo), C.byref(co))
     if rc != abi.OK:
-        raise DegpuError(rc, "degpu_solve_ensemble_crossing_host")
+        raise DegpuError(rc, fn)
     return EnsembleResult(**out), (ct, cy, cc)
+
+
+def solve_ensemble_crossing(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
+                            component: int, threshold: float, direction: int = abi.CROSS_BOTH,
+                            max_points: int = 16, family=None, n_params: Optional[int] = None):
+    """Solve n IVPs (host arrays) with crossing detection (degpu_solve_ensemble_crossing_host):
+    the crate's `.crossing(component, threshold, direction)` output.  Returns the EnsembleResult
+    and (t [max_points, n], y [max_points, dim, n], count [n])."""
+    cr = abi.Crossing(component=component, direction=direction, max_points=max_points, threshold=threshold)
+    return _solve_crossing_host("degpu_solve_ensemble_crossing_host", "crossing", cr, rhs_id, dim, t0, tf, y0,
+                                params, rtol, atol, method, max_points, family, n_params)
+
+
+def solve_ensemble_hyperplane(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
+                              components, point, normal, direction: int = abi.CROSS_BOTH, max_points: int = 16,
+                              family=None, n_params: Optional[int] = None):
+    """Solve n IVPs (host arrays) with hyperplane crossing detection
+    (degpu_solve_ensemble_hyperplane_host): the crate's `.hyperplane_crossing(point, normal,
+    extractor, direction)` output with the extractor given as state components
+    (pos[j] = y[components[j]]).  Returns what solve_ensemble_crossing returns."""
+    hp = abi.make_hyperplane(components, point, normal, direction, max_points)
+    return _solve_crossing_host("degpu_solve_ensemble_hyperplane_host", "hyperplane", hp, rhs_id, dim, t0, tf, y0,
+                                params, rtol, atol, method, max_points, family, n_params)
 
 
 def set_mixed_min_rtol(method: int, min_rtol: float) -> None:
@@ -318,7 +344,17 @@ class IVP:
     def crossing(self, component: int, threshold: float, direction: int = abi.CROSS_BOTH, max_points: int = 1024):
         """The crate's IVP::crossing (src/ivp.rs:682-693): the solution holds the points where
         y[component] crosses `threshold` in `direction` (replaces t_eval)."""
-        self._crossing = (component, threshold, direction, max_points)
+        self._crossing = ("component", (component, threshold), direction, max_points)
+        self._t_eval = None
+        return self
+
+    def hyperplane_crossing(self, point, normal, components, direction: int = abi.CROSS_BOTH,
+                            max_points: int = 1024):
+        """The crate's IVP::hyperplane_crossing (src/ivp.rs:695-706): the solution holds the
+        points where pos = y[components] crosses the plane through `point` with `normal` in
+        `direction` (replaces t_eval).  The crate's extractor function is given here as the list
+        of state components it picks."""
+        self._crossing = ("plane", (list(components), list(point), list(normal)), direction, max_points)
         self._t_eval = None
         return self
 
@@ -326,11 +362,13 @@ class IVP:
         m = self._method or ExplicitRungeKutta.dopri5()
         d = len(self.y0)
         if self._crossing is not None:
-            comp, thr, direction, cap = self._crossing
-            r, (ct, cy, cc) = solve_ensemble_crossing(
-                self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),
-                np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m._rtol], [m._atol], m,
-                comp, thr, direction, cap)
+            kind, spec, direction, cap = self._crossing
+            args = (self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),
+                    np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m._rtol], [m._atol], m)
+            if kind == "plane":
+                r, (ct, cy, cc) = solve_ensemble_hyperplane(*args, *spec, direction, cap)
+            else:
+                r, (ct, cy, cc) = solve_ensemble_crossing(*args, *spec, direction, cap)
             k = min(int(cc[0]), cap)
             st = STATUS_NAMES.get(int(r.status[0]), str(int(r.status[0])))
             return Solution([float(v) for v in ct[:k, 0]], [cy[j, :, 0].copy() for j in range(k)], st,

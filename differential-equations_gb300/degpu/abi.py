@@ -73,6 +73,27 @@ class CrossingOut(C.Structure):
 
 
 CROSS_BOTH, CROSS_POSITIVE, CROSS_NEGATIVE = 0, 1, -1
+HYPERPLANE_MAX_DIM = 8
+
+
+class Hyperplane(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("direction", C.c_int32), ("max_points", C.c_int32),
+                ("reserved", C.c_int32), ("components", C.c_int32 * HYPERPLANE_MAX_DIM),
+                ("point", C.c_double * HYPERPLANE_MAX_DIM), ("normal", C.c_double * HYPERPLANE_MAX_DIM)]
+
+
+def make_hyperplane(components, point, normal, direction=CROSS_BOTH, max_points=16) -> Hyperplane:
+    """degpu_hyperplane from sequences: pos[j] = y[components[j]], plane through `point` with
+    `normal` (scaled to unit length by the library)."""
+    m = len(components)
+    if not (1 <= m <= HYPERPLANE_MAX_DIM) or len(point) != m or len(normal) != m:
+        raise ValueError("hyperplane: 1..8 components, with a point and a normal of the same length")
+    hp = Hyperplane(dim=m, direction=direction, max_points=max_points)
+    for j in range(m):
+        hp.components[j] = int(components[j])
+        hp.point[j] = float(point[j])
+        hp.normal[j] = float(normal[j])
+    return hp
 
 
 class GrayScott(C.Structure):
@@ -110,6 +131,12 @@ SIGNATURES = {
                                                 C.c_void_p]),
     "degpu_solve_ensemble_crossing_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
                                                      C.POINTER(Crossing), C.POINTER(BatchOut), C.POINTER(CrossingOut)]),
+    "degpu_solve_ensemble_hyperplane": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                                  C.POINTER(Hyperplane), C.POINTER(BatchOut),
+                                                  C.POINTER(CrossingOut), C.c_void_p]),
+    "degpu_solve_ensemble_hyperplane_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg),
+                                                       C.POINTER(BatchIn), C.POINTER(Hyperplane),
+                                                       C.POINTER(BatchOut), C.POINTER(CrossingOut)]),
     "degpu_eval_rhs": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP,
                                  C.c_void_p]),
     "degpu_register_rhs_nvrtc": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, I32P, C.c_char_p,

@@ -256,6 +256,37 @@ degpu_status degpu_solve_ensemble_crossing_host(const degpu_problem* problem, co
                                                 const degpu_batch_in* in, const degpu_crossing* crossing,
                                                 degpu_batch_out* out, degpu_crossing_out* crossing_out);
 
+/* Hyperplane crossing detection: the crate's `.hyperplane_crossing(point, normal, extractor,
+ * direction)` output (HyperplaneCrossingSolout, src/solout/hyperplane.rs; IVP::hyperplane_crossing,
+ * src/ivp.rs:695-706). The extractor is a list of state components:
+ * pos[j] = y[components[j]], j < dim. The monitored quantity is the signed distance
+ * (pos - point) . normal, with the normal scaled to unit length when its norm exceeds the FP64
+ * machine epsilon (as the crate's constructor does). Unlike component crossings, a step that
+ * starts or ends exactly on the plane also counts as a crossing. The location search and the
+ * outputs are those of degpu_solve_ensemble_crossing. */
+#define DEGPU_HYPERPLANE_MAX_DIM 8
+
+typedef struct {
+    int32_t dim;         /* components extracted, 1 <= dim <= DEGPU_HYPERPLANE_MAX_DIM        */
+    int32_t direction;   /* degpu_crossing_direction, on the signed distance                   */
+    int32_t max_points;  /* capacity per instance of the outputs (>= 0)                        */
+    int32_t reserved;
+    int32_t components[DEGPU_HYPERPLANE_MAX_DIM]; /* extractor: state index of pos[j]          */
+    double point[DEGPU_HYPERPLANE_MAX_DIM];       /* a point of the plane, in extracted space  */
+    double normal[DEGPU_HYPERPLANE_MAX_DIM];      /* its normal (any length)                   */
+} degpu_hyperplane;
+
+/* degpu_solve_ensemble_crossing with a hyperplane instead of a component threshold; device
+ * pointers, stream-ordered. Same families, methods and precisions. */
+degpu_status degpu_solve_ensemble_hyperplane(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                             const degpu_batch_in* in, const degpu_hyperplane* plane,
+                                             degpu_batch_out* out, degpu_crossing_out* crossing_out, void* stream);
+
+/* Same with HOST pointers, synchronous. */
+degpu_status degpu_solve_ensemble_hyperplane_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                                  const degpu_batch_in* in, const degpu_hyperplane* plane,
+                                                  degpu_batch_out* out, degpu_crossing_out* crossing_out);
+
 /* One evaluation of a built-in right-hand side for every instance (`ODE::diff`,
  * src/ode/ode.rs:20-44), device pointers: dydt[c*n+i] = f_i(t[i], y_i). */
 degpu_status degpu_eval_rhs(int32_t rhs_id, int32_t precision, int64_t n, int32_t dim, int32_t n_params,

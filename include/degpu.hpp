@@ -132,6 +132,7 @@ class ExplicitRungeKutta {
     // GPU knobs
     ExplicitRungeKutta& precision(degpu_precision p) { cfg_.precision = p; return *this; }
     ExplicitRungeKutta& kernel(degpu_kernel k) { cfg_.kernel = k; return *this; }
+    ExplicitRungeKutta& dense_mode(degpu_dense_mode d) { cfg_.dense_mode = d; return *this; }
     const degpu_method_cfg& cfg() const { return cfg_; }
     double rtol() const { return rtol_; }
     double atol() const { return atol_; }
@@ -152,7 +153,12 @@ struct System {
     static System exponential_growth(double k) { return {DEGPU_RHS_EXP_GROWTH, {k}}; }
     static System harmonic(double k) { return {DEGPU_RHS_HARMONIC, {k}}; }
     static System fpu_beta(double beta) { return {DEGPU_RHS_FPU_BETA, {beta}}; }
+    static System brusselator(double a, double b) { return {DEGPU_RHS_BRUSSELATOR, {a, b}}; }
+    static System cr3bp(double mu) { return {DEGPU_RHS_CR3BP, {mu}}; }
 };
+
+// src/solout/crossing.rs:17-26
+enum class CrossingDirection { Both = DEGPU_CROSS_BOTH, Positive = DEGPU_CROSS_POSITIVE, Negative = DEGPU_CROSS_NEGATIVE };
 
 // Results of an ensemble solve, structure of arrays (layout of degpu.h).
 struct EnsembleResult {
@@ -210,9 +216,43 @@ class IVP {
         return p;
     }
     IVP& method(const ExplicitRungeKutta& m) { m_ = m; return *this; }
-    IVP& t_eval(std::vector<double> pts) { te_ = std::move(pts); return *this; }
+    IVP& t_eval(std::vector<double> pts) {
+        te_ = std::move(pts);
+        cross_ = 0;
+        return *this;
+    }
+    // src/ivp.rs:682-693: the solution holds the points where y[component] crosses threshold
+    IVP& crossing(int32_t component, double threshold, CrossingDirection dir = CrossingDirection::Both,
+                  int32_t max_points = 1024) {
+        cross_ = 1;
+        cr_ = degpu_crossing{component, (int32_t)dir, max_points, 0, threshold};
+        te_.clear();
+        return *this;
+    }
+    // src/ivp.rs:695-706: the points where pos = y[components] crosses the plane through point
+    // with normal; the crate's extractor function is given as the components it picks
+    IVP& hyperplane_crossing(const std::vector<double>& point, const std::vector<double>& normal,
+                             const std::vector<int32_t>& components, CrossingDirection dir = CrossingDirection::Both,
+                             int32_t max_points = 1024) {
+        cross_ = 2;
+        hp_ = degpu_hyperplane{};
+        hp_.dim = (int32_t)components.size();
+        hp_.direction = (int32_t)dir;
+        hp_.max_points = max_points;
+        for (size_t j = 0; j < components.size() && j < DEGPU_HYPERPLANE_MAX_DIM; ++j) {
+            hp_.components[j] = components[j];
+            hp_.point[j] = j < point.size() ? point[j] : NAN;
+            hp_.normal[j] = j < normal.size() ? normal[j] : NAN;
+        }
+        if (components.size() > DEGPU_HYPERPLANE_MAX_DIM || point.size() != components.size() ||
+            normal.size() != components.size())
+            hp_.dim = 0;  // rejected as bad input by the library
+        te_.clear();
+        return *this;
+    }
 
     Result<Solution> solve() const {
+        if (cross_) return solve_crossing();
         const int32_t d = (int32_t)y0_.size();
         EnsembleResult r;
         try {
@@ -255,10 +295,63 @@ class IVP {
     }
 
    private:
+    static Result<Solution> status_error(int32_t status, double t, const std::vector<double>& y) {
+        switch (status) {
+            case DEGPU_ERR_BAD_INPUT:
+                return Result<Solution>::err(Error{ErrorKind::BadInput, "Invalid input: step size or interval"});
+            case DEGPU_ERR_MAX_STEPS: return Result<Solution>::err(Error{ErrorKind::MaxSteps, "MaxSteps", t, y});
+            case DEGPU_ERR_STEP_SIZE: return Result<Solution>::err(Error{ErrorKind::StepSize, "StepSize", t, y});
+            default: return Result<Solution>::err(Error{ErrorKind::Stiffness, "Stiffness", t, y});
+        }
+    }
+
+    // One instance through degpu_solve_ensemble_crossing_host / _hyperplane_host.
+    Result<Solution> solve_crossing() const {
+        const int32_t d = (int32_t)y0_.size();
+        const int32_t cap = cross_ == 1 ? cr_.max_points : hp_.max_points;
+        const size_t m = cap > 0 ? (size_t)cap : 0;
+        std::vector<double> yf(d), tf(1), ct(m), cy(m * d);
+        std::vector<int64_t> acc(1), rej(1), fev(1);
+        std::vector<int32_t> st(1), cc(1);
+        double t0 = t0_, t1 = tf_, rtol = m_.rtol(), atol = m_.atol();
+        degpu_problem pb{sys_.rhs_id, d, (int32_t)sys_.params.size(), 0};
+        degpu_batch_in in{};
+        in.n = 1;
+        in.t0 = &t0;
+        in.tf = &t1;
+        in.y0 = y0_.data();
+        in.params = sys_.params.empty() ? nullptr : sys_.params.data();
+        in.rtol = &rtol;
+        in.atol = &atol;
+        degpu_batch_out out{yf.data(), tf.data(), nullptr, acc.data(), rej.data(), fev.data(), st.data()};
+        degpu_crossing_out co{m ? ct.data() : nullptr, m ? cy.data() : nullptr, cc.data()};
+        const degpu_status rc = cross_ == 1 ? degpu_solve_ensemble_crossing_host(&pb, &m_.cfg(), &in, &cr_, &out, &co)
+                                            : degpu_solve_ensemble_hyperplane_host(&pb, &m_.cfg(), &in, &hp_, &out, &co);
+        if (rc == DEGPU_BAD_INPUT) return Result<Solution>::err(Error{ErrorKind::BadInput, "Invalid input: crossing"});
+        if (rc != DEGPU_OK)
+            return Result<Solution>::err(Error{ErrorKind::Device, std::string("crossing solve: ") + degpu_status_string(rc)});
+        if (st[0] != DEGPU_COMPLETE) return status_error(st[0], tf[0], yf);
+        Solution s;
+        s.evals = (size_t)fev[0];
+        s.accepted = (size_t)acc[0];
+        s.rejected = (size_t)rej[0];
+        const size_t k = std::min(m, (size_t)cc[0]);
+        for (size_t j = 0; j < k; ++j) {
+            s.t.push_back(ct[j]);
+            std::vector<double> yj(d);
+            for (int32_t c = 0; c < d; ++c) yj[c] = cy[j * d + c];
+            s.y.push_back(std::move(yj));
+        }
+        return Result<Solution>::ok_value(std::move(s));
+    }
+
     System sys_{};
     double t0_ = 0, tf_ = 0;
     std::vector<double> y0_, te_;
     ExplicitRungeKutta m_ = ExplicitRungeKutta::dopri5();
+    int cross_ = 0;  // 0 none, 1 component crossing, 2 hyperplane crossing
+    degpu_crossing cr_{};
+    degpu_hyperplane hp_{};
 };
 
 }  // namespace degpu

@@ -85,8 +85,8 @@ void oracle_libm_pow_batch(const double* x, const double* y, double* out, int64_
 
 // Solve one instance i of the batch into the outputs.
 static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
-                           degpu_batch_out* out, int64_t i, const Math& math, const degpu_crossing* cr = nullptr,
-                           degpu_crossing_out* co = nullptr) {
+                           degpu_batch_out* out, int64_t i, const Math& math, const CrossingSolout* proto = nullptr,
+                           int64_t max_points = 0, degpu_crossing_out* co = nullptr) {
     const int64_t n = in->n;
     int rhs = in->family ? in->family[i] : pb->rhs_id;
     // per-instance dimension: given explicitly (ragged batches) or the family's own
@@ -116,15 +116,11 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
         tep = &te;
     }
     CrossingSolout cs;
-    if (cr) {
-        cs.comp = cr->component;
-        cs.threshold = cr->threshold;
-        cs.direction = cr->direction;
-    }
+    if (proto) cs = *proto;
     Result r = solve_one(cfg->method, ode, in->t0[i], in->tf[i], y0, set, math, tep,
-                         cfg->dense_mode == DEGPU_DENSE_HAIRER, cr ? &cs : nullptr);
-    if (cr && co) {
-        const int64_t m = cr->max_points;
+                         cfg->dense_mode == DEGPU_DENSE_HAIRER, proto ? &cs : nullptr);
+    if (proto && co) {
+        const int64_t m = max_points;
         co->count[i] = (int32_t)cs.t.size();
         for (int64_t k = 0; k < m; ++k) {
             const bool have = (size_t)k < cs.t.size();
@@ -159,7 +155,33 @@ int oracle_solve_ensemble_crossing(const degpu_problem* pb, const degpu_method_c
     if (cr->component < 0 || cr->component >= pb->dim || cr->max_points < 0) return 1;
     Math math;
     math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
-    for_instances(in->n, threads, [&](int64_t i) { solve_instance(pb, cfg, in, out, i, math, cr, co); });
+    CrossingSolout proto;
+    proto.comp = cr->component;
+    proto.threshold = cr->threshold;
+    proto.direction = cr->direction;
+    for_instances(in->n, threads,
+                  [&](int64_t i) { solve_instance(pb, cfg, in, out, i, math, &proto, cr->max_points, co); });
+    return 0;
+}
+
+// Hyperplane crossing detection (HyperplaneCrossingSolout) for every instance; outputs laid out
+// as degpu_solve_ensemble_hyperplane's.  Returns 0 on success, 1 on bad input.
+int oracle_solve_ensemble_hyperplane(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                     const degpu_hyperplane* hp, degpu_batch_out* out, degpu_crossing_out* co,
+                                     int threads, int math_mode) {
+    if (!pb || !cfg || !in || !out || !hp || !co || in->n < 0 || !out->y_final || in->n_eval > 0) return 1;
+    if (hp->dim < 1 || hp->dim > DEGPU_HYPERPLANE_MAX_DIM || hp->max_points < 0) return 1;
+    std::vector<int> comps(hp->components, hp->components + hp->dim);
+    for (int c : comps)
+        if (c < 0 || c >= pb->dim) return 1;
+    Math math;
+    math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
+    CrossingSolout proto;
+    proto.direction = hp->direction;
+    proto.set_plane(comps, std::vector<double>(hp->point, hp->point + hp->dim),
+                    std::vector<double>(hp->normal, hp->normal + hp->dim));
+    for_instances(in->n, threads,
+                  [&](int64_t i) { solve_instance(pb, cfg, in, out, i, math, &proto, hp->max_points, co); });
     return 0;
 }
 

@@ -13,7 +13,7 @@
 //   cubic Hermite ................... src/interpolate.rs:40-60
 //   Adaptive ERK (RKF45, Cash-Karp)  src/methods/erk/adaptive/ordinary.rs:16-290
 //   TEvalSolout ..................... src/solout/t_eval.rs:82-171
-//   CrossingSolout .................. src/solout/crossing.rs:200-330
+//   CrossingSolout .................. src/solout/crossing.rs:200-330, src/solout/hyperplane.rs
 //   tableaus ........................ src/tableau/runge_kutta.rs:39-70, src/tableau/dorman_prince.rs:37-381
 //
 // Compile with -ffp-contract=off: Rust never contracts a*b+c into an FMA, so neither may this.
@@ -677,37 +677,76 @@ struct TEvalSolout {
 };
 
 // ---------------------------------------------------------------------------------------------
-// Crossing detection: CrossingSolout (src/solout/crossing.rs:200-330). After each call (at t0 and
-// after every accepted step) the offset y[comp] - threshold is compared in sign with the previous
-// one; a crossing in the requested direction is located by find_crossing_newton on the step's
+// Crossing detection: CrossingSolout (src/solout/crossing.rs:200-330) and
+// HyperplaneCrossingSolout (src/solout/hyperplane.rs). After each call (at t0 and after every
+// accepted step) the monitored offset is compared in sign with the previous one:
+//   * component form: y[comp] - threshold;
+//   * hyperplane form: the signed distance (pos - point) . normal, pos[j] = y[plane_comp[j]],
+//     with the normal scaled to unit length at construction; leaving or reaching the plane
+//     exactly also counts as a crossing.
+// A crossing in the requested direction is located by find_crossing_newton on the step's
 // interpolant, or by the linear estimate when that does not converge.
 // ---------------------------------------------------------------------------------------------
 struct CrossingSolout {
     int comp = 0;
     double threshold = 0.0;
     int direction = 0;  // 0 both, 1 positive (from below), -1 negative
+    bool plane = false;
+    std::vector<int> plane_comp;
+    std::vector<double> plane_point, plane_normal;
     bool have_last = false;
     double last_offset = 0.0;
     std::vector<double> t;  // crossings in the order found
     std::vector<State> y;
 
+    // HyperplaneCrossingSolout::new: normal *= 1/|normal| when |normal| > eps; the squared norm
+    // folds from zero in component order (src/traits.rs:574-576), scale_by multiplies each
+    // component (src/traits.rs:323-326).
+    void set_plane(const std::vector<int>& comps, const std::vector<double>& point, const std::vector<double>& normal) {
+        plane = true;
+        plane_comp = comps;
+        plane_point = point;
+        plane_normal = normal;
+        double nn = 0.0;
+        for (double v : plane_normal) nn = nn + v * v;
+        const double norm = std::sqrt(nn);
+        if (norm > std::numeric_limits<double>::epsilon()) {
+            const double inv = 1.0 / norm;
+            for (double& v : plane_normal) v = v * inv;
+        }
+    }
+
+    // crossing.rs:207 / hyperplane.rs signed_distance: (extract(y) - point).dot(normal), the dot
+    // folded from zero in component order (src/traits.rs:551-555)
+    double offset(const State& v) const {
+        if (!plane) return v[comp] - threshold;
+        double sum = 0.0;
+        for (size_t j = 0; j < plane_comp.size(); ++j) {
+            const double d = v[plane_comp[j]] - plane_point[j];
+            sum = sum + d * plane_normal[j];
+        }
+        return sum;
+    }
+
     void solout(double t_curr, double t_prev, const State& y_curr, Interpolator& interp) {
-        const double offset = y_curr[comp] - threshold;
+        const double off = offset(y_curr);
         if (have_last) {
-            const bool is_crossing = rust_signum(last_offset) != rust_signum(offset);  // crossing.rs:210
+            bool is_crossing = rust_signum(last_offset) != rust_signum(off);  // crossing.rs:210
+            if (plane)  // hyperplane.rs: the zero cases
+                is_crossing = is_crossing || (last_offset == 0.0 && off != 0.0) || (last_offset != 0.0 && off == 0.0);
             if (is_crossing) {
                 bool record;  // crossing.rs:214-218
                 if (direction > 0)
-                    record = last_offset < 0.0 && offset >= 0.0;
+                    record = last_offset < 0.0 && off >= 0.0;
                 else if (direction < 0)
-                    record = last_offset > 0.0 && offset <= 0.0;
+                    record = last_offset > 0.0 && off <= 0.0;
                 else
                     record = true;
                 if (record) {
                     double tc;
-                    if (!find_crossing_newton(interp, t_prev, t_curr, last_offset, offset, tc)) {
+                    if (!find_crossing_newton(interp, t_prev, t_curr, last_offset, off, tc)) {
                         // crossing.rs:234-238: linear estimate
-                        const double frac = -last_offset / (offset - last_offset);
+                        const double frac = -last_offset / (off - last_offset);
                         tc = t_prev + frac * (t_curr - t_prev);
                     }
                     t.push_back(tc);
@@ -715,42 +754,43 @@ struct CrossingSolout {
                 }
             }
         }
-        last_offset = offset;
+        last_offset = off;
         have_last = true;
     }
 
-    // crossing.rs:254-328
+    // crossing.rs:254-328; the hyperplane form breaks on a derivative below eps (not 10 eps)
+    // and has no step-change test
     bool find_crossing_newton(Interpolator& interp, double t_lower, double t_upper, double offset_lower,
                               double offset_upper, double& t_out) const {
         const double eps = std::numeric_limits<double>::epsilon();
         double t = t_lower - offset_lower * (t_upper - t_lower) / (offset_upper - offset_lower);
         const double tolerance = eps * 100.0;
-        double offset;
+        double off;
         for (int it = 0; it < 10; ++it) {
-            offset = interp.interpolate(t)[comp] - threshold;
-            if (std::fabs(offset) < tolerance) {
+            off = offset(interp.interpolate(t));
+            if (std::fabs(off) < tolerance) {
                 t_out = t;
                 return true;
             }
             const double delta_t = (t_upper - t_lower) * 1e-6;
             const double t_plus = t + delta_t;
-            const double offset_plus = interp.interpolate(t_plus)[comp] - threshold;
-            const double derivative = (offset_plus - offset) / delta_t;
-            if (std::fabs(derivative) < eps * 10.0) break;
-            const double t_new = t - offset / derivative;
+            const double offset_plus = offset(interp.interpolate(t_plus));
+            const double derivative = (offset_plus - off) / delta_t;
+            if (std::fabs(derivative) < (plane ? eps : eps * 10.0)) break;
+            const double t_new = t - off / derivative;
             if (t_new < t_lower || t_new > t_upper) {
                 t = (t_lower + t_upper) / 2.0;
             } else {
                 const double change = std::fabs(t_new - t);
-                if (change < tolerance * 0.1) {
+                if (!plane && change < tolerance * 0.1) {
                     t = t_new;
                     break;
                 }
                 t = t_new;
             }
         }
-        offset = interp.interpolate(t)[comp] - threshold;
-        if (std::fabs(offset) < tolerance * 10.0) {
+        off = offset(interp.interpolate(t));
+        if (std::fabs(off) < tolerance * 10.0) {
             t_out = t;
             return true;
         }

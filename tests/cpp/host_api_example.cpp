@@ -30,6 +30,28 @@ int main() {
     auto er = solve_ensemble(DEGPU_RHS_HARMONIC, 2, 1, {0.0, 0.0}, {10.0, 5.0}, {1.0, 1.0, 0.0, 0.0}, {1.0, 1.0},
                              {1e-10, 1e-10}, {1e-12, 1e-12}, ExplicitRungeKutta::dop853());
     if (er.status[0] != DEGPU_COMPLETE || std::fabs(er.y_final[0] - std::cos(10.0)) > 1e-8) { std::printf("ens\n"); return 6; }
+    // crossings of the harmonic oscillator x = cos t: x = 0 at pi/2 + j pi, x + v = 0 at pi/4 + j pi
+    const double pi = 3.141592653589793;
+    auto hm = ExplicitRungeKutta::dop853().rtol(1e-11).atol(1e-11).dense_mode(DEGPU_DENSE_HAIRER);
+    auto cx = IVP::ode(System::harmonic(1.0), 0.0, 10.0, {1.0, 0.0}).method(hm).crossing(0, 0.0).solve();
+    if (!cx.ok() || cx.value().t.size() != 3 || std::fabs(cx.value().t[1] - 1.5 * pi) > 1e-9) {
+        std::printf("crossing\n");
+        return 7;
+    }
+    auto hx = IVP::ode(System::harmonic(1.0), 0.0, 10.0, {1.0, 0.0})
+                  .method(hm)
+                  .hyperplane_crossing({0.0, 0.0}, {2.0, 2.0}, {0, 1}, CrossingDirection::Negative)
+                  .solve();
+    // the signed distance (x + v)/sqrt(2) falls through zero at pi/4 + 2 j pi
+    if (!hx.ok() || hx.value().t.size() != 2 || std::fabs(hx.value().t[1] - 2.25 * pi) > 1e-9) {
+        std::printf("hyperplane\n");
+        return 8;
+    }
+    auto hb = IVP::ode(System::harmonic(1.0), 0.0, 1.0, {1.0, 0.0}).hyperplane_crossing({0.0}, {1.0, 0.0}, {0}).solve();
+    if (hb.ok() || hb.error().kind != ErrorKind::BadInput) {
+        std::printf("hyperplane bad input\n");
+        return 9;
+    }
     std::printf("ok\n");
     return 0;
 }

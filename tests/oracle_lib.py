@@ -42,6 +42,11 @@ def lib():
                                                      C.POINTER(abi.BatchOut), C.POINTER(abi.CrossingOut), C.c_int,
                                                      C.c_int]
         L.oracle_solve_ensemble_crossing.restype = C.c_int
+        L.oracle_solve_ensemble_hyperplane.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.MethodCfg),
+                                                       C.POINTER(abi.BatchIn), C.POINTER(abi.Hyperplane),
+                                                       C.POINTER(abi.BatchOut), C.POINTER(abi.CrossingOut),
+                                                       C.c_int, C.c_int]
+        L.oracle_solve_ensemble_hyperplane.restype = C.c_int
         L.oracle_eval_rhs.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP, C.c_int]
         for nm in ("oracle_cr_pow", "oracle_libm_pow"):
             getattr(L, nm).argtypes = [C.c_double, C.c_double]
@@ -135,6 +140,26 @@ def solve_crossing(batch: Batch, cfg, component, threshold, direction=0, max_poi
     rc = lib().oracle_solve_ensemble_crossing(C.byref(batch.problem), C.byref(cfg), C.byref(batch.batch_in()),
                                               C.byref(cr), C.byref(Batch.batch_out(out)), C.byref(co), threads,
                                               math_mode)
+    assert rc == 0
+    out.update(cross_t=ct, cross_y=cy, cross_count=cc)
+    return out
+
+
+def solve_hyperplane(batch: Batch, cfg, components, point, normal, direction=0, max_points=16, threads=None,
+                     math_mode=1):
+    """Oracle solve with hyperplane crossing detection (HyperplaneCrossingSolout): returns the
+    ordinary outputs plus cross_t, cross_y and cross_count as solve_crossing does."""
+    out = batch.new_outputs()
+    n, dim = batch.n, batch.problem.dim
+    ct = np.empty((max_points, n))
+    cy = np.empty((max_points, dim, n))
+    cc = np.empty(n, np.int32)
+    hp = abi.make_hyperplane(components, point, normal, direction, max_points)
+    co = abi.CrossingOut(t=p(ct), y=p(cy), count=abi.ptr(cc, C.c_int32))
+    threads = threads or os.cpu_count() or 1
+    rc = lib().oracle_solve_ensemble_hyperplane(C.byref(batch.problem), C.byref(cfg), C.byref(batch.batch_in()),
+                                                C.byref(hp), C.byref(Batch.batch_out(out)), C.byref(co), threads,
+                                                math_mode)
     assert rc == 0
     out.update(cross_t=ct, cross_y=cy, cross_count=cc)
     return out

@@ -15,6 +15,12 @@ R = abi.RHS
 
 
 def gpu_crossing(e, cfg, comp, thr, direction, max_points):
+    cr = abi.Crossing(component=comp, direction=direction, max_points=max_points, threshold=thr)
+    return gpu_solve_crossing(e, cfg, "degpu_solve_ensemble_crossing", cr, max_points)
+
+
+def gpu_solve_crossing(e, cfg, fn, spec, max_points):
+    """One device-pointer crossing entry point (component or hyperplane spec) on torch tensors."""
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
     T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
@@ -31,13 +37,12 @@ def gpu_crossing(e, cfg, comp, thr, direction, max_points):
     bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
                       accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
                       fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
-    cr = abi.Crossing(component=comp, direction=direction, max_points=max_points, threshold=thr)
     co = abi.CrossingOut(t=abi.ptr(out["cross_t"]), y=abi.ptr(out["cross_y"]),
                          count=abi.ptr(out["cross_count"], C.c_int32))
     prob = abi.Problem(rhs_id=e.rhs_id, dim=e.dim, n_params=e.params.shape[0])
     stream = torch.cuda.Stream()
-    rc = abi.load().degpu_solve_ensemble_crossing(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(cr),
-                                                  C.byref(bo), C.byref(co), C.c_void_p(stream.cuda_stream))
+    rc = getattr(abi.load(), fn)(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(spec), C.byref(bo), C.byref(co),
+                                 C.c_void_p(stream.cuda_stream))
     stream.synchronize()
     assert rc == abi.OK, rc
     return {k: v.cpu().numpy() for k, v in out.items()}
