@@ -179,6 +179,35 @@ static EnsArgs make_args(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     return a;
 }
 
+// The requested output times: TEvalSolout::new's stable ascending sort (descending instances walk
+// it backwards), uploaded with its permutation; every output starts as NaN, so points the solve
+// never reaches stay NaN. Without a dense output array there are no output times.
+static degpu_status prepare_t_eval(EnsArgs& a, const degpu_problem* pb, const degpu_batch_in* in,
+                                   degpu_batch_out* out, const double* t_eval_host, Scratch& scratch,
+                                   cudaStream_t s) {
+    if (a.n_eval > 0 && !out->dense) a.n_eval = 0;
+    if (a.n_eval == 0) return DEGPU_OK;
+    std::vector<int32_t> perm(a.n_eval);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) { return t_eval_host[x] < t_eval_host[y]; });
+    std::vector<double> sorted(a.n_eval);
+    for (int e = 0; e < a.n_eval; ++e) sorted[e] = t_eval_host[perm[e]];
+    double* d_t = scratch.alloc<double>(a.n_eval);
+    int32_t* d_p = scratch.alloc<int32_t>(a.n_eval);
+    if (!d_t || !d_p) return DEGPU_OOM;
+    if (cudaMemcpyAsync(d_t, sorted.data(), a.n_eval * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d_p, perm.data(), a.n_eval * sizeof(int32_t), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return DEGPU_CUDA_ERROR;
+    a.t_eval = d_t;
+    a.eval_perm = d_p;
+    // the host vectors must outlive the async copies
+    if (cudaStreamSynchronize(s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    // 0xFF bytes form a quiet NaN
+    const size_t bytes = (size_t)in->n_eval * pb->dim * in->n * sizeof(double);
+    if (cudaMemsetAsync(out->dense, 0xFF, bytes, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
+    return DEGPU_OK;
+}
+
 // Core of degpu_solve_ensemble.  `family_host` / `t_eval_host` are host copies of the
 // corresponding device arrays (or NULL when absent).
 static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
@@ -190,35 +219,11 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
     Scratch scratch(s);
 
     EnsArgs a = make_args(pb, cfg, in, out);
-    const bool dense = a.n_eval > 0 && out->dense;
-    if (a.n_eval > 0 && !out->dense) a.n_eval = 0;
-
-    // TEvalSolout::new: stable sort ascending; descending instances walk it backwards
-    if (a.n_eval > 0) {
-        std::vector<int32_t> perm(a.n_eval);
-        std::iota(perm.begin(), perm.end(), 0);
-        std::stable_sort(perm.begin(), perm.end(),
-                         [&](int32_t x, int32_t y) { return t_eval_host[x] < t_eval_host[y]; });
-        std::vector<double> sorted(a.n_eval);
-        for (int e = 0; e < a.n_eval; ++e) sorted[e] = t_eval_host[perm[e]];
-        double* d_t = scratch.alloc<double>(a.n_eval);
-        int32_t* d_p = scratch.alloc<int32_t>(a.n_eval);
-        if (!d_t || !d_p) return DEGPU_OOM;
-        if (cudaMemcpyAsync(d_t, sorted.data(), a.n_eval * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-            cudaMemcpyAsync(d_p, perm.data(), a.n_eval * sizeof(int32_t), cudaMemcpyHostToDevice, s) != cudaSuccess)
-            return DEGPU_CUDA_ERROR;
-        a.t_eval = d_t;
-        a.eval_perm = d_p;
-        // the host vectors must outlive the async copies
-        cudaError_t e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return DEGPU_CUDA_ERROR;
-        // every output time starts as NaN: points the solve never reaches stay NaN
+    {
+        degpu_status st = prepare_t_eval(a, pb, in, out, t_eval_host, scratch, s);
+        if (st != DEGPU_OK) return st;
     }
-    if (dense) {
-        size_t bytes = (size_t)in->n_eval * pb->dim * n * sizeof(double);
-        // 0xFF bytes form a quiet NaN
-        if (cudaMemsetAsync(out->dense, 0xFF, bytes, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
-    }
+    const bool dense = a.n_eval > 0;
 
     // ragged (per-instance dimension) problems go to the warp-per-system kernel
     if (pb->rhs_id == DEGPU_RHS_FPU_BETA) {
@@ -363,14 +368,17 @@ static degpu_status validate(const degpu_problem* pb, const degpu_method_cfg* cf
     return DEGPU_OK;
 }
 
-// What a crossing-detection solve monitors: a component against a threshold
-// (degpu_crossing) or the signed distance to a hyperplane (degpu_hyperplane).
+// What a crossing- or event-detection solve monitors: a component against a threshold
+// (degpu_crossing, mode 0), the signed distance to a hyperplane (degpu_hyperplane, mode 1) or an
+// event function (degpu_event, mode 2).
 struct CrossSpec {
-    int32_t plane = 0, comp = 0, dir = 0, max_points = 0;
-    double value = 0.0;  // threshold; for a plane, sum |point_j normal_j|
-    int32_t dim = 0;
+    int32_t mode = 0, comp = 0, dir = 0, max_points = 0;
+    double value = 0.0;  // threshold; plane: sum |point_j normal_j|; event: offset
+    int32_t dim = 0;     // terms
     int32_t comps[DEGPU_HYPERPLANE_MAX_DIM] = {};
-    double point[DEGPU_HYPERPLANE_MAX_DIM] = {}, normal[DEGPU_HYPERPLANE_MAX_DIM] = {};
+    double point[DEGPU_HYPERPLANE_MAX_DIM] = {}, normal[DEGPU_HYPERPLANE_MAX_DIM] = {};  // event: weights in normal
+    int32_t event_kind = 0, terminate = 0;
+    double t_weight = 0.0;
     int32_t max_comp = 0;  // largest state index read
 };
 
@@ -391,7 +399,7 @@ static bool make_spec(const degpu_crossing* cr, int32_t dim, CrossSpec& sp) {
 static bool make_spec(const degpu_hyperplane* hp, int32_t dim, CrossSpec& sp) {
     if (hp->dim < 1 || hp->dim > DEGPU_HYPERPLANE_MAX_DIM || hp->max_points < 0) return false;
     if (hp->direction < -1 || hp->direction > 1) return false;
-    sp.plane = 1;
+    sp.mode = 1;
     sp.dir = hp->direction;
     sp.max_points = hp->max_points;
     sp.dim = hp->dim;
@@ -416,11 +424,34 @@ static bool make_spec(const degpu_hyperplane* hp, int32_t dim, CrossSpec& sp) {
     return true;
 }
 
-// degpu_solve_ensemble_crossing / _hyperplane: one run-to-completion crossing-detection launch
+// EventWrappedSolout's event (src/solout/event.rs:299-521) in one of the two built-in forms.
+static bool make_spec(const degpu_event* ev, int32_t dim, CrossSpec& sp) {
+    if (ev->kind != DEGPU_EVENT_LINEAR && ev->kind != DEGPU_EVENT_MAX_ABS) return false;
+    const int32_t min_terms = ev->kind == DEGPU_EVENT_MAX_ABS ? 1 : 0;
+    if (ev->n_terms < min_terms || ev->n_terms > DEGPU_EVENT_MAX_TERMS) return false;
+    if (ev->max_points < 0 || ev->terminate < 0 || ev->direction < -1 || ev->direction > 1) return false;
+    sp.mode = 2;
+    sp.dir = ev->direction;
+    sp.max_points = ev->max_points;
+    sp.dim = ev->n_terms;
+    sp.event_kind = ev->kind;
+    sp.terminate = ev->terminate;
+    sp.t_weight = ev->t_weight;
+    sp.value = ev->offset;
+    for (int j = 0; j < ev->n_terms; ++j) {
+        if (ev->components[j] < 0 || ev->components[j] >= dim) return false;
+        sp.comps[j] = ev->components[j];
+        sp.max_comp = std::max(sp.max_comp, ev->components[j]);
+        sp.normal[j] = ev->weights[j];
+    }
+    return true;
+}
+
+// degpu_solve_ensemble_crossing / _hyperplane / _event: one run-to-completion detection launch
 // per (family, precision) work list.
 static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                                   const CrossSpec& cr, degpu_batch_out* out, degpu_crossing_out* co,
-                                  cudaStream_t s) {
+                                  const double* t_eval_host, cudaStream_t s) {
     const int64_t n = in->n;
     Scratch scratch(s);
     std::vector<int32_t> fam_host;
@@ -455,7 +486,12 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
             return DEGPU_UNSUPPORTED;
     }
     EnsArgs a = make_args(pb, cfg, in, out);
-    a.n_eval = 0;
+    if (cr.mode == 2) {  // events keep the output times as their base output
+        degpu_status st = prepare_t_eval(a, pb, in, out, t_eval_host, scratch, s);
+        if (st != DEGPU_OK) return st;
+    } else {
+        a.n_eval = 0;
+    }
     a.cross_comp = cr.comp;
     a.cross_dir = cr.dir;
     a.cross_max = cr.max_points;
@@ -463,12 +499,15 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
     a.cross_t = co->t;
     a.cross_y = co->y;
     a.cross_count = co->count;
-    a.cross_plane = cr.plane;
-    a.plane_dim = cr.dim;
+    a.cross_mode = cr.mode;
+    a.n_terms = cr.dim;
+    a.event_kind = cr.event_kind;
+    a.event_terminate = cr.terminate;
+    a.event_tw = cr.t_weight;
     for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j) {
-        a.plane_comp[j] = cr.comps[j];
-        a.plane_point[j] = cr.point[j];
-        a.plane_normal[j] = cr.normal[j];
+        a.term_comp[j] = cr.comps[j];
+        a.term_a[j] = cr.point[j];
+        a.term_w[j] = cr.normal[j];
     }
     if (cr.max_points > 0) {
         // 0xFF bytes form a quiet NaN: slots past an instance's count stay NaN
@@ -518,12 +557,21 @@ static degpu_status crossing_entry(const degpu_problem* pb, const degpu_method_c
     if (!sd || !co) return DEGPU_BAD_INPUT;
     degpu_status v = validate(pb, cfg, in, out);
     if (v != DEGPU_OK || in->n == 0) return v;
-    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
     CrossSpec cr;
     if (!make_spec(sd, pb->dim, cr)) return DEGPU_BAD_INPUT;
+    // output times are the base output of events only (crossings replace them)
+    if ((in->n_eval > 0 && cr.mode != 2) || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
     if (!co->count || (cr.max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
     ensure_registered();
-    return crossing_impl(pb, cfg, in, cr, out, co, s);
+    std::vector<double> te;
+    if (in->n_eval > 0 && out->dense) {
+        te.resize(in->n_eval);
+        if (cudaMemcpyAsync(te.data(), in->t_eval, in->n_eval * sizeof(double), cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+    }
+    return crossing_impl(pb, cfg, in, cr, out, co, te.empty() ? nullptr : te.data(), s);
 }
 
 // Shared body of the host-pointer crossing entry points: copies in, solves, copies back.
@@ -534,11 +582,12 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
     if (!sd || !co) return DEGPU_BAD_INPUT;
     degpu_status v = validate(pb, cfg, in, out);
     if (v != DEGPU_OK || in->n == 0) return v;
-    if (in->n_eval > 0 || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
     CrossSpec cr;
     if (!make_spec(sd, pb->dim, cr)) return DEGPU_BAD_INPUT;
+    if ((in->n_eval > 0 && cr.mode != 2) || in->dims || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_UNSUPPORTED;
     if (!co->count || (cr.max_points > 0 && (!co->t || !co->y))) return DEGPU_BAD_INPUT;
     ensure_registered();
+    const size_t ne = (in->n_eval > 0 && out->dense) ? (size_t)in->n_eval : 0;
     cudaStream_t s;
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return DEGPU_CUDA_ERROR;
     degpu_status st = DEGPU_OK;
@@ -562,8 +611,11 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
         din.rtol = (const double*)up(in->rtol, n * 8);
         din.atol = (const double*)up(in->atol, n * 8);
         din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
+        din.t_eval = ne > 0 ? (const double*)up(in->t_eval, ne * 8) : nullptr;
+        din.n_eval = (int32_t)ne;
         dout.y_final = sc.alloc<double>(d * n);
         dout.t_final = out->t_final ? sc.alloc<double>(n) : nullptr;
+        dout.dense = ne > 0 ? sc.alloc<double>(ne * d * n) : nullptr;
         dout.accepted = out->accepted ? sc.alloc<int64_t>(n) : nullptr;
         dout.rejected = out->rejected ? sc.alloc<int64_t>(n) : nullptr;
         dout.fevals = out->fevals ? sc.alloc<int64_t>(n) : nullptr;
@@ -572,10 +624,10 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
         dco.y = m > 0 ? sc.alloc<double>(m * d * n) : nullptr;
         dco.count = sc.alloc<int32_t>(n);
         if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final || !dco.count ||
-            (m > 0 && (!dco.t || !dco.y))) {
+            (m > 0 && (!dco.t || !dco.y)) || (ne > 0 && (!din.t_eval || !dout.dense))) {
             st = DEGPU_OOM;
         } else {
-            st = crossing_impl(pb, cfg, &din, cr, &dout, &dco, s);
+            st = crossing_impl(pb, cfg, &din, cr, &dout, &dco, ne > 0 ? in->t_eval : nullptr, s);
         }
         if (st == DEGPU_OK) {
             auto down = [&](void* dst, const void* src, size_t bytes) {
@@ -583,6 +635,7 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
             };
             down(out->y_final, dout.y_final, d * n * 8);
             down(out->t_final, dout.t_final, n * 8);
+            down(out->dense, dout.dense, ne * d * n * 8);
             down(out->accepted, dout.accepted, n * 8);
             down(out->rejected, dout.rejected, n * 8);
             down(out->fevals, dout.fevals, n * 8);
@@ -684,6 +737,18 @@ degpu_status degpu_solve_ensemble_hyperplane(const degpu_problem* pb, const degp
                                              const degpu_batch_in* in, const degpu_hyperplane* hp,
                                              degpu_batch_out* out, degpu_crossing_out* co, void* stream) {
     return crossing_entry(pb, cfg, in, hp, out, co, (cudaStream_t)stream);
+}
+
+degpu_status degpu_solve_ensemble_event(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                        const degpu_event* ev, degpu_batch_out* out, degpu_crossing_out* co,
+                                        void* stream) {
+    return crossing_entry(pb, cfg, in, ev, out, co, (cudaStream_t)stream);
+}
+
+degpu_status degpu_solve_ensemble_event_host(const degpu_problem* pb, const degpu_method_cfg* cfg,
+                                             const degpu_batch_in* in, const degpu_event* ev, degpu_batch_out* out,
+                                             degpu_crossing_out* co) {
+    return crossing_host_entry(pb, cfg, in, ev, out, co);
 }
 
 degpu_status degpu_solve_ensemble_hyperplane_host(const degpu_problem* pb, const degpu_method_cfg* cfg,

@@ -62,23 +62,117 @@ struct EnsArgs {
     int32_t n_params;
     const int32_t* family;           // per-instance family id (multi-family persistent kernel)
     unsigned long long* ticket;      // persistent queue head
-    // crossing detection (erk_cross_kernel): y[cross_comp] - cross_value changes sign
-    int32_t cross_comp, cross_dir, cross_max;  // dir: 0 both, 1 from below, -1 from above
+    // crossing and event detection (erk_cross_kernel), by cross_mode:
+    //  0 component crossing: y[cross_comp] - cross_value changes sign;
+    //  1 hyperplane crossing: sum_j (y[term_comp[j]] - term_a[j]) term_w[j], j < n_terms, with
+    //    term_w of unit length; cross_value = sum_j |term_a[j] term_w[j]| (the scale of the mixed
+    //    form's FP32 search tolerance);
+    //  2 event: g(t, y) = ((sum_j term_w[j] y[term_comp[j]]) + event_tw t) + cross_value (LINEAR)
+    //    or max_j |y[term_comp[j]]| + cross_value (MAX_ABS); event_terminate events end the solve.
+    int32_t cross_mode, cross_comp, cross_dir, cross_max;  // dir: 0 both, 1 from below, -1 from above
     double cross_value;
     double* cross_t;       // [cross_max][n]
     double* cross_y;       // [cross_max][dmax][n]
     int32_t* cross_count;  // [n]
-    // hyperplane crossings (cross_plane != 0): the offset is (pos - point) . normal with
-    // pos[j] = y[plane_comp[j]], the normal already of unit length; cross_value then holds
-    // sum |point_j normal_j|, the scale of the mixed form's FP32 search tolerance
-    int32_t cross_plane, plane_dim;
-    int32_t plane_comp[DEGPU_HYPERPLANE_MAX_DIM];
-    double plane_point[DEGPU_HYPERPLANE_MAX_DIM];
-    double plane_normal[DEGPU_HYPERPLANE_MAX_DIM];
+    int32_t n_terms, event_kind, event_terminate;
+    int32_t term_comp[DEGPU_HYPERPLANE_MAX_DIM];
+    double term_a[DEGPU_HYPERPLANE_MAX_DIM];
+    double term_w[DEGPU_HYPERPLANE_MAX_DIM];
+    double event_tw;
 };
 
 // f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
 __device__ __forceinline__ double rs_signum(double x) { return x != x ? x : copysign(1.0, x); }
+
+static_assert(DEGPU_EVENT_MAX_TERMS == DEGPU_HYPERPLANE_MAX_DIM, "event terms and plane components share arrays");
+
+// Brent–Dekker root search as the crate runs it for events (src/solout/event.rs:395-490): at most
+// 50 iterations of inverse quadratic interpolation or secant steps, taken when they stay well
+// inside the bracket, else bisection; converged when half the bracket is within
+// max(abs_tol, rel_tol |b|) or g vanishes. f(x, ok) evaluates g on the step's interpolant and
+// clears ok when x lies outside the step (the crate's interpolator then fails and no root is
+// returned).
+template <class F>
+__device__ bool brent_dekker(double a, double b, double fa, double fb, double abs_tol, double rel_tol, F f,
+                             double& root) {
+    if (fabs(fa) < fabs(fb)) {
+        double x = a;
+        a = b;
+        b = x;
+        x = fa;
+        fa = fb;
+        fb = x;
+    }
+    double c = a, fc = fa, d = b - a, e = d;
+    const double one = 1.0, two = 2.0, half = one / two, three = 3.0;
+    for (int it = 0; it < 50; ++it) {
+        if (fb == 0.0) {
+            root = b;
+            return true;
+        }
+        if (rs_signum(fa) == rs_signum(fb)) {
+            a = c;
+            fa = fc;
+            c = b;
+            fc = fb;
+            d = b - a;
+            e = d;
+        }
+        if (fabs(fa) < fabs(fb)) {
+            c = b;
+            b = a;
+            a = c;
+            fc = fb;
+            fb = fa;
+            fa = fc;
+        }
+        const double tol = fmax(abs_tol, rel_tol * fabs(b));
+        const double m = half * (a - b);
+        if (fabs(m) <= tol || fb == 0.0) {
+            root = b;
+            return true;
+        }
+        bool use_bis = true;
+        if (fabs(e) > tol && fabs(fa) > fabs(fb)) {
+            const double s = fb / fa;
+            double p, q;
+            if (a == c) {
+                p = two * m * s;
+                q = one - s;
+            } else {
+                const double q1 = fa / fc;
+                const double r = fb / fc;
+                p = s * (two * m * q1 * (q1 - r) - (b - a) * (r - one));
+                q = (q1 - one) * (r - one) * (s - one);
+            }
+            if (q > 0.0)
+                p = -p;
+            else
+                q = -q;
+            if (fabs(two * p) < (three * m * q - fabs(tol * q)) && p < fabs(e * half * q)) {
+                e = d;
+                d = p / q;
+                use_bis = false;
+            }
+        }
+        if (use_bis) {
+            d = m;
+            e = m;
+        }
+        a = b;
+        fa = fb;
+        if (fabs(d) > tol)
+            b = b + d;
+        else
+            b = b + (m > 0.0 ? tol : -tol);
+        bool ok = true;
+        fb = f(b, ok);
+        if (!ok) return false;
+        c = a;
+        fc = fa;
+    }
+    return false;
+}
 
 // Conversions between FP32 and FP64 done with integer operations on the bit patterns, for the
 // mixed form's per-step bookkeeping: a hardware conversion involving FP64 occupies the FP64 pipe,
@@ -150,9 +244,12 @@ struct Lane {
     int mod100;  // steps % 100, kept incrementally (the stiffness test runs every 100th attempt)
     int next_eval;
     int status;
-    double last_off;     // crossing detection: previous offset y[comp] - value
+    double last_off;     // crossing detection: previous offset (events: previous g)
     bool have_last_off;
-    int ncross;
+    int ncross;          // crossings / events recorded
+    int nevents;         // events counted (recorded or within 1e-14 of the last point)
+    double last_push;    // events: time of the last point of the crate's solution
+    bool have_push;
     bool last_rejected;
     bool done;
 
@@ -414,13 +511,13 @@ struct Lane {
     // (src/traits.rs:551-555).
     template <class Get>
     __device__ __forceinline__ double offset_by(Get get, const EnsArgs& a) const {
-        if (!a.cross_plane) return get(a.cross_comp) - a.cross_value;
+        if (a.cross_mode == 0) return get(a.cross_comp) - a.cross_value;
         double sum = 0.0;
 #pragma unroll
         for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
-            if (j < a.plane_dim) {
-                const double d = get(a.plane_comp[j]) - a.plane_point[j];
-                sum = sum + d * a.plane_normal[j];
+            if (j < a.n_terms) {
+                const double d = get(a.term_comp[j]) - a.term_a[j];
+                sum = sum + d * a.term_w[j];
             }
         return sum;
     }
@@ -435,7 +532,7 @@ struct Lane {
     __device__ bool find_crossing_newton(double t_lower, double t_upper, double off_lower, double off_upper,
                                          double& t_out, const EnsArgs& a) const {
         const double eps = 2.220446049250313e-16;
-        const bool plane = a.cross_plane != 0;
+        const bool plane = a.cross_mode == 1;
         double tt = t_lower - off_lower * (t_upper - t_lower) / (off_upper - off_lower);
         const double tolerance = eps * 100.0;
         double offset;
@@ -473,7 +570,7 @@ struct Lane {
     // to FP32 (100 units of FP32 rounding of the monitored quantity's scale: |threshold|, or
     // sum |point_j normal_j| for a hyperplane); the linear estimate when it does not converge.
     __device__ float find_crossing_sigma(float off_l, float off_u, const EnsArgs& a) const {
-        const bool plane = a.cross_plane != 0;
+        const bool plane = a.cross_mode == 1;
         const float thr = (float)a.cross_value;
         const float tol = 100.0f * 1.1920929e-7f * fmaxf(1.0f, fabsf(thr));
         const float lin = -off_l / (off_u - off_l);
@@ -484,9 +581,9 @@ struct Lane {
             float sum = 0.0f;
 #pragma unroll
             for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
-                if (j < a.plane_dim)
-                    sum += ((float)comp_value(v, a.plane_comp[j]) - (float)a.plane_point[j]) *
-                           (float)a.plane_normal[j];
+                if (j < a.n_terms)
+                    sum += ((float)comp_value(v, a.term_comp[j]) - (float)a.term_a[j]) *
+                           (float)a.term_w[j];
             return sum;
         };
         float sg = lin, offset;
@@ -520,7 +617,7 @@ struct Lane {
         if (have_last_off) {
             bool is_crossing = rs_signum(last_off) != rs_signum(offset);
             // hyperplane.rs: leaving or reaching the plane exactly also counts
-            if (a.cross_plane)
+            if (a.cross_mode == 1)
                 is_crossing = is_crossing || (last_off == 0.0 && offset != 0.0) || (last_off != 0.0 && offset == 0.0);
             if (is_crossing) {
                 bool record;
@@ -560,11 +657,101 @@ struct Lane {
         have_last_off = true;
     }
 
-    __device__ void solout(const EnsArgs& a) {
-        if constexpr (CROSS) {
-            crossing_solout(a);
+    // ----- event detection: EventWrappedSolout, src/solout/event.rs:299-521 -----------------------
+    // g(te, y) for the state given component by component (LINEAR folds from zero in term order;
+    // MAX_ABS folds f64::max from the first term)
+    template <class Get>
+    __device__ __forceinline__ double event_by(double te, Get get, const EnsArgs& a) const {
+        if (a.event_kind == DEGPU_EVENT_MAX_ABS) {
+            double m = fabs(get(a.term_comp[0]));
+#pragma unroll
+            for (int j = 1; j < DEGPU_EVENT_MAX_TERMS; ++j)
+                if (j < a.n_terms) m = fmax(m, fabs(get(a.term_comp[j])));
+            return m + a.cross_value;
+        }
+        double sum = 0.0;
+#pragma unroll
+        for (int j = 0; j < DEGPU_EVENT_MAX_TERMS; ++j)
+            if (j < a.n_terms) {
+                const double term = a.term_w[j] * get(a.term_comp[j]);
+                sum = sum + term;
+            }
+        const double tt = a.event_tw * te;
+        sum = sum + tt;
+        return sum + a.cross_value;
+    }
+    __device__ void event_solout(const EnsArgs& a) {
+        const double g_curr = event_by(
+            t,
+            [&](int c) {
+                double v = comp_value(y, c);
+                if constexpr (P::KAHAN) v = v - comp_value(yc, c);
+                return v;
+            },
+            a);
+        if (!have_last_off) {  // the first call (at t0) only records g
+            have_last_off = true;
+            last_off = g_curr;
             return;
         }
+        const double g_prev = last_off;
+        const bool sign_change = rs_signum(g_prev) != rs_signum(g_curr);
+        bool direction_ok;
+        if (a.cross_dir > 0)
+            direction_ok = sign_change && g_prev < 0.0 && g_curr >= 0.0;
+        else if (a.cross_dir < 0)
+            direction_ok = sign_change && g_prev > 0.0 && g_curr <= 0.0;
+        else
+            direction_ok = sign_change;
+        if (direction_ok) {
+            double lo = t_prev, hi = t, flo = g_prev, fhi = g_curr;
+            if ((dir > 0.0 && lo > hi) || (dir < 0.0 && lo < hi)) {
+                double x = lo;
+                lo = hi;
+                hi = x;
+                x = flo;
+                flo = fhi;
+                fhi = x;
+            }
+            // the crate's tolerances (event.rs:329-330); the mixed form's FP32 states resolve g to
+            // about 1e-7 of its scale, so it stops at 1e-6 relative instead
+            const double rel_tol = P::KAHAN ? 1e-6 : 1e-12;
+            double te;
+            if (flo * fhi <= 0.0 &&
+                brent_dekker(lo, hi, flo, fhi, 1e-14, rel_tol,
+                             [&](double x, bool& ok) {
+                                 if (x < t_prev || x > t) {  // Error::OutOfBounds
+                                     ok = false;
+                                     return 0.0;
+                                 }
+                                 S v[D];
+                                 interpolate(x, v, a);
+                                 return event_by(x, [&](int c) { return comp_value(v, c); }, a);
+                             },
+                             te)) {
+                if (!have_push || fabs(te - last_push) > 1e-14) {
+                    if (ncross < a.cross_max) {
+                        S v[D];
+                        interpolate(te, v, a);
+                        const int64_t n = a.n;
+                        a.cross_t[(int64_t)ncross * n + inst] = te;
+                        double* out = a.cross_y + ((int64_t)ncross * a.dmax) * n + inst;
+#pragma unroll
+                        for (int c = 0; c < D; ++c) out[(int64_t)c * n] = (double)v[c];
+                    }
+                    ncross += 1;
+                    have_push = true;
+                    last_push = te;
+                }
+                nevents += 1;
+                if (a.event_terminate > 0 && nevents >= a.event_terminate) status = DEGPU_INTERRUPTED;
+            }
+        }
+        last_off = g_curr;
+    }
+
+    // TEvalSolout (src/solout/t_eval.rs:82-137) at the requested times within the step
+    __device__ void teval_solout(const EnsArgs& a) {
         if constexpr (DENSE) {
             int idx = next_eval;
             while (idx < a.n_eval) {
@@ -579,6 +766,10 @@ struct Lane {
                         interpolate(te, v, a);
                         write_dense(idx, v, a);
                     }
+                    if constexpr (CROSS) {
+                        have_push = true;
+                        last_push = te;
+                    }
                     idx += 1;
                 } else {
                     if ((dir > 0.0 && te > t) || (dir < 0.0 && te < t)) break;
@@ -587,6 +778,26 @@ struct Lane {
             }
             next_eval = idx;
         }
+    }
+
+    __device__ void solout(const EnsArgs& a) {
+        if constexpr (CROSS) {
+            if (a.cross_mode != 2) {
+                crossing_solout(a);
+                return;
+            }
+            // EventWrappedSolout: the base output first (the output times, else DefaultSolout,
+            // which pushes every step's end), then the event
+            if (a.n_eval > 0) {
+                teval_solout(a);
+            } else {
+                have_push = true;
+                last_push = t;
+            }
+            event_solout(a);
+            return;
+        }
+        teval_solout(a);
     }
 
     // ----- start one instance ------------------------------------------------------------------
@@ -627,6 +838,9 @@ struct Lane {
             have_last_off = false;
             last_off = 0.0;
             ncross = 0;
+            nevents = 0;
+            last_push = 0.0;
+            have_push = false;
         }
         last_rejected = false;
         done = false;
@@ -1309,6 +1523,12 @@ struct Lane {
         }
         acc += 1;
         solout(a);
+        if constexpr (CROSS) {
+            if (status == DEGPU_INTERRUPTED) {  // ControlFlag::Terminate (solve_ivp.rs:254-259)
+                done = true;
+                return;
+            }
+        }
         if constexpr (MIX) {
             if (last_step) {
                 done = true;  // t == tf

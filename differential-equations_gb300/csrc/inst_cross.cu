@@ -1,4 +1,4 @@
-// inst_cross.cu — crossing-detection kernels, FP64 fast and mixed arithmetic.
+// inst_cross.cu — crossing- and event-detection kernels, FP64 fast and mixed arithmetic.
 #include "registry.cuh"
 
 namespace degpu {
@@ -10,12 +10,16 @@ void register_cross_fast_mixed() {
     register_cross_all_methods<RhsHarmonic, PrecFast>();
     register_cross_all_methods<RhsBrusselator, PrecFast>();
     register_cross_all_methods<RhsCr3bp, PrecFast>();
+    register_cross_all_methods<RhsLogistic, PrecFast>();
+    register_cross_all_methods<RhsExpGrowth, PrecFast>();
     register_cross_all_methods<RhsVanDerPol, PrecMixed>();
     register_cross_all_methods<RhsPendulum, PrecMixed>();
     register_cross_all_methods<RhsLorenz, PrecMixed>();
     register_cross_all_methods<RhsHarmonic, PrecMixed>();
     register_cross_all_methods<RhsBrusselator, PrecMixed>();
     register_cross_all_methods<RhsCr3bp, PrecMixed>();
+    register_cross_all_methods<RhsLogistic, PrecMixed>();
+    register_cross_all_methods<RhsExpGrowth, PrecMixed>();
 }
 
 }  // namespace degpu

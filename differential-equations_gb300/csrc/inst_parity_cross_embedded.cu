@@ -12,6 +12,8 @@ void register_cross_embedded_parity() {
     register_cross_embedded_methods<RhsHarmonic, PrecParity>();
     register_cross_embedded_methods<RhsBrusselator, PrecParity>();
     register_cross_embedded_methods<RhsCr3bp, PrecParity>();
+    register_cross_embedded_methods<RhsLogistic, PrecParity>();
+    register_cross_embedded_methods<RhsExpGrowth, PrecParity>();
 }
 
 }  // namespace degpu

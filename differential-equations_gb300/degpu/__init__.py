@@ -20,10 +20,10 @@ from . import abi
 
 __all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
            "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing", "solve_ensemble_hyperplane",
-           "write_csv", "rust_debug_f64"]
+           "solve_ensemble_event", "write_csv", "rust_debug_f64"]
 
 STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
-                abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness"}
+                abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness", abi.INTERRUPTED: "Interrupted"}
 
 
 class DegpuError(RuntimeError):
@@ -167,7 +167,7 @@ class EnsembleResult:
 
 
 def _solve_crossing_host(fn, name, spec, rhs_id, dim, t0, tf, y0, params, rtol, atol, method, max_points, family,
-                         n_params):
+                         n_params, t_eval=None):
     lib = abi.load()
     y0 = np.asarray(y0, dtype=np.float64)
     n = y0.shape[1]
@@ -178,13 +178,17 @@ def _solve_crossing_host(fn, name, spec, rhs_id, dim, t0, tf, y0, params, rtol, 
         and np.size(params) else np.zeros((1, n))
     np_ = n_params if n_params is not None else params.shape[0]
     fam_a = None if family is None else np.ascontiguousarray(family, dtype=np.int32)
-    out = dict(y_final=np.empty((dim, n)), t_final=np.empty(n), dense=None, accepted=np.empty(n, np.int64),
-               rejected=np.empty(n, np.int64), fevals=np.empty(n, np.int64), status=np.empty(n, np.int32))
+    te = None if t_eval is None or len(t_eval) == 0 else _f64(np.asarray(t_eval, dtype=np.float64))
+    ne = 0 if te is None else len(te)
+    out = dict(y_final=np.empty((dim, n)), t_final=np.empty(n), dense=np.empty((ne, dim, n)) if ne else None,
+               accepted=np.empty(n, np.int64), rejected=np.empty(n, np.int64), fevals=np.empty(n, np.int64),
+               status=np.empty(n, np.int32))
     ct, cy, cc = np.empty((max_points, n)), np.empty((max_points, dim, n)), np.empty(n, np.int32)
     prob = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=np_)
     bi = abi.BatchIn(n=n, t0=abi.ptr(t0), tf=abi.ptr(tf), y0=abi.ptr(y0), params=abi.ptr(params),
-                     rtol=abi.ptr(rtol), atol=abi.ptr(atol), family=abi.ptr(fam_a, C.c_int32), n_eval=0)
-    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
+                     rtol=abi.ptr(rtol), atol=abi.ptr(atol), family=abi.ptr(fam_a, C.c_int32), n_eval=ne,
+                     t_eval=abi.ptr(te))
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]), dense=abi.ptr(out["dense"]),
                       accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
                       fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
     co = abi.CrossingOut(t=abi.ptr(ct), y=abi.ptr(cy), count=abi.ptr(cc, C.c_int32))
@@ -215,6 +219,17 @@ def solve_ensemble_hyperplane(rhs_id: int, dim: int, t0, tf, y0, params, rtol, a
     hp = abi.make_hyperplane(components, point, normal, direction, max_points)
     return _solve_crossing_host("degpu_solve_ensemble_hyperplane_host", "hyperplane", hp, rhs_id, dim, t0, tf, y0,
                                 params, rtol, atol, method, max_points, family, n_params)
+
+
+def solve_ensemble_event(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
+                         event: "abi.Event", t_eval=None, family=None, n_params: Optional[int] = None):
+    """Solve n IVPs (host arrays) with event detection (degpu_solve_ensemble_event_host): the
+    crate's `.event(&event)` wrapped around the output times (`t_eval`) or around the default
+    per-step output.  Returns the EnsembleResult (dense = the output times) and the event points
+    (t [max_points, n], y [max_points, dim, n], count [n]); a terminal event leaves the
+    instance's status INTERRUPTED."""
+    return _solve_crossing_host("degpu_solve_ensemble_event_host", "event", event, rhs_id, dim, t0, tf, y0, params,
+                                rtol, atol, method, event.max_points, family, n_params, t_eval)
 
 
 def set_mixed_min_rtol(method: int, min_rtol: float) -> None:
@@ -327,6 +342,7 @@ class IVP:
         self._method: Optional[ExplicitRungeKutta] = None
         self._t_eval = None
         self._crossing = None
+        self._event = None
 
     @classmethod
     def ode(cls, system: System, t0, tf, y0):
@@ -358,9 +374,34 @@ class IVP:
         self._t_eval = None
         return self
 
+    def event(self, ev: "abi.Event"):
+        """The crate's IVP::event (src/ivp.rs:661-679): wraps the current output (t_eval, or the
+        final point) with event detection (abi.make_event).  The solution holds the output points
+        and the recorded events in time order; a terminal event ends it with status
+        "Interrupted"."""
+        self._event = ev
+        self._crossing = None
+        return self
+
     def solve(self) -> Solution:
         m = self._method or ExplicitRungeKutta.dopri5()
         d = len(self.y0)
+        if self._event is not None:
+            r, (ct, cy, cc) = solve_ensemble_event(
+                self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),
+                np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m._rtol], [m._atol], m,
+                self._event, t_eval=self._t_eval)
+            st = STATUS_NAMES.get(int(r.status[0]), str(int(r.status[0])))
+            k = min(int(cc[0]), self._event.max_points)
+            pts = [(float(ct[j, 0]), cy[j, :, 0].copy()) for j in range(k)]
+            if self._t_eval is not None:
+                pts += [(float(self._t_eval[i]), r.dense[i, :, 0].copy()) for i in range(len(self._t_eval))
+                        if not np.isnan(r.dense[i, 0, 0])]
+            else:
+                pts.append((float(r.t_final[0]), r.y_final[:, 0].copy()))
+            pts.sort(key=lambda p: p[0], reverse=self.tf < self.t0)
+            return Solution([p[0] for p in pts], [p[1] for p in pts], st, int(r.accepted[0]), int(r.rejected[0]),
+                            int(r.fevals[0]))
         if self._crossing is not None:
             kind, spec, direction, cap = self._crossing
             args = (self.system.rhs_id, d, [self.t0], [self.tf], self.y0.reshape(d, 1),

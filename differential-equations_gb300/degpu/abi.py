@@ -24,7 +24,7 @@ KERNEL_AUTO, KERNEL_THREAD, KERNEL_WARP, KERNEL_PERSISTENT = 0, 1, 2, 3
 # degpu_dense_mode
 DENSE_REFERENCE, DENSE_HAIRER = 0, 1
 # degpu_instance_status
-COMPLETE, ERR_BAD_INPUT, ERR_MAX_STEPS, ERR_STEP_SIZE, ERR_STIFFNESS = range(5)
+COMPLETE, ERR_BAD_INPUT, ERR_MAX_STEPS, ERR_STEP_SIZE, ERR_STIFFNESS, INTERRUPTED = range(6)
 # degpu_rhs_id
 RHS = dict(
     LORENZ=1, VAN_DER_POL=2, PENDULUM=3, FPU_BETA=4, EXP_GROWTH=5, LINEAR=6, HARMONIC=7,
@@ -82,6 +82,32 @@ class Hyperplane(C.Structure):
                 ("point", C.c_double * HYPERPLANE_MAX_DIM), ("normal", C.c_double * HYPERPLANE_MAX_DIM)]
 
 
+EVENT_MAX_TERMS = 8
+EVENT_LINEAR, EVENT_MAX_ABS = 0, 1
+
+
+class Event(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("direction", C.c_int32), ("terminate", C.c_int32),
+                ("max_points", C.c_int32), ("n_terms", C.c_int32), ("reserved", C.c_int32),
+                ("components", C.c_int32 * EVENT_MAX_TERMS), ("weights", C.c_double * EVENT_MAX_TERMS),
+                ("t_weight", C.c_double), ("offset", C.c_double)]
+
+
+def make_event(kind=EVENT_LINEAR, components=(), weights=None, t_weight=0.0, offset=0.0, direction=CROSS_BOTH,
+               terminate=0, max_points=16) -> Event:
+    """degpu_event: LINEAR g = ((sum_j weights[j] y[components[j]]) + t_weight t) + offset, or
+    MAX_ABS g = max_j |y[components[j]]| + offset; `terminate` events stop the solve (0: never)."""
+    m = len(components)
+    if m > EVENT_MAX_TERMS or (weights is not None and len(weights) != m):
+        raise ValueError("event: at most 8 terms, one weight per term")
+    ev = Event(kind=kind, direction=direction, terminate=terminate, max_points=max_points, n_terms=m,
+               t_weight=float(t_weight), offset=float(offset))
+    for j in range(m):
+        ev.components[j] = int(components[j])
+        ev.weights[j] = 1.0 if weights is None else float(weights[j])
+    return ev
+
+
 def make_hyperplane(components, point, normal, direction=CROSS_BOTH, max_points=16) -> Hyperplane:
     """degpu_hyperplane from sequences: pos[j] = y[components[j]], plane through `point` with
     `normal` (scaled to unit length by the library)."""
@@ -137,6 +163,11 @@ SIGNATURES = {
     "degpu_solve_ensemble_hyperplane_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg),
                                                        C.POINTER(BatchIn), C.POINTER(Hyperplane),
                                                        C.POINTER(BatchOut), C.POINTER(CrossingOut)]),
+    "degpu_solve_ensemble_event": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                             C.POINTER(Event), C.POINTER(BatchOut), C.POINTER(CrossingOut),
+                                             C.c_void_p]),
+    "degpu_solve_ensemble_event_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
+                                                  C.POINTER(Event), C.POINTER(BatchOut), C.POINTER(CrossingOut)]),
     "degpu_eval_rhs": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP,
                                  C.c_void_p]),
     "degpu_register_rhs_nvrtc": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, I32P, C.c_char_p,

@@ -93,7 +93,9 @@ typedef enum {
     DEGPU_ERR_BAD_INPUT = 1,   /* Error::BadInput  (src/utils.rs:60-157, src/ode/solve_ivp.rs:139-147) */
     DEGPU_ERR_MAX_STEPS = 2,   /* Error::MaxSteps  (dormandprince/ordinary.rs:82-92, fixed/ordinary.rs:64-75) */
     DEGPU_ERR_STEP_SIZE = 3,   /* Error::StepSize  (dormandprince/ordinary.rs:70-80)                   */
-    DEGPU_ERR_STIFFNESS = 4    /* Error::Stiffness (dormandprince/ordinary.rs:176-186)                 */
+    DEGPU_ERR_STIFFNESS = 4,   /* Error::Stiffness (dormandprince/ordinary.rs:176-186)                 */
+    DEGPU_INTERRUPTED = 5      /* Ok(Solution) with Status::Interrupted: a terminal event stopped the
+                                  solve (src/ode/solve_ivp.rs:254-259)                              */
 } degpu_instance_status;
 
 /* Built-in right-hand sides (CUDA __device__ twins of `ODE::diff`, src/ode/ode.rs:20-44).
@@ -286,6 +288,48 @@ degpu_status degpu_solve_ensemble_hyperplane(const degpu_problem* problem, const
 degpu_status degpu_solve_ensemble_hyperplane_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
                                                   const degpu_batch_in* in, const degpu_hyperplane* plane,
                                                   degpu_batch_out* out, degpu_crossing_out* crossing_out);
+
+/* Event detection: the crate's `.event(&event)` (EventWrappedSolout, src/solout/event.rs:299-521;
+ * IVP::event, src/ivp.rs:661-679). After every accepted step the event function g(t, y) at the
+ * step's end is compared in sign with its previous value (the first value is taken at t0). On a
+ * change of sign in `direction`, the event time is located by the crate's Brent–Dekker search on
+ * the step's interpolant (at most 50 iterations, tolerance max(1e-14, 1e-12 |t|)). The event is
+ * recorded unless it lies within 1e-14 of the last point of the crate's solution (the step's end
+ * without output times, else the last output time or event), counted either way, and after
+ * `terminate` counted events the instance stops with DEGPU_INTERRUPTED. The event functions are
+ * the forms of the crate's examples and tests:
+ *   DEGPU_EVENT_LINEAR   g = ((sum_j weights[j] y[components[j]]) + t_weight t) + offset
+ *                        (e.g. `y[0] - 0.9 * m`, `t - 10.0`);
+ *   DEGPU_EVENT_MAX_ABS  g = max_j |y[components[j]]| + offset
+ *                        (e.g. `theta.abs().max(omega.abs()) - 0.01`). */
+#define DEGPU_EVENT_MAX_TERMS 8
+typedef enum { DEGPU_EVENT_LINEAR = 0, DEGPU_EVENT_MAX_ABS = 1 } degpu_event_kind;
+
+typedef struct {
+    int32_t kind;        /* degpu_event_kind                                                    */
+    int32_t direction;   /* degpu_crossing_direction (EventConfig::direction)                   */
+    int32_t terminate;   /* EventConfig::terminate: stop after this many events; 0 = never      */
+    int32_t max_points;  /* capacity per instance of the event outputs (>= 0)                   */
+    int32_t n_terms;     /* terms used: 0..8 for LINEAR, 1..8 for MAX_ABS                        */
+    int32_t reserved;
+    int32_t components[DEGPU_EVENT_MAX_TERMS]; /* state index of each term                      */
+    double weights[DEGPU_EVENT_MAX_TERMS];     /* LINEAR: weight of each term                   */
+    double t_weight;     /* LINEAR: weight of t                                                 */
+    double offset;
+} degpu_event;
+
+/* degpu_solve_ensemble with event detection, device pointers, stream-ordered. Output times
+ * (in->n_eval > 0) are the base output as in the crate (`.t_eval(..).event(..)`); the event
+ * points go to event_out (laid out as degpu_crossing_out). Same families, methods and
+ * precisions as degpu_solve_ensemble_crossing. */
+degpu_status degpu_solve_ensemble_event(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                        const degpu_batch_in* in, const degpu_event* event, degpu_batch_out* out,
+                                        degpu_crossing_out* event_out, void* stream);
+
+/* Same with HOST pointers, synchronous. */
+degpu_status degpu_solve_ensemble_event_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                             const degpu_batch_in* in, const degpu_event* event,
+                                             degpu_batch_out* out, degpu_crossing_out* event_out);
 
 /* One evaluation of a built-in right-hand side for every instance (`ODE::diff`,
  * src/ode/ode.rs:20-44), device pointers: dydt[c*n+i] = f_i(t[i], y_i). */

@@ -76,6 +76,7 @@ struct Solution {
     std::size_t evals = 0;      // Evals.function
     std::size_t accepted = 0;   // Steps.accepted
     std::size_t rejected = 0;   // Steps.rejected
+    bool interrupted = false;   // Status::Interrupted (a terminal event ended the solve)
 
     // Solution::to_csv (src/solution.rs:190-226): header t,y0,..,yN-1 and one row per point, numbers
     // in Rust's Debug format; the parent directory is created when missing.  False on an I/O error.
@@ -218,7 +219,15 @@ class IVP {
     IVP& method(const ExplicitRungeKutta& m) { m_ = m; return *this; }
     IVP& t_eval(std::vector<double> pts) {
         te_ = std::move(pts);
-        cross_ = 0;
+        if (cross_ != 3) cross_ = 0;
+        return *this;
+    }
+    // src/ivp.rs:661-679: wraps the current output (t_eval, else the final point) with event
+    // detection; the solution holds the output points and the recorded events in time order, and a
+    // terminal event ends it with Status::Interrupted (Solution::interrupted)
+    IVP& event(const degpu_event& ev) {
+        cross_ = 3;
+        ev_ = ev;
         return *this;
     }
     // src/ivp.rs:682-693: the solution holds the points where y[component] crosses threshold
@@ -305,10 +314,10 @@ class IVP {
         }
     }
 
-    // One instance through degpu_solve_ensemble_crossing_host / _hyperplane_host.
+    // One instance through degpu_solve_ensemble_crossing_host / _hyperplane_host / _event_host.
     Result<Solution> solve_crossing() const {
         const int32_t d = (int32_t)y0_.size();
-        const int32_t cap = cross_ == 1 ? cr_.max_points : hp_.max_points;
+        const int32_t cap = cross_ == 1 ? cr_.max_points : cross_ == 2 ? hp_.max_points : ev_.max_points;
         const size_t m = cap > 0 ? (size_t)cap : 0;
         std::vector<double> yf(d), tf(1), ct(m), cy(m * d);
         std::vector<int64_t> acc(1), rej(1), fev(1);
@@ -323,24 +332,52 @@ class IVP {
         in.params = sys_.params.empty() ? nullptr : sys_.params.data();
         in.rtol = &rtol;
         in.atol = &atol;
-        degpu_batch_out out{yf.data(), tf.data(), nullptr, acc.data(), rej.data(), fev.data(), st.data()};
+        const bool with_te = cross_ == 3 && !te_.empty();
+        std::vector<double> dense(with_te ? te_.size() * (size_t)d : 0);
+        if (with_te) {
+            in.t_eval = te_.data();
+            in.n_eval = (int32_t)te_.size();
+        }
+        degpu_batch_out out{yf.data(), tf.data(), with_te ? dense.data() : nullptr, acc.data(), rej.data(), fev.data(),
+                            st.data()};
         degpu_crossing_out co{m ? ct.data() : nullptr, m ? cy.data() : nullptr, cc.data()};
-        const degpu_status rc = cross_ == 1 ? degpu_solve_ensemble_crossing_host(&pb, &m_.cfg(), &in, &cr_, &out, &co)
-                                            : degpu_solve_ensemble_hyperplane_host(&pb, &m_.cfg(), &in, &hp_, &out, &co);
+        degpu_status rc;
+        if (cross_ == 1)
+            rc = degpu_solve_ensemble_crossing_host(&pb, &m_.cfg(), &in, &cr_, &out, &co);
+        else if (cross_ == 2)
+            rc = degpu_solve_ensemble_hyperplane_host(&pb, &m_.cfg(), &in, &hp_, &out, &co);
+        else
+            rc = degpu_solve_ensemble_event_host(&pb, &m_.cfg(), &in, &ev_, &out, &co);
         if (rc == DEGPU_BAD_INPUT) return Result<Solution>::err(Error{ErrorKind::BadInput, "Invalid input: crossing"});
         if (rc != DEGPU_OK)
             return Result<Solution>::err(Error{ErrorKind::Device, std::string("crossing solve: ") + degpu_status_string(rc)});
-        if (st[0] != DEGPU_COMPLETE) return status_error(st[0], tf[0], yf);
+        if (st[0] != DEGPU_COMPLETE && st[0] != DEGPU_INTERRUPTED) return status_error(st[0], tf[0], yf);
         Solution s;
         s.evals = (size_t)fev[0];
         s.accepted = (size_t)acc[0];
         s.rejected = (size_t)rej[0];
+        s.interrupted = st[0] == DEGPU_INTERRUPTED;
+        std::vector<std::pair<double, std::vector<double>>> pts;
         const size_t k = std::min(m, (size_t)cc[0]);
         for (size_t j = 0; j < k; ++j) {
-            s.t.push_back(ct[j]);
             std::vector<double> yj(d);
             for (int32_t c = 0; c < d; ++c) yj[c] = cy[j * d + c];
-            s.y.push_back(std::move(yj));
+            pts.emplace_back(ct[j], std::move(yj));
+        }
+        if (cross_ == 3) {  // the base output: output times reached, else the final point
+            if (with_te) {
+                for (size_t e = 0; e < te_.size(); ++e)
+                    if (!std::isnan(dense[e * d])) pts.emplace_back(te_[e], std::vector<double>(dense.begin() + e * d, dense.begin() + (e + 1) * d));
+            } else {
+                pts.emplace_back(tf[0], yf);
+            }
+            const bool fwd = tf_ >= t0_;
+            std::stable_sort(pts.begin(), pts.end(),
+                             [&](const auto& x, const auto& y) { return fwd ? x.first < y.first : x.first > y.first; });
+        }
+        for (auto& p : pts) {
+            s.t.push_back(p.first);
+            s.y.push_back(std::move(p.second));
         }
         return Result<Solution>::ok_value(std::move(s));
     }
@@ -349,9 +386,10 @@ class IVP {
     double t0_ = 0, tf_ = 0;
     std::vector<double> y0_, te_;
     ExplicitRungeKutta m_ = ExplicitRungeKutta::dopri5();
-    int cross_ = 0;  // 0 none, 1 component crossing, 2 hyperplane crossing
+    int cross_ = 0;  // 0 none, 1 component crossing, 2 hyperplane crossing, 3 event
     degpu_crossing cr_{};
     degpu_hyperplane hp_{};
+    degpu_event ev_{};
 };
 
 }  // namespace degpu

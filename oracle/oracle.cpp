@@ -86,7 +86,8 @@ void oracle_libm_pow_batch(const double* x, const double* y, double* out, int64_
 // Solve one instance i of the batch into the outputs.
 static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                            degpu_batch_out* out, int64_t i, const Math& math, const CrossingSolout* proto = nullptr,
-                           int64_t max_points = 0, degpu_crossing_out* co = nullptr) {
+                           int64_t max_points = 0, degpu_crossing_out* co = nullptr,
+                           const EventSolout* eproto = nullptr) {
     const int64_t n = in->n;
     int rhs = in->family ? in->family[i] : pb->rhs_id;
     // per-instance dimension: given explicitly (ragged batches) or the family's own
@@ -117,16 +118,20 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
     }
     CrossingSolout cs;
     if (proto) cs = *proto;
+    EventSolout es;
+    if (eproto) es = *eproto;
     Result r = solve_one(cfg->method, ode, in->t0[i], in->tf[i], y0, set, math, tep,
-                         cfg->dense_mode == DEGPU_DENSE_HAIRER, proto ? &cs : nullptr);
-    if (proto && co) {
+                         cfg->dense_mode == DEGPU_DENSE_HAIRER, proto ? &cs : nullptr, eproto ? &es : nullptr);
+    if ((proto || eproto) && co) {
+        const std::vector<double>& pt = proto ? cs.t : es.t;
+        const std::vector<State>& py = proto ? cs.y : es.y;
         const int64_t m = max_points;
-        co->count[i] = (int32_t)cs.t.size();
+        co->count[i] = (int32_t)pt.size();
         for (int64_t k = 0; k < m; ++k) {
-            const bool have = (size_t)k < cs.t.size();
-            co->t[k * n + i] = have ? cs.t[k] : NAN;
+            const bool have = (size_t)k < pt.size();
+            co->t[k * n + i] = have ? pt[k] : NAN;
             for (int c = 0; c < dmax; ++c)
-                co->y[(k * dmax + c) * n + i] = (have && c < d) ? cs.y[k][c] : NAN;
+                co->y[(k * dmax + c) * n + i] = (have && c < d) ? py[k][c] : NAN;
         }
     }
     for (int c = 0; c < d; ++c) out->y_final[(int64_t)c * n + i] = r.y_final.size() == (size_t)d ? r.y_final[c] : NAN;
@@ -182,6 +187,35 @@ int oracle_solve_ensemble_hyperplane(const degpu_problem* pb, const degpu_method
                     std::vector<double>(hp->normal, hp->normal + hp->dim));
     for_instances(in->n, threads,
                   [&](int64_t i) { solve_instance(pb, cfg, in, out, i, math, &proto, hp->max_points, co); });
+    return 0;
+}
+
+// Event detection (EventWrappedSolout over the output times, or over DefaultSolout when there are
+// none) for every instance; event points laid out as degpu_solve_ensemble_event's.  Returns 0 on
+// success, 1 on bad input.
+int oracle_solve_ensemble_event(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                const degpu_event* ev, degpu_batch_out* out, degpu_crossing_out* co, int threads,
+                                int math_mode) {
+    if (!pb || !cfg || !in || !out || !ev || !co || in->n < 0 || !out->y_final) return 1;
+    if (ev->kind != DEGPU_EVENT_LINEAR && ev->kind != DEGPU_EVENT_MAX_ABS) return 1;
+    if (ev->n_terms < (ev->kind == DEGPU_EVENT_MAX_ABS ? 1 : 0) || ev->n_terms > DEGPU_EVENT_MAX_TERMS) return 1;
+    if (ev->max_points < 0 || ev->terminate < 0 || ev->direction < -1 || ev->direction > 1) return 1;
+    EventSolout proto;
+    proto.kind = ev->kind;
+    proto.direction = ev->direction;
+    proto.terminate = ev->terminate;
+    proto.t_weight = ev->t_weight;
+    proto.offset = ev->offset;
+    for (int j = 0; j < ev->n_terms; ++j) {
+        if (ev->components[j] < 0 || ev->components[j] >= pb->dim) return 1;
+        proto.comp.push_back(ev->components[j]);
+        proto.w.push_back(ev->weights[j]);
+    }
+    Math math;
+    math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
+    for_instances(in->n, threads, [&](int64_t i) {
+        solve_instance(pb, cfg, in, out, i, math, nullptr, ev->max_points, co, &proto);
+    });
     return 0;
 }
 

@@ -14,6 +14,7 @@
 //   Adaptive ERK (RKF45, Cash-Karp)  src/methods/erk/adaptive/ordinary.rs:16-290
 //   TEvalSolout ..................... src/solout/t_eval.rs:82-171
 //   CrossingSolout .................. src/solout/crossing.rs:200-330, src/solout/hyperplane.rs
+//   EventSolout ..................... src/solout/event.rs:67-521
 //   tableaus ........................ src/tableau/runge_kutta.rs:39-70, src/tableau/dorman_prince.rs:37-381
 //
 // Compile with -ffp-contract=off: Rust never contracts a*b+c into an FMA, so neither may this.
@@ -617,7 +618,19 @@ struct Interpolator {
     virtual State interpolate(double t_interp) = 0;
 };
 
+// The time of the last point pushed to the solution by any solout (`solution.t.last()`), which
+// EventWrappedSolout compares with a new event time before it pushes it.
+struct PushLog {
+    bool any = false;
+    double last = 0.0;
+    void push(double t) {
+        any = true;
+        last = t;
+    }
+};
+
 struct TEvalSolout {
+    PushLog* log = nullptr;         // optional: records the pushed times
     std::vector<double> t_evals;    // sorted by direction
     std::vector<int> order;         // t_evals[k] came from caller index order[k]
     size_t next_eval_idx = 0;
@@ -664,6 +677,7 @@ struct TEvalSolout {
                     (*out)[order[idx]] = y_curr;
                 else
                     (*out)[order[idx]] = interp.interpolate(t_eval);
+                if (log) log->push(t_eval);
                 idx += 1;
             } else {
                 if ((integration_direction > 0.0 && t_eval > t_curr) ||
@@ -793,6 +807,174 @@ struct CrossingSolout {
         if (std::fabs(off) < tolerance * 10.0) {
             t_out = t;
             return true;
+        }
+        return false;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Event detection: EventWrappedSolout (src/solout/event.rs:299-521; EventSolout, event.rs:67-297,
+// is the same detector without a base). After the base output of each call, the event function
+// g(t, y) at the step's end is compared in sign with its value at the previous call (the first
+// call, at t0, only records it). A change of sign in the requested direction is located by the
+// crate's Brent–Dekker search on the step's interpolant; a located event is pushed unless it lies
+// within abs_tol of the last point already in the solution, is counted either way, and ends the
+// solve (Status::Interrupted) once `terminate` events were counted. The event functions are the
+// two forms of the crate's examples:
+//   LINEAR  g = ((sum_j w_j y[c_j]) + w_t t) + offset, folded from zero in term order
+//           (`y[0] - 0.9 * m`, `t - 10.0`, `y.infected - 1.0`);
+//   MAX_ABS g = max_j |y[c_j]| + offset, f64::max folded from the first term
+//           (`theta.abs().max(omega.abs()) - 0.01`).
+// ---------------------------------------------------------------------------------------------
+struct EventSolout {
+    int kind = DEGPU_EVENT_LINEAR;
+    std::vector<int> comp;
+    std::vector<double> w;
+    double t_weight = 0.0, offset = 0.0;
+    int direction = 0;   // CrossingDirection
+    int terminate = 0;   // EventConfig::terminate; 0 = None
+    double integration_direction = 1.0;
+    double rel_tol = 1e-12, abs_tol = 1e-14;  // event.rs:329-330
+    bool have_last = false;
+    double last_g = 0.0;
+    int64_t event_count = 0;
+    PushLog* log = nullptr;
+    std::vector<double> t;  // pushed event points
+    std::vector<State> y;
+
+    double g(double te, const State& v) const {
+        if (kind == DEGPU_EVENT_MAX_ABS) {
+            double m = std::fabs(v[comp[0]]);
+            for (size_t j = 1; j < comp.size(); ++j) m = std::fmax(m, std::fabs(v[comp[j]]));  // f64::max
+            return m + offset;
+        }
+        double sum = 0.0;
+        for (size_t j = 0; j < comp.size(); ++j) {
+            const double term = w[j] * v[comp[j]];
+            sum = sum + term;
+        }
+        const double tt = t_weight * te;
+        sum = sum + tt;
+        return sum + offset;
+    }
+
+    // Returns true when the solve is to stop (ControlFlag::Terminate).
+    bool solout(double t_curr, double t_prev, const State& y_curr, Interpolator& interp) {
+        const double g_curr = g(t_curr, y_curr);
+        if (!have_last) {  // event.rs:335-350: the first call only records g
+            have_last = true;
+            last_g = g_curr;
+            return false;
+        }
+        const double g_prev = last_g;
+        const bool sign_change = rust_signum(g_prev) != rust_signum(g_curr);
+        bool direction_ok;
+        if (direction > 0)
+            direction_ok = sign_change && g_prev < 0.0 && g_curr >= 0.0;
+        else if (direction < 0)
+            direction_ok = sign_change && g_prev > 0.0 && g_curr <= 0.0;
+        else
+            direction_ok = sign_change;
+        if (direction_ok) {
+            double a = t_prev, b = t_curr, fa = g_prev, fb = g_curr;
+            if ((integration_direction > 0.0 && a > b) || (integration_direction < 0.0 && a < b)) {
+                std::swap(a, b);
+                std::swap(fa, fb);
+            }
+            double t_event;
+            if (fa * fb <= 0.0 && brent_dekker(a, b, fa, fb, t_prev, t_curr, interp, t_event)) {
+                const State y_event = interp.interpolate(t_event);
+                const bool push_point = !log->any || std::fabs(t_event - log->last) > abs_tol;
+                if (push_point) {
+                    t.push_back(t_event);
+                    y.push_back(y_event);
+                    log->push(t_event);
+                }
+                event_count += 1;
+                if (terminate > 0 && event_count >= terminate) {
+                    last_g = g_curr;
+                    return true;
+                }
+            }
+        }
+        last_g = g_curr;
+        return false;
+    }
+
+    // event.rs:395-490. The crate's interpolator refuses times outside [t_prev, t_curr]
+    // (OutOfBounds), which ends the search without a root.
+    bool brent_dekker(double a, double b, double fa, double fb, double t_lo, double t_hi, Interpolator& interp,
+                      double& root) const {
+        if (std::fabs(fa) < std::fabs(fb)) {
+            std::swap(a, b);
+            std::swap(fa, fb);
+        }
+        double c = a, fc = fa, d = b - a, e = d;
+        const double one = 1.0, two = 2.0, half = one / two, three = 3.0;
+        for (int it = 0; it < 50; ++it) {
+            if (fb == 0.0) {
+                root = b;
+                return true;
+            }
+            if (rust_signum(fa) == rust_signum(fb)) {
+                a = c;
+                fa = fc;
+                c = b;
+                fc = fb;
+                d = b - a;
+                e = d;
+            }
+            if (std::fabs(fa) < std::fabs(fb)) {
+                c = b;
+                b = a;
+                a = c;
+                fc = fb;
+                fb = fa;
+                fa = fc;
+            }
+            const double tol = std::fmax(abs_tol, rel_tol * std::fabs(b));
+            const double m = half * (a - b);
+            if (std::fabs(m) <= tol || fb == 0.0) {
+                root = b;
+                return true;
+            }
+            bool use_bis = true;
+            if (std::fabs(e) > tol && std::fabs(fa) > std::fabs(fb)) {
+                const double s = fb / fa;
+                double p, q;
+                if (a == c) {
+                    p = two * m * s;
+                    q = one - s;
+                } else {
+                    const double q1 = fa / fc;
+                    const double r = fb / fc;
+                    p = s * (two * m * q1 * (q1 - r) - (b - a) * (r - one));
+                    q = (q1 - one) * (r - one) * (s - one);
+                }
+                if (q > 0.0)
+                    p = -p;
+                else
+                    q = -q;
+                if (std::fabs(two * p) < (three * m * q - std::fabs(tol * q)) && p < std::fabs(e * half * q)) {
+                    e = d;
+                    d = p / q;
+                    use_bis = false;
+                }
+            }
+            if (use_bis) {
+                d = m;
+                e = m;
+            }
+            a = b;
+            fa = fb;
+            if (std::fabs(d) > tol)
+                b = b + d;
+            else
+                b = b + (m > 0.0 ? tol : -tol);
+            if (b < t_lo || b > t_hi) return false;  // interpolate(b).ok()?
+            fb = g(b, interp.interpolate(b));
+            c = a;
+            fc = fa;
         }
         return false;
     }
@@ -1234,7 +1416,7 @@ struct Result {
 
 template <class Solver>
 Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const State& y0,
-                 const std::vector<double>* t_eval, CrossingSolout* cross = nullptr) {
+                 const std::vector<double>* t_eval, CrossingSolout* cross = nullptr, EventSolout* event = nullptr) {
     Result r;
     double integration_direction;
     {
@@ -1260,8 +1442,17 @@ Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const Sta
     TEvalSolout* te = nullptr;
     TEvalSolout te_obj(t_eval ? *t_eval : std::vector<double>{}, t0, tf, &r.dense);
     if (t_eval) te = &te_obj;
+    // EventWrappedSolout's base: TEvalSolout, or DefaultSolout (every step's end is pushed)
+    PushLog log;
+    te_obj.log = &log;
+    if (event) {
+        event->log = &log;
+        event->integration_direction = integration_direction;
+    }
     if (te) te->solout(solver.t, solver.t_prev, solver.y, solver);
+    if (!te) log.push(solver.t);
     if (cross) cross->solout(solver.t, solver.t_prev, solver.y, solver);
+    if (event) event->solout(solver.t, solver.t_prev, solver.y, solver);  // records g(t0, y0) only
     solver.status = Status::Solving;
 
     const double eps10 = std::numeric_limits<double>::epsilon() * 10.0;
@@ -1285,7 +1476,15 @@ Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const Sta
         }
         r.accepted += 1;
         if (te) te->solout(solver.t, solver.t_prev, solver.y, solver);
+        if (!te) log.push(solver.t);
         if (cross) cross->solout(solver.t, solver.t_prev, solver.y, solver);
+        if (event && event->solout(solver.t, solver.t_prev, solver.y, solver)) {
+            // ControlFlag::Terminate (solve_ivp.rs:254-259)
+            r.outcome.status = DEGPU_INTERRUPTED;
+            r.t_final = solver.t;
+            r.y_final = solver.y;
+            return r;
+        }
         if (std::fabs(tf - solver.t) <= eps10) break;
     }
     r.outcome.status = DEGPU_COMPLETE;
@@ -1297,26 +1496,26 @@ Result solve_ode(Solver& solver, const Ode& ode, double t0, double tf, const Sta
 // One IVP solve with one of the three methods.
 inline Result solve_one(int method, const Ode& ode, double t0, double tf, const State& y0, const Settings& set,
                         const Math& math, const std::vector<double>* t_eval, bool hairer_dense = false,
-                        CrossingSolout* cross = nullptr) {
+                        CrossingSolout* cross = nullptr, EventSolout* event = nullptr) {
     if (method == DEGPU_RK4) {
         FixedRK s;
         s.tab = tableau_rk4();
         s.set = set;
-        return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
+        return solve_ode(s, ode, t0, tf, y0, t_eval, cross, event);
     }
     if (method == DEGPU_RKF45 || method == DEGPU_CASH_KARP) {
         AdaptiveRK s;
         s.tab = method == DEGPU_RKF45 ? tableau_rkf45() : tableau_cash_karp();
         s.set = set;
         s.math = math;
-        return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
+        return solve_ode(s, ode, t0, tf, y0, t_eval, cross, event);
     }
     DormandPrince s;
     s.tab = method == DEGPU_DOP853 ? tableau_dop853() : tableau_dopri5();
     s.set = set;
     s.math = math;
     s.hairer_dense = hairer_dense;
-    return solve_ode(s, ode, t0, tf, y0, t_eval, cross);
+    return solve_ode(s, ode, t0, tf, y0, t_eval, cross, event);
 }
 
 }  // namespace oracle

@@ -52,6 +52,25 @@ int main() {
         std::printf("hyperplane bad input\n");
         return 9;
     }
+    // the crate's logistic example (examples/ode/03_logistic_growth): terminal event y - 0.9 m at ln 81
+    degpu_event ev{};
+    ev.kind = DEGPU_EVENT_LINEAR;
+    ev.terminate = 1;
+    ev.max_points = 4;
+    ev.n_terms = 1;
+    ev.components[0] = 0;
+    ev.weights[0] = 1.0;
+    ev.offset = -(0.9 * 10.0);
+    auto lg = IVP::ode(System{DEGPU_RHS_LOGISTIC, {1.0, 10.0}}, 0.0, 10.0, {1.0})
+                  .method(ExplicitRungeKutta::dop853().rtol(1e-12).atol(1e-12))
+                  .t_eval({0.0, 2.0, 4.0, 6.0})
+                  .event(ev)
+                  .solve();
+    if (!lg.ok() || !lg.value().interrupted || lg.value().t.size() != 4 ||
+        std::fabs(lg.value().t[3] - std::log(81.0)) > 1e-7 || std::fabs(lg.value().y[3][0] - 9.0) > 1e-7) {
+        std::printf("event\n");
+        return 10;
+    }
     std::printf("ok\n");
     return 0;
 }

@@ -47,6 +47,11 @@ def lib():
                                                        C.POINTER(abi.BatchOut), C.POINTER(abi.CrossingOut),
                                                        C.c_int, C.c_int]
         L.oracle_solve_ensemble_hyperplane.restype = C.c_int
+        L.oracle_solve_ensemble_event.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.MethodCfg),
+                                                  C.POINTER(abi.BatchIn), C.POINTER(abi.Event),
+                                                  C.POINTER(abi.BatchOut), C.POINTER(abi.CrossingOut), C.c_int,
+                                                  C.c_int]
+        L.oracle_solve_ensemble_event.restype = C.c_int
         L.oracle_eval_rhs.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP, C.c_int]
         for nm in ("oracle_cr_pow", "oracle_libm_pow"):
             getattr(L, nm).argtypes = [C.c_double, C.c_double]
@@ -160,6 +165,26 @@ def solve_hyperplane(batch: Batch, cfg, components, point, normal, direction=0, 
     rc = lib().oracle_solve_ensemble_hyperplane(C.byref(batch.problem), C.byref(cfg), C.byref(batch.batch_in()),
                                                 C.byref(hp), C.byref(Batch.batch_out(out)), C.byref(co), threads,
                                                 math_mode)
+    assert rc == 0
+    out.update(cross_t=ct, cross_y=cy, cross_count=cc)
+    return out
+
+
+def solve_event(batch: Batch, cfg, event, threads=None, math_mode=1):
+    """Oracle solve with event detection (EventWrappedSolout over the batch's output times, or
+    over the default per-step output): returns the ordinary outputs (dense included when the
+    batch has output times) plus cross_t, cross_y and cross_count for the recorded events."""
+    out = batch.new_outputs()
+    n, dim = batch.n, batch.problem.dim
+    mp = event.max_points
+    ct = np.empty((mp, n))
+    cy = np.empty((mp, dim, n))
+    cc = np.empty(n, np.int32)
+    co = abi.CrossingOut(t=p(ct), y=p(cy), count=abi.ptr(cc, C.c_int32))
+    threads = threads or os.cpu_count() or 1
+    rc = lib().oracle_solve_ensemble_event(C.byref(batch.problem), C.byref(cfg), C.byref(batch.batch_in()),
+                                           C.byref(event), C.byref(Batch.batch_out(out)), C.byref(co), threads,
+                                           math_mode)
     assert rc == 0
     out.update(cross_t=ct, cross_y=cy, cross_count=cc)
     return out

@@ -1,0 +1,207 @@
+"""Event detection on the device (degpu_solve_ensemble_event) against the oracle's restatement of
+the crate's EventWrappedSolout and its Brent–Dekker search (src/solout/event.rs:299-521): with
+FP64 parity arithmetic every event count, event time and state, every output time, counter and
+final state (terminal events included) is bit for bit the oracle's; the fast and mixed forms find
+the same events within their accuracy."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from degpu import abi, workloads as W
+from test_gpu_crossing import assert_same, cfg_for, family_ensemble
+
+pytestmark = pytest.mark.gpu
+R = abi.RHS
+
+
+def gpu_event(e, cfg, ev, t_eval=None):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    keep = dict(t0=T(e.t0), tf=T(e.tf), y0=T(e.y0), params=T(e.params), rtol=T(e.rtol), atol=T(e.atol))
+    if e.family is not None:
+        keep["family"] = T(e.family, torch.int32)
+    ne = 0 if t_eval is None else len(t_eval)
+    if ne:
+        keep["t_eval"] = T(t_eval)
+    bi = abi.BatchIn(n=e.n, t0=abi.ptr(keep["t0"]), tf=abi.ptr(keep["tf"]), y0=abi.ptr(keep["y0"]),
+                     params=abi.ptr(keep["params"]), rtol=abi.ptr(keep["rtol"]), atol=abi.ptr(keep["atol"]),
+                     family=abi.ptr(keep.get("family"), C.c_int32), t_eval=abi.ptr(keep.get("t_eval")), n_eval=ne)
+    E = lambda *shape, dt=torch.float64: torch.empty(shape, dtype=dt, device=dev)
+    mp = ev.max_points
+    out = dict(y_final=E(e.dim, e.n), t_final=E(e.n), accepted=E(e.n, dt=torch.int64),
+               rejected=E(e.n, dt=torch.int64), fevals=E(e.n, dt=torch.int64), status=E(e.n, dt=torch.int32),
+               cross_t=E(mp, e.n), cross_y=E(mp, e.dim, e.n), cross_count=E(e.n, dt=torch.int32))
+    if ne:
+        out["dense"] = E(ne, e.dim, e.n)
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]),
+                      dense=abi.ptr(out.get("dense")), accepted=abi.ptr(out["accepted"], C.c_int64),
+                      rejected=abi.ptr(out["rejected"], C.c_int64), fevals=abi.ptr(out["fevals"], C.c_int64),
+                      status=abi.ptr(out["status"], C.c_int32))
+    co = abi.CrossingOut(t=abi.ptr(out["cross_t"]), y=abi.ptr(out["cross_y"]),
+                         count=abi.ptr(out["cross_count"], C.c_int32))
+    prob = abi.Problem(rhs_id=e.rhs_id, dim=e.dim, n_params=e.params.shape[0])
+    stream = torch.cuda.Stream()
+    rc = abi.load().degpu_solve_ensemble_event(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(ev), C.byref(bo),
+                                               C.byref(co), C.c_void_p(stream.cuda_stream))
+    stream.synchronize()
+    assert rc == abi.OK, rc
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def oracle_event(e, cfg, ev, t_eval=None):
+    b = O.Batch(e.rhs_id, e.dim, e.params.shape[0], e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, family=e.family,
+                t_eval=t_eval)
+    return O.solve_event(b, cfg, ev)
+
+
+def assert_same_event(g, o):
+    assert_same(g, o)
+    assert np.array_equal(g["t_final"], o["t_final"])
+    if "dense" in g:
+        assert np.array_equal(g["dense"], o["dense"], equal_nan=True)
+
+
+# event functions on each family's orbit: (kind, components, weights, t_weight, offset)
+EVENTS = {
+    "VAN_DER_POL": (abi.EVENT_LINEAR, [0, 1], [1.0, 0.25], 0.0, -0.5),
+    "PENDULUM": (abi.EVENT_MAX_ABS, [0, 1], None, 0.0, -1.5),
+    "LORENZ": (abi.EVENT_LINEAR, [2], [1.0], 0.0, -25.0),
+}
+
+
+def make(fam, direction=abi.CROSS_BOTH, terminate=0, max_points=4):
+    kind, comps, w, tw, off = EVENTS[fam]
+    return abi.make_event(kind, comps, w, tw, off, direction, terminate, max_points)
+
+
+@pytest.mark.parametrize("fam", ["VAN_DER_POL", "PENDULUM", "LORENZ"])
+@pytest.mark.parametrize("method,h0", [(abi.DOPRI5, 0.0), (abi.DOP853, 0.0), (abi.RK4, 1e-3),
+                                       (abi.RKF45, 0.0), (abi.CASH_KARP, 0.0)])
+def test_event_parity(fam, method, h0):
+    e = family_ensemble(fam, 500, first=4000)
+    cfg = cfg_for(method, h0=h0)
+    ev = make(fam, max_points=2)
+    g = gpu_event(e, cfg, ev)
+    o = oracle_event(e, cfg, ev)
+    assert np.mean(o["cross_count"] > 0) > 0.5
+    assert np.any(o["cross_count"] > ev.max_points)  # capacity overflow is exercised
+    assert_same_event(g, o)
+
+
+@pytest.mark.parametrize("terminate", [1, 3])
+@pytest.mark.parametrize("direction", [abi.CROSS_BOTH, abi.CROSS_POSITIVE, abi.CROSS_NEGATIVE])
+def test_terminal_event_parity_with_output_times(terminate, direction):
+    """Output times as the base output (`.t_eval(..).event(..)`), terminal events, the family
+    map: counters, final states, output times and events bit for bit."""
+    e = W.config1(n=900, first=30000)
+    e.tf = np.minimum(e.tf, 12.0)
+    cfg = cfg_for(abi.DOP853)
+    ev = abi.make_event(abi.EVENT_LINEAR, [0], [1.0], 0.0, -0.2, direction, terminate, 4)
+    t_eval = np.array([0.0, 0.7, 2.5, 2.5, 6.0, 11.0, 3.3])
+    g = gpu_event(e, cfg, ev, t_eval)
+    o = oracle_event(e, cfg, ev, t_eval)
+    assert np.any(o["status"] == abi.INTERRUPTED) and np.any(o["status"] == abi.COMPLETE)
+    assert_same_event(g, o)
+
+
+def test_logistic_example_and_duplicate_rule_parity():
+    """The crate's logistic example (terminal y - 0.9 m, DOP853 at 1e-12) over an ensemble of
+    growth rates, and the event t - 1 against an output time at 1 (counted, not recorded)."""
+    n = 256
+    k = np.linspace(0.5, 2.0, n)
+    e = W.Ensemble("logistic", abi.DOP853, n, 1, 2, np.zeros(n), np.full(n, 10.0), np.ones((1, n)),
+                   np.stack([k, np.full(n, 10.0)]), np.full(n, 1e-12), np.full(n, 1e-12), rhs_id=R["LOGISTIC"])
+    cfg = cfg_for(abi.DOP853)
+    ev = abi.make_event(abi.EVENT_LINEAR, [0], [1.0], offset=-(0.9 * 10.0), terminate=1)
+    g = gpu_event(e, cfg, ev)
+    o = oracle_event(e, cfg, ev)
+    assert np.all(o["status"] == abi.INTERRUPTED)
+    assert np.max(np.abs(o["cross_t"][0] - np.log(81.0) / k)) < 1e-7
+    assert_same_event(g, o)
+    ev1 = abi.make_event(abi.EVENT_LINEAR, [], t_weight=1.0, offset=-1.0, terminate=1)
+    for te in (None, np.array([0.5, 1.0, 2.0])):
+        g = gpu_event(e, cfg_for(abi.DOPRI5), ev1, te)
+        o = oracle_event(e, cfg_for(abi.DOPRI5), ev1, te)
+        assert np.all(o["cross_count"] == (0 if te is not None else 1))
+        assert_same_event(g, o)
+
+
+def test_event_cr3bp_parity():
+    n = 200
+    rng = np.random.default_rng(3)
+    base = np.array([1.021881345465263, 0.0, -0.182, 0.0, -0.102950816739606, 0.0])
+    y0 = base[:, None] * (1.0 + 1e-3 * rng.standard_normal((6, n)))
+    e = W.Ensemble("cr3bp", abi.DOP853, n, 6, 1, np.zeros(n), np.full(n, 4.5), np.ascontiguousarray(y0),
+                   np.full((1, n), 0.012150585609624), np.full(n, 1e-10), np.full(n, 1e-10), rhs_id=R["CR3BP"])
+    ev = abi.make_event(abi.EVENT_LINEAR, [1], [1.0], max_points=8)  # y = 0 plane of the rotating frame
+    for method in (abi.DOPRI5, abi.DOP853):
+        g = gpu_event(e, cfg_for(method), ev)
+        o = oracle_event(e, cfg_for(method), ev)
+        assert np.all(o["cross_count"] >= 2)
+        assert_same_event(g, o)
+
+
+# The crate's Brent–Dekker variant keeps no bracket after its first step, so the events it returns
+# leave |g| at up to ~2e-3 on this ensemble (median 1e-4); the mixed form's FP32 states steer the
+# same search to other points within that band.
+@pytest.mark.parametrize("precision,tol", [(abi.FP64_FAST, 1e-7), (abi.MIXED, 5e-3)])
+def test_event_fast_and_mixed(precision, tol):
+    """Non-chaotic Van der Pol: the same events, at times within the form's accuracy."""
+    e = family_ensemble("VAN_DER_POL", 400, first=20000)
+    e.rtol[:] = 1e-8
+    e.atol[:] = 1e-10
+    ev = make("VAN_DER_POL", max_points=10)
+    g = gpu_event(e, cfg_for(abi.DOPRI5, precision), ev)
+    o = oracle_event(e, cfg_for(abi.DOPRI5), ev)
+    assert np.array_equal(g["cross_count"], o["cross_count"])
+    m = ~np.isnan(o["cross_t"])
+    assert np.array_equal(m, ~np.isnan(g["cross_t"]))
+    assert np.max(np.abs(g["cross_t"][m] - o["cross_t"][m])) < tol
+
+
+def test_event_bad_input():
+    pytest.importorskip("torch")
+    lib = abi.load()
+    cfg = cfg_for(abi.DOPRI5)
+    prob = abi.Problem(rhs_id=R["VAN_DER_POL"], dim=2, n_params=1)
+    bi = abi.BatchIn(n=4)
+    bo = abi.BatchOut()
+    co = abi.CrossingOut()
+    for ev in (abi.make_event(abi.EVENT_LINEAR, [2], [1.0]),  # component >= dim
+               abi.make_event(abi.EVENT_MAX_ABS, []),  # MAX_ABS needs a term
+               abi.make_event(kind=7, components=[0]),
+               abi.make_event(abi.EVENT_LINEAR, [0], terminate=-1),
+               abi.make_event(abi.EVENT_LINEAR, [0], direction=3)):
+        assert lib.degpu_solve_ensemble_event(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(ev), C.byref(bo),
+                                              C.byref(co), None) == abi.BAD_INPUT
+
+
+def test_ivp_builder_event_and_host_entry():
+    """IVP::ode(..).t_eval(..).event(..).method(..).solve(): the crate's logistic example, and the
+    host entry point returns what the device entry point returns."""
+    import degpu
+
+    m = degpu.ExplicitRungeKutta.dop853().rtol(1e-12).atol(1e-12)
+    ev = abi.make_event(abi.EVENT_LINEAR, [0], [1.0], offset=-9.0, terminate=1)
+    sol = degpu.IVP.ode(degpu.System(abi.RHS["LOGISTIC"], [1.0, 10.0], 1), 0.0, 10.0, [1.0]).method(m) \
+        .t_eval([0.0, 2.0, 4.0, 6.0, 8.0, 10.0]).event(ev).solve()
+    assert sol.status == "Interrupted"
+    assert sol.t[:3] == [0.0, 2.0, 4.0] and abs(sol.t[3] - math.log(81.0)) < 1e-7 and len(sol.t) == 4
+    assert abs(sol.y[3][0] - 9.0) < 1e-7
+
+    e = family_ensemble("PENDULUM", 300, first=777)
+    cfg = cfg_for(abi.DOPRI5)
+    ev = make("PENDULUM", terminate=2)
+    te = np.array([0.5, 4.0, 9.0])
+    g = gpu_event(e, cfg, ev, te)
+    meth = degpu.ExplicitRungeKutta(abi.DOPRI5)
+    meth.cfg = cfg
+    r, (ct, cy, cc) = degpu.solve_ensemble_event(e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol,
+                                                 meth, ev, t_eval=te)
+    assert np.array_equal(cc, g["cross_count"]) and np.array_equal(r.status, g["status"])
+    assert np.array_equal(ct, g["cross_t"], equal_nan=True) and np.array_equal(cy, g["cross_y"], equal_nan=True)
+    assert np.array_equal(r.dense, g["dense"], equal_nan=True) and np.array_equal(r.y_final, g["y_final"])
