@@ -17,6 +17,8 @@
 //    (quadratic convergence), then the factor x^(2^-54/5) = exp(2^-54 ln(x)/5) that turns 1/5
 //    into the binary64 value 0.2 = (1/5)(1 + 2^-54) (truncated exponential series);
 //  - x^(±1/8): three double-double square roots (Karp–Markstein correction);
+//  - x^(±1/q), q = 6, 7, 9: Newton on s^-q = x finished in double-double, reciprocal for the
+//    positive exponent, and the same exp correction for binary64 1/q;
 //  - sin/cos: Cody–Waite reduction by pi/2 split into 33+33+53+53 bits (valid for |x| < 2^20),
 //    reduction to |u| <= 1/128 around the table point j/64, double-double Taylor series and
 //    the angle-addition formulas with the table sin(j/64), cos(j/64).
@@ -150,13 +152,78 @@ DD_HD dd inv_root_dd(double xs, int q) {
     return fast_two_sum(s, s * e * iq);
 }
 
+// s^q as a double-double, q >= 2 (q - 1 products; relative error a few units of 2^-104).
+DD_HD dd dd_pow_int(double s, int q) {
+    dd p = two_prod(s, s);
+    for (int i = 2; i < q; ++i) p = dd_mul_d(p, s);
+    return p;
+}
+
+// x^(-1/q) as a double-double for q in {6, 7, 9} and finite x in [2^-800, 2^800]: the scheme of
+// inv_root_dd with s^q formed by dd_pow_int.
+DD_HD dd inv_root_dd_q(double xs, int q) {
+    int ex = 0;
+    double m = frexp(xs, &ex);
+    float t = -((float)ex + log2f((float)m)) / (float)q;
+    float kf = floorf(t);
+    double s = ldexp((double)exp2f(t - kf), (int)kf);
+    const double q1 = (double)(q + 1), iq = 1.0 / (double)q;
+    for (int it = 0; it < 2; ++it) {
+        double sq = s;
+        for (int i = 1; i < q; ++i) sq = sq * s;
+        s = s * (q1 - xs * sq) * iq;
+    }
+    dd xsq = dd_mul_d(dd_pow_int(s, q), xs);
+    double e = (1.0 - xsq.hi) - xsq.lo;  // 1 - xsq.hi is exact: xsq.hi is within 2^-50 of 1
+    return fast_two_sum(s, s * e * iq);
+}
+
+// pow(x, y) for y = ±1/q, q in {6, 7, 9} (the controller and initial-step exponents of Verner's
+// pairs): x^(±1/q) in double-double, then the factor x^(±d/q) with d = q |y| - 1 (the relative
+// difference between binary64 y and ±1/q, exact from TwoProduct), as exp(g) = 1 + g + g^2/2.
+DD_HD double pow_root_q(double x, double y, int q) {
+    if (x != x) return x;
+    if (x < 0.0) return (x - x) / (x - x);  // NaN
+    if (x == 0.0) return y < 0.0 ? 1.0 / 0.0 : 0.0;
+    if (x == 1.0 / 0.0) return y < 0.0 ? 0.0 : x;
+    // bring x into [2^-800, 2^800] by a multiple of q binades
+    const int E = q * (800 / q);
+    double xs = x, post = 1.0;
+    if (x < 0x1p-800) {
+        xs = ldexp(x, E);
+        post = ldexp(1.0, -E / q);
+    } else if (x > 0x1p+800) {
+        xs = ldexp(x, -E);
+        post = ldexp(1.0, E / q);
+    }
+    dd r = inv_root_dd_q(xs, q);
+    if (y < 0.0)
+        post = 1.0 / post;  // exact: power of two
+    else
+        r = dd_recip(r);
+    const dd qy = two_prod((double)q, fabs(y));
+    const double d = (qy.hi - 1.0) + qy.lo;
+    double g = d / (double)q * log(x);
+    if (y < 0.0) g = -g;
+    g = g + 0.5 * g * g;
+    const double tt = r.lo + r.hi * g;
+    return (r.hi + tt) * post;
+}
+
 // pow(x, y) for the exponents of the crate's controller and initial-step heuristic:
-// y in {0.2, -0.2, 0.125, -0.125} (binary64 values of ±1/5 and ±1/8).  Other y fall back to the
-// platform pow and are not guaranteed to be correctly rounded.
+// y = ±1/q for q in {5, 6, 7, 8, 9} (binary64 values; 0.2 and 0.125 for DOPRI5 / the order-5
+// pairs and DOP853).  Other y fall back to the platform pow and are not guaranteed to be correctly
+// rounded.
 DD_HD double pow_ctrl(double x, double y) {
     const bool fifth = (y == 0.2 || y == -0.2);
     const bool eighth = (y == 0.125 || y == -0.125);
-    if (!(fifth || eighth)) return pow(x, y);
+    if (!(fifth || eighth)) {
+        const double ay = fabs(y);
+        if (ay == 1.0 / 6.0) return pow_root_q(x, y, 6);
+        if (ay == 1.0 / 7.0) return pow_root_q(x, y, 7);
+        if (ay == 1.0 / 9.0) return pow_root_q(x, y, 9);
+        return pow(x, y);
+    }
     // IEEE special cases of pow for these y
     if (x != x) return x;
     if (x < 0.0) return (x - x) / (x - x);  // NaN

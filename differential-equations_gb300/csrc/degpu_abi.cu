@@ -64,6 +64,14 @@ void ensure_registered() {
         register_cross_embedded_fast_mixed();
         register_embedded_parity();
         register_embedded_fast_mixed();
+        register_verner65_parity();
+        register_verner76_parity();
+        register_verner87_parity();
+        register_verner98_parity();
+        register_verner65_fast();
+        register_verner76_fast();
+        register_verner87_fast();
+        register_verner98_fast();
     });
 }
 
@@ -85,9 +93,10 @@ struct Scratch {
     }
 };
 
-static bool valid_method(int m) {
-    return m == DEGPU_RK4 || m == DEGPU_DOPRI5 || m == DEGPU_DOP853 || m == DEGPU_RKF45 || m == DEGPU_CASH_KARP;
-}
+static bool valid_method(int m) { return m >= DEGPU_RK4 && m <= DEGPU_RKV989E; }
+
+// The mixed-precision bound a method uses: the order-5 embedded pairs share DOPRI5's.
+static int bound_method(int m) { return m == DEGPU_DOP853 ? DEGPU_DOP853 : DEGPU_DOPRI5; }
 
 // Mixed-precision bounds of DOPRI5 [0] and DOP853 [1]: the rtol below which an instance of a
 // mixed solve runs in FP64.  Below the FP32 rounding level of the stage states the error
@@ -120,8 +129,10 @@ static std::atomic<double>& mixed_bound(int m) {
 
 double mixed_split(const degpu_method_cfg* cfg) {
     if (cfg->precision != DEGPU_MIXED || cfg->method == DEGPU_RK4) return 0.0;
-    // the order-5 embedded pairs (RKF45, Cash-Karp) share DOPRI5's bound
-    return mixed_bound(cfg->method == DEGPU_DOP853 ? DEGPU_DOP853 : DEGPU_DOPRI5).load();
+    // Verner's pairs: their stage sums carry coefficients up to 1.5e4 (RKV877e), whose
+    // cancellation FP32 cannot resolve, so every instance of a mixed solve runs in FP64
+    if (cfg->method >= DEGPU_RKV655E) return INFINITY;
+    return mixed_bound(bound_method(cfg->method)).load();
 }
 
 static bool valid_prec(int p) { return p == DEGPU_FP64_PARITY || p == DEGPU_FP64_FAST || p == DEGPU_MIXED; }
@@ -680,9 +691,9 @@ degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol) {
 }
 
 double degpu_mixed_min_rtol(int32_t method) {
-    if (method == DEGPU_RKF45 || method == DEGPU_CASH_KARP) method = DEGPU_DOPRI5;
-    if (method != DEGPU_DOPRI5 && method != DEGPU_DOP853) return 0.0;
-    return mixed_bound(method).load();
+    if (!valid_method(method) || method == DEGPU_RK4) return 0.0;
+    if (method >= DEGPU_RKV655E) return INFINITY;
+    return mixed_bound(bound_method(method)).load();
 }
 
 degpu_status degpu_rhs_info(int32_t rhs_id, int32_t* dim, int32_t* n_params) {

@@ -209,7 +209,11 @@ struct Lane {
     static constexpr int I = Tab::I;
     static constexpr int NS = Tab::S;
     static constexpr int O = Tab::ORDER;
-    static constexpr int NC = DENSE ? (Tab::DP ? O : 2) : 1;  // Hermite keeps y_prev, dydt_prev
+    // dense-output rows: the DP coefficients; Hermite: y_prev, dydt_prev; Verner: y_prev and the
+    // step's I stages
+    static constexpr int NC = DENSE ? (Tab::DP ? O : (Tab::HAS_BI ? 1 + I : 2)) : 1;
+    // stage rows of an embedded step: the dense-output stages only when they are read
+    static constexpr int KN = (DENSE && Tab::HAS_BI) ? I : NS;
     static constexpr int NPP = Rhs::NP > 0 ? Rhs::NP : 1;
     using S = typename P::S;
     static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
@@ -435,6 +439,25 @@ struct Lane {
                     }
                     out[c] = cont[0][c] + ss * accv;
                 }
+            } else if constexpr (Tab::HAS_BI) {
+                // adaptive/ordinary.rs:251-275: per stage the polynomial sum_j BI[i][j] s^(j+1) by
+                // Horner's rule, then y_prev + sum_i (cont_i h_prev) k_i in stage order
+                const double hp = P::KAHAN ? t - t_prev : h_prev;
+                const S ss = P::from((te - t_prev) / hp), hs = P::from(hp);
+#pragma unroll
+                for (int c = 0; c < D; ++c) out[c] = cont[0][c];
+                static_for<0, I>([&](auto i) {
+                    constexpr int ii = decltype(i)::value;
+                    S ci = (S)Tab::bi(ii, O - 1);
+                    static_for<0, O - 1>([&](auto jr) {
+                        constexpr int j = O - 2 - decltype(jr)::value;
+                        ci = ci * ss + (S)Tab::bi(ii, j);
+                    });
+                    ci = ci * ss;
+                    const S w = ci * hs;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) out[c] = out[c] + w * cont[1 + ii][c];
+                });
             } else {
                 // cubic Hermite over [t_prev, t] with y_prev=cont[0], dydt_prev=cont[1], y, k0
                 double t0 = t_prev, t1 = t;
@@ -484,6 +507,21 @@ struct Lane {
                     }
                     out[c] = cont[0][c] + ss * accv;
                 }
+            } else if constexpr (Tab::HAS_BI) {
+                const S hs = P::from(t - t_prev);
+#pragma unroll
+                for (int c = 0; c < D; ++c) out[c] = cont[0][c];
+                static_for<0, I>([&](auto i) {
+                    constexpr int ii = decltype(i)::value;
+                    S ci = (S)Tab::bi(ii, O - 1);
+                    static_for<0, O - 1>([&](auto jr) {
+                        constexpr int j = O - 2 - decltype(jr)::value;
+                        ci = ci * ss + (S)Tab::bi(ii, j);
+                    });
+                    const S w = (ci * ss) * hs;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) out[c] = out[c] + w * cont[1 + ii][c];
+                });
             } else {
                 const S hh = P::from(t - t_prev);
                 const S s2 = ss * ss, s3 = s2 * ss;
@@ -1227,11 +1265,12 @@ struct Lane {
             return 3;
         }
         steps += 1;
-        S k[NS][D];
+        S k[KN][D];
 #pragma unroll
         for (int c = 0; c < D; ++c) k[0][c] = k0[c];
         S ys[D];
-        static_for<1, NS>([&](auto i) {
+        // stage i from the step's start: y + sum_j (a_ij h) k_j in order (add_scaled)
+        auto stage = [&](auto i) {
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = y[c];
             static_for<0, decltype(i)::value>([&](auto j) {
@@ -1246,7 +1285,8 @@ struct Lane {
                 rhs_at((float)Tab::c(i) * hf, ys, k[i]);
             else
                 rhs(t + Tab::c(i) * h, ys, k[i]);
-        });
+        };
+        static_for<1, NS>(stage);
         fev += NS - 1;
         // y_high = y + sum (b_i h) k_i and y_low = y + sum (bl_i h) k_i, each accumulated in order
         // (add_scaled, traits.rs:316-320); their difference is the error estimate
@@ -1337,12 +1377,26 @@ struct Lane {
         int result;
         if (accept) {
             if constexpr (DENSE) {
+                if constexpr (Tab::HAS_BI) {
+                    // the dense-output stages (adaptive/ordinary.rs:146-163), from the step's start
+                    static_for<NS, I>(stage);
 #pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    cont[0][c] = y[c];
-                    cont[1][c] = k[0][c];
+                    for (int c = 0; c < D; ++c) cont[0][c] = y[c];
+                    static_for<0, I>([&](auto i) {
+#pragma unroll
+                        for (int c = 0; c < D; ++c) cont[1 + decltype(i)::value][c] = k[i][c];
+                    });
+                } else {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        cont[0][c] = y[c];
+                        cont[1][c] = k[0][c];
+                    }
                 }
             }
+            // the crate evaluates the dense-output stages on every accepted step; without
+            // requested output nothing reads them, so only their count is kept
+            if constexpr (Tab::HAS_BI) fev += I - NS;
             t_prev = t;
             if constexpr (MIX) {
                 h_lim = fabsf(hf) * 1e-14f;
@@ -1368,11 +1422,17 @@ struct Lane {
                 y[c] = yh[c];
                 yc[c] = ycn[c];
             }
-            if constexpr (PHASE)
-                rhs_at(0.0f, y, k0);  // FSAL is off for both tableaus
-            else
-                rhs(t, y, k0);
-            fev += 1;
+            if constexpr (Tab::FSAL) {
+                // first same as last (ordinary.rs:174-177): the last stage is the new derivative
+#pragma unroll
+                for (int c = 0; c < D; ++c) k0[c] = k[NS - 1][c];
+            } else {
+                if constexpr (PHASE)
+                    rhs_at(0.0f, y, k0);
+                else
+                    rhs(t, y, k0);
+                fev += 1;
+            }
             result = 1;
         } else {
             last_rejected = true;

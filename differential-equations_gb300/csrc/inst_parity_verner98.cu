@@ -1,0 +1,22 @@
+// inst_parity_verner98.cu — Verner's pairs RKV988e and RKV989e of the Adaptive family, FP64 parity
+// arithmetic (compiled with -fmad=false like every inst_parity_* translation unit), one system per
+// thread, with and without dense output.
+#include "registry.cuh"
+
+namespace degpu {
+
+template <class Rhs>
+static void reg() {
+    register_thread_variant<TabRKV988E, Rhs, PrecParity>();
+    register_thread_variant<TabRKV989E, Rhs, PrecParity>();
+}
+
+void register_verner98_parity() {
+    reg<RhsExpGrowth>();
+    reg<RhsHarmonic>();
+    reg<RhsVanDerPol>();
+    reg<RhsPendulum>();
+    reg<RhsLorenz>();
+}
+
+}  // namespace degpu

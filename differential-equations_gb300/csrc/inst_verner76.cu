@@ -1,0 +1,20 @@
+// inst_verner76.cu — Verner's pairs RKV766e and RKV767e of the Adaptive family, FP64 fast arithmetic
+// (also what a mixed solve of these pairs runs), one system per thread, with and without dense
+// output.
+#include "registry.cuh"
+
+namespace degpu {
+
+template <class Rhs, class P>
+static void reg() {
+    register_thread_variant<TabRKV766E, Rhs, P>();
+    register_thread_variant<TabRKV767E, Rhs, P>();
+}
+
+void register_verner76_fast() {
+    reg<RhsVanDerPol, PrecFast>();
+    reg<RhsPendulum, PrecFast>();
+    reg<RhsLorenz, PrecFast>();
+}
+
+}  // namespace degpu

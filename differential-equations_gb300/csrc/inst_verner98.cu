@@ -1,0 +1,20 @@
+// inst_verner98.cu — Verner's pairs RKV988e and RKV989e of the Adaptive family, FP64 fast arithmetic
+// (also what a mixed solve of these pairs runs), one system per thread, with and without dense
+// output.
+#include "registry.cuh"
+
+namespace degpu {
+
+template <class Rhs, class P>
+static void reg() {
+    register_thread_variant<TabRKV988E, Rhs, P>();
+    register_thread_variant<TabRKV989E, Rhs, P>();
+}
+
+void register_verner98_fast() {
+    reg<RhsVanDerPol, PrecFast>();
+    reg<RhsPendulum, PrecFast>();
+    reg<RhsLorenz, PrecFast>();
+}
+
+}  // namespace degpu

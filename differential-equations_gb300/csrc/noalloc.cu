@@ -129,7 +129,8 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     if (in->n < 0) return DEGPU_BAD_INPUT;
     if (in->n > NA_MAX) return DEGPU_BAD_INPUT;  // beyond DEGPU_NOALLOC_MAX_INSTANCES
     if (in->n == 0) return DEGPU_OK;
-    if (cfg->method < DEGPU_RK4 || cfg->method > DEGPU_CASH_KARP) return DEGPU_BAD_INPUT;
+    if (cfg->method < DEGPU_RK4 || cfg->method > DEGPU_RKV989E) return DEGPU_BAD_INPUT;
+    if (cfg->method > DEGPU_CASH_KARP) return DEGPU_UNSUPPORTED;  // Verner's pairs: not in the fixed lists
     if (cfg->precision < DEGPU_FP64_PARITY || cfg->precision > DEGPU_MIXED || cfg->max_steps < 0) return DEGPU_BAD_INPUT;
     if (!in->t0 || !in->tf || !in->y0 || !in->rtol || !in->atol || !out->y_final) return DEGPU_BAD_INPUT;
     if (in->n_eval > 0 || in->dims) return DEGPU_UNSUPPORTED;
@@ -162,7 +163,7 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
 
     // the lists, counts and heads from the previous call are still in the array: clear them
     if (cudaMemsetAsync(scratch, 0, NA_ZERO_END, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
-    const double inv_order = cfg->method == DEGPU_DOP853 ? 0.125 : cfg->method == DEGPU_RK4 ? 0.0 : 0.2;
+    const double inv_order = method_inv_order(cfg->method);
     const unsigned blocks = (unsigned)((n + 255) / 256);
     na_count_kernel<<<blocks, 256, 0, s>>>(n, in->t0, in->tf, in->rtol, in->params, pb->n_params, in->family,
                                            pb->rhs_id, inv_order, cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, scratch,

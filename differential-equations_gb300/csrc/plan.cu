@@ -99,7 +99,7 @@ static degpu_status run_plan(const degpu_method_cfg* cfg, const EnsArgs& a, cons
     int* pos = (int*)(pl.items + n);
     int* key = pos + n;
     if (cudaMemsetAsync(pl.blk, 0, head_bytes, s) != cudaSuccess) return DEGPU_CUDA_ERROR;
-    const double inv_order = cfg->method == DEGPU_DOP853 ? 0.125 : cfg->method == DEGPU_RK4 ? 0.0 : 0.2;
+    const double inv_order = method_inv_order(cfg->method);
     unsigned blocks = (unsigned)((n + 255) / 256);
     plan_count_kernel<<<blocks, 256, 0, s>>>(n, a.t0, a.tf, a.rtol, a.params, a.n_params, family_dev, fam_const,
                                               inv_order, cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, cells, pos, key,

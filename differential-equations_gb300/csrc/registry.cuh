@@ -27,11 +27,21 @@ std::map<VariantKey, EnsLaunchFn>& ens_registry();
 
 template <class Tab>
 constexpr int method_id() {
-    return std::is_same<Tab, TabRK4>::value        ? DEGPU_RK4
-           : std::is_same<Tab, TabDopri5>::value   ? DEGPU_DOPRI5
-           : std::is_same<Tab, TabDop853>::value   ? DEGPU_DOP853
-           : std::is_same<Tab, TabRKF45>::value    ? DEGPU_RKF45
-                                                   : DEGPU_CASH_KARP;
+    return Tab::METHOD;
+}
+
+// 1 / order of the method's error estimate (0 for fixed steps): the rtol exponent of the cost
+// model that orders the work lists.
+inline double method_inv_order(int method) {
+    switch (method) {
+        case DEGPU_RK4: return 0.0;
+        case DEGPU_DOP853: return 1.0 / 8.0;
+        case DEGPU_RKV655E: case DEGPU_RKV656E: return 1.0 / 6.0;
+        case DEGPU_RKV766E: case DEGPU_RKV767E: return 1.0 / 7.0;
+        case DEGPU_RKV877E: case DEGPU_RKV878E: return 1.0 / 8.0;
+        case DEGPU_RKV988E: case DEGPU_RKV989E: return 1.0 / 9.0;
+        default: return 1.0 / 5.0;
+    }
 }
 
 int device_sm_count();
@@ -182,6 +192,14 @@ void register_cross_embedded_parity();
 void register_cross_embedded_fast_mixed();
 void register_embedded_parity();
 void register_embedded_fast_mixed();
+void register_verner65_parity();
+void register_verner76_parity();
+void register_verner87_parity();
+void register_verner98_parity();
+void register_verner65_fast();
+void register_verner76_fast();
+void register_verner87_fast();
+void register_verner98_fast();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to

@@ -1,7 +1,7 @@
 // tableau.cuh — Butcher tableaus of the methods, as compile-time constants.
 //
 // Values are the crate's (src/tableau/runge_kutta.rs:39-70 and :335-480,
-// src/tableau/dorman_prince.rs:37-118 and :155-381); every coefficient is a binary64 constant evaluated exactly as the crate's
+// src/tableau/dorman_prince.rs:37-118 and :155-381, src/tableau/verner.rs); every coefficient is a binary64 constant evaluated exactly as the crate's
 // `T::from_f64(x)` of the same literal or quotient.  Being constexpr, each coefficient is an
 // immediate operand after unrolling, and terms whose coefficient is zero are removed at compile
 // time (`if constexpr`).  Removing a term `acc + 0*k` leaves every finite result unchanged bit for
@@ -9,11 +9,13 @@
 // the sign of an exact zero, which no right-hand side here can turn into a different non-zero value.
 #pragma once
 
+#include "../../include/degpu.h"
+
 namespace degpu {
 
 struct TabRK4 {
-    static constexpr int S = 4, I = 4, ORDER = 4;
-    static constexpr bool ADAPTIVE = false, DP = false, HAS_BH = false, FSAL = false;
+    static constexpr int S = 4, I = 4, ORDER = 4, METHOD = DEGPU_RK4;
+    static constexpr bool ADAPTIVE = false, DP = false, HAS_BH = false, FSAL = false, HAS_BI = false;
     static constexpr double C[4] = {0.0, 0.5, 0.5, 1.0};
     static constexpr double A[4][4] = {{0, 0, 0, 0}, {0.5, 0, 0, 0}, {0, 0.5, 0, 0}, {0, 0, 1.0, 0}};
     static constexpr double B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
@@ -29,9 +31,9 @@ struct TabRK4 {
 };
 
 struct TabDopri5 {
-    static constexpr int S = 7, I = 7, ORDER = 5;
+    static constexpr int S = 7, I = 7, ORDER = 5, METHOD = DEGPU_DOPRI5;
     // FSAL: the last row of A equals b and c = 1, so the last stage's state is y_new
-    static constexpr bool ADAPTIVE = true, DP = true, HAS_BH = false, FSAL = true;
+    static constexpr bool ADAPTIVE = true, DP = true, HAS_BH = false, FSAL = true, HAS_BI = false;
     static constexpr double C[7] = {0.0, 0.2, 0.3, 0.8, 8.0 / 9.0, 1.0, 1.0};
     static constexpr double A[7][7] = {
         {0, 0, 0, 0, 0, 0, 0},
@@ -68,8 +70,8 @@ __host__ __device__ constexpr bool fsal_holds() {
 static_assert(fsal_holds<TabDopri5>(), "DOPRI5: last row of A must equal b with c = 1");
 
 struct TabDop853 {
-    static constexpr int S = 12, I = 16, ORDER = 8;
-    static constexpr bool ADAPTIVE = true, DP = true, HAS_BH = true, FSAL = false;
+    static constexpr int S = 12, I = 16, ORDER = 8, METHOD = DEGPU_DOP853;
+    static constexpr bool ADAPTIVE = true, DP = true, HAS_BH = true, FSAL = false, HAS_BI = false;
     static constexpr double C[16] = {0.0,
                                      5.260015195876773E-2,
                                      7.89002279381516E-2,
@@ -170,8 +172,8 @@ __host__ __device__ __forceinline__ void static_for(F&& f) {
 // ordinary.rs:63-212): y_high from b, y_low from BL (the crate's `bh`), an infinity norm of their
 // difference, cubic Hermite dense output; order 5 in the controller for both.
 struct TabRKF45 {  // src/tableau/runge_kutta.rs:335-406 (Fehlberg 1969)
-    static constexpr int S = 6, I = 6, ORDER = 5;
-    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = false;
+    static constexpr int S = 6, I = 6, ORDER = 5, METHOD = DEGPU_RKF45;
+    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = false, HAS_BI = false;
     static constexpr double C[6] = {0.0, 1.0 / 4.0, 3.0 / 8.0, 12.0 / 13.0, 1.0, 1.0 / 2.0};
     static constexpr double A[6][6] = {{0, 0, 0, 0, 0, 0},
                                        {1.0 / 4.0, 0, 0, 0, 0, 0},
@@ -194,8 +196,8 @@ struct TabRKF45 {  // src/tableau/runge_kutta.rs:335-406 (Fehlberg 1969)
 };
 
 struct TabCashKarp {  // src/tableau/runge_kutta.rs:420-480 (Cash and Karp 1990)
-    static constexpr int S = 6, I = 6, ORDER = 5;
-    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = false;
+    static constexpr int S = 6, I = 6, ORDER = 5, METHOD = DEGPU_CASH_KARP;
+    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = false, HAS_BI = false;
     static constexpr double C[6] = {0.0, 1.0 / 5.0, 3.0 / 10.0, 3.0 / 5.0, 1.0, 7.0 / 8.0};
     static constexpr double A[6][6] = {
         {0, 0, 0, 0, 0, 0},
@@ -218,5 +220,35 @@ struct TabCashKarp {  // src/tableau/runge_kutta.rs:420-480 (Cash and Karp 1990)
     __host__ __device__ static constexpr double er(int i) { return ER[i]; }
     __host__ __device__ static constexpr double bi(int i, int j) { return BI[i][j]; }
 };
+
+// Verner's pairs of the crate's Adaptive family (src/tableau/verner.rs; constructors
+// src/methods/erk/adaptive/mod.rs:59-122): the embedded pair of TabRKF45 with more stages, plus
+// I - S dense-output stages evaluated on every accepted step and interpolation weights BI
+// (adaptive/ordinary.rs:146-163, 251-275). The coefficient tables are generated from the crate's
+// literals by gen_verner_tables.py.
+namespace verner {
+#include "verner_tables.inc"
+}
+
+template <class V, int M>
+struct TabVerner {
+    static constexpr int S = V::S, I = V::I, ORDER = V::ORDER, METHOD = M;
+    static constexpr bool ADAPTIVE = true, DP = false, HAS_BH = false, FSAL = V::FSAL, HAS_BI = true;
+    __host__ __device__ static constexpr double c(int i) { return V::C[i]; }
+    __host__ __device__ static constexpr double a(int i, int j) { return V::A[i][j]; }
+    __host__ __device__ static constexpr double b(int i) { return V::B[i]; }
+    __host__ __device__ static constexpr double bl(int i) { return V::BH[i]; }
+    __host__ __device__ static constexpr double bh(int i) { return 0.0; }
+    __host__ __device__ static constexpr double er(int i) { return 0.0; }
+    __host__ __device__ static constexpr double bi(int i, int j) { return V::BI[i][j]; }
+};
+using TabRKV655E = TabVerner<verner::rkv655e, DEGPU_RKV655E>;
+using TabRKV656E = TabVerner<verner::rkv656e, DEGPU_RKV656E>;
+using TabRKV766E = TabVerner<verner::rkv766e, DEGPU_RKV766E>;
+using TabRKV767E = TabVerner<verner::rkv767e, DEGPU_RKV767E>;
+using TabRKV877E = TabVerner<verner::rkv877e, DEGPU_RKV877E>;
+using TabRKV878E = TabVerner<verner::rkv878e, DEGPU_RKV878E>;
+using TabRKV988E = TabVerner<verner::rkv988e, DEGPU_RKV988E>;
+using TabRKV989E = TabVerner<verner::rkv989e, DEGPU_RKV989E>;
 
 }  // namespace degpu

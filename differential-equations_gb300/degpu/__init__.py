@@ -64,6 +64,46 @@ class ExplicitRungeKutta:
     def cash_karp(cls):  # src/methods/erk/adaptive/mod.rs:51-58
         return cls(abi.CASH_KARP)
 
+    @classmethod
+    def rkv655e(cls):
+        """Verner's RKV655e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV655E)
+
+    @classmethod
+    def rkv656e(cls):
+        """Verner's RKV656e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV656E)
+
+    @classmethod
+    def rkv766e(cls):
+        """Verner's RKV766e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV766E)
+
+    @classmethod
+    def rkv767e(cls):
+        """Verner's RKV767e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV767E)
+
+    @classmethod
+    def rkv877e(cls):
+        """Verner's RKV877e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV877E)
+
+    @classmethod
+    def rkv878e(cls):
+        """Verner's RKV878e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV878E)
+
+    @classmethod
+    def rkv988e(cls):
+        """Verner's RKV988e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV988E)
+
+    @classmethod
+    def rkv989e(cls):
+        """Verner's RKV989e pair (src/methods/erk/adaptive/mod.rs, src/tableau/verner.rs)."""
+        return cls(abi.RKV989E)
+
     def rtol(self, v):
         self._rtol = v
         return self

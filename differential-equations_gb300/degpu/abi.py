@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(PKG_ROOT, "csrc", "libdegpu.so")
 OK, BAD_INPUT, OOM, TIMEOUT, CUDA_ERROR, UNSUPPORTED = range(6)
 # degpu_method
 RK4, DOPRI5, DOP853, RKF45, CASH_KARP = 0, 1, 2, 3, 4
+RKV655E, RKV656E, RKV766E, RKV767E, RKV877E, RKV878E, RKV988E, RKV989E = range(5, 13)
 # degpu_precision
 FP64_PARITY, FP64_FAST, MIXED = 0, 1, 2
 # degpu_kernel

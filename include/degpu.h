@@ -54,14 +54,25 @@ typedef enum {
 
 /* Methods: constructors in src/methods/erk/fixed/mod.rs:69-75 (rk4),
  * src/methods/erk/dormandprince/mod.rs:45-58 (dop853, dopri5) and
- * src/methods/erk/adaptive/mod.rs:43-58 (rkf45, cash_karp: embedded pair, infinity-norm error,
- * Stiffness after 100 consecutive rejections, cubic Hermite dense output). */
+ * src/methods/erk/adaptive/mod.rs:43-122 (the Adaptive family: embedded pair, infinity-norm
+ * error, Stiffness after 100 consecutive rejections). rkf45 and cash_karp use cubic Hermite
+ * dense output; Verner's pairs rkvPQRe (order P(Q), interpolant of order R; tableaus
+ * src/tableau/verner.rs) evaluate extra stages on every accepted step and interpolate with
+ * their own weights; rkv655e and rkv656e reuse their last stage (FSAL). */
 typedef enum {
     DEGPU_RK4 = 0,
     DEGPU_DOPRI5 = 1,
     DEGPU_DOP853 = 2,
     DEGPU_RKF45 = 3,
-    DEGPU_CASH_KARP = 4
+    DEGPU_CASH_KARP = 4,
+    DEGPU_RKV655E = 5,  /* 6(5), 9 stages + 1 dense stage   */
+    DEGPU_RKV656E = 6,  /* 6(5), 9 stages + 3 dense stages  */
+    DEGPU_RKV766E = 7,  /* 7(6), 10 stages + 3 dense stages */
+    DEGPU_RKV767E = 8,  /* 7(6), 10 stages + 6 dense stages */
+    DEGPU_RKV877E = 9,  /* 8(7), 13 stages + 4 dense stages */
+    DEGPU_RKV878E = 10, /* 8(7), 13 stages + 8 dense stages */
+    DEGPU_RKV988E = 11, /* 9(8), 16 stages + 5 dense stages */
+    DEGPU_RKV989E = 12  /* 9(8), 16 stages + 10 dense stages */
 } degpu_method;
 
 /* Arithmetic of the solve.
@@ -180,7 +191,9 @@ void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method);
 degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol);
 
 /* The bound in force for `method` (0 for RK4 and unknown methods).  RKF45 and Cash-Karp (order-5
- * pairs) use DOPRI5's bound. */
+ * pairs) use DOPRI5's bound.  Verner's pairs return +infinity: their stage sums carry coefficients
+ * up to 1.5e4, whose cancellation FP32 cannot resolve, so a DEGPU_MIXED solve runs all their
+ * instances in DEGPU_FP64_FAST arithmetic. */
 double degpu_mixed_min_rtol(int32_t method);
 
 /* Dimension and parameter count of a built-in family (dim = -1 for variable-size families).

@@ -121,6 +121,15 @@ class ExplicitRungeKutta {
     static ExplicitRungeKutta dop853() { return ExplicitRungeKutta(DEGPU_DOP853); }
     static ExplicitRungeKutta rkf45() { return ExplicitRungeKutta(DEGPU_RKF45); }        // adaptive/mod.rs:43-50
     static ExplicitRungeKutta cash_karp() { return ExplicitRungeKutta(DEGPU_CASH_KARP); }  // adaptive/mod.rs:51-58
+    // Verner's pairs, adaptive/mod.rs:59-122 (tableaus src/tableau/verner.rs)
+    static ExplicitRungeKutta rkv655e() { return ExplicitRungeKutta(DEGPU_RKV655E); }
+    static ExplicitRungeKutta rkv656e() { return ExplicitRungeKutta(DEGPU_RKV656E); }
+    static ExplicitRungeKutta rkv766e() { return ExplicitRungeKutta(DEGPU_RKV766E); }
+    static ExplicitRungeKutta rkv767e() { return ExplicitRungeKutta(DEGPU_RKV767E); }
+    static ExplicitRungeKutta rkv877e() { return ExplicitRungeKutta(DEGPU_RKV877E); }
+    static ExplicitRungeKutta rkv878e() { return ExplicitRungeKutta(DEGPU_RKV878E); }
+    static ExplicitRungeKutta rkv988e() { return ExplicitRungeKutta(DEGPU_RKV988E); }
+    static ExplicitRungeKutta rkv989e() { return ExplicitRungeKutta(DEGPU_RKV989E); }
     ExplicitRungeKutta& rtol(double v) { rtol_ = v; return *this; }
     ExplicitRungeKutta& atol(double v) { atol_ = v; return *this; }
     ExplicitRungeKutta& h0(double v) { cfg_.h0 = v; return *this; }

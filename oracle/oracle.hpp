@@ -11,7 +11,8 @@
 //   constrain / validate ............ src/utils.rs:22-157
 //   State algebra ................... src/traits.rs:316-410
 //   cubic Hermite ................... src/interpolate.rs:40-60
-//   Adaptive ERK (RKF45, Cash-Karp)  src/methods/erk/adaptive/ordinary.rs:16-290
+//   Adaptive ERK (RKF45, Cash-Karp,  src/methods/erk/adaptive/ordinary.rs:16-290,
+//   Verner RKV655e..RKV989e) ........ src/tableau/verner.rs
 //   TEvalSolout ..................... src/solout/t_eval.rs:82-171
 //   CrossingSolout .................. src/solout/crossing.rs:200-330, src/solout/hyperplane.rs
 //   EventSolout ..................... src/solout/event.rs:67-521
@@ -61,15 +62,16 @@ struct Tableau {
     int S = 0;       // stages
     int I = 0;       // stages incl. dense-output stages
     int order = 0;   // O
-    double c[16] = {};
-    double a[16][16] = {};
-    double b[16] = {};
-    double bh[16] = {};
+    double c[32] = {};
+    double a[32][32] = {};
+    double b[32] = {};
+    double bh[32] = {};
     bool has_bh = false;
-    double er[16] = {};
+    double er[32] = {};
     bool has_er = false;
-    double bi[16][16] = {};
+    double bi[32][32] = {};
     bool has_bi = false;
+    bool fsal = false;  // adaptive family: the last stage is the next step's first (ordinary.rs:174-177)
 };
 
 // src/tableau/runge_kutta.rs:39-70; constructor src/methods/erk/fixed/mod.rs:69-75 (O=4, S=I=4).
@@ -120,6 +122,49 @@ inline Tableau tableau_cash_karp() {
     t.bh[4] = 277.0 / 14336.0; t.bh[5] = 1.0 / 4.0;
     t.has_bh = true;
     return t;
+}
+
+// Verner's pairs (src/tableau/verner.rs; S, I, O and FSAL from src/methods/erk/adaptive/mod.rs:59-122).
+// The coefficient tables are the crate's literals, generated into verner_tables.inc by
+// differential-equations_gb300/csrc/gen_verner_tables.py.
+namespace verner {
+#include "verner_tables.inc"
+}
+template <class V>
+inline Tableau tableau_verner() {
+    Tableau t;
+    t.S = V::S;
+    t.I = V::I;
+    t.order = V::ORDER;
+    t.fsal = V::FSAL;
+    for (int i = 0; i < V::I; ++i) {
+        t.c[i] = V::C[i];
+        for (int j = 0; j < V::I; ++j) {
+            t.a[i][j] = V::A[i][j];
+            t.bi[i][j] = V::BI[i][j];
+        }
+    }
+    for (int i = 0; i < V::S; ++i) {
+        t.b[i] = V::B[i];
+        t.bh[i] = V::BH[i];
+    }
+    t.has_bh = true;
+    t.has_bi = true;
+    return t;
+}
+inline Tableau tableau_for_method(int method) {
+    switch (method) {
+        case DEGPU_RKF45: return tableau_rkf45();
+        case DEGPU_CASH_KARP: return tableau_cash_karp();
+        case DEGPU_RKV655E: return tableau_verner<verner::rkv655e>();
+        case DEGPU_RKV656E: return tableau_verner<verner::rkv656e>();
+        case DEGPU_RKV766E: return tableau_verner<verner::rkv766e>();
+        case DEGPU_RKV767E: return tableau_verner<verner::rkv767e>();
+        case DEGPU_RKV877E: return tableau_verner<verner::rkv877e>();
+        case DEGPU_RKV878E: return tableau_verner<verner::rkv878e>();
+        case DEGPU_RKV988E: return tableau_verner<verner::rkv988e>();
+        default: return tableau_verner<verner::rkv989e>();
+    }
 }
 
 // src/tableau/dorman_prince.rs:37-118; constructor dormandprince/mod.rs:52-58 (O=5, S=I=7).
@@ -1266,10 +1311,22 @@ struct AdaptiveRK : Interpolator {
                 status = Status::Solving;
                 scale = std::fmin(scale, 1.0);
             }
+            if (tab.has_bi) {  // ordinary.rs:146-163: the dense-output stages, from the step's start
+                for (int i = 0; i < tab.I - S; ++i) {
+                    State ys = y;
+                    for (int j = 0; j < S + i; ++j) add_scaled(ys, tab.a[S + i][j] * h, k[j]);
+                    ode.diff(t + tab.c[S + i] * h, ys, k[S + i]);
+                }
+                fevals += tab.I - S;
+            }
             t += h;
             y = y_high;
-            ode.diff(t, y, dydt);
-            fevals += 1;
+            if (tab.fsal) {  // ordinary.rs:171-180
+                dydt = k[S - 1];
+            } else {
+                ode.diff(t, y, dydt);
+                fevals += 1;
+            }
         } else {
             status = Status::RejectedStep;
             stiffness_counter += 1;
@@ -1286,8 +1343,20 @@ struct AdaptiveRK : Interpolator {
         return true;
     }
 
-    // adaptive/ordinary.rs:236-290 without `bi` -> cubic Hermite (src/interpolate.rs:40-60)
+    // adaptive/ordinary.rs:236-290: with `bi`, Horner in s per stage and y_prev + sum (cont_i
+    // h_prev) k_i; without, cubic Hermite (src/interpolate.rs:40-60)
     State interpolate(double t_interp) override {
+        if (tab.has_bi) {
+            const double s = (t_interp - t_prev) / h_prev;
+            State out = y_prev;
+            for (int i = 0; i < tab.I; ++i) {
+                double ci = tab.bi[i][tab.order - 1];
+                for (int j = tab.order - 2; j >= 0; --j) ci = ci * s + tab.bi[i][j];
+                ci *= s;
+                add_scaled(out, ci * h_prev, k[i]);
+            }
+            return out;
+        }
         double t0 = t_prev, t1 = t;
         double hh = t1 - t0;
         double s = (t_interp - t0) / hh;
@@ -1503,9 +1572,9 @@ inline Result solve_one(int method, const Ode& ode, double t0, double tf, const 
         s.set = set;
         return solve_ode(s, ode, t0, tf, y0, t_eval, cross, event);
     }
-    if (method == DEGPU_RKF45 || method == DEGPU_CASH_KARP) {
+    if (method >= DEGPU_RKF45) {
         AdaptiveRK s;
-        s.tab = method == DEGPU_RKF45 ? tableau_rkf45() : tableau_cash_karp();
+        s.tab = tableau_for_method(method);
         s.set = set;
         s.math = math;
         return solve_ode(s, ode, t0, tf, y0, t_eval, cross, event);

@@ -71,6 +71,12 @@ int main() {
         std::printf("event\n");
         return 10;
     }
+    // tests/ode/accuracy.rs:395-422 with Verner's RKV989e at its defaults
+    auto vr = IVP::ode(System::harmonic(1.0), 0.0, 10.0, {1.0, 0.0}).method(ExplicitRungeKutta::rkv989e()).solve();
+    if (!vr.ok() || std::fabs(vr.value().y.back()[0] - (-0.83907153)) >= 1e-3) {
+        std::printf("verner\n");
+        return 11;
+    }
     std::printf("ok\n");
     return 0;
 }

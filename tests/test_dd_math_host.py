@@ -29,7 +29,7 @@ def H():
     return h
 
 
-@pytest.mark.parametrize("y", [0.2, -0.2, 0.125, -0.125])
+@pytest.mark.parametrize("y", [0.2, -0.2, 0.125, -0.125, 1 / 6, -1 / 6, 1 / 7, -1 / 7, 1 / 9, -1 / 9])
 def test_pow_ctrl_correctly_rounded(H, y):
     rng = np.random.default_rng(11)
     n = 200_000
@@ -45,7 +45,7 @@ def test_pow_ctrl_correctly_rounded(H, y):
 
 def test_pow_ctrl_special_values(H):
     x = np.array([0.0, np.inf, 1.0, np.nan, 5e-324, 1.7976931348623157e308])
-    for y in (0.2, -0.2, 0.125, -0.125):
+    for y in (0.2, -0.2, 0.125, -0.125, 1 / 6, -1 / 6, 1 / 7, -1 / 7, 1 / 9, -1 / 9):
         out = np.empty(len(x))
         H.degpu_host_pow_ctrl(O.p(x), y, O.p(out), len(x))
         ref = np.array([O.lib().oracle_cr_pow(v, y) for v in x])

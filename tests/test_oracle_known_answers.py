@@ -56,8 +56,42 @@ def test_accuracy_known_answers(case, math_mode):
             assert abs(o["y_final"][c, 0] - e) < tol, (name, method, c, o["y_final"][c, 0], e)
 
 
+VERNER = [abi.RKV655E, abi.RKV766E, abi.RKV767E, abi.RKV877E, abi.RKV878E, abi.RKV988E, abi.RKV989E]
+# tests/ode/accuracy.rs: the Verner pairs at their defaults (rtol = atol = 1e-6), one tolerance per
+# system for all of them (accuracy.rs:124-151, 233-260, 342-369, 451-478, 560-587). RKV656e is not
+# in the crate's tests; it is held to the same tolerances.
+VERNER_CASES = [
+    ("exp+", R["EXP_GROWTH"], [1.0], 0.0, 10.0, [1.0], [22026.46579479], 1e-1),
+    ("exp-", R["EXP_GROWTH"], [1.0], 0.0, -10.0, [22026.46579479], [1.0], 1e-2),
+    ("linear", R["LINEAR"], [1.0, 1.0], 0.0, 10.0, [1.0], [44051.93158958], 1e1),
+    ("harmonic", R["HARMONIC"], [1.0], 0.0, 10.0, [1.0, 0.0], [-0.83907153, 0.54402111], 1e-3),
+    ("logistic", R["LOGISTIC"], [1.0, 10.0], 0.0, 10.0, [0.1], [9.95525518], 1e-3),
+]
+
+
+@pytest.mark.parametrize("method", VERNER + [abi.RKV656E])
+@pytest.mark.parametrize("case", VERNER_CASES, ids=[c[0] for c in VERNER_CASES])
+def test_verner_accuracy_known_answers(case, method):
+    name, rhs, p, t0, tf, y0, expected, tol = case
+    o = solve1(rhs, len(y0), p, t0, tf, y0, method)
+    assert o["status"][0] == abi.COMPLETE
+    for c, e in enumerate(expected):
+        assert abs(o["y_final"][c, 0] - e) < tol, (name, method, c, o["y_final"][c, 0], e)
+
+
+def test_verner_counters():
+    # adaptive/ordinary.rs: S - 1 stages per attempt, I - S dense-output stages and (without FSAL)
+    # one derivative per acceptance, k0 plus the doubly counted h_init pair at init
+    for method, S, I, fsal in [(abi.RKV655E, 9, 10, True), (abi.RKV656E, 9, 12, True), (abi.RKV766E, 10, 13, False),
+                               (abi.RKV989E, 16, 26, False)]:
+        o = solve1(R["HARMONIC"], 2, [1.0], 0.0, 10.0, [1.0, 0.0], method)
+        acc, rej, fe = o["accepted"][0], o["rejected"][0], o["fevals"][0]
+        assert fe == 5 + (S - 1) * (acc + rej) + (I - S) * acc + (0 if fsal else acc), (method, fe)
+
+
 @pytest.mark.parametrize("method,h0", [(abi.DOP853, 0.0), (abi.DOPRI5, 0.0), (abi.RK4, 0.01), (abi.RKF45, 0.0),
-                                       (abi.CASH_KARP, 0.0)])
+                                       (abi.CASH_KARP, 0.0), (abi.RKV655E, 0.0), (abi.RKV877E, 0.0),
+                                       (abi.RKV988E, 0.0)])
 def test_interpolation_known_answer(method, h0):
     # tests/ode/interpolation.rs:14-87: t_eval [0.5, 1.0, 1.69] on exp growth, |y(0.5) - e^0.5| < 1e-3
     o = solve1(R["EXP_GROWTH"], 1, [1.0], 0.0, 2.0, [1.0], method, h0=h0, t_eval=[0.5, 1.0, 1.69])
