@@ -239,6 +239,8 @@ def _oracle_solve(e, method, threads, math_mode=0):
 
 # the hyperplane workload's plane: pos = (y0, y1) through (0.1, -0.2) with normal (1, 1)
 PLANE = ([0, 1], [0.1, -0.2], [1.0, 1.0])
+# the event workload: g = y0 - 0.2 (linear), terminal after the third event
+EVENT = dict(kind=0, components=[0], weights=[1.0], t_weight=0.0, offset=-0.2, terminate=3)
 
 
 def run_crossing(args, torch, dev, lib):
@@ -248,6 +250,7 @@ def run_crossing(args, torch, dev, lib):
     (the plane of PLANE); up to 8 points kept per instance; FP64 parity and mixed; CPU baseline =
     the oracle's CrossingSolout on a sample."""
     plane = args.workload == "hyperplane"
+    event = args.workload == "event"
     n = args.n
     e = W.config1(n=n)
     T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
@@ -267,6 +270,9 @@ def run_crossing(args, torch, dev, lib):
     if plane:
         cr = abi.make_hyperplane(*PLANE, abi.CROSS_BOTH, mp)
         fn = lib.degpu_solve_ensemble_hyperplane
+    elif event:
+        cr = abi.make_event(max_points=mp, **EVENT)
+        fn = lib.degpu_solve_ensemble_event
     else:
         cr = abi.Crossing(component=0, direction=abi.CROSS_BOTH, max_points=mp, threshold=0.0)
         fn = lib.degpu_solve_ensemble_crossing
@@ -296,18 +302,78 @@ def run_crossing(args, torch, dev, lib):
     t = time.perf_counter()
     if plane:
         O.solve_hyperplane(b, cfg, *PLANE, abi.CROSS_BOTH, mp, threads=threads, math_mode=0)
+    elif event:
+        O.solve_event(b, cfg, abi.make_event(max_points=mp, **EVENT), threads=threads, math_mode=0)
     else:
         O.solve_crossing(b, cfg, 0, 0.0, abi.CROSS_BOTH, mp, threads=threads, math_mode=0)
     dt = time.perf_counter() - t
     what = (f"hyperplane_crossing(point {PLANE[1]}, normal {PLANE[2]}, components {PLANE[0]}, Both)" if plane
-            else "crossing(0, 0.0, Both)")
-    line = {"metric": f"IVP solves/sec with {'hyperplane ' if plane else ''}crossing detection (uneven ensemble, DOPRI5)",
+            else "event(y0 - 0.2, Both, terminate after 3)" if event else "crossing(0, 0.0, Both)")
+    kind = "hyperplane crossing" if plane else "event" if event else "crossing"
+    line = {"metric": f"IVP solves/sec with {kind} detection (uneven ensemble, DOPRI5)",
             "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
             "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 parity beside)", "data": "synthetic (seeded SplitMix64)",
             "config": {"workload": f"uneven ensemble {n} instances, {what}, {mp} points kept"},
             "variants": res,
             "cpu_baseline": {"value": s_n / dt, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"first {s_n} instances (host libm)"}}
+    print(json.dumps(line))
+
+
+def run_bvp(args, torch, dev, lib):
+    """Boundary value problems by shooting: an ensemble of pipe heat-transfer BVPs
+    (T'' = b^2 (T - T_amb), T(0) = 373.15, T'(10) = 0; b ~ U[0.05, 0.4], T_amb ~ U[280, 300];
+    the crate's BVP test system) solved by multiple shooting with 5 segments (DOP853, rtol 1e-10,
+    atol 1e-12, tolerance 1e-8) through degpu_solve_bvp_host: every IVP of a Newton iteration of
+    the whole batch is one ensemble solve; host arrays in and out (end to end). FP64 parity and
+    FP64 fast; CPU baseline = the oracle's MultipleShooting on a sample."""
+    import degpu
+
+    n = args.bvp_n
+    rng = np.random.default_rng(2024)
+    beta, amb = rng.uniform(0.05, 0.4, n), rng.uniform(280.0, 300.0, n)
+    guess = np.stack([np.full(n, 373.15), rng.uniform(-10.0, 0.0, n)])
+    params = np.stack([beta, amb])
+    bvp = abi.make_bvp([(0, 0, 373.15), (1, 1, 0.0)], abi.BVP_MULTIPLE, 5, tolerance=1e-8)
+    res = {}
+    for name, prec in (("fp64-fast", abi.FP64_FAST), ("fp64-parity", abi.FP64_PARITY)):
+        m = degpu.ExplicitRungeKutta(abi.DOP853)
+        m.cfg.precision, m.cfg.max_steps = prec, 10_000_000
+        run = lambda: degpu.solve_bvp(abi.RHS["PIPE_HEAT"], 2, 0.0, 10.0, guess, params, 1e-10, 1e-12, m, bvp)
+        r = run()  # warm-up
+        t = time.perf_counter()
+        reps = max(1, args.steps)
+        for _ in range(reps):
+            r = run()
+        dt = (time.perf_counter() - t) / reps
+        ok = float(np.mean(r.solution.status == abi.COMPLETE))
+        res[name] = {"bvp_per_s": n / dt, "ms": dt * 1e3, "complete": ok,
+                     "newton_iterations_mean": float(np.mean(r.iterations)),
+                     # launched: the initial-node shot, 5 segment + 10 column shots per pass
+                     # (iterations + the converging pass), the final shot
+                     "ivp_solves": int(np.sum(2 + (r.iterations.astype(np.int64) + 1) * 15))}
+        print(json.dumps({"bvp_variant": name, **res[name]}), flush=True)
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib as O
+
+    s_n = min(args.bvp_cpu_sample, n)
+    threads = os.cpu_count() or 1
+    b = O.Batch(abi.RHS["PIPE_HEAT"], 2, 2, np.zeros(s_n), np.full(s_n, 10.0), guess[:, :s_n], params[:, :s_n],
+                np.full(s_n, 1e-10), np.full(s_n, 1e-12))
+    cfg = abi.default_cfg(abi.DOP853)
+    cfg.max_steps = 10_000_000
+    t = time.perf_counter()
+    O.solve_bvp(b, cfg, bvp, threads=threads, math_mode=0)
+    dt = time.perf_counter() - t
+    line = {"metric": "BVP solves/sec, multiple shooting (pipe heat transfer ensemble, DOP853)",
+            "value": res["fp64-fast"]["bvp_per_s"], "unit": "BVP/s", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": True, "dtype": "f64 (parity beside)", "data": "synthetic (seeded numpy)",
+            "config": {"workload": f"{n} pipe heat-transfer BVPs, multiple shooting 5 segments, tolerance 1e-8"},
+            "variants": res,
+            "e2e": {"value": res["fp64-fast"]["bvp_per_s"], "unit": "BVP/s",
+                    "note": "host arrays in and out through degpu_solve_bvp_host"},
+            "cpu_baseline": {"value": s_n / dt, "unit": "BVP/s", "cores": threads, "kind": "port",
+                             "sample": f"first {s_n} BVPs (host libm)"}}
     print(json.dumps(line))
 
 
@@ -658,8 +724,10 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--workload", default="uneven",
                     choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing", "hyperplane",
-                             "adaptive"],
+                             "event", "adaptive", "bvp"],
                     help="uneven = the headline 1M-instance ensemble; the others print their own line")
+    ap.add_argument("--bvp-n", type=int, default=65536)
+    ap.add_argument("--bvp-cpu-sample", type=int, default=2000)
     ap.add_argument("--fpu-n", type=int, default=131072)
     ap.add_argument("--fpu-cpu-sample", type=int, default=200)
     ap.add_argument("--fpu-mixed-max-steps", type=int, default=200_000)
@@ -691,7 +759,8 @@ def main():
     if args.workload != "uneven":
         if rank == 0:
             {"lorenz4096": run_lorenz4096, "fpu": run_fpu, "gray-scott": run_gray_scott,
-             "serving": run_serving, "crossing": run_crossing, "hyperplane": run_crossing,
+             "serving": run_serving, "crossing": run_crossing, "hyperplane": run_crossing, "event": run_crossing,
+             "bvp": run_bvp,
              "adaptive": run_adaptive}[args.workload](args, torch, dev, lib)
         return
 

@@ -151,6 +151,7 @@ static void builtin_info(int id, int& dim, int& np) {
         case DEGPU_RHS_HIRES: dim = 8; np = 0; return;
         case DEGPU_RHS_BRUSSELATOR: dim = 2; np = 2; return;
         case DEGPU_RHS_CR3BP: dim = 6; np = 1; return;
+        case DEGPU_RHS_PIPE_HEAT: dim = 2; np = 2; return;
         default: dim = 0; np = -1; return;
     }
 }

@@ -1,5 +1,5 @@
-// inst_embedded.cu — the Adaptive ERK family (RKF45, Cash-Karp), FP64 fast and mixed arithmetic,
-// one system per thread.
+// inst_embedded.cu — the Adaptive ERK family (RKF45, Cash-Karp), and DOPRI5 / DOP853 on the
+// harmonic and pipe-heat systems, FP64 fast and mixed arithmetic, one system per thread.
 #include "registry.cuh"
 
 namespace degpu {
@@ -10,7 +10,18 @@ static void reg_pair() {
     register_thread_variant<TabCashKarp, Rhs, P>();
 }
 
+// DOPRI5 / DOP853 on the linear test systems the shooting methods are tested with.
+template <class Rhs, class P>
+static void reg_dp() {
+    register_thread_variant<TabDopri5, Rhs, P>();
+    register_thread_variant<TabDop853, Rhs, P>();
+}
+
 void register_embedded_fast_mixed() {
+    reg_dp<RhsHarmonic, PrecFast>();
+    reg_dp<RhsPipeHeat, PrecFast>();
+    reg_dp<RhsHarmonic, PrecMixed>();
+    reg_dp<RhsPipeHeat, PrecMixed>();
     reg_pair<RhsVanDerPol, PrecFast>();
     reg_pair<RhsPendulum, PrecFast>();
     reg_pair<RhsLorenz, PrecFast>();

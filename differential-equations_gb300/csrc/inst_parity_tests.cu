@@ -23,5 +23,6 @@ void register_parity_tests() {
     reg_all<RhsHires>();
     reg_all<RhsBrusselator>();
     reg_all<RhsCr3bp>();
+    reg_all<RhsPipeHeat>();
 }
 }  // namespace degpu

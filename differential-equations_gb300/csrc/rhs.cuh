@@ -271,6 +271,18 @@ struct RhsBrusselator : BuiltinRhs {
     }
 };
 
+// tests/bvp/systems.rs:25-57 (pipe heat transfer): heat_loss_rate.powi(2) -> b*b.
+struct RhsPipeHeat : BuiltinRhs {
+    static constexpr int ID = 13, D = 2, NP = 2;
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
+        using S = typename P::S;
+        const S b = (S)p[0], amb = (S)p[1];
+        dydt[0] = y[1];
+        dydt[1] = (b * b) * (y[0] - amb);
+    }
+};
+
 // tests/ode/systems.rs:122-153; powi(2) -> x*x, powi(3) -> x*(x*x) as LLVM expands them.
 struct RhsCr3bp : BuiltinRhs {
     static constexpr int ID = 12, D = 6, NP = 1;

@@ -20,10 +20,11 @@ from . import abi
 
 __all__ = ["abi", "ExplicitRungeKutta", "IVP", "System", "EnsembleResult", "solve_ensemble", "DegpuError",
            "Solution", "set_mixed_min_rtol", "mixed_min_rtol", "solve_ensemble_crossing", "solve_ensemble_hyperplane",
-           "solve_ensemble_event", "write_csv", "rust_debug_f64"]
+           "solve_ensemble_event", "solve_bvp", "BVP", "Shooting", "BvpResult", "write_csv", "rust_debug_f64"]
 
 STATUS_NAMES = {abi.COMPLETE: "Complete", abi.ERR_BAD_INPUT: "BadInput", abi.ERR_MAX_STEPS: "MaxSteps",
-                abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness", abi.INTERRUPTED: "Interrupted"}
+                abi.ERR_STEP_SIZE: "StepSize", abi.ERR_STIFFNESS: "Stiffness", abi.INTERRUPTED: "Interrupted",
+                abi.ERR_LINEAR_ALGEBRA: "LinearAlgebra"}
 
 
 class DegpuError(RuntimeError):
@@ -190,6 +191,11 @@ class System:
         return System(abi.RHS["BRUSSELATOR"], [a, b], 2)
 
     @staticmethod
+    def pipe_heat(heat_loss_rate, ambient):
+        """T'' = b^2 (T - T_amb) as (T, T') (tests/bvp/systems.rs:25-57)."""
+        return System(abi.RHS["PIPE_HEAT"], [heat_loss_rate, ambient], 2)
+
+    @staticmethod
     def cr3bp(mu):
         """Circular restricted three-body problem, state (x, y, z, vx, vy, vz)."""
         return System(abi.RHS["CR3BP"], [mu], 6)
@@ -270,6 +276,119 @@ def solve_ensemble_event(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, 
     instance's status INTERRUPTED."""
     return _solve_crossing_host("degpu_solve_ensemble_event_host", "event", event, rhs_id, dim, t0, tf, y0, params,
                                 rtol, atol, method, event.max_points, family, n_params, t_eval)
+
+
+@dataclass
+class BvpResult:
+    solution: EnsembleResult  # the final IVP from the converged y(t0): y_final = y(tf), dense
+    y_a: np.ndarray           # [dim, n] converged initial states (NaN where a solve failed)
+    iterations: np.ndarray    # [n] Newton iterations
+    jacobian: np.ndarray      # [n] Jacobian columns formed
+
+
+def solve_bvp(rhs_id: int, dim: int, t0, tf, y_guess, params, rtol, atol, method: ExplicitRungeKutta,
+              bvp: "abi.Bvp", t_eval=None, n_params: Optional[int] = None) -> BvpResult:
+    """Solve n two-point boundary value problems by shooting (degpu_solve_bvp_host): the crate's
+    `BVP::ode(&problem, t0, tf, y_guess).method(Shooting::single(erk) | Shooting::multiple(erk))`
+    with the boundary rows of `bvp` (abi.make_bvp).  Every IVP of a Newton iteration of the whole
+    batch is one ensemble solve on the device."""
+    lib = abi.load()
+    y_guess = np.asarray(y_guess, dtype=np.float64)
+    n = y_guess.shape[1]
+    bc = lambda v: _f64(np.broadcast_to(np.asarray(v, dtype=np.float64), (n,)).copy())
+    t0, tf, rtol, atol = bc(t0), bc(tf), bc(rtol), bc(atol)
+    y_guess = _f64(y_guess)
+    params = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, n)) if params is not None \
+        and np.size(params) else np.zeros((1, n))
+    np_ = n_params if n_params is not None else params.shape[0]
+    te = None if t_eval is None or len(t_eval) == 0 else _f64(np.asarray(t_eval, dtype=np.float64))
+    ne = 0 if te is None else len(te)
+    out = dict(y_final=np.empty((dim, n)), t_final=np.empty(n), dense=np.empty((ne, dim, n)) if ne else None,
+               accepted=np.empty(n, np.int64), rejected=np.empty(n, np.int64), fevals=np.empty(n, np.int64),
+               status=np.empty(n, np.int32))
+    ya, it, jac = np.empty((dim, n)), np.empty(n, np.int32), np.empty(n, np.int64)
+    prob = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=np_)
+    bi = abi.BatchIn(n=n, t0=abi.ptr(t0), tf=abi.ptr(tf), y0=abi.ptr(y_guess), params=abi.ptr(params),
+                     rtol=abi.ptr(rtol), atol=abi.ptr(atol), t_eval=abi.ptr(te), n_eval=ne)
+    bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]), dense=abi.ptr(out["dense"]),
+                      accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
+                      fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))
+    vo = abi.BvpOut(y_a=abi.ptr(ya), iterations=abi.ptr(it, C.c_int32), jacobian=abi.ptr(jac, C.c_int64))
+    rc = lib.degpu_solve_bvp_host(C.byref(prob), C.byref(method.cfg), C.byref(bi), C.byref(bvp), C.byref(bo),
+                                  C.byref(vo))
+    if rc != abi.OK:
+        raise DegpuError(rc, "degpu_solve_bvp_host")
+    return BvpResult(EnsembleResult(**out), ya, it, jac)
+
+
+class Shooting:
+    """The crate's shooting methods (src/methods/bvp/shooting): Shooting.single(erk) and
+    Shooting.multiple(erk).segments(m), with .tolerance() and .max_iterations()."""
+
+    def __init__(self, erk: ExplicitRungeKutta, method: int):
+        self.erk, self.method_id, self._segments, self._tol, self._iters = erk, method, 4, 1e-6, 100
+
+    @classmethod
+    def single(cls, erk: ExplicitRungeKutta):
+        return cls(erk, abi.BVP_SINGLE)
+
+    @classmethod
+    def multiple(cls, erk: ExplicitRungeKutta):
+        return cls(erk, abi.BVP_MULTIPLE)
+
+    def segments(self, m: int):
+        self._segments = m
+        return self
+
+    def tolerance(self, tol: float):
+        self._tol = tol
+        return self
+
+    def max_iterations(self, k: int):
+        self._iters = k
+        return self
+
+
+class BVP:
+    """Single-instance builder with the crate's shape (src/bvp.rs): BVP.ode(system, t0, tf,
+    y_guess, boundary_rows).method(Shooting...).t_eval(pts).solve() -> Solution whose first point
+    is y(t0) and last y(tf).  boundary_rows: (side, component, value) with r = y_side[c] - value."""
+
+    def __init__(self, system: System, t0, tf, y_guess, rows):
+        self.system, self.t0, self.tf = system, t0, tf
+        self.y_guess = np.asarray(y_guess, dtype=np.float64).reshape(-1)
+        self.rows = list(rows)
+        self._method: Optional[Shooting] = None
+        self._t_eval = None
+
+    @classmethod
+    def ode(cls, system: System, t0, tf, y_guess, rows):
+        return cls(system, t0, tf, y_guess, rows)
+
+    def method(self, m: Shooting):
+        self._method = m
+        return self
+
+    def t_eval(self, pts):
+        self._t_eval = list(pts)
+        return self
+
+    def solve(self) -> Solution:
+        m = self._method or Shooting.single(ExplicitRungeKutta.dop853())
+        d = len(self.y_guess)
+        bvp = abi.make_bvp(self.rows, m.method_id, m._segments, m._iters, m._tol)
+        r = solve_bvp(self.system.rhs_id, d, [self.t0], [self.tf], self.y_guess.reshape(d, 1),
+                      np.asarray(self.system.params, dtype=np.float64).reshape(-1, 1), [m.erk._rtol], [m.erk._atol],
+                      m.erk, bvp, t_eval=self._t_eval)
+        s = r.solution
+        st = STATUS_NAMES.get(int(s.status[0]), str(int(s.status[0])))
+        if self._t_eval is not None:
+            ts = [float(v) for i, v in enumerate(self._t_eval) if not np.isnan(s.dense[i, 0, 0])]
+            ys = [s.dense[i, :, 0].copy() for i in range(len(self._t_eval)) if not np.isnan(s.dense[i, 0, 0])]
+        else:
+            ts = [float(self.t0), float(s.t_final[0])]
+            ys = [r.y_a[:, 0].copy(), s.y_final[:, 0].copy()]
+        return Solution(ts, ys, st, int(s.accepted[0]), int(s.rejected[0]), int(s.fevals[0]))
 
 
 def set_mixed_min_rtol(method: int, min_rtol: float) -> None:

@@ -25,11 +25,11 @@ KERNEL_AUTO, KERNEL_THREAD, KERNEL_WARP, KERNEL_PERSISTENT = 0, 1, 2, 3
 # degpu_dense_mode
 DENSE_REFERENCE, DENSE_HAIRER = 0, 1
 # degpu_instance_status
-COMPLETE, ERR_BAD_INPUT, ERR_MAX_STEPS, ERR_STEP_SIZE, ERR_STIFFNESS, INTERRUPTED = range(6)
+COMPLETE, ERR_BAD_INPUT, ERR_MAX_STEPS, ERR_STEP_SIZE, ERR_STIFFNESS, INTERRUPTED, ERR_LINEAR_ALGEBRA = range(7)
 # degpu_rhs_id
 RHS = dict(
     LORENZ=1, VAN_DER_POL=2, PENDULUM=3, FPU_BETA=4, EXP_GROWTH=5, LINEAR=6, HARMONIC=7,
-    LOGISTIC=8, ROBERTSON=9, HIRES=10, BRUSSELATOR=11, CR3BP=12,
+    LOGISTIC=8, ROBERTSON=9, HIRES=10, BRUSSELATOR=11, CR3BP=12, PIPE_HEAT=13,
 )
 RHS_NVRTC_BASE = 1000
 
@@ -109,6 +109,32 @@ def make_event(kind=EVENT_LINEAR, components=(), weights=None, t_weight=0.0, off
     return ev
 
 
+BVP_SINGLE, BVP_MULTIPLE = 0, 1
+BVP_MAX_UNKNOWNS = 64
+
+
+class Bvp(C.Structure):
+    _fields_ = [("method", C.c_int32), ("segments", C.c_int32), ("max_iterations", C.c_int32),
+                ("reserved", C.c_int32), ("tolerance", C.c_double), ("side", C.c_int32 * HYPERPLANE_MAX_DIM),
+                ("component", C.c_int32 * HYPERPLANE_MAX_DIM), ("value", C.c_double * HYPERPLANE_MAX_DIM)]
+
+
+class BvpOut(C.Structure):
+    _fields_ = [("y_a", DP), ("iterations", I32P), ("jacobian", I64P)]
+
+
+def make_bvp(rows, method=BVP_SINGLE, segments=4, max_iterations=100, tolerance=1e-6) -> Bvp:
+    """degpu_bvp from residual rows (side, component, value): r_i = y_side[component] - value,
+    side 0 = y(t0), 1 = y(tf); the crate's shooting defaults (100 iterations, tolerance 1e-6,
+    4 segments)."""
+    if not 1 <= len(rows) <= HYPERPLANE_MAX_DIM:
+        raise ValueError("bvp: one residual row per state component (at most 8)")
+    b = Bvp(method=method, segments=segments, max_iterations=max_iterations, tolerance=tolerance)
+    for i, (side, comp, value) in enumerate(rows):
+        b.side[i], b.component[i], b.value[i] = int(side), int(comp), float(value)
+    return b
+
+
 def make_hyperplane(components, point, normal, direction=CROSS_BOTH, max_points=16) -> Hyperplane:
     """degpu_hyperplane from sequences: pos[j] = y[components[j]], plane through `point` with
     `normal` (scaled to unit length by the library)."""
@@ -169,6 +195,8 @@ SIGNATURES = {
                                              C.c_void_p]),
     "degpu_solve_ensemble_event_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
                                                   C.POINTER(Event), C.POINTER(BatchOut), C.POINTER(CrossingOut)]),
+    "degpu_solve_bvp_host": (C.c_int, [C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn), C.POINTER(Bvp),
+                                       C.POINTER(BatchOut), C.POINTER(BvpOut)]),
     "degpu_eval_rhs": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP,
                                  C.c_void_p]),
     "degpu_register_rhs_nvrtc": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, I32P, C.c_char_p,

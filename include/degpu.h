@@ -105,8 +105,10 @@ typedef enum {
     DEGPU_ERR_MAX_STEPS = 2,   /* Error::MaxSteps  (dormandprince/ordinary.rs:82-92, fixed/ordinary.rs:64-75) */
     DEGPU_ERR_STEP_SIZE = 3,   /* Error::StepSize  (dormandprince/ordinary.rs:70-80)                   */
     DEGPU_ERR_STIFFNESS = 4,   /* Error::Stiffness (dormandprince/ordinary.rs:176-186)                 */
-    DEGPU_INTERRUPTED = 5      /* Ok(Solution) with Status::Interrupted: a terminal event stopped the
+    DEGPU_INTERRUPTED = 5,     /* Ok(Solution) with Status::Interrupted: a terminal event stopped the
                                   solve (src/ode/solve_ivp.rs:254-259)                              */
+    DEGPU_ERR_LINEAR_ALGEBRA = 6 /* Error::LinearAlgebra: a singular shooting Jacobian
+                                    (src/methods/bvp/shooting/single.rs, lu_decomp)                 */
 } degpu_instance_status;
 
 /* Built-in right-hand sides (CUDA __device__ twins of `ODE::diff`, src/ode/ode.rs:20-44).
@@ -124,6 +126,7 @@ typedef enum {
     DEGPU_RHS_HIRES = 10,       /* d=8, p=[]                        tests/ode/systems.rs:175-190  */
     DEGPU_RHS_BRUSSELATOR = 11, /* d=2, p=[a, b]                    tests/ode/systems.rs:103-120  */
     DEGPU_RHS_CR3BP = 12,       /* d=6, p=[mu]                      tests/ode/systems.rs:122-153  */
+    DEGPU_RHS_PIPE_HEAT = 13,   /* d=2, p=[heat_loss_rate, ambient] tests/bvp/systems.rs:25-57    */
     DEGPU_RHS_NVRTC_BASE = 1000 /* ids >= this were returned by degpu_register_rhs_nvrtc          */
 } degpu_rhs_id;
 
@@ -343,6 +346,48 @@ degpu_status degpu_solve_ensemble_event(const degpu_problem* problem, const degp
 degpu_status degpu_solve_ensemble_event_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
                                              const degpu_batch_in* in, const degpu_event* event,
                                              degpu_batch_out* out, degpu_crossing_out* event_out);
+
+/* Boundary value problems by shooting: the crate's `BVP::ode(&problem, t0, tf, y_guess)
+ * .method(Shooting::single(erk) | Shooting::multiple(erk).segments(m)).solve()` (src/bvp.rs,
+ * src/methods/bvp/shooting/{single,multiple}.rs) for every instance of a batch. Newton on the
+ * shooting unknowns (the initial state; for multiple shooting the states at the m + 1 mesh nodes
+ * t0 + (tf - t0) i / m) with a forward-difference Jacobian (step sqrt(eps) max(|u_j|, 1)) and the
+ * crate's LU with partial pivoting; it stops when the residual's max norm is <= tolerance, then
+ * solves the IVP from t0 with the converged initial state into the ordinary outputs (y_final =
+ * y(tf), dense = the output times). Every IVP of every Newton iteration of the whole batch is one
+ * ensemble solve on the device.
+ * The boundary residual is r_i = y_side[component_i] - value_i (side 0: y(t0), 1: y(tf)), i < dim:
+ * the form of every boundary function of the crate's tests and examples.
+ * Per-instance status: COMPLETE; the status of a failing IVP; DEGPU_ERR_MAX_STEPS when Newton does
+ * not converge in max_iterations; DEGPU_ERR_LINEAR_ALGEBRA for a singular Jacobian.
+ * Multiple shooting needs one interval [t0, tf] for the whole batch. A DEGPU_MIXED configuration
+ * runs its shots in DEGPU_FP64_FAST arithmetic: the Jacobian's perturbation (~1.5e-8 relative) is
+ * below FP32 resolution. */
+#define DEGPU_BVP_MAX_UNKNOWNS 64
+typedef enum { DEGPU_BVP_SINGLE = 0, DEGPU_BVP_MULTIPLE = 1 } degpu_bvp_method;
+
+typedef struct {
+    int32_t method;          /* degpu_bvp_method                                               */
+    int32_t segments;        /* multiple shooting: mesh segments m >= 1 (crate default 4)       */
+    int32_t max_iterations;  /* Newton iterations (crate default 100)                          */
+    int32_t reserved;
+    double tolerance;        /* residual max-norm tolerance (crate default 1e-6)                */
+    int32_t side[DEGPU_HYPERPLANE_MAX_DIM];      /* residual row i: 0 = y(t0), 1 = y(tf)       */
+    int32_t component[DEGPU_HYPERPLANE_MAX_DIM]; /* state index of row i                       */
+    double value[DEGPU_HYPERPLANE_MAX_DIM];      /* r_i = y_side[component] - value            */
+} degpu_bvp;
+
+typedef struct {
+    double* y_a;          /* [dim][n] converged initial state (the solution's first point)     */
+    int32_t* iterations;  /* [n] Newton iterations taken (Evals::newton)                        */
+    int64_t* jacobian;    /* [n] Jacobian columns formed (Evals::jacobian)                      */
+} degpu_bvp_out;
+
+/* in->y0 holds the guesses; out->accepted / rejected / fevals receive the totals over every IVP
+ * solved for the instance (the crate's Solution.steps / evals). HOST pointers, synchronous. */
+degpu_status degpu_solve_bvp_host(const degpu_problem* problem, const degpu_method_cfg* cfg,
+                                  const degpu_batch_in* in, const degpu_bvp* bvp, degpu_batch_out* out,
+                                  degpu_bvp_out* bvp_out);
 
 /* One evaluation of a built-in right-hand side for every instance (`ODE::diff`,
  * src/ode/ode.rs:20-44), device pointers: dydt[c*n+i] = f_i(t[i], y_i). */

@@ -10,6 +10,7 @@
 #include <thread>
 
 #include "oracle.hpp"
+#include "oracle_bvp.hpp"
 #include "oracle_mol.hpp"
 
 #if defined(__x86_64__) || defined(__i386__)
@@ -215,6 +216,76 @@ int oracle_solve_ensemble_event(const degpu_problem* pb, const degpu_method_cfg*
     math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
     for_instances(in->n, threads, [&](int64_t i) {
         solve_instance(pb, cfg, in, out, i, math, nullptr, ev->max_points, co, &proto);
+    });
+    return 0;
+}
+
+// Boundary value problems by shooting (SingleShooting / MultipleShooting) for every instance;
+// outputs laid out as degpu_solve_bvp_host's.  Returns 0 on success, 1 on bad input.
+int oracle_solve_bvp(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                     const degpu_bvp* bvp, degpu_batch_out* out, degpu_bvp_out* bo, int threads, int math_mode) {
+    if (!pb || !cfg || !in || !out || !bvp || !bo || in->n < 0 || !out->y_final) return 1;
+    const int dim = pb->dim;
+    if (dim < 1 || dim > DEGPU_HYPERPLANE_MAX_DIM) return 1;
+    BvpSpec spec;
+    spec.method = bvp->method;
+    spec.segments = bvp->segments;
+    spec.max_iterations = bvp->max_iterations;
+    spec.tolerance = bvp->tolerance;
+    for (int i = 0; i < dim; ++i) {
+        if (bvp->side[i] < 0 || bvp->side[i] > 1 || bvp->component[i] < 0 || bvp->component[i] >= dim) return 1;
+        spec.side.push_back(bvp->side[i]);
+        spec.comp.push_back(bvp->component[i]);
+        spec.value.push_back(bvp->value[i]);
+    }
+    Math math;
+    math.mode = math_mode == 0 ? MathMode::Libm : MathMode::CorrectlyRounded;
+    const int64_t n = in->n;
+    std::vector<double> te;
+    if (in->n_eval > 0 && in->t_eval) te.assign(in->t_eval, in->t_eval + in->n_eval);
+    for_instances(n, threads, [&](int64_t i) {
+        int fam_dim, fam_np;
+        builtin_info(pb->rhs_id, fam_dim, fam_np);
+        State guess(dim);
+        for (int c = 0; c < dim; ++c) guess[c] = in->y0[(int64_t)c * n + i];
+        std::vector<double> p(pb->n_params);
+        for (int q = 0; q < pb->n_params; ++q) p[q] = in->params[(int64_t)q * n + i];
+        BuiltinOde ode(pb->rhs_id, dim, p, math);
+        BvpSolver sv{cfg->method, ode, Settings{}, math, cfg->dense_mode == DEGPU_DENSE_HAIRER, BvpResult{}};
+        sv.set.rtol = in->rtol[i];
+        sv.set.atol = in->atol[i];
+        sv.set.h0 = cfg->h0;
+        sv.set.h_min = cfg->h_min;
+        sv.set.h_max = cfg->h_max;
+        sv.set.max_steps = cfg->max_steps;
+        sv.set.safety_factor = cfg->safety_factor;
+        sv.set.min_scale = cfg->min_scale;
+        sv.set.max_scale = cfg->max_scale;
+        const std::vector<double>* tep = te.empty() ? nullptr : &te;
+        if (spec.method == DEGPU_BVP_MULTIPLE)
+            sv.multiple(spec, in->t0[i], in->tf[i], guess, tep);
+        else
+            sv.single(spec, in->t0[i], in->tf[i], guess, tep);
+        const BvpResult& r = sv.out;
+        const Result& f = r.final;
+        for (int c = 0; c < dim; ++c) {
+            out->y_final[(int64_t)c * n + i] = f.y_final.size() == (size_t)dim ? f.y_final[c] : NAN;
+            bo->y_a[(int64_t)c * n + i] = r.status == DEGPU_COMPLETE ? r.y_a[c] : NAN;
+        }
+        if (out->t_final) out->t_final[i] = f.t_final;
+        if (out->accepted) out->accepted[i] = r.accepted;
+        if (out->rejected) out->rejected[i] = r.rejected;
+        if (out->fevals) out->fevals[i] = r.fevals;
+        if (out->status) out->status[i] = r.status;
+        if (bo->iterations) bo->iterations[i] = (int32_t)r.iterations;
+        if (bo->jacobian) bo->jacobian[i] = r.jacobian;
+        if (out->dense && tep) {
+            for (int e = 0; e < in->n_eval; ++e)
+                for (int c = 0; c < dim; ++c) {
+                    const bool have = r.status == DEGPU_COMPLETE && (size_t)e < f.dense.size();
+                    out->dense[((int64_t)e * dim + c) * n + i] = have ? f.dense[e][c] : NAN;
+                }
+        }
     });
     return 0;
 }

@@ -446,6 +446,7 @@ inline void builtin_info(int rhs_id, int& dim, int& np) {
         case DEGPU_RHS_HIRES: dim = 8; np = 0; return;
         case DEGPU_RHS_BRUSSELATOR: dim = 2; np = 2; return;
         case DEGPU_RHS_CR3BP: dim = 6; np = 1; return;
+        case DEGPU_RHS_PIPE_HEAT: dim = 2; np = 2; return;
         default: dim = 0; np = -1; return;
     }
 }
@@ -521,6 +522,12 @@ inline void BuiltinOde::diff(double t, const State& y, State& dydt) const {
             double a = p[0], b = p[1], y1 = y[0], y2 = y[1];
             dydt[0] = a + y1 * y1 * y2 - (b + 1.0) * y1;
             dydt[1] = b * y1 - y1 * y1 * y2;
+            return;
+        }
+        case DEGPU_RHS_PIPE_HEAT: {  // tests/bvp/systems.rs:45-50; powi(2) -> b*b
+            const double b = p[0], amb = p[1];
+            dydt[0] = y[1];
+            dydt[1] = (b * b) * (y[0] - amb);
             return;
         }
         case DEGPU_RHS_CR3BP: {                                          // systems.rs:131-152

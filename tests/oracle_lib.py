@@ -52,6 +52,10 @@ def lib():
                                                   C.POINTER(abi.BatchOut), C.POINTER(abi.CrossingOut), C.c_int,
                                                   C.c_int]
         L.oracle_solve_ensemble_event.restype = C.c_int
+        L.oracle_solve_bvp.argtypes = [C.POINTER(abi.Problem), C.POINTER(abi.MethodCfg), C.POINTER(abi.BatchIn),
+                                       C.POINTER(abi.Bvp), C.POINTER(abi.BatchOut), C.POINTER(abi.BvpOut), C.c_int,
+                                       C.c_int]
+        L.oracle_solve_bvp.restype = C.c_int
         L.oracle_eval_rhs.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.c_int32, DP, DP, DP, DP, C.c_int]
         for nm in ("oracle_cr_pow", "oracle_libm_pow"):
             getattr(L, nm).argtypes = [C.c_double, C.c_double]
@@ -187,4 +191,22 @@ def solve_event(batch: Batch, cfg, event, threads=None, math_mode=1):
                                            math_mode)
     assert rc == 0
     out.update(cross_t=ct, cross_y=cy, cross_count=cc)
+    return out
+
+
+def solve_bvp(batch: Batch, cfg, bvp, threads=None, math_mode=1):
+    """Oracle shooting solve of every instance (the batch's y0 are the guesses): the ordinary
+    outputs of the final IVP (y_final = y(tf), dense at the batch's output times), totals in
+    accepted / rejected / fevals, plus y_a [dim, n], iterations [n] and jacobian [n]."""
+    out = batch.new_outputs()
+    n, dim = batch.n, batch.problem.dim
+    ya = np.empty((dim, n))
+    it = np.empty(n, np.int32)
+    jac = np.empty(n, np.int64)
+    bo = abi.BvpOut(y_a=p(ya), iterations=abi.ptr(it, C.c_int32), jacobian=abi.ptr(jac, C.c_int64))
+    threads = threads or os.cpu_count() or 1
+    rc = lib().oracle_solve_bvp(C.byref(batch.problem), C.byref(cfg), C.byref(batch.batch_in()), C.byref(bvp),
+                                C.byref(Batch.batch_out(out)), C.byref(bo), threads, math_mode)
+    assert rc == 0
+    out.update(y_a=ya, iterations=it, jacobian=jac)
     return out
