@@ -18,38 +18,47 @@
 
 namespace {
 
-struct Shot {
-    double t0, tf;
-    std::vector<double> y0;
-};
-
-// One ensemble solve of a list of shots sharing parameters per instance.
+// One ensemble solve of a list of shots (t0, tf, y0), each owned by an instance of the batch whose
+// parameters and tolerances it uses. Shots are stored flat (y0 row-major per shot) and transposed
+// into the ensemble's structure-of-arrays layout when the batch runs.
 struct ShotBatch {
-    std::vector<Shot> shots;
-    std::vector<int64_t> owner;  // instance of each shot
+    int dim = 0;
+    std::vector<double> t0, tf, y0;
+    std::vector<int64_t> owner;
     // results
     std::vector<double> y_final, t_final, dense;
     std::vector<int64_t> accepted, rejected, fevals;
     std::vector<int32_t> status;
 
-    int64_t add(int64_t inst, double t0, double tf, const std::vector<double>& y0) {
-        shots.push_back({t0, tf, y0});
+    explicit ShotBatch(int d) : dim(d) {}
+    int64_t size() const { return (int64_t)owner.size(); }
+    // a shot from y; component pc (if >= 0) replaced by pv
+    int64_t add(int64_t inst, double a, double b, const double* y, int pc = -1, double pv = 0.0) {
+        const int64_t k = size();
+        t0.push_back(a);
+        tf.push_back(b);
+        y0.insert(y0.end(), y, y + dim);
+        if (pc >= 0) y0[(size_t)k * dim + pc] = pv;
         owner.push_back(inst);
-        return (int64_t)shots.size() - 1;
+        return k;
+    }
+    const double* start(int64_t k) const { return &y0[(size_t)k * dim]; }
+    double end(int64_t k, int c) const { return y_final[(size_t)c * owner.size() + k]; }
+    std::vector<double> yf(int64_t k) const {
+        std::vector<double> v(dim);
+        for (int c = 0; c < dim; ++c) v[c] = end(k, c);
+        return v;
     }
 
     degpu_status run(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                      const std::vector<double>* t_eval) {
-        const int64_t m = (int64_t)shots.size();
-        const int dim = pb->dim, np = pb->n_params;
+        const int64_t m = size();
+        const int np = pb->n_params;
         if (m == 0) return DEGPU_OK;
-        std::vector<double> t0(m), tf(m), y0((size_t)dim * m), params((size_t)(np > 0 ? np : 1) * m), rtol(m),
-            atol(m);
+        std::vector<double> ys((size_t)dim * m), params((size_t)(np > 0 ? np : 1) * m), rtol(m), atol(m);
         for (int64_t k = 0; k < m; ++k) {
             const int64_t i = owner[k];
-            t0[k] = shots[k].t0;
-            tf[k] = shots[k].tf;
-            for (int c = 0; c < dim; ++c) y0[(size_t)c * m + k] = shots[k].y0[c];
+            for (int c = 0; c < dim; ++c) ys[(size_t)c * m + k] = y0[(size_t)k * dim + c];
             for (int q = 0; q < np; ++q) params[(size_t)q * m + k] = in->params[(int64_t)q * in->n + i];
             rtol[k] = in->rtol[i];
             atol[k] = in->atol[i];
@@ -66,7 +75,7 @@ struct ShotBatch {
         bi.n = m;
         bi.t0 = t0.data();
         bi.tf = tf.data();
-        bi.y0 = y0.data();
+        bi.y0 = ys.data();
         bi.params = np > 0 ? params.data() : nullptr;
         bi.rtol = rtol.data();
         bi.atol = atol.data();
@@ -75,11 +84,6 @@ struct ShotBatch {
         degpu_batch_out bo{y_final.data(), t_final.data(), ne ? dense.data() : nullptr, accepted.data(),
                            rejected.data(),   fevals.data(),  status.data()};
         return degpu_solve_ensemble_host(pb, cfg, &bi, &bo);
-    }
-    std::vector<double> yf(int64_t k, int dim) const {
-        std::vector<double> v(dim);
-        for (int c = 0; c < dim; ++c) v[c] = y_final[(size_t)c * shots.size() + k];
-        return v;
     }
 };
 
@@ -178,18 +182,15 @@ degpu_status single_shooting(const degpu_problem* pb, const degpu_method_cfg* cf
     const int dim = pb->dim;
     const Boundary bd{dim, bvp};
     for (int it = 0; it < bvp->max_iterations; ++it) {
-        ShotBatch b;
+        ShotBatch b(dim);
         for (int64_t i = 0; i < in->n; ++i) {
             Inst& s = st[i];
             if (s.phase != Inst::ACTIVE) continue;
-            s.base = b.add(i, in->t0[i], in->tf[i], s.u);
-            for (int j = 0; j < dim; ++j) {
-                std::vector<double> yp = s.u;
-                yp[j] = s.u[j] + kSqrtEps * std::fmax(std::fabs(s.u[j]), 1.0);
-                b.add(i, in->t0[i], in->tf[i], yp);
-            }
+            s.base = b.add(i, in->t0[i], in->tf[i], s.u.data());
+            for (int j = 0; j < dim; ++j)
+                b.add(i, in->t0[i], in->tf[i], s.u.data(), j, s.u[j] + kSqrtEps * std::fmax(std::fabs(s.u[j]), 1.0));
         }
-        if (b.shots.empty()) break;
+        if (b.size() == 0) break;
         degpu_status rc = b.run(pb, cfg, in, nullptr);
         if (rc != DEGPU_OK) return rc;
         for (int64_t i = 0; i < in->n; ++i) {
@@ -198,11 +199,11 @@ degpu_status single_shooting(const degpu_problem* pb, const degpu_method_cfg* cf
             const int64_t k0 = s.base;
             s.count(b, k0);
             if (b.status[k0] != DEGPU_COMPLETE) {
-                s.fail(b.status[k0], b.t_final[k0], b.yf(k0, dim));
+                s.fail(b.status[k0], b.t_final[k0], b.yf(k0));
                 continue;
             }
             std::vector<double> res(dim), resp(dim), jac((size_t)dim * dim);
-            const std::vector<double> yb = b.yf(k0, dim);
+            const std::vector<double> yb = b.yf(k0);
             bd.eval(s.u.data(), yb.data(), res.data());
             if (max_norm(res) <= bvp->tolerance) {
                 s.phase = Inst::CONVERGED;
@@ -213,14 +214,13 @@ degpu_status single_shooting(const degpu_problem* pb, const degpu_method_cfg* cf
                 const int64_t kj = k0 + 1 + j;
                 s.count(b, kj);
                 if (b.status[kj] != DEGPU_COMPLETE) {
-                    s.fail(b.status[kj], b.t_final[kj], b.yf(kj, dim));
+                    s.fail(b.status[kj], b.t_final[kj], b.yf(kj));
                     ok = false;
                     break;
                 }
                 const double pert = kSqrtEps * std::fmax(std::fabs(s.u[j]), 1.0);
-                const std::vector<double>& yp = b.shots[kj].y0;
-                const std::vector<double> ybp = b.yf(kj, dim);
-                bd.eval(yp.data(), ybp.data(), resp.data());
+                const std::vector<double> ybp = b.yf(kj);
+                bd.eval(b.start(kj), ybp.data(), resp.data());
                 s.jacobian += 1;
                 for (int r = 0; r < dim; ++r) jac[(size_t)r * dim + j] = (resp[r] - res[r]) / pert;
             }
@@ -249,16 +249,16 @@ degpu_status multiple_shooting(const degpu_problem* pb, const degpu_method_cfg* 
     for (int i = 0; i <= segs; ++i) mesh[i] = t0 + span * (double)i / (double)segs;
     {
         // initial_nodes (multiple.rs:108-126): one shot over [t0, tf] with output at the mesh
-        ShotBatch b;
-        for (int64_t i = 0; i < in->n; ++i) b.add(i, t0, tf, st[i].u);
+        ShotBatch b(dim);
+        for (int64_t i = 0; i < in->n; ++i) b.add(i, t0, tf, st[i].u.data());
         degpu_status rc = b.run(pb, cfg, in, &mesh);
         if (rc != DEGPU_OK) return rc;
-        const int64_t m = (int64_t)b.shots.size();
+        const int64_t m = b.size();
         for (int64_t i = 0; i < in->n; ++i) {
             Inst& s = st[i];
             s.count(b, i);
             if (b.status[i] != DEGPU_COMPLETE) {
-                s.fail(b.status[i], b.t_final[i], b.yf(i, dim));
+                s.fail(b.status[i], b.t_final[i], b.yf(i));
                 continue;
             }
             std::vector<double> nodes((size_t)unknowns);
@@ -277,23 +277,21 @@ degpu_status multiple_shooting(const degpu_problem* pb, const degpu_method_cfg* 
         }
     }
     for (int it = 0; it < bvp->max_iterations; ++it) {
-        ShotBatch b;
+        ShotBatch b(dim);
         for (int64_t i = 0; i < in->n; ++i) {
             Inst& s = st[i];
             if (s.phase != Inst::ACTIVE) continue;
-            s.base = (int64_t)b.shots.size();
-            for (int g = 0; g < segs; ++g)
-                b.add(i, mesh[g], mesh[g + 1], std::vector<double>(s.u.begin() + (size_t)g * dim,
-                                                                   s.u.begin() + (size_t)(g + 1) * dim));
+            s.base = b.size();
+            for (int g = 0; g < segs; ++g) b.add(i, mesh[g], mesh[g + 1], &s.u[(size_t)g * dim]);
             // one shot per column whose node starts a segment
             for (int j = 0; j < segs * dim; ++j) {
                 const int node = j / dim, c = j % dim;
-                std::vector<double> y0(s.u.begin() + (size_t)node * dim, s.u.begin() + (size_t)(node + 1) * dim);
-                y0[c] = y0[c] + kSqrtEps * std::fmax(std::fabs(y0[c]), 1.0);
-                b.add(i, mesh[node], mesh[node + 1], y0);
+                const double v = s.u[j];
+                b.add(i, mesh[node], mesh[node + 1], &s.u[(size_t)node * dim], c,
+                      v + kSqrtEps * std::fmax(std::fabs(v), 1.0));
             }
         }
-        if (b.shots.empty()) break;
+        if (b.size() == 0) break;
         degpu_status rc = b.run(pb, cfg, in, nullptr);
         if (rc != DEGPU_OK) return rc;
         std::vector<double> res(unknowns), resp(unknowns), jac((size_t)unknowns * unknowns), yend, yendp;
@@ -308,12 +306,12 @@ degpu_status multiple_shooting(const degpu_problem* pb, const degpu_method_cfg* 
             for (int g = 0; g < segs; ++g) {
                 s.count(b, k0 + g);
                 if (b.status[k0 + g] != DEGPU_COMPLETE) {
-                    s.fail(b.status[k0 + g], b.t_final[k0 + g], b.yf(k0 + g, dim));
+                    s.fail(b.status[k0 + g], b.t_final[k0 + g], b.yf(k0 + g));
                     ok = false;
                     break;
                 }
                 for (int c = 0; c < dim; ++c) {
-                    yend[(size_t)g * dim + c] = b.y_final[(size_t)c * b.shots.size() + k0 + g];
+                    yend[(size_t)g * dim + c] = b.end(k0 + g, c);
                     res[(size_t)(g + 1) * dim + c] = yend[(size_t)g * dim + c] - s.u[(size_t)(g + 1) * dim + c];
                 }
             }
@@ -335,12 +333,12 @@ degpu_status multiple_shooting(const degpu_problem* pb, const degpu_method_cfg* 
                         const int64_t kp = k0 + segs + j;
                         s.count(b, kp);
                         if (b.status[kp] != DEGPU_COMPLETE) {
-                            s.fail(b.status[kp], b.t_final[kp], b.yf(kp, dim));
+                            s.fail(b.status[kp], b.t_final[kp], b.yf(kp));
                             ok = false;
                             break;
                         }
                         for (int q = 0; q < dim; ++q)
-                            yendp[(size_t)g * dim + q] = b.y_final[(size_t)q * b.shots.size() + kp];
+                            yendp[(size_t)g * dim + q] = b.end(kp, q);
                     } else {
                         s.count(b, k0 + g);
                     }
@@ -414,15 +412,14 @@ extern "C" degpu_status degpu_solve_bvp_host(const degpu_problem* pb, const degp
             st[i].fail(DEGPU_ERR_MAX_STEPS, in->t0[i],
                        multi ? std::vector<double>(st[i].u.begin(), st[i].u.begin() + dim) : guess[i]);
     // the final solve from the converged initial state, into the caller's outputs
-    ShotBatch fin;
+    ShotBatch fin(dim);
     std::vector<double> te;
     if (in->n_eval > 0 && out->dense) te.assign(in->t_eval, in->t_eval + in->n_eval);
     for (int64_t i = 0; i < n; ++i)
-        if (st[i].phase == Inst::CONVERGED)
-            st[i].base = fin.add(i, in->t0[i], in->tf[i], std::vector<double>(st[i].u.begin(), st[i].u.begin() + dim));
+        if (st[i].phase == Inst::CONVERGED) st[i].base = fin.add(i, in->t0[i], in->tf[i], st[i].u.data());
     rc = fin.run(pb, cfg, in, te.empty() ? nullptr : &te);
     if (rc != DEGPU_OK) return rc;
-    const int64_t fm = (int64_t)fin.shots.size();
+    const int64_t fm = fin.size();
     const int ne = (int)te.size();
     for (int64_t i = 0; i < n; ++i) {
         Inst& s = st[i];
@@ -435,7 +432,7 @@ extern "C" degpu_status degpu_solve_bvp_host(const degpu_problem* pb, const degp
             s.count(fin, k);
             status = fin.status[k];
             tfin = fin.t_final[k];
-            yfin = fin.yf(k, dim);
+            yfin = fin.yf(k);
         }
         for (int c = 0; c < dim; ++c) {
             out->y_final[(int64_t)c * n + i] = yfin.size() == (size_t)dim ? yfin[c] : NAN;
