@@ -1,8 +1,8 @@
 """Builds libdegpu.so in place: every CUDA translation unit for sm_103a, in parallel.
 
 Usage: python build.py [--jobs N] [--verbose]
-The parity translation units (inst_parity_*.cu) are compiled with -fmad=false so that no
-multiply-add on that path is contracted into an FMA.
+The parity translation units (inst_parity_*.cu) and the shooting Newton kernels (bvp.cu) are
+compiled with -fmad=false so that no multiply-add on those paths is contracted into an FMA.
 """
 import argparse
 import concurrent.futures as cf
@@ -43,7 +43,9 @@ def flags_for(src):
     f = list(ARCH) + list(COMMON)
     # extra nvcc flags for tuning experiments, e.g. DEGPU_NVCC_EXTRA="-DDEGPU_MIXED_MIN_BLOCKS=8"
     f += os.environ.get("DEGPU_NVCC_EXTRA", "").split()
-    if name.startswith("inst_parity"):
+    # the parity kernels, and the shooting Newton kernels (bvp.cu), which restate the crate's
+    # arithmetic on the device
+    if name.startswith("inst_parity") or name == "bvp.cu":
         f += PARITY
     return f
 
