@@ -83,6 +83,7 @@ struct EnsArgs {
 
 // f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
 __device__ __forceinline__ double rs_signum(double x) { return x != x ? x : copysign(1.0, x); }
+__device__ __forceinline__ float rs_signum(float x) { return x != x ? x : copysignf(1.0f, x); }
 
 static_assert(DEGPU_EVENT_MAX_TERMS == DEGPU_HYPERPLANE_MAX_DIM, "event terms and plane components share arrays");
 
@@ -91,22 +92,22 @@ static_assert(DEGPU_EVENT_MAX_TERMS == DEGPU_HYPERPLANE_MAX_DIM, "event terms an
 // inside the bracket, else bisection; converged when half the bracket is within
 // max(abs_tol, rel_tol |b|) or g vanishes. f(x, ok) evaluates g on the step's interpolant and
 // clears ok when x lies outside the step (the crate's interpolator then fails and no root is
-// returned).
-template <class F>
-__device__ bool brent_dekker(double a, double b, double fa, double fb, double abs_tol, double rel_tol, F f,
-                             double& root) {
+// returned). R is double, or float for the mixed form's search in the step's normalised
+// coordinate.
+template <class R, class F>
+__device__ bool brent_dekker(R a, R b, R fa, R fb, R abs_tol, R rel_tol, F f, R& root) {
     if (fabs(fa) < fabs(fb)) {
-        double x = a;
+        R x = a;
         a = b;
         b = x;
         x = fa;
         fa = fb;
         fb = x;
     }
-    double c = a, fc = fa, d = b - a, e = d;
-    const double one = 1.0, two = 2.0, half = one / two, three = 3.0;
+    R c = a, fc = fa, d = b - a, e = d;
+    const R one = 1, two = 2, half = one / two, three = 3;
     for (int it = 0; it < 50; ++it) {
-        if (fb == 0.0) {
+        if (fb == (R)0) {
             root = b;
             return true;
         }
@@ -126,26 +127,26 @@ __device__ bool brent_dekker(double a, double b, double fa, double fb, double ab
             fb = fa;
             fa = fc;
         }
-        const double tol = fmax(abs_tol, rel_tol * fabs(b));
-        const double m = half * (a - b);
-        if (fabs(m) <= tol || fb == 0.0) {
+        const R tol = fmax(abs_tol, rel_tol * fabs(b));
+        const R m = half * (a - b);
+        if (fabs(m) <= tol || fb == (R)0) {
             root = b;
             return true;
         }
         bool use_bis = true;
         if (fabs(e) > tol && fabs(fa) > fabs(fb)) {
-            const double s = fb / fa;
-            double p, q;
+            const R s = fb / fa;
+            R p, q;
             if (a == c) {
                 p = two * m * s;
                 q = one - s;
             } else {
-                const double q1 = fa / fc;
-                const double r = fb / fc;
+                const R q1 = fa / fc;
+                const R r = fb / fc;
                 p = s * (two * m * q1 * (q1 - r) - (b - a) * (r - one));
                 q = (q1 - one) * (r - one) * (s - one);
             }
-            if (q > 0.0)
+            if (q > (R)0)
                 p = -p;
             else
                 q = -q;
@@ -164,7 +165,7 @@ __device__ bool brent_dekker(double a, double b, double fa, double fb, double ab
         if (fabs(d) > tol)
             b = b + d;
         else
-            b = b + (m > 0.0 ? tol : -tol);
+            b = b + (m > (R)0 ? tol : -tol);
         bool ok = true;
         fb = f(b, ok);
         if (!ok) return false;
@@ -536,13 +537,14 @@ struct Lane {
 
     // ----- crossing detection: CrossingSolout (src/solout/crossing.rs:200-330) and
     // HyperplaneCrossingSolout (src/solout/hyperplane.rs) ------------------------------------
-    __device__ __forceinline__ double comp_value(const S* v, int comp) const {
+    __device__ __forceinline__ S comp_s(const S* v, int comp) const {
         S r = v[0];
 #pragma unroll
         for (int c = 1; c < D; ++c)
             if (c == comp) r = v[c];
-        return (double)r;
+        return r;
     }
+    __device__ __forceinline__ double comp_value(const S* v, int comp) const { return (double)comp_s(v, comp); }
     // The monitored offset of a state given component by component: y[comp] - threshold
     // (crossing.rs:207), or the hyperplane's signed distance (pos - point) . normal
     // (hyperplane.rs signed_distance), the dot product folded from zero in component order
@@ -718,6 +720,22 @@ struct Lane {
         sum = sum + tt;
         return sum + a.cross_value;
     }
+    // The mixed form's FP32 event function: the time term as base + w_t (t - t_prev), base =
+    // w_t t_prev + offset taken once per step in FP64, so that FP32 carries only the in-step part.
+    __device__ __forceinline__ float event_f32(const S* v, float base, float dt_term, const EnsArgs& a) const {
+        if (a.event_kind == DEGPU_EVENT_MAX_ABS) {
+            float m = fabsf((float)comp_s(v, a.term_comp[0]));
+#pragma unroll
+            for (int j = 1; j < DEGPU_EVENT_MAX_TERMS; ++j)
+                if (j < a.n_terms) m = fmaxf(m, fabsf((float)comp_s(v, a.term_comp[j])));
+            return m + (float)a.cross_value;
+        }
+        float sum = 0.0f;
+#pragma unroll
+        for (int j = 0; j < DEGPU_EVENT_MAX_TERMS; ++j)
+            if (j < a.n_terms) sum += (float)a.term_w[j] * (float)comp_s(v, a.term_comp[j]);
+        return sum + dt_term + base;
+    }
     __device__ void event_solout(const EnsArgs& a) {
         const double g_curr = event_by(
             t,
@@ -751,22 +769,47 @@ struct Lane {
                 flo = fhi;
                 fhi = x;
             }
-            // the crate's tolerances (event.rs:329-330); the mixed form's FP32 states resolve g to
-            // about 1e-7 of its scale, so it stops at 1e-6 relative instead
-            const double rel_tol = P::KAHAN ? 1e-6 : 1e-12;
             double te;
-            if (flo * fhi <= 0.0 &&
-                brent_dekker(lo, hi, flo, fhi, 1e-14, rel_tol,
-                             [&](double x, bool& ok) {
-                                 if (x < t_prev || x > t) {  // Error::OutOfBounds
-                                     ok = false;
-                                     return 0.0;
-                                 }
-                                 S v[D];
-                                 interpolate(x, v, a);
-                                 return event_by(x, [&](int c) { return comp_value(v, c); }, a);
-                             },
-                             te)) {
+            bool found;
+            if constexpr (P::KAHAN) {
+                // mixed: the same search on sg in [0, 1] (t_prev to t) in FP32 on the FP32
+                // interpolant, stopping at 1e-6 of the step; a backward step locates nothing, as
+                // the crate's interpolator refuses every time inside it
+                float sg = 0.0f;
+                found = false;
+                if (dir > 0.0 && flo * fhi <= 0.0) {
+                    const float hspan = (float)(t - t_prev);
+                    const float base = (float)(a.event_tw * t_prev + a.cross_value);
+                    const float twf = (float)a.event_tw;
+                    found = brent_dekker(0.0f, 1.0f, (float)flo, (float)fhi, 1e-6f, 0.0f,
+                                         [&](float x, bool& ok) {
+                                             if (x < 0.0f || x > 1.0f) {
+                                                 ok = false;
+                                                 return 0.0f;
+                                             }
+                                             S v[D];
+                                             interpolate_sigma(x, v, a);
+                                             return event_f32(v, base, twf * (x * hspan), a);
+                                         },
+                                         sg);
+                }
+                te = t_prev + (double)sg * (t - t_prev);
+            } else {
+                // the crate's tolerances (event.rs:329-330)
+                found = flo * fhi <= 0.0 &&
+                        brent_dekker(lo, hi, flo, fhi, 1e-14, 1e-12,
+                                     [&](double x, bool& ok) {
+                                         if (x < t_prev || x > t) {  // Error::OutOfBounds
+                                             ok = false;
+                                             return 0.0;
+                                         }
+                                         S v[D];
+                                         interpolate(x, v, a);
+                                         return event_by(x, [&](int c) { return comp_value(v, c); }, a);
+                                     },
+                                     te);
+            }
+            if (found) {
                 if (!have_push || fabs(te - last_push) > 1e-14) {
                     if (ncross < a.cross_max) {
                         S v[D];

@@ -205,3 +205,21 @@ def test_ivp_builder_event_and_host_entry():
     assert np.array_equal(cc, g["cross_count"]) and np.array_equal(r.status, g["status"])
     assert np.array_equal(ct, g["cross_t"], equal_nan=True) and np.array_equal(cy, g["cross_y"], equal_nan=True)
     assert np.array_equal(r.dense, g["dense"], equal_nan=True) and np.array_equal(r.y_final, g["y_final"])
+
+
+@pytest.mark.parametrize("precision", [abi.FP64_PARITY, abi.MIXED])
+def test_backward_integration_locates_no_event(precision):
+    """Backward steps: the crate's interpolator refuses every time inside them, so no event is
+    counted; the solve runs to tf on both sides."""
+    n = 128
+    rng = np.random.default_rng(13)
+    e = W.Ensemble("harmonic-back", abi.DOPRI5, n, 2, 1, np.zeros(n), np.full(n, -10.0),
+                   np.stack([rng.uniform(0.5, 1.5, n), np.zeros(n)]), rng.uniform(0.5, 2.0, (1, n)),
+                   np.full(n, 1e-9), np.full(n, 1e-11), rhs_id=R["HARMONIC"])
+    ev = abi.make_event(abi.EVENT_LINEAR, [0], [1.0], terminate=1)
+    g = gpu_event(e, cfg_for(abi.DOPRI5, precision), ev)
+    o = oracle_event(e, cfg_for(abi.DOPRI5), ev)
+    assert np.all(o["cross_count"] == 0) and np.all(o["status"] == abi.COMPLETE)
+    assert np.all(g["cross_count"] == 0) and np.all(g["status"] == abi.COMPLETE)
+    if precision == abi.FP64_PARITY:
+        assert_same_event(g, o)
