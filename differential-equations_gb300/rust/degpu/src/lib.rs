@@ -30,6 +30,16 @@ impl Method {
     pub fn rk4(h0: f64) -> Self { let mut m = Self::new(sys::DEGPU_RK4); m.cfg.h0 = h0; m }
     pub fn dopri5() -> Self { Self::new(sys::DEGPU_DOPRI5) }
     pub fn dop853() -> Self { Self::new(sys::DEGPU_DOP853) }
+    pub fn rkf45() -> Self { Self::new(sys::DEGPU_RKF45) }
+    pub fn cash_karp() -> Self { Self::new(sys::DEGPU_CASH_KARP) }
+    pub fn rkv655e() -> Self { Self::new(sys::DEGPU_RKV655E) }
+    pub fn rkv656e() -> Self { Self::new(sys::DEGPU_RKV656E) }
+    pub fn rkv766e() -> Self { Self::new(sys::DEGPU_RKV766E) }
+    pub fn rkv767e() -> Self { Self::new(sys::DEGPU_RKV767E) }
+    pub fn rkv877e() -> Self { Self::new(sys::DEGPU_RKV877E) }
+    pub fn rkv878e() -> Self { Self::new(sys::DEGPU_RKV878E) }
+    pub fn rkv988e() -> Self { Self::new(sys::DEGPU_RKV988E) }
+    pub fn rkv989e() -> Self { Self::new(sys::DEGPU_RKV989E) }
     pub fn rtol(mut self, v: f64) -> Self { self.rtol = v; self }
     pub fn atol(mut self, v: f64) -> Self { self.atol = v; self }
     pub fn max_steps(mut self, v: i64) -> Self { self.cfg.max_steps = v; self }

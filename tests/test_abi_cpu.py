@@ -35,6 +35,26 @@ def test_library_exports_every_declared_symbol():
     assert set(declared_functions()) <= set(abi.SIGNATURES)
 
 
+def test_rust_binding_declares_every_entry_point_and_struct():
+    """The Rust sys crate a maintainer would add to the crate binds every function and struct of
+    the header (it cannot be compiled here: no Rust toolchain)."""
+    rs = open(os.path.join(REPO, "differential-equations_gb300", "rust", "degpu-sys", "src", "lib.rs")).read()
+    bound = set(re.findall(r"pub fn (degpu_[a-z_0-9]+)\(", rs))
+    assert set(declared_functions()) <= bound, sorted(set(declared_functions()) - bound)
+    src = open(os.path.join(REPO, "include", "degpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    structs = set(re.findall(r"typedef struct\s*\{[^{}]*\}\s*(degpu_[a-z_0-9]+)\s*;", src))
+    structs |= set(re.findall(r"typedef struct (degpu_[a-z_0-9]+) degpu_[a-z_0-9]+;", src))
+    assert {"degpu_batch_in", "degpu_event", "degpu_bvp", "degpu_server"} <= structs
+    rs_structs = set(re.findall(r"pub struct (degpu_[a-z_0-9]+)", rs))
+    assert structs <= rs_structs, sorted(structs - rs_structs)
+    # the field counts of the structs that cross the boundary by value agree with ctypes
+    for name, cls in [("degpu_crossing", abi.Crossing), ("degpu_hyperplane", abi.Hyperplane),
+                      ("degpu_event", abi.Event), ("degpu_bvp", abi.Bvp), ("degpu_method_cfg", abi.MethodCfg)]:
+        body = re.search(r"pub struct %s \{(.*?)\}" % name, rs, flags=re.S).group(1)
+        assert len(re.findall(r"pub \w+:", body)) == len(cls._fields_), name
+
+
 def test_defaults_match_crate():
     lib = abi.load()
     cfg = abi.MethodCfg()
