@@ -516,10 +516,14 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
     a.event_kind = cr.event_kind;
     a.event_terminate = cr.terminate;
     a.event_tw = cr.t_weight;
+    a.cross_value_f = (float)cr.value;
+    a.event_tw_f = (float)cr.t_weight;
     for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j) {
         a.term_comp[j] = cr.comps[j];
         a.term_a[j] = cr.point[j];
         a.term_w[j] = cr.normal[j];
+        a.term_a_f[j] = (float)cr.point[j];
+        a.term_w_f[j] = (float)cr.normal[j];
     }
     if (cr.max_points > 0) {
         // 0xFF bytes form a quiet NaN: slots past an instance's count stay NaN

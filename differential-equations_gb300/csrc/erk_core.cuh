@@ -79,6 +79,19 @@ struct EnsArgs {
     double term_a[DEGPU_HYPERPLANE_MAX_DIM];
     double term_w[DEGPU_HYPERPLANE_MAX_DIM];
     double event_tw;
+    // FP32 copies for the mixed form (its per-step offsets are FP32 data)
+    float cross_value_f, event_tw_f;
+    float term_a_f[DEGPU_HYPERPLANE_MAX_DIM], term_w_f[DEGPU_HYPERPLANE_MAX_DIM];
+};
+
+// PickT<B, T, F>::type: T when B, else F (no standard library under run-time compilation).
+template <bool B, class T, class F>
+struct PickT {
+    using type = T;
+};
+template <class T, class F>
+struct PickT<false, T, F> {
+    using type = F;
 };
 
 // f64::signum (Rust std): +-1 for signed zeros and infinities, NaN for NaN.
@@ -249,7 +262,9 @@ struct Lane {
     int mod100;  // steps % 100, kept incrementally (the stiffness test runs every 100th attempt)
     int next_eval;
     int status;
-    double last_off;     // crossing detection: previous offset (events: previous g)
+    // crossing detection: previous offset (events: previous g); FP32 in the mixed form
+    using OffT = typename PickT<P::KAHAN, float, double>::type;
+    OffT last_off;
     bool have_last_off;
     int ncross;          // crossings / events recorded
     int nevents;         // events counted (recorded or within 1e-14 of the last point)
@@ -611,19 +626,17 @@ struct Lane {
     // sum |point_j normal_j| for a hyperplane); the linear estimate when it does not converge.
     __device__ float find_crossing_sigma(float off_l, float off_u, const EnsArgs& a) const {
         const bool plane = a.cross_mode == 1;
-        const float thr = (float)a.cross_value;
+        const float thr = a.cross_value_f;
         const float tol = 100.0f * 1.1920929e-7f * fmaxf(1.0f, fabsf(thr));
         const float lin = -off_l / (off_u - off_l);
         auto off_at = [&](float sg) {
             S v[D];
             interpolate_sigma(sg, v, a);
-            if (!plane) return (float)comp_value(v, a.cross_comp) - thr;
+            if (!plane) return (float)comp_s(v, a.cross_comp) - thr;
             float sum = 0.0f;
 #pragma unroll
             for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
-                if (j < a.n_terms)
-                    sum += ((float)comp_value(v, a.term_comp[j]) - (float)a.term_a[j]) *
-                           (float)a.term_w[j];
+                if (j < a.n_terms) sum += ((float)comp_s(v, a.term_comp[j]) - a.term_a_f[j]) * a.term_w_f[j];
             return sum;
         };
         float sg = lin, offset;
@@ -646,25 +659,38 @@ struct Lane {
         return fabsf(offset) < tol * 10.0f ? sg : lin;
     }
 
+    // The mixed form's offset at the step's end in FP32: (y - compensation) against the FP32 copies
+    // of the threshold or plane.
+    __device__ __forceinline__ float state_offset_f32(const EnsArgs& a) const {
+        if (a.cross_mode == 0) return (comp_s(y, a.cross_comp) - a.cross_value_f) - comp_s(yc, a.cross_comp);
+        float sum = 0.0f;
+#pragma unroll
+        for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
+            if (j < a.n_terms) {
+                const int c = a.term_comp[j];
+                sum += ((comp_s(y, c) - a.term_a_f[j]) - comp_s(yc, c)) * a.term_w_f[j];
+            }
+        return sum;
+    }
+
     __device__ void crossing_solout(const EnsArgs& a) {
-        const double offset = offset_by(
-            [&](int c) {
-                double v = comp_value(y, c);
-                if constexpr (P::KAHAN) v = v - comp_value(yc, c);
-                return v;
-            },
-            a);
+        OffT offset;
+        if constexpr (P::KAHAN)
+            offset = state_offset_f32(a);
+        else
+            offset = offset_by([&](int c) { return comp_value(y, c); }, a);
+        const OffT zero = (OffT)0;
         if (have_last_off) {
             bool is_crossing = rs_signum(last_off) != rs_signum(offset);
             // hyperplane.rs: leaving or reaching the plane exactly also counts
             if (a.cross_mode == 1)
-                is_crossing = is_crossing || (last_off == 0.0 && offset != 0.0) || (last_off != 0.0 && offset == 0.0);
+                is_crossing = is_crossing || (last_off == zero && offset != zero) || (last_off != zero && offset == zero);
             if (is_crossing) {
                 bool record;
                 if (a.cross_dir > 0)
-                    record = last_off < 0.0 && offset >= 0.0;
+                    record = last_off < zero && offset >= zero;
                 else if (a.cross_dir < 0)
-                    record = last_off > 0.0 && offset <= 0.0;
+                    record = last_off > zero && offset <= zero;
                 else
                     record = true;
                 if (record) {
@@ -672,7 +698,7 @@ struct Lane {
                     S v[D];
                     if constexpr (P::KAHAN) {
                         // mixed: the same search in the step's normalised coordinate, in FP32
-                        const float sg = find_crossing_sigma((float)last_off, (float)offset, a);
+                        const float sg = find_crossing_sigma(last_off, offset, a);
                         tc = t_prev + (double)sg * (t - t_prev);
                         if (ncross < a.cross_max) interpolate_sigma(sg, v, a);
                     } else {
@@ -728,46 +754,50 @@ struct Lane {
 #pragma unroll
             for (int j = 1; j < DEGPU_EVENT_MAX_TERMS; ++j)
                 if (j < a.n_terms) m = fmaxf(m, fabsf((float)comp_s(v, a.term_comp[j])));
-            return m + (float)a.cross_value;
+            return m + a.cross_value_f;
         }
         float sum = 0.0f;
 #pragma unroll
         for (int j = 0; j < DEGPU_EVENT_MAX_TERMS; ++j)
-            if (j < a.n_terms) sum += (float)a.term_w[j] * (float)comp_s(v, a.term_comp[j]);
+            if (j < a.n_terms) sum += a.term_w_f[j] * (float)comp_s(v, a.term_comp[j]);
         return sum + dt_term + base;
     }
     __device__ void event_solout(const EnsArgs& a) {
-        const double g_curr = event_by(
-            t,
-            [&](int c) {
-                double v = comp_value(y, c);
-                if constexpr (P::KAHAN) v = v - comp_value(yc, c);
-                return v;
-            },
-            a);
+        OffT g_curr;
+        if constexpr (P::KAHAN) {
+            // mixed: g at the step's end in FP32 on y - compensation; the time term in FP64 once
+            S sv[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) sv[c] = y[c] - yc[c];
+            const float base = a.event_tw != 0.0 ? (float)(a.event_tw * t + a.cross_value) : a.cross_value_f;
+            g_curr = event_f32(sv, base, 0.0f, a);
+        } else {
+            g_curr = event_by(t, [&](int c) { return comp_value(y, c); }, a);
+        }
         if (!have_last_off) {  // the first call (at t0) only records g
             have_last_off = true;
             last_off = g_curr;
             return;
         }
-        const double g_prev = last_off;
+        const OffT g_prev = last_off, zero = (OffT)0;
         const bool sign_change = rs_signum(g_prev) != rs_signum(g_curr);
         bool direction_ok;
         if (a.cross_dir > 0)
-            direction_ok = sign_change && g_prev < 0.0 && g_curr >= 0.0;
+            direction_ok = sign_change && g_prev < zero && g_curr >= zero;
         else if (a.cross_dir < 0)
-            direction_ok = sign_change && g_prev > 0.0 && g_curr <= 0.0;
+            direction_ok = sign_change && g_prev > zero && g_curr <= zero;
         else
             direction_ok = sign_change;
         if (direction_ok) {
-            double lo = t_prev, hi = t, flo = g_prev, fhi = g_curr;
+            double lo = t_prev, hi = t;
+            OffT flo = g_prev, fhi = g_curr;
             if ((dir > 0.0 && lo > hi) || (dir < 0.0 && lo < hi)) {
-                double x = lo;
+                const double x = lo;
                 lo = hi;
                 hi = x;
-                x = flo;
+                const OffT f = flo;
                 flo = fhi;
-                fhi = x;
+                fhi = f;
             }
             double te;
             bool found;
@@ -777,11 +807,12 @@ struct Lane {
                 // the crate's interpolator refuses every time inside it
                 float sg = 0.0f;
                 found = false;
-                if (dir > 0.0 && flo * fhi <= 0.0) {
+                if (dir > 0.0 && flo * fhi <= 0.0f) {
                     const float hspan = (float)(t - t_prev);
-                    const float base = (float)(a.event_tw * t_prev + a.cross_value);
-                    const float twf = (float)a.event_tw;
-                    found = brent_dekker(0.0f, 1.0f, (float)flo, (float)fhi, 1e-6f, 0.0f,
+                    const float base =
+                        a.event_tw != 0.0 ? (float)(a.event_tw * t_prev + a.cross_value) : a.cross_value_f;
+                    const float twf = a.event_tw_f;
+                    found = brent_dekker(0.0f, 1.0f, flo, fhi, 1e-6f, 0.0f,
                                          [&](float x, bool& ok) {
                                              if (x < 0.0f || x > 1.0f) {
                                                  ok = false;
@@ -917,7 +948,7 @@ struct Lane {
         next_eval = 0;
         if constexpr (CROSS) {
             have_last_off = false;
-            last_off = 0.0;
+            last_off = (OffT)0;
             ncross = 0;
             nevents = 0;
             last_push = 0.0;
