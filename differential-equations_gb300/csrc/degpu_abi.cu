@@ -58,6 +58,7 @@ void ensure_registered() {
         register_mixed();
         register_parity_multi();
         register_multi_fast_mixed();
+        register_multi_cross();
         register_cross_parity();
         register_cross_fast_mixed();
         register_cross_embedded_parity();
@@ -542,6 +543,10 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
     if (prod) {
         EnsArgs ma = a;
         ma.count = n;
+        // the persistent multi-family kernel where it is built (fast and mixed DOPRI5 / DOP853),
+        // else one run-to-completion launch per (precision, family) list
+        if (multi_registry().count({cfg->method, cfg->precision, 2}))
+            return multi_solve(cfg, ma, in->family, pb->rhs_id, true, s, true);
         return sorted_thread_solve(cfg, ma, in->family, pb->rhs_id, true, s, true);
     }
     for (auto& kv : lists) {

@@ -1709,19 +1709,20 @@ struct MultiQueue {
     unsigned long long* head;     // [3] per-family list heads
 };
 
-template <class Tab, class P, bool DENSE, class R0, class R1, class R2>
+template <class Tab, class P, bool DENSE, class R0, class R1, class R2, bool CROSS>
 struct MultiLane {
     union {
-        Lane<Tab, R0, P, DENSE> l0;
-        Lane<Tab, R1, P, DENSE> l1;
-        Lane<Tab, R2, P, DENSE> l2;
+        Lane<Tab, R0, P, DENSE, CROSS> l0;
+        Lane<Tab, R1, P, DENSE, CROSS> l1;
+        Lane<Tab, R2, P, DENSE, CROSS> l2;
     };
     __device__ MultiLane() {}
 };
 
-template <class Tab, class P, bool DENSE, class R0, class R1, class R2>
+// CROSS: crossing or event detection (the lanes of erk_cross_kernel) instead of output times only.
+template <class Tab, class P, bool DENSE, class R0, class R1, class R2, bool CROSS = false>
 __global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(EnsArgs a, MultiQueue q) {
-    MultiLane<Tab, P, DENSE, R0, R1, R2> M;
+    MultiLane<Tab, P, DENSE, R0, R1, R2, CROSS> M;
     const int64_t cnt[3] = {q.count[0], q.count[1], q.count[2]};
     const int64_t st[3] = {q.start[0], q.start[1], q.start[2]};
     // every warp starts on the longest list and moves on to the next family when it runs dry, so

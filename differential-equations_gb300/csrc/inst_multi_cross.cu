@@ -1,0 +1,12 @@
+// inst_multi_cross.cu — multi-family persistent kernels with crossing / event detection, FP64 fast
+// and mixed (the fast one serves a mixed solve's instances below the mixed-precision bound).
+#include "registry.cuh"
+
+namespace degpu {
+void register_multi_cross() {
+    register_multi_cross<TabDopri5, PrecFast>();
+    register_multi_cross<TabDopri5, PrecMixed>();
+    register_multi_cross<TabDop853, PrecFast>();
+    register_multi_cross<TabDop853, PrecMixed>();
+}
+}  // namespace degpu

@@ -112,8 +112,8 @@ static degpu_status run_plan(const degpu_method_cfg* cfg, const EnsArgs& a, cons
 // Plans and launches one multi-family persistent solve (two launches when a mixed solve splits
 // by rtol).  Returns DEGPU_UNSUPPORTED when no kernel is registered for the combination.
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
-                         bool dense, cudaStream_t s) {
-    const int d = dense ? 1 : 0;
+                         bool dense, cudaStream_t s, bool crossing) {
+    const int d = crossing ? 2 : (dense ? 1 : 0);
     auto it = multi_registry().find({cfg->method, cfg->precision, d});
     if (it == multi_registry().end()) return DEGPU_UNSUPPORTED;
     const double split = mixed_split(cfg);

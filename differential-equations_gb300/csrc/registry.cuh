@@ -156,9 +156,9 @@ void register_round_all_methods() {
 using MultiLaunchFn = cudaError_t (*)(const EnsArgs& a, const MultiQueue& q, int64_t total, cudaStream_t s);
 std::map<std::tuple<int, int, int>, MultiLaunchFn>& multi_registry();
 
-template <class Tab, class P, bool DENSE>
+template <class Tab, class P, bool DENSE, bool CROSS = false>
 cudaError_t launch_multi(const EnsArgs& a, const MultiQueue& q, int64_t total, cudaStream_t s) {
-    auto kern = erk_multi_kernel<Tab, P, DENSE, RhsVanDerPol, RhsPendulum, RhsLorenz>;
+    auto kern = erk_multi_kernel<Tab, P, DENSE, RhsVanDerPol, RhsPendulum, RhsLorenz, CROSS>;
     static int blocks_per_sm = -1;
     if (blocks_per_sm < 0) {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, 128, 0);
@@ -173,10 +173,15 @@ cudaError_t launch_multi(const EnsArgs& a, const MultiQueue& q, int64_t total, c
     return cudaGetLastError();
 }
 
+// Keys (method, precision, kind): kind 0 final states, 1 output times, 2 crossing / event detection.
 template <class Tab, class P>
 void register_multi() {
     multi_registry()[{method_id<Tab>(), P::ID, 0}] = &launch_multi<Tab, P, false>;
     multi_registry()[{method_id<Tab>(), P::ID, 1}] = &launch_multi<Tab, P, true>;
+}
+template <class Tab, class P>
+void register_multi_cross() {
+    multi_registry()[{method_id<Tab>(), P::ID, 2}] = &launch_multi<Tab, P, true, true>;
 }
 
 // Per-translation-unit registration hooks (called once by the ABI).
@@ -186,6 +191,7 @@ void register_fast();
 void register_mixed();
 void register_parity_multi();
 void register_multi_fast_mixed();
+void register_multi_cross();
 void register_cross_parity();
 void register_cross_fast_mixed();
 void register_cross_embedded_parity();
@@ -228,7 +234,7 @@ __device__ __forceinline__ double plan_log2_cost(int slot, double span, double r
 
 // Longest-first planning + one multi-family persistent launch per precision class (plan.cu).
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
-                         bool dense, cudaStream_t s);
+                         bool dense, cudaStream_t s, bool crossing = false);
 
 // One run-to-completion launch per (precision class, family) over the same longest-first lists;
 // `crossing` launches the crossing-detection kernels (dense = 1) instead.
