@@ -379,8 +379,9 @@ def run_bvp(args, torch, dev, lib):
 
 def run_adaptive(args, torch, dev, lib):
     """The crate's Adaptive ERK family (RKF45, Cash-Karp) on the uneven ensemble (--n instances,
-    rtol ~ logU[1e-9,1e-5]): FP64 parity and mixed, one run-to-completion launch per family over
-    the longest-first lists; CPU baseline = the oracle on a sample."""
+    rtol ~ logU[1e-9,1e-5]): mixed on the multi-family persistent kernel, FP64 parity one
+    run-to-completion launch per family over the longest-first lists; CPU baseline = the oracle
+    on a sample."""
     n = args.n
     e = W.config1(n=n)
     keep, bi, out, bo = _device_batch(torch, e, dev)

@@ -59,6 +59,7 @@ void ensure_registered() {
         register_parity_multi();
         register_multi_fast_mixed();
         register_multi_cross();
+        register_multi_embedded();
         register_cross_parity();
         register_cross_fast_mixed();
         register_cross_embedded_parity();

@@ -192,6 +192,7 @@ void register_mixed();
 void register_parity_multi();
 void register_multi_fast_mixed();
 void register_multi_cross();
+void register_multi_embedded();
 void register_cross_parity();
 void register_cross_fast_mixed();
 void register_cross_embedded_parity();

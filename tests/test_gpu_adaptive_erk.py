@@ -77,3 +77,18 @@ def test_adaptive_erk_fast_and_mixed_accuracy(method, precision, tol):
     assert np.all(g.status == abi.COMPLETE)
     rel = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.maximum(np.max(np.abs(o["y_final"]), axis=0), 1e-300)
     assert np.median(rel) < tol
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("precision", [abi.FP64_FAST, abi.MIXED])
+def test_adaptive_erk_persistent_equals_thread(method, precision):
+    """The multi-family persistent kernel runs the same per-instance arithmetic as the
+    one-system-per-thread launches: identical results, bit for bit, in both forms (the mixed one
+    with its FP64 class below the bound)."""
+    e = W.config1(n=3 * 3000, first=70_000)
+    e.tf = np.minimum(e.tf, 10.0)
+    g_p = gpu_solve(e, cfg_for(method, precision, kernel=abi.KERNEL_PERSISTENT))
+    g_t = gpu_solve(e, cfg_for(method, precision, kernel=abi.KERNEL_THREAD))
+    assert np.array_equal(g_p.status, g_t.status)
+    assert np.array_equal(g_p.accepted, g_t.accepted) and np.array_equal(g_p.fevals, g_t.fevals)
+    assert np.array_equal(g_p.y_final, g_t.y_final)
