@@ -33,7 +33,7 @@ enum : int32_t { ACTIVE = 0, CONVERGED = 1, DONE = 2 };
 // Per-instance Newton state and the batch's settings (device arrays, structure of arrays).
 struct Dev {
     int64_t n;
-    int dim, U, segs, np, max_iter;
+    int dim, U, segs, np;
     double tol;
     const double *t0, *tf, *params, *rtol, *atol;  // the caller's inputs
     double* u;      // [U][n] unknowns: y(t0), or the mesh nodes
@@ -455,7 +455,6 @@ extern "C" degpu_status degpu_solve_bvp_host(const degpu_problem* pb, const degp
         d.U = U;
         d.segs = segs;
         d.np = np;
-        d.max_iter = bvp->max_iterations;
         d.tol = bvp->tolerance;
         for (int i = 0; i < DEGPU_HYPERPLANE_MAX_DIM; ++i) {
             d.side[i] = bvp->side[i];

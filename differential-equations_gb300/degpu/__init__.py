@@ -212,8 +212,10 @@ class EnsembleResult:
     status: np.ndarray
 
 
-def _solve_crossing_host(fn, name, spec, rhs_id, dim, t0, tf, y0, params, rtol, atol, method, max_points, family,
+def _solve_crossing_host(fn, spec, rhs_id, dim, t0, tf, y0, params, rtol, atol, method, max_points, family,
                          n_params, t_eval=None):
+    """One host-pointer detection entry point `fn` (crossing, hyperplane or event) with its spec
+    struct: host arrays in, (EnsembleResult, (t, y, count)) out."""
     lib = abi.load()
     y0 = np.asarray(y0, dtype=np.float64)
     n = y0.shape[1]
@@ -251,7 +253,7 @@ def solve_ensemble_crossing(rhs_id: int, dim: int, t0, tf, y0, params, rtol, ato
     the crate's `.crossing(component, threshold, direction)` output.  Returns the EnsembleResult
     and (t [max_points, n], y [max_points, dim, n], count [n])."""
     cr = abi.Crossing(component=component, direction=direction, max_points=max_points, threshold=threshold)
-    return _solve_crossing_host("degpu_solve_ensemble_crossing_host", "crossing", cr, rhs_id, dim, t0, tf, y0,
+    return _solve_crossing_host("degpu_solve_ensemble_crossing_host", cr, rhs_id, dim, t0, tf, y0,
                                 params, rtol, atol, method, max_points, family, n_params)
 
 
@@ -263,7 +265,7 @@ def solve_ensemble_hyperplane(rhs_id: int, dim: int, t0, tf, y0, params, rtol, a
     extractor, direction)` output with the extractor given as state components
     (pos[j] = y[components[j]]).  Returns what solve_ensemble_crossing returns."""
     hp = abi.make_hyperplane(components, point, normal, direction, max_points)
-    return _solve_crossing_host("degpu_solve_ensemble_hyperplane_host", "hyperplane", hp, rhs_id, dim, t0, tf, y0,
+    return _solve_crossing_host("degpu_solve_ensemble_hyperplane_host", hp, rhs_id, dim, t0, tf, y0,
                                 params, rtol, atol, method, max_points, family, n_params)
 
 
@@ -274,7 +276,7 @@ def solve_ensemble_event(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, 
     per-step output.  Returns the EnsembleResult (dense = the output times) and the event points
     (t [max_points, n], y [max_points, dim, n], count [n]); a terminal event leaves the
     instance's status INTERRUPTED."""
-    return _solve_crossing_host("degpu_solve_ensemble_event_host", "event", event, rhs_id, dim, t0, tf, y0, params,
+    return _solve_crossing_host("degpu_solve_ensemble_event_host", event, rhs_id, dim, t0, tf, y0, params,
                                 rtol, atol, method, event.max_points, family, n_params, t_eval)
 
 
