@@ -233,12 +233,20 @@ struct Lane {
     static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
     static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
+    // Mixed form without output: t as an FP32 pair th + tl (about 48 bits), advanced and compared
+    // with tf in FP32 arithmetic, so that an accepted step issues no FP64 instruction. The built-in
+    // families read no t (a drive phase is advanced as an FP32 pair too); run-time (NVRTC)
+    // families keep the FP64 t they may read.
+    static constexpr bool FFT = MIX && !DENSE && FloatParamsOf<Rhs>::value;
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
     // itself, and the evaluation the crate repeats at the new point on acceptance is that stage.
     static constexpr bool FSAL_MIX = MIX && Tab::FSAL;
 
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
+    float th, tl, tfh, tfl;  // FFT: t = th + tl, tf = tfh + tfl
+    bool at_tf;              // FFT: the last step ended exactly at tf
+    float phl, omh, oml;     // FFT with a drive phase: phase = ph0 + phl, rate = omh + oml
     double rem;    // tf - t (mixed form of RK4)
     float h_lim;   // 1e-14 |h_prev| in FP32 (mixed form's step-size guard)
     // Mixed form of the adaptive methods (MIX): the step size, the remaining span used by the
@@ -287,6 +295,50 @@ struct Lane {
         else
             rhs(t + (double)dt, yy, dd);
     }
+
+    // FFT: t += hf as an FP32 pair (TwoSum, then FastTwoSum), or t = tf after a clamped last step
+    __device__ __forceinline__ void ff_advance() {
+        if (last_step) {
+            th = tfh;
+            tl = tfl;
+            at_tf = true;
+            return;
+        }
+        const float s = th + hf;
+        const float bp = s - th;
+        const float e = (th - (s - bp)) + (hf - bp);
+        const float lo = tl + e;
+        const float hi = s + lo;
+        tl = lo - (hi - s);
+        th = hi;
+    }
+    // FFT with a drive phase: phase += Omega hf as an FP32 pair (the product's error from fmaf and
+    // the rate's low part), reduced by 2 pi (an FP32 pair) to [-pi, pi]
+    __device__ __forceinline__ void ff_phase_advance() {
+        const float pr = omh * hf;
+        const float pe = fmaf(omh, hf, -pr) + oml * hf;
+        float s = ph0 + pr;
+        float bp = s - ph0;
+        float e = (ph0 - (s - bp)) + (pr - bp);
+        float lo = (phl + e) + pe;
+        float hi = s + lo;
+        phl = lo - (hi - s);
+        ph0 = hi;
+        if (fabsf(ph0) > 3.14159265f) {
+            const float k = rintf(ph0 * 0.159154943f);
+            const float q = k * 6.28318548f;                   // 2 pi = 6.28318548f - 1.74845553e-7f
+            const float qe = fmaf(k, 6.28318548f, -q) + k * -1.74845553e-7f;
+            s = ph0 - q;
+            bp = s - ph0;
+            e = (ph0 - (s - bp)) + (-q - bp);
+            lo = (phl + e) - qe;
+            hi = s + lo;
+            phl = lo - (hi - s);
+            ph0 = hi;
+        }
+    }
+    // FFT: tf - t in FP32 (exact in its leading part when t is near tf)
+    __device__ __forceinline__ float ff_rem() const { return (tfh - th) + (tfl - tl); }
 
     // Type of the per-component error terms and their sum: FP64, except in the mixed form built
     // with the FP32 controller (P::F32_CTRL), whose terms are FP32 stage data.
@@ -986,6 +1038,22 @@ struct Lane {
             fwd = dir > 0.0;
             last_step = false;
         }
+        if constexpr (FFT) {
+            th = (float)t0;
+            tl = (float)(t0 - (double)th);
+            tfh = (float)tf;
+            tfl = (float)(tf - (double)tfh);
+            at_tf = false;
+            if constexpr (PHASE) {
+                // the phase at t0 reduced to [-pi, pi] in FP64, kept as an FP32 pair
+                const double om = p[Rhs::PHASE_RATE], ph = om * t0;
+                const double r = fma(-rint(ph * 0.15915494309189535), 6.283185307179586, ph);
+                ph0 = (float)r;
+                phl = (float)(r - (double)ph0);
+                omh = (float)om;
+                oml = (float)(om - (double)omh);
+            }
+        }
         if constexpr (PHASE)
             rhs_at(0.0f, y, k0);
         else
@@ -1145,7 +1213,10 @@ struct Lane {
             accept = errd <= 1.0;
         if (accept) {
             double t_new;
-            if constexpr (MIX)
+            if constexpr (FFT) {
+                ff_advance();
+                t_new = t;  // t itself is not kept up to date (finish() forms it from th + tl)
+            } else if constexpr (MIX)
                 t_new = last_step ? tf : t + widen_f32(hf);  // a clamped last step ends exactly at tf
             else
                 t_new = t + h;
@@ -1214,7 +1285,12 @@ struct Lane {
                 h_prev = h;
             }
             t = t_new;
-            if constexpr (PHASE) ph0 = Rhs::phase(t, p);
+            if constexpr (PHASE) {
+                if constexpr (FFT)
+                    ff_phase_advance();
+                else
+                    ph0 = Rhs::phase(t, p);
+            }
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 y[c] = ynew[c];
@@ -1485,7 +1561,10 @@ struct Lane {
                 else
                     scale = fmin(scale, 1.0);
             }
-            if constexpr (MIX) {
+            if constexpr (FFT) {
+                ff_advance();
+                if constexpr (PHASE) ff_phase_advance();
+            } else if constexpr (MIX) {
                 t = last_step ? tf : t + widen_f32(hf);  // a clamped last step ends exactly at tf
                 if constexpr (PHASE) ph0 = Rhs::phase(t, p);
             } else {
@@ -1667,7 +1746,10 @@ struct Lane {
             if (last_step) {
                 done = true;  // t == tf
             } else {
-                remf = narrow_rz(tf - t);
+                if constexpr (FFT)
+                    remf = ff_rem();
+                else
+                    remf = narrow_rz(tf - t);
                 if (fabsf(remf) <= (float)eps10) done = true;
             }
         } else if constexpr (P::KAHAN) {
@@ -1683,7 +1765,12 @@ struct Lane {
 #pragma unroll
         for (int c = 0; c < D; ++c) a.y_final[(int64_t)c * n + inst] = (double)y[c] - (double)yc[c];
         for (int c = D; c < a.dmax; ++c) a.y_final[(int64_t)c * n + inst] = 0.0;
-        if (a.t_final) a.t_final[inst] = t;
+        if (a.t_final) {
+            if constexpr (FFT)
+                a.t_final[inst] = at_tf ? tf : (double)th + (double)tl;
+            else
+                a.t_final[inst] = t;
+        }
         if (a.accepted) a.accepted[inst] = acc;
         if (a.rejected) a.rejected[inst] = rej;
         if (a.fevals) a.fevals[inst] = fev;

@@ -157,6 +157,7 @@ struct RhsPendulum : BuiltinRhs {
     // Mixed form: the drive phase Omega t reduced to [-pi, pi] in FP64 once per accepted step;
     // a stage at t + dt adds Omega dt to it in FP32 (diff_phase), so the stages need no FP64.
     static constexpr bool PHASE = true;
+    static constexpr int PHASE_RATE = 2;  // the parameter that is d(phase)/dt (Omega)
     __device__ static __forceinline__ float phase(double t, const double* p) {
         double ph = p[2] * t;
         double k = rint(ph * 0.15915494309189535);

@@ -81,7 +81,8 @@ typedef enum {
  *  FP64_FAST   — FP64 with FMA contraction and the fast CUDA math library.
  *  MIXED       — stage right-hand sides, stage combinations, the error norm, the step-size
  *                controller and the step size in FP32; y_{n+1} accumulated with Kahan
- *                compensation; t in FP64 (RK4: t and h in FP64).
+ *                compensation; t as an FP32 pair (about 48 bits, FP64 when output times,
+ *                crossings or events need it; RK4: t and h in FP64).
  *                Instances whose rtol is below the method's mixed-precision bound
  *                (degpu_set_mixed_min_rtol) run in FP64_FAST arithmetic instead. */
 typedef enum { DEGPU_FP64_PARITY = 0, DEGPU_FP64_FAST = 1, DEGPU_MIXED = 2 } degpu_precision;
