@@ -74,6 +74,12 @@ void ensure_registered() {
         register_verner76_fast();
         register_verner87_fast();
         register_verner98_fast();
+        register_verner_cross65_parity();
+        register_verner_cross76_parity();
+        register_verner_cross87_parity();
+        register_verner_cross98_parity();
+        register_verner_cross6576_fast();
+        register_verner_cross8798_fast();
     });
 }
 

@@ -237,7 +237,7 @@ struct Lane {
     // with tf in FP32 arithmetic, so that an accepted step issues no FP64 instruction. The built-in
     // families read no t (a drive phase is advanced as an FP32 pair too); run-time (NVRTC)
     // families keep the FP64 t they may read.
-    static constexpr bool FFT = MIX && !DENSE && FloatParamsOf<Rhs>::value;
+    static constexpr bool FFT = MIX && !DENSE;
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
     // itself, and the evaluation the crate repeats at the new point on acceptance is that stage.
     static constexpr bool FSAL_MIX = MIX && Tab::FSAL;
@@ -287,13 +287,20 @@ struct Lane {
         else
             Rhs::template diff<P>(tt, yy, dd, p);
     }
+    // The current time: under FFT the FP32 pair (dead code for autonomous families), else t.
+    __device__ __forceinline__ double tnow() const {
+        if constexpr (FFT)
+            return (double)th + (double)tl;
+        else
+            return t;
+    }
     // Right-hand side at t + dt in the mixed form: a family with a drive phase adds Omega dt to
     // the phase at t in FP32; the others get the stage time t + dt (unused by autonomous ones).
     __device__ __forceinline__ void rhs_at(float dt, const S* yy, S* dd) const {
         if constexpr (PHASE)
             Rhs::template diff_phase<P>(ph0, dt, yy, dd, pf);
         else
-            rhs(t + (double)dt, yy, dd);
+            rhs(tnow() + (double)dt, yy, dd);
     }
 
     // FFT: t += hf as an FP32 pair (TwoSum, then FastTwoSum), or t = tf after a clamped last step
@@ -1226,6 +1233,8 @@ struct Lane {
                 for (int c = 0; c < D; ++c) dydt[c] = k[NS - 1][c];
             } else if constexpr (PHASE) {
                 rhs_at(hf, ynew, dydt);
+            } else if constexpr (FFT) {
+                rhs(tnow(), ynew, dydt);
             } else {
                 rhs(t_new, ynew, dydt);
             }
@@ -1583,7 +1592,7 @@ struct Lane {
                 if constexpr (PHASE)
                     rhs_at(0.0f, y, k0);
                 else
-                    rhs(t, y, k0);
+                    rhs(tnow(), y, k0);
                 fev += 1;
             }
             result = 1;

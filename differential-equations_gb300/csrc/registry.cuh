@@ -207,6 +207,12 @@ void register_verner65_fast();
 void register_verner76_fast();
 void register_verner87_fast();
 void register_verner98_fast();
+void register_verner_cross65_parity();
+void register_verner_cross76_parity();
+void register_verner_cross87_parity();
+void register_verner_cross98_parity();
+void register_verner_cross6576_fast();
+void register_verner_cross8798_fast();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to

@@ -69,3 +69,22 @@ def test_threshold_and_capacity():
     assert int(o["cross_count"][0]) == 3
     assert np.allclose(o["cross_t"][:, 0], [math.pi / 3, 5 * math.pi / 3], atol=1e-9)
     assert np.allclose(o["cross_y"][:, 0, 0], 0.5, atol=1e-9)
+
+
+def test_verner_harmonic_zero_crossings():
+    """Verner's pairs on the same oscillators: every crossing is found. Newton's search on the
+    6(5) and 7(6) pairs' interpolants converges to the root; on the larger pairs the
+    interpolant's rounding at some crossings stays above the crate's convergence test (100 eps)
+    and the crate falls back to the linear estimate, up to ~5e-4 away."""
+    ks = [1.0, 2.0, 0.5]
+    b = harmonic_batch(ks, 10.0, 1e-11)
+    for method in range(abi.RKV655E, abi.RKV989E + 1):
+        cfg = abi.default_cfg(method)
+        cfg.max_steps = 10_000_000
+        o = O.solve_crossing(b, cfg, component=0, threshold=0.0, direction=abi.CROSS_BOTH, max_points=8)
+        tol = 1e-11 if method <= abi.RKV766E else 1e-3
+        for i, k in enumerate(ks):
+            w = math.sqrt(k)
+            exact = [(math.pi / 2 + j * math.pi) / w for j in range(16) if (math.pi / 2 + j * math.pi) / w < 10.0]
+            assert int(o["cross_count"][i]) == len(exact)
+            assert np.max(np.abs(o["cross_t"][:len(exact), i] - exact)) < tol
