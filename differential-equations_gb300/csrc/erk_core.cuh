@@ -234,10 +234,10 @@ struct Lane {
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
     static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
     // Mixed form without output: t as an FP32 pair th + tl (about 48 bits), advanced and compared
-    // with tf in FP32 arithmetic, so that an accepted step issues no FP64 instruction. The built-in
-    // families read no t (a drive phase is advanced as an FP32 pair too); run-time (NVRTC)
-    // families keep the FP64 t they may read.
-    static constexpr bool FFT = MIX && !DENSE;
+    // with tf in FP32 arithmetic, so that an accepted step issues no FP64 instruction. A drive
+    // phase is advanced as an FP32 pair too; a right-hand side that reads t gets th + tl widened
+    // (tnow). The FP64-controller build (DEGPU_MIXED_F32_CTRL=0) keeps t in FP64 as well.
+    static constexpr bool FFT = MIX && !DENSE && P::F32_CTRL;
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
     // itself, and the evaluation the crate repeats at the new point on acceptance is that stage.
     static constexpr bool FSAL_MIX = MIX && Tab::FSAL;
