@@ -264,8 +264,14 @@ typedef struct {
 } degpu_crossing_out;
 
 /* degpu_solve_ensemble with crossing detection instead of output times (in->n_eval must be 0),
- * device pointers, stream-ordered. Families: Van der Pol, pendulum, Lorenz, harmonic oscillator,
- * Brusselator and CR3BP (DEGPU_UNSUPPORTED otherwise); every method and precision. */
+ * device pointers, stream-ordered. Built combinations (DEGPU_UNSUPPORTED otherwise):
+ *  - RK4, DOPRI5, DOP853: Van der Pol, pendulum, Lorenz, harmonic oscillator, Brusselator, CR3BP,
+ *    logistic and exponential growth, every precision;
+ *  - RKF45, Cash-Karp: those eight families in FP64 parity; Van der Pol, pendulum and Lorenz in
+ *    FP64 fast and mixed;
+ *  - Verner's pairs: Van der Pol, pendulum, Lorenz and the harmonic oscillator in FP64 parity;
+ *    the first three in FP64 fast and mixed (a mixed solve runs these pairs in FP64 fast).
+ * The hyperplane and event entry points below build on the same kernels. */
 degpu_status degpu_solve_ensemble_crossing(const degpu_problem* problem, const degpu_method_cfg* cfg,
                                            const degpu_batch_in* in, const degpu_crossing* crossing,
                                            degpu_batch_out* out, degpu_crossing_out* crossing_out, void* stream);
