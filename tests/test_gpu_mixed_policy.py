@@ -81,3 +81,31 @@ def test_rk4_has_no_bound(bound):
     assert degpu.mixed_min_rtol(abi.RK4) == 0.0
     with pytest.raises(degpu.DegpuError):
         degpu.set_mixed_min_rtol(abi.RK4, 1e-8)
+
+
+@pytest.mark.parametrize("method", [abi.DOPRI5, abi.DOP853, abi.RKF45])
+@pytest.mark.parametrize("kernel", [abi.KERNEL_PERSISTENT, abi.KERNEL_THREAD])
+def test_mixed_time_pair_ends_at_tf_and_tracks_fp64(method, kernel):
+    """The mixed form keeps t (and the pendulum's drive phase) as an FP32 pair when no output times
+    are requested. With t0 far from zero (the pair's low part carries the offset's FP32 rounding)
+    every completed instance ends exactly at tf, and the final states stay as close to the FP64
+    solve as they are with t0 = 0."""
+    errs = []
+    for shift in (0.0, 1000.3):
+        e = W.config1(n=3000, first=777)
+        e.rtol = np.maximum(e.rtol, 1e-8)
+        e.atol = 1e-2 * e.rtol
+        nonchaotic = e.family != abi.RHS["LORENZ"]
+        e.t0 = e.t0 + shift
+        e.tf = e.t0 + np.minimum(e.tf - (e.t0 - shift), 20.0)
+        mixed = run(e, method, abi.MIXED, kernel)
+        fast = run(e, method, abi.FP64_FAST, kernel)
+        ok = mixed.status == abi.COMPLETE
+        assert ok.mean() > 0.99
+        assert np.array_equal(mixed.t_final[ok], e.tf[ok])
+        sel = ok & nonchaotic & (fast.status == abi.COMPLETE)
+        rel = np.max(np.abs(mixed.y_final[:, sel] - fast.y_final[:, sel]), axis=0) / \
+            np.maximum(np.max(np.abs(fast.y_final[:, sel]), axis=0), 1e-300)
+        errs.append(np.median(rel))
+    assert errs[0] < 1e-4 and errs[1] < 1e-4
+    assert errs[1] < 10 * errs[0] + 1e-6
