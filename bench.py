@@ -378,10 +378,12 @@ def run_bvp(args, torch, dev, lib):
 
 
 def run_adaptive(args, torch, dev, lib):
-    """The crate's Adaptive ERK family (RKF45, Cash-Karp) on the uneven ensemble (--n instances,
-    rtol ~ logU[1e-9,1e-5]): mixed on the multi-family persistent kernel, FP64 parity one
-    run-to-completion launch per family over the longest-first lists; CPU baseline = the oracle
-    on a sample."""
+    """The crate's Adaptive ERK family (RKF45, Cash-Karp; with --workload verner three of Verner's
+    pairs) on the uneven ensemble (--n instances, rtol ~ logU[1e-9,1e-5]): mixed on the
+    multi-family persistent kernel (Verner: FP64 fast, what their mixed solve runs), FP64 parity
+    one run-to-completion launch per family over the longest-first lists; CPU baseline = the
+    oracle on a sample."""
+    verner = args.workload == "verner"
     n = args.n
     e = W.config1(n=n)
     keep, bi, out, bo = _device_batch(torch, e, dev)
@@ -389,8 +391,14 @@ def run_adaptive(args, torch, dev, lib):
     stream = torch.cuda.Stream(device=dev)
     res = {}
     threads = os.cpu_count() or 1
-    for mname, method in (("rkf45", abi.RKF45), ("cash_karp", abi.CASH_KARP)):
-        for pname, prec in (("mixed", abi.MIXED), ("fp64-parity", abi.FP64_PARITY)):
+    if verner:  # a mixed solve of these pairs runs FP64 fast
+        methods = (("rkv656e", abi.RKV656E), ("rkv878e", abi.RKV878E), ("rkv989e", abi.RKV989E))
+        precs = (("fp64-fast", abi.FP64_FAST), ("fp64-parity", abi.FP64_PARITY))
+    else:
+        methods = (("rkf45", abi.RKF45), ("cash_karp", abi.CASH_KARP))
+        precs = (("mixed", abi.MIXED), ("fp64-parity", abi.FP64_PARITY))
+    for mname, method in methods:
+        for pname, prec in precs:
             cfg = abi.default_cfg(method)
             cfg.precision, cfg.max_steps = prec, e.max_steps
             f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
@@ -404,13 +412,16 @@ def run_adaptive(args, torch, dev, lib):
         s_e = e.subset(np.arange(args.cpu_sample // 2))
         _, dt = _oracle_solve(s_e, method, threads)
         res[f"{mname}-cpu"] = {"solves_per_s": s_e.n / dt, "cores": threads, "sample": s_e.n}
-    line = {"metric": "IVP solves/sec (uneven ensemble, RKF45 and Cash-Karp)",
-            "value": res["rkf45-mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-            "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 parity beside)", "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": f"uneven ensemble {n} instances, rtol~logU[1e-9,1e-5], RKF45 / Cash-Karp"},
+    head, label = (methods[0][0], "Verner RKV656e / RKV878e / RKV989e") if verner else ("rkf45", "RKF45 / Cash-Karp")
+    line = {"metric": f"IVP solves/sec (uneven ensemble, {label})",
+            "value": res[f"{head}-{precs[0][0]}"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "higher_is_better": True,
+            "dtype": "f64 (parity beside)" if verner else "f32/f64 mixed (fp64 parity beside)",
+            "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": f"uneven ensemble {n} instances, rtol~logU[1e-9,1e-5], {label}"},
             "variants": res,
-            "cpu_baseline": {"value": res["rkf45-cpu"]["solves_per_s"], "unit": "solves/s", "cores": threads,
-                             "kind": "port", "sample": f"first {args.cpu_sample // 2} instances, RKF45 (host libm)"}}
+            "cpu_baseline": {"value": res[f"{head}-cpu"]["solves_per_s"], "unit": "solves/s", "cores": threads,
+                             "kind": "port", "sample": f"first {args.cpu_sample // 2} instances, {head} (host libm)"}}
     print(json.dumps(line))
 
 
@@ -725,7 +736,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--workload", default="uneven",
                     choices=["uneven", "lorenz4096", "fpu", "gray-scott", "serving", "crossing", "hyperplane",
-                             "event", "adaptive", "bvp"],
+                             "event", "adaptive", "verner", "bvp"],
                     help="uneven = the headline 1M-instance ensemble; the others print their own line")
     ap.add_argument("--bvp-n", type=int, default=65536)
     ap.add_argument("--bvp-cpu-sample", type=int, default=2000)
@@ -762,7 +773,7 @@ def main():
             {"lorenz4096": run_lorenz4096, "fpu": run_fpu, "gray-scott": run_gray_scott,
              "serving": run_serving, "crossing": run_crossing, "hyperplane": run_crossing, "event": run_crossing,
              "bvp": run_bvp,
-             "adaptive": run_adaptive}[args.workload](args, torch, dev, lib)
+             "adaptive": run_adaptive, "verner": run_adaptive}[args.workload](args, torch, dev, lib)
         return
 
     # each rank solves its own slice of instances (weak scaling: instances are independent)
