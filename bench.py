@@ -32,14 +32,24 @@ from degpu import abi, workloads as W  # noqa: E402
 VARIANTS = {
     # name: (precision, kernel)
     "mixed-persistent": (abi.MIXED, abi.KERNEL_PERSISTENT),
-    "fp64-persistent": (abi.FP64_PARITY, abi.KERNEL_PERSISTENT),
-    "fp64-plain": (abi.FP64_PARITY, abi.KERNEL_THREAD),
-    "fp64fast-persistent": (abi.FP64_FAST, abi.KERNEL_PERSISTENT),
+    # the FP64 error norm, controller, accept decision and t over the same FP32 stages
+    "mixedf64ctrl-persistent": (abi.MIXED_FP64_CTRL, abi.KERNEL_PERSISTENT),
     "mixed-thread": (abi.MIXED, abi.KERNEL_THREAD),
     # FP32 stages for every instance: the mixed-precision bound switched off for this variant
     "mixed-persistent-nosplit": (abi.MIXED, abi.KERNEL_PERSISTENT),
+    # plain FP64: FMA contraction with the correctly rounded controller power; one
+    # run-to-completion launch per family ("fp64-plain") or the persistent work queue
+    "fp64-plain": (abi.FP64_PLAIN, abi.KERNEL_THREAD),
+    "fp64plain-persistent": (abi.FP64_PLAIN, abi.KERNEL_PERSISTENT),
+    "fp64fast-persistent": (abi.FP64_FAST, abi.KERNEL_PERSISTENT),
+    # the crate's operation order bit for bit (no contraction)
+    "fp64-parity": (abi.FP64_PARITY, abi.KERNEL_THREAD),
+    "fp64parity-persistent": (abi.FP64_PARITY, abi.KERNEL_PERSISTENT),
 }
 NOSPLIT = {"mixed-persistent-nosplit"}
+MIXED_PRECISIONS = (abi.MIXED, abi.MIXED_FP64_CTRL)
+# rtol decades of the uneven ensemble (rtol ~ logU[1e-9, 1e-5])
+DECADES = ((1e-9, 1e-8), (1e-8, 1e-7), (1e-7, 1e-6), (1e-6, 1e-5))
 
 # Algorithmic FP operations of one attempted DOPRI5 step of a d-dimensional system whose
 # right-hand side costs F operations (mul/add/div/sqrt = 1, pow/sin/cos not counted):
@@ -122,78 +132,148 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(e: W.Ensemble, sample: int, threads: int):
-    """The oracle (crate restatement, host libm) on the first `sample` instances."""
+def sample_index(n: int, sample: int) -> np.ndarray:
+    """Every k-th instance of the ensemble (k not a multiple of 3, so that the families, which
+    alternate by index, stay equally represented)."""
+    if sample >= n:
+        return np.arange(n)
+    k = max(1, n // sample)
+    while k > 1 and k % 3 == 0:
+        k -= 1
+    return (np.arange(sample) * k) % n
+
+
+def cpu_baseline(e: W.Ensemble, sample: int, threads: int, warm: bool = True):
+    """The oracle (crate restatement, host libm) on `sample` instances spread over the ensemble,
+    after a short untimed warm-up solve (threads created, pages touched)."""
     sys.path.insert(0, os.path.join(REPO, "tests"))
     import oracle_lib as O
 
-    s = e.subset(np.arange(sample))
+    s = e.subset(sample_index(e.n, sample))
     b = O.Batch(0, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, s.rtol, s.atol, family=s.family)
     cfg = abi.default_cfg(abi.DOPRI5)
     cfg.max_steps = s.max_steps
+    if warm:
+        w = s.subset(np.arange(min(s.n, 256)))
+        O.solve(O.Batch(0, w.dim, w.n_params, w.t0, w.tf, w.y0, w.params, w.rtol, w.atol, family=w.family), cfg,
+                threads=threads, math_mode=0)
     t = time.perf_counter()
     O.solve(b, cfg, threads=threads, math_mode=0)
     dt = time.perf_counter() - t
-    return sample / dt, dt
+    return s.n / dt, dt
 
 
-def accuracy_report(e: W.Ensemble, y_gpu: np.ndarray, per_family: int = 1000, threads: int = 0):
-    """Final-state error of the GPU result against (a) the FP64 oracle at the same tolerances
-    (the crate's CPU solver, restated) and (b) an FP64 oracle run at rtol = atol = 1e-13
-    (DOP853), on `per_family` instances of each family.  Relative error = max_c |a_c - b_c| /
-    max_c |b_c|.  Lorenz instances with rho > ~24.7 are chaotic over these horizons, so their
-    errors against any other trajectory grow to O(1); the table reports them as measured."""
-    sys.path.insert(0, os.path.join(REPO, "tests"))
-    import oracle_lib as O
+def uneven_config(n: int) -> dict:
+    """The `config` of the uneven-ensemble line, shared by both arms."""
+    return {"workload": f"uneven ensemble {n} instances/GPU: 1/3 Van der Pol, 1/3 damped driven pendulum, "
+                        f"1/3 Lorenz; t_end~U[5,50], rtol~logU[1e-9,1e-5], atol=1e-2 rtol, DOPRI5",
+            "l2": "flushed (256 MB write) between timed iterations"}
 
-    threads = threads or (os.cpu_count() or 1)
-    idx = np.concatenate([np.nonzero(e.family == f)[0][:per_family] for f in W.FAMILIES_C1])
-    s = e.subset(idx)
-    b = O.Batch(0, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, s.rtol, s.atol, family=s.family)
-    cfg = abi.default_cfg(abi.DOPRI5)
-    cfg.max_steps = s.max_steps
-    same = O.solve(b, cfg, threads=threads, math_mode=1)["y_final"]
-    bt = O.Batch(0, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, np.full(s.n, 1e-13), np.full(s.n, 1e-13),
-                 family=s.family)
-    cfg8 = abi.default_cfg(abi.DOP853)
-    cfg8.max_steps = 50_000_000
-    tight = O.solve(bt, cfg8, threads=threads, math_mode=1)["y_final"]
-    g = y_gpu[:, idx]
 
+class AccuracySample:
+    """Reference solutions for the accuracy report, on `per_family` instances of each family:
+    an FP64 oracle run at rtol = atol = 1e-13 (DOP853), the closest available stand-in for the
+    exact solution.  Relative error = max_c |a_c - b_c| / max_c |b_c|."""
+
+    def __init__(self, e: W.Ensemble, per_family: int = 1000, threads: int = 0):
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        import oracle_lib as O
+
+        threads = threads or (os.cpu_count() or 1)
+        self.idx = np.concatenate([np.nonzero(e.family == f)[0][:per_family] for f in W.FAMILIES_C1])
+        s = e.subset(self.idx)
+        bt = O.Batch(0, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, np.full(s.n, 1e-13), np.full(s.n, 1e-13),
+                     family=s.family)
+        cfg8 = abi.default_cfg(abi.DOP853)
+        cfg8.max_steps = 50_000_000
+        t = time.perf_counter()
+        self.tight = O.solve(bt, cfg8, threads=threads, math_mode=1)["y_final"]
+        self.oracle_s = time.perf_counter() - t
+        self.family = s.family
+        self.rtol = s.rtol
+        self.per_family = per_family
+
+    @staticmethod
     def rel(a, ref):
         return np.max(np.abs(a - ref), axis=0) / np.maximum(np.max(np.abs(ref), axis=0), 1e-300)
 
-    out = {}
-    names = {abi.RHS["VAN_DER_POL"]: "van_der_pol", abi.RHS["PENDULUM"]: "pendulum", abi.RHS["LORENZ"]: "lorenz"}
-    for f in W.FAMILIES_C1:
-        m = s.family == f
-        r_same = rel(g[:, m], same[:, m])
-        r_tight = rel(g[:, m], tight[:, m])
-        r_fp64_tight = rel(same[:, m], tight[:, m])
-        q = lambda v: {"median": float(np.median(v)), "p90": float(np.percentile(v, 90)), "max": float(np.max(v))}
-        out[names[f]] = {"vs_fp64_oracle": q(r_same), "frac_le_1e-6_vs_fp64_oracle": float(np.mean(r_same <= 1e-6)),
-                         "vs_tight_oracle": q(r_tight), "fp64_oracle_vs_tight": q(r_fp64_tight)}
-        if f == abi.RHS["LORENZ"]:
-            nc = s.params[1, m] < 24.0  # non-chaotic Lorenz (rho below the chaotic onset)
-            out[names[f]]["nonchaotic_vs_fp64_oracle"] = q(r_same[nc]) if nc.any() else None
-    out["sample"] = f"first {per_family} instances of each family; tight oracle = DOP853 rtol=atol=1e-13"
-    return out
+    def table(self, y: np.ndarray, floor: np.ndarray = None):
+        """Per family and rtol decade: error of the full-ensemble result `y` [3, n] against the
+        tight oracle (median, p90, share <= 1e-6), and the same for `floor` (the FP64 result at
+        the same tolerances) when given."""
+        g = y[:, self.idx]
+        f64 = floor[:, self.idx] if floor is not None else None
+        names = {abi.RHS["VAN_DER_POL"]: "van_der_pol", abi.RHS["PENDULUM"]: "pendulum",
+                 abi.RHS["LORENZ"]: "lorenz"}
+        out = {}
+        for f in W.FAMILIES_C1:
+            rows = {}
+            for lo, hi in DECADES:
+                m = (self.family == f) & (self.rtol >= lo) & (self.rtol < hi)
+                if not m.any():
+                    continue
+                r = self.rel(g[:, m], self.tight[:, m])
+                row = {"n": int(m.sum()), "median": float(np.median(r)), "p90": float(np.percentile(r, 90)),
+                       "frac_le_1e-6": float(np.mean(r <= 1e-6))}
+                if f64 is not None:
+                    r64 = self.rel(f64[:, m], self.tight[:, m])
+                    row["fp64_floor"] = {"median": float(np.median(r64)), "frac_le_1e-6": float(np.mean(r64 <= 1e-6))}
+                    rd = self.rel(g[:, m], f64[:, m])
+                    row["vs_fp64_same_tol_median"] = float(np.median(rd))
+                rows[f"{lo:.0e}..{hi:.0e}"] = row
+            out[names[f]] = rows
+        return out
+
+    def meets_fp64_floor(self, tab):
+        """The decades (family, rtol decade) where the FP64 result itself reaches 1e-6 against the
+        tight oracle on the median, and whether the variant does there too."""
+        qual, ok = [], True
+        for fam, rows in tab.items():
+            for dec, row in rows.items():
+                fl = row.get("fp64_floor")
+                if fl and fl["median"] <= 1e-6:
+                    qual.append(f"{fam} {dec}")
+                    ok = ok and row["median"] <= 1e-6
+        return {"decades_where_fp64_meets_1e-6": qual, "variant_meets_1e-6_there": ok}
 
 
-def _clock_ms(fn, stream, torch, reps, warmup=True):
-    """Mean CUDA-event time of fn() on `stream` over `reps` calls (after one warm-up call)."""
+def agreement(acc, rej, y, acc_ref, rej_ref, y_ref, conditioned):
+    """Per instance, how a variant's solve agrees with the crate's (the FP64 parity path, which
+    equals the oracle bit for bit): share with equal accepted and rejected step counts, and share
+    whose final state is within 1e-12 relative, over all instances and over the well-conditioned
+    ones (those whose final state moves by at most 1e-12 when y0 is perturbed by 1e-14)."""
+    same_steps = (acc == acc_ref) & (rej == rej_ref)
+    r = np.max(np.abs(y - y_ref), axis=0) / np.maximum(np.max(np.abs(y_ref), axis=0), 1e-300)
+    within = r <= 1e-12
+    return {"step_count_agreement": float(np.mean(same_steps)),
+            "final_state_within_1e-12": float(np.mean(within)),
+            "final_state_within_1e-12_conditioned": float(np.mean(within[conditioned])) if conditioned.any() else None,
+            "conditioned_instances": int(conditioned.sum()),
+            "step_count_agreement_conditioned": float(np.mean(same_steps[conditioned])) if conditioned.any() else None}
+
+
+def _clock_ms(fn, stream, torch, reps, warmup=True, flush=None, clocks=None):
+    """Mean CUDA-event time of fn() on `stream` over `reps` calls (after one warm-up call); with
+    `flush`, that buffer is overwritten on the stream before each timed call (outside the events),
+    so every call starts with a cold L2; `clocks` samples the SM clocks over the timed calls."""
     if warmup:
         fn()
     stream.synchronize()
+    if clocks:
+        clocks.start()
     ms = []
     for _ in range(reps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         fn()
         b.record(stream)
         b.synchronize()
         ms.append(a.elapsed_time(b))
-    return float(np.mean(ms))
+    ck = clocks.stop() if clocks else None
+    return (float(np.mean(ms)), ck) if clocks else float(np.mean(ms))
 
 
 def _device_batch(torch, e, dev, dims=None):
@@ -236,6 +316,10 @@ def _oracle_solve(e, method, threads, math_mode=0):
     o = O.solve(b, cfg, threads=threads, math_mode=math_mode)
     return o, time.perf_counter() - t
 
+
+# DRAM bytes (read + write) of the four FP32 Gray-Scott passes of one RK4 step at 4096^2, from an
+# ncu capture of gs_pass_vec_kernel<float>
+GS_NCU_TRAFFIC_FP32 = 1.84e9
 
 # the hyperplane workload's plane: pos = (y0, y1) through (0.1, -0.2) with normal (1, 1)
 PLANE = ([0, 1], [0.1, -0.2], [1.0, 1.0])
@@ -425,33 +509,68 @@ def run_adaptive(args, torch, dev, lib):
     print(json.dumps(line))
 
 
-def run_lorenz4096(args, torch, dev, lib):
-    """4096 Lorenz IVPs (d=3), DOPRI5 rtol=1e-8 atol=1e-10 on [0, 20]: plain FP64 parity kernel,
-    persistent parity kernel, and the CPU oracle with every host thread."""
+def fp64_peak_of(lib):
+    pk = C.c_double(0.0)
+    lib.degpu_internal_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    lib.degpu_internal_fma_peak(1, C.byref(pk))
+    return pk.value
+
+
+def run_lorenz4096(args, torch, dev, lib, fp64_peak=None, emit=True):
+    """4096 Lorenz IVPs (d=3), DOPRI5 rtol=1e-8 atol=1e-10 on [0, 20], FP64: the parity kernel
+    (the crate's operation order, equal to the oracle bit for bit), the plain FP64 kernel (FMA
+    contraction), their persistent forms and the mixed form; the CPU oracle with every host
+    thread on all 4096 instances.  L2 flushed before every timed solve."""
     e = W.config0()
+    fp64_peak = fp64_peak or fp64_peak_of(lib)
     stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     keep, bi, out, bo = _device_batch(torch, e, dev)
     prob = abi.Problem(rhs_id=e.rhs_id, dim=3, n_params=3)
-    res = {}
-    for name, (prec, kern) in (("fp64-plain", (abi.FP64_PARITY, abi.KERNEL_THREAD)),
-                               ("fp64-persistent", (abi.FP64_PARITY, abi.KERNEL_PERSISTENT)),
+    threads = os.cpu_count() or 1
+    o, _ = _oracle_solve(e, abi.DOPRI5, threads, math_mode=1)
+    res, ck = {}, None
+    for name, (prec, kern) in (("fp64-parity", (abi.FP64_PARITY, abi.KERNEL_THREAD)),
+                               ("fp64-plain", (abi.FP64_PLAIN, abi.KERNEL_THREAD)),
+                               ("fp64parity-persistent", (abi.FP64_PARITY, abi.KERNEL_PERSISTENT)),
+                               ("fp64plain-persistent", (abi.FP64_PLAIN, abi.KERNEL_PERSISTENT)),
                                ("mixed-persistent", (abi.MIXED, abi.KERNEL_PERSISTENT))):
         cfg = abi.default_cfg(abi.DOPRI5)
         cfg.precision, cfg.kernel, cfg.max_steps = prec, kern, e.max_steps
         f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
                                              C.c_void_p(stream.cuda_stream))
-        ms = _clock_ms(f, stream, torch, max(1, args.steps))
-        res[name] = {"solves_per_s": e.n / (ms * 1e-3), "ms": ms}
-    threads = os.cpu_count() or 1
-    o, dt = _oracle_solve(e, abi.DOPRI5, threads)
+        if name == "fp64-parity":
+            ms, ck = _clock_ms(f, stream, torch, max(3, min(args.steps, 10)), flush=flush, clocks=Clocks())
+        else:
+            ms = _clock_ms(f, stream, torch, 3, flush=flush)
+        ga, gr = out["accepted"].cpu().numpy(), out["rejected"].cpu().numpy()
+        gy = out["y_final"].cpu().numpy()
+        r = np.max(np.abs(gy - o["y_final"]), axis=0) / np.max(np.abs(o["y_final"]), axis=0)
+        ops = flops_of(np.full(e.n, e.rhs_id), ga, gr)
+        res[name] = {"solves_per_s": e.n / (ms * 1e-3), "ms": ms,
+                     "step_count_agreement_with_oracle": float(np.mean((ga == o["accepted"]) & (gr == o["rejected"]))),
+                     "final_state_within_1e-12_of_oracle": float(np.mean(r <= 1e-12)),
+                     "bitwise_equal_to_oracle": bool(np.array_equal(gy, o["y_final"])),
+                     "fp64_algorithmic_frac": ops / (ms * 1e-3) / 1e12 / fp64_peak}
+    cdt = min(_oracle_solve(e, abi.DOPRI5, threads)[1] for _ in range(2))  # libm, the first run warms up
+    head = res["fp64-parity"]
+    a64 = head["fp64_algorithmic_frac"] * fp64_peak
     line = {"metric": "IVP solves/sec (4096 Lorenz, DOPRI5 rtol=1e-8 atol=1e-10, t in [0,20])",
-            "value": res["fp64-plain"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": "lorenz-4096"}, "variants": res,
+            "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": max(3, min(args.steps, 10)),
+            "ms_per_step": head["ms"], "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+            "config": {"workload": "lorenz-4096 (rho~U[10,50], y0=(1,1,1)+N(0,0.01)), DOPRI5 rtol=1e-8 atol=1e-10, "
+                                   "t in [0,20]", "variant": "fp64-parity (one run-to-completion launch)",
+                       "l2": "flushed (256 MB write) before every timed solve"},
+            "variants": res, "clocks": ck,
             "step_attempts": int((o["accepted"] + o["rejected"]).sum()),
-            "cpu_baseline": {"value": e.n / dt, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": "all 4096 instances (host libm)"}}
-    print(json.dumps(line))
+            "roofline": {"bound": "fp64", "achieved": a64, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": head["fp64_algorithmic_frac"], "traffic": None, "kernel": "erk_thread_kernel",
+                         "peak_source": "self-measured FP64 FMA probe"},
+            "cpu_baseline": {"value": e.n / cdt, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": "all 4096 instances (host libm, second of two runs)"}}
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def fpu_energy(torch, y, dims, beta):
@@ -468,43 +587,63 @@ def fpu_energy(torch, y, dims, beta):
     return (p * p).sum(0) / 2 + (dlt * dlt / 2 + beta[None, :] * dlt ** 4 / 4).sum(0)
 
 
-def run_fpu(args, torch, dev, lib):
-    """131,072 FPU-beta chains (2..128 masses), DOP853 rtol=1e-10 atol=1e-12 on [0,100] with 64
-    output times: group-per-system kernel, FP64 parity and mixed; energy drift from the dense
-    output; CPU oracle on a sample."""
-    n = args.fpu_n
+def fpu_step_ops(dims, accepted, rejected):
+    """Algorithmic FP operations of DOP853 on FPU-beta chains with output times (FMA = 2): per
+    attempted step 2*103*d stage combinations + 12 d, 11 right-hand sides of about 3.5 d each; per
+    accepted step 4 more right-hand sides and 2*(42+68)*d for the dense coefficients."""
+    d = dims.astype(np.float64)
+    F = 3.5 * d
+    att = (accepted + rejected).astype(np.float64)
+    return float(np.sum(att * (206 * d + 12 * d + 11 * F) + accepted * (4 * F + 220 * d)))
+
+
+def run_fpu(args, torch, dev, lib, n=None, emit=True):
+    """FPU-beta chains (2..128 masses), DOP853 rtol=1e-10 atol=1e-12 on [0,100] with 64 output
+    times: group-per-system kernel, FP64 parity, FP64 fast and the library's mixed form (whose
+    precision bound runs rtol 1e-10 in FP64); energy drift from the dense output; CPU oracle on a
+    sample.  With `n`, the first n chains of the 131,072."""
+    n = n or args.fpu_n
     e = W.config2(n=n)
     stream = torch.cuda.Stream(device=dev)
     keep, bi, out, bo = _device_batch(torch, e, dev, dims=e.dims)
     prob = abi.Problem(rhs_id=e.rhs_id, dim=e.dim, n_params=1)
-    res = {}
+    res, ck = {}, None
     dims_t = keep["dims"]
     beta_t = keep["params"][0]
     bound = lib.degpu_mixed_min_rtol(abi.DOP853)
-    # "mixed": the library's mixed form, whose precision bound sends every chain (rtol 1e-10) to
-    # FP64; "mixed-nosplit": FP32 stages forced on every chain, which cannot reach rtol 1e-10 —
-    # its attempted steps are capped so that chains whose error estimate sits on the FP32 noise
-    # floor end (as MaxSteps) in bounded time
-    for name, prec in (("fp64", abi.FP64_PARITY), ("mixed", abi.MIXED), ("mixed-nosplit", abi.MIXED)):
+    fp64_peak = fp64_peak_of(lib)
+    names = [("fp64", abi.FP64_PARITY), ("fp64-fast", abi.FP64_FAST), ("mixed", abi.MIXED)]
+    if emit:
+        # FP32 stages forced on every chain, which cannot reach rtol 1e-10: attempted steps are
+        # capped so that chains whose error estimate sits on the FP32 noise floor end (as
+        # MaxSteps) in bounded time
+        names.append(("mixed-nosplit", abi.MIXED))
+    for name, prec in names:
         cfg = abi.default_cfg(abi.DOP853)
         nosplit = name == "mixed-nosplit"
         lib.degpu_set_mixed_min_rtol(abi.DOP853, 0.0 if nosplit else bound)
         cfg.precision, cfg.max_steps = prec, e.max_steps if not nosplit else args.fpu_mixed_max_steps
         f = lambda: lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo),
                                              C.c_void_p(stream.cuda_stream))
-        ms = _clock_ms(f, stream, torch, max(1, args.steps), warmup=False)
+        if name == "fp64":
+            ms, ck = _clock_ms(f, stream, torch, max(1, min(args.steps, 3)), warmup=False, clocks=Clocks())
+        else:
+            ms = _clock_ms(f, stream, torch, 1, warmup=False)
         h0 = fpu_energy(torch, out["dense"][0], dims_t, beta_t)
         h1 = fpu_energy(torch, out["dense"][-1], dims_t, beta_t)
         ok = (out["status"] == 0).cpu().numpy()
         drift = ((h1 - h0).abs() / h0.abs()).cpu().numpy()[ok]
         st = out["status"].cpu().numpy()
+        ops = fpu_step_ops(e.dims, out["accepted"].cpu().numpy(), out["rejected"].cpu().numpy())
         res[name] = {"solves_per_s": n / (ms * 1e-3), "ms": ms,
                      "energy_drift_rel": {"median": float(np.median(drift)), "p99": float(np.percentile(drift, 99)),
                                           "max": float(np.max(drift))} if ok.any() else None,
                      "step_attempts": int((out["accepted"] + out["rejected"]).sum().item()),
+                     "fp64_algorithmic_frac": ops / (ms * 1e-3) / 1e12 / fp64_peak if name != "mixed-nosplit" else None,
                      "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}}
         res[name]["fp64_chains"] = int((e.rtol < (0.0 if nosplit else bound)).sum()) if prec == abi.MIXED else n
-        print(json.dumps({"fpu_variant": name, **res[name]}), flush=True)
+        if emit:
+            print(json.dumps({"fpu_variant": name, **res[name]}), flush=True)
         if name == "fp64":
             y64 = out["dense"][-1].clone()
         else:
@@ -514,24 +653,36 @@ def run_fpu(args, torch, dev, lib):
                                           if d.numel() else None)
     lib.degpu_set_mixed_min_rtol(abi.DOP853, bound)
     threads = os.cpu_count() or 1
-    s = e.subset(np.arange(args.fpu_cpu_sample))
+    s = e.subset(np.arange(min(n, args.fpu_cpu_sample)))
     s.dim = e.dim
+    _oracle_solve(s.subset(np.arange(min(s.n, 16))), abi.DOP853, threads)  # warm-up
     o, dt = _oracle_solve(s, abi.DOP853, threads)
+    head = res["fp64"]
     line = {"metric": "IVP solves/sec (FPU-beta chains, DOP853 + 64 dense outputs)",
-            "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-            "higher_is_better": True, "dtype": "f32/f64 mixed (f64 below rtol %g)" % bound,
+            "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": max(1, min(args.steps, 3)),
+            "ms_per_step": head["ms"], "higher_is_better": True, "dtype": "f64",
             "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": f"fpu-beta {n} chains, masses int-logU[2,128], t in [0,100]",
-                       "mixed_min_rtol": bound}, "variants": res,
-            "cpu_baseline": {"value": args.fpu_cpu_sample / dt, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": f"first {args.fpu_cpu_sample} chains (host libm)"}}
-    print(json.dumps(line))
+            "config": {"workload": f"fpu-beta: the first {n} of the 131,072 chains (masses int-logU[2,128]), "
+                                   f"DOP853 rtol=1e-10 atol=1e-12, t in [0,100], 64 output times",
+                       "variant": "fp64 (parity, group-per-system kernel)", "mixed_min_rtol": bound,
+                       "l2": "not flushed; chain state lives in registers and shared memory"},
+            "variants": res, "clocks": ck,
+            "roofline": {"bound": "fp64", "achieved": head["fp64_algorithmic_frac"] * fp64_peak, "peak": fp64_peak,
+                         "unit": "TFLOP/s", "frac": head["fp64_algorithmic_frac"], "traffic": None,
+                         "kernel": "erk_group_kernel", "peak_source": "self-measured FP64 FMA probe"},
+            "cpu_baseline": {"value": s.n / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"first {s.n} chains (host libm)"}}
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
-def run_gray_scott(args, torch, dev, lib):
+def run_gray_scott(args, torch, dev, lib, emit=True):
     """2-D Gray-Scott, 4096 x 4096 periodic, RK4 dt = 0.2 dx^2/Du, 1000 steps, FP64 and FP32:
-    time per step and algorithmic HBM bandwidth (240 / 120 B per node per step) vs the measured
-    copy bandwidth."""
+    time per step and algorithmic HBM bandwidth against the measured copy bandwidth, on two byte
+    models per node and RK4 step: this build's passes (15 arrays of 2 fields: 240 / 120 B FP64 /
+    FP32) and the minimal one (13 arrays: 208 / 104 B).  The inputs (134 / 268 MB) are larger
+    than L2; the 1000 steps are one timed call."""
     nx = ny = args.gs_n
     dx = 1.0 / 4096
     p = W.GRAY_SCOTT
@@ -543,7 +694,7 @@ def run_gray_scott(args, torch, dev, lib):
     mp = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(mp):
         peak = json.load(open(mp)).get("hbm_gbs")
-    res = {}
+    res, ck = {}, None
     steps = args.gs_steps
     for name, prec, tdt, bpn in (("fp32", abi.MIXED, torch.float32, 120), ("fp64", abi.FP64_FAST, torch.float64, 240),
                                  ("fp64-parity", abi.FP64_PARITY, torch.float64, 240)):
@@ -551,11 +702,17 @@ def run_gray_scott(args, torch, dev, lib):
         v = torch.as_tensor(v0, dtype=tdt, device=dev)
         f = lambda: lib.degpu_gray_scott_rk4(C.byref(gs), prec, 0.0, dt, steps, C.c_void_p(u.data_ptr()),
                                              C.c_void_p(v.data_ptr()), C.c_void_p(stream.cuda_stream))
-        ms = _clock_ms(f, stream, torch, 1)
+        if name == "fp32":
+            ms, ck = _clock_ms(f, stream, torch, 1, clocks=Clocks())
+        else:
+            ms = _clock_ms(f, stream, torch, 1)
         per_step = ms / steps
         gbs = bpn * nx * ny / (per_step * 1e-3) / 1e9
+        gbs_min = (bpn * 13 // 15) * nx * ny / (per_step * 1e-3) / 1e9
         res[name] = {"ms_per_step": per_step, "algorithmic_GBps": gbs,
                      "frac_of_measured_hbm": (gbs / peak) if peak else None,
+                     "algorithmic_GBps_13_arrays": gbs_min,
+                     "frac_of_measured_hbm_13_arrays": (gbs_min / peak) if peak else None,
                      "node_steps_per_s": nx * ny / (per_step * 1e-3)}
     # CPU baseline: the oracle's restatement of SemiDiscretePde::diff on a 256x256 grid, 4 steps
     sys.path.insert(0, os.path.join(REPO, "tests"))
@@ -572,10 +729,18 @@ def run_gray_scott(args, torch, dev, lib):
             "unit": "node-steps/s", "n_gpus": 1, "steps": steps, "higher_is_better": True,
             "dtype": "f32 (fp64 reported beside)", "data": "synthetic (seeded squares)",
             "config": {"workload": f"gray-scott {nx}x{ny} periodic, dt=0.2dx^2/Du, {steps} RK4 steps"},
-            "variants": res, "hbm_peak_GBps": peak,
+            "ms_per_step": res["fp32"]["ms_per_step"],
+            "variants": res, "hbm_peak_GBps": peak, "clocks": ck,
+            "roofline": {"bound": "hbm", "achieved": res["fp32"]["algorithmic_GBps"], "peak": peak, "unit": "GB/s",
+                         "frac": res["fp32"]["frac_of_measured_hbm"], "kernel": "gs_pass_vec_kernel<float>",
+                         "traffic": GS_NCU_TRAFFIC_FP32, "traffic_unit": "bytes per RK4 step (4 launches)",
+                         "bytes_per_node_step": 120,
+                         "frac_13_arrays": res["fp32"]["frac_of_measured_hbm_13_arrays"]},
             "cpu_baseline": {"value": cn * cn * 4 / cdt, "unit": "node-steps/s", "cores": threads, "kind": "port",
                              "sample": "256x256 grid, 4 RK4 steps, FP64 (restated SemiDiscretePde::diff)"}}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def serving_requests(count, seed_base=7_000_000):
@@ -704,7 +869,7 @@ def run_reference(args):
     sample = args.cpu_sample
     vals = []
     for i in range(args.warmup + args.steps):
-        v, _ = cpu_baseline(e, sample, threads)
+        v, _ = cpu_baseline(e, sample, threads, warm=False)
         if i >= args.warmup:
             vals.append(v)
     v = float(np.mean(vals))
@@ -712,10 +877,10 @@ def run_reference(args):
         "impl": "reference", "metric": "IVP solves/sec (uneven ensemble, DOPRI5)", "value": v, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": f"uneven ensemble {n_all} instances (VdP/pendulum/Lorenz), DOPRI5",
-                   "sample_instances": sample},
+        "config": uneven_config(n_all),
         "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample} instances of the workload per step"},
+                         "sample": f"{sample} instances spread over the workload (every k-th) per step; "
+                                   f"C++ restatement of the crate's solver with host libm"},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -728,8 +893,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", default="mixed-persistent", choices=list(VARIANTS))
-    ap.add_argument("--compare", default="fp64-plain,mixed-persistent-nosplit",
+    ap.add_argument("--compare", default="fp64-plain,fp64plain-persistent,fp64fast-persistent,fp64parity-persistent,"
+                                         "mixedf64ctrl-persistent,mixed-persistent-nosplit",
                     help="comma list of extra variants timed once each")
+    ap.add_argument("--accuracy-per-family", type=int, default=1000)
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 4096-Lorenz, Gray-Scott and FPU-chain lines of the default run")
+    ap.add_argument("--fpu-slice", type=int, default=16384,
+                    help="chains of the FPU-beta configuration timed in the default run")
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--cpu-sample", type=int, default=12000)
     ap.add_argument("--no-cpu", action="store_true")
@@ -850,6 +1021,7 @@ def main():
     status = d_out["status"].cpu().numpy()
     acc = d_out["accepted"].cpu().numpy()
     rej = d_out["rejected"].cpu().numpy()
+    y_head = d_out["y_final"].cpu().numpy()
     value = n * world / (ms * 1e-3)
     steps_per_s = float((acc + rej).sum()) * world / (ms * 1e-3)
     fam = e.family
@@ -864,16 +1036,20 @@ def main():
     fp64_peak = pk.value
     lib.degpu_internal_fma_peak(0, C.byref(pk))
     fp32_peak = pk.value
-    total_ops = flops_of(fam, acc, rej)
-    if prec != abi.MIXED:
-        fp64_ops, fp32_ops = total_ops, 0.0
-    else:
+
+    def split_ops(variant, a_, r_):
+        """(FP64, FP32) algorithmic operations of a variant's solve."""
+        p_ = VARIANTS[variant][0]
+        total = flops_of(fam, a_, r_)
+        if p_ not in MIXED_PRECISIONS:
+            return total, 0.0
         # instances below the mixed-precision bound run every operation in FP64
-        split = 0.0 if args.variant in NOSPLIT else bound
-        lo = e.rtol < split
+        lo = e.rtol < (0.0 if variant in NOSPLIT else bound)
         hi = ~lo
-        fp64_ops = flops_of(fam[lo], acc[lo], rej[lo]) + fp64_ops_mixed(fam[hi], acc[hi], rej[hi])
-        fp32_ops = total_ops - fp64_ops
+        f64 = flops_of(fam[lo], a_[lo], r_[lo]) + fp64_ops_mixed(fam[hi], a_[hi], r_[hi])
+        return f64, total - f64
+
+    fp64_ops, fp32_ops = split_ops(args.variant, acc, rej)
     t_s = ms * 1e-3 / world
     a64 = fp64_ops / t_s / 1e12
     a32 = fp32_ops / t_s / 1e12
@@ -910,51 +1086,97 @@ def main():
         assert rc == abi.OK
     e2e = n * world / (float(np.mean(e2e_ms)) * 1e-3)
 
-    accuracy = None
-    if rank == 0 and not args.no_accuracy:
-        accuracy = accuracy_report(e, d_out["y_final"].cpu().numpy())
-
-    extra = {}
+    # the other variants, timed once each; their results feed the accuracy and agreement reports
+    extra, results = {}, {args.variant: (acc, rej, y_head)}
     for v in [x for x in args.compare.split(",") if x in VARIANTS and x != args.variant]:
         set_split(v)
         t, _ = timed(cfg_of(v), 1, 1)
+        va, vr = d_out["accepted"].cpu().numpy(), d_out["rejected"].cpu().numpy()
+        results[v] = (va, vr, d_out["y_final"].cpu().numpy())
         extra[v] = {"solves_per_s": n * world / (t * 1e-3), "ms": t,
                     "status_counts": {str(k): int(c) for k, c in
                                       zip(*np.unique(d_out["status"].cpu().numpy(), return_counts=True))}}
-        if VARIANTS[v][0] != abi.MIXED:
-            # algorithmic FP64 rate of an FP64 variant against the FP64 FMA peak
-            va, vr = d_out["accepted"].cpu().numpy(), d_out["rejected"].cpu().numpy()
-            a64v = flops_of(fam, va, vr) / (t * 1e-3 / world) / 1e12
-            extra[v]["fp64_algorithmic"] = {"achieved": a64v, "peak": fp64_peak, "unit": "TFLOP/s",
-                                            "frac": a64v / fp64_peak}
-        if v in NOSPLIT and rank == 0 and not args.no_accuracy:
-            extra[v]["accuracy"] = accuracy_report(e, d_out["y_final"].cpu().numpy())
+        o64, o32 = split_ops(v, va, vr)
+        extra[v]["fp64_algorithmic"] = {"achieved": o64 / (t * 1e-3 / world) / 1e12, "peak": fp64_peak,
+                                        "unit": "TFLOP/s", "frac": o64 / (t * 1e-3 / world) / 1e12 / fp64_peak}
+        if o32:
+            extra[v]["fp32_algorithmic"] = {"achieved": o32 / (t * 1e-3 / world) / 1e12, "peak": fp32_peak,
+                                            "unit": "TFLOP/s", "frac": o32 / (t * 1e-3 / world) / 1e12 / fp32_peak}
     set_split(args.variant)
+
+    # agreement with the crate's solve (the FP64 parity path, bit for bit the oracle's) over the
+    # whole ensemble, for every FP64 variant that is not the parity path itself
+    agree = None
+    if rank == 0 and not args.no_accuracy:
+        ref_name = next((v for v in ("fp64parity-persistent", "fp64-parity") if v in results), None)
+        if ref_name is None:
+            set_split("fp64parity-persistent")
+            timed(cfg_of("fp64parity-persistent"), 1, 0)
+            ref_name = "fp64parity-persistent"
+            results[ref_name] = (d_out["accepted"].cpu().numpy(), d_out["rejected"].cpu().numpy(),
+                                 d_out["y_final"].cpu().numpy())
+        ra, rr, ry = results[ref_name]
+        # conditioning: the parity solve again with y0 perturbed by 1e-14 relative
+        pert = d_in["y0"] * (1.0 + 1e-14)
+        saved = d_in["y0"].clone()
+        d_in["y0"].copy_(pert)
+        timed(cfg_of("fp64parity-persistent"), 1, 0)
+        d_in["y0"].copy_(saved)
+        yp = d_out["y_final"].cpu().numpy()
+        cond = (np.max(np.abs(yp - ry), axis=0) / np.maximum(np.max(np.abs(ry), axis=0), 1e-300)) <= 1e-12
+        agree = {"reference": f"{ref_name} (equal to the oracle bit for bit)",
+                 "conditioned": "instances whose final state moves by <= 1e-12 relative when y0 is perturbed by "
+                                "1e-14 relative", "conditioned_share": float(np.mean(cond))}
+        for v, (va, vr, vy) in results.items():
+            if VARIANTS[v][0] in (abi.FP64_PLAIN, abi.FP64_FAST):
+                agree[v] = agreement(va, vr, vy, ra, rr, ry, cond)
+        set_split(args.variant)
+
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        acc_s = AccuracySample(e, per_family=args.accuracy_per_family)
+        floor_name = next((v for v in ("fp64fast-persistent", "fp64-plain", "fp64plain-persistent") if v in results),
+                          None)
+        floor = results[floor_name][2] if floor_name else None
+        accuracy = {"reference": "FP64 oracle (DOP853) at rtol = atol = 1e-13",
+                    "sample": f"first {args.accuracy_per_family} instances of each family",
+                    "floor": f"{floor_name}: FP64 at the same tolerances", "oracle_s": acc_s.oracle_s, "variants": {}}
+        for v, (_va, _vr, vy) in results.items():
+            if VARIANTS[v][0] in MIXED_PRECISIONS:
+                tab = acc_s.table(vy, floor)
+                accuracy["variants"][v] = {"by_family_and_rtol": tab, "rule": acc_s.meets_fp64_floor(tab)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, dt = cpu_baseline(e, args.cpu_sample, threads)
         cpu = {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"first {args.cpu_sample} instances of the workload ({dt:.1f} s, host libm)"}
+               "sample": f"{args.cpu_sample} instances spread over the workload (every k-th), {dt:.1f} s, "
+                         f"host libm; C++ restatement of the crate's solver"}
+
+    configs = {}
+    if rank == 0 and not args.no_configs:
+        configs["lorenz4096"] = run_lorenz4096(args, torch, dev, lib, fp64_peak, emit=False)
+        configs["gray_scott_4096"] = run_gray_scott(args, torch, dev, lib, emit=False)
+        configs["fpu_slice"] = run_fpu(args, torch, dev, lib, n=args.fpu_slice, emit=False)
 
     # per solve: persistent variants = 3 planning kernels + 1 multi-family ensemble kernel;
     # thread variants = one ensemble kernel per family
     per_solve = 4 if VARIANTS[args.variant][1] == abi.KERNEL_PERSISTENT else 3
-    if prec == abi.MIXED and args.variant not in NOSPLIT and bound > 0.0:
+    if prec in MIXED_PRECISIONS and args.variant not in NOSPLIT and bound > 0.0:
         per_solve += 1 if VARIANTS[args.variant][1] == abi.KERNEL_PERSISTENT else 3  # FP64 part
     launches = per_solve * args.steps
+    cfgd = uneven_config(n)
+    cfgd.update({"variant": args.variant,
+                 "mixed_min_rtol": (0.0 if args.variant in NOSPLIT else bound) if prec in MIXED_PRECISIONS else None,
+                 "fp64_instances": int((e.rtol < bound).sum()) if prec in MIXED_PRECISIONS and
+                 args.variant not in NOSPLIT else (n if prec not in MIXED_PRECISIONS else 0)})
     line = {
         "metric": "IVP solves/sec (uneven ensemble, DOPRI5)", "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32/f64 mixed" if prec == abi.MIXED else "f64",
+        "vs_baseline": None, "dtype": "f32/f64 mixed" if prec in MIXED_PRECISIONS else "f64",
         "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": f"uneven ensemble {n} instances/GPU: 1/3 Van der Pol, 1/3 damped driven pendulum, "
-                               f"1/3 Lorenz; t_end~U[5,50], rtol~logU[1e-9,1e-5], DOPRI5",
-                   "variant": args.variant, "l2": "flushed (256 MB write) between timed iterations",
-                   "mixed_min_rtol": (0.0 if args.variant in NOSPLIT else bound) if prec == abi.MIXED else None,
-                   "fp64_instances": int((e.rtol < bound).sum()) if prec == abi.MIXED and args.variant not in NOSPLIT
-                   else (n if prec != abi.MIXED else 0)},
+        "config": cfgd,
         "steps_per_s": steps_per_s,
         "status_counts": {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
         "roofline": roof,
@@ -963,7 +1185,9 @@ def main():
         "gpu_launches": launches,
         "clocks": ck,
         "variants": extra,
+        "agreement_with_crate": agree,
         "accuracy": accuracy,
+        "configs": configs,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -21,7 +21,7 @@
 #include <vector>
 
 #include "registry.cuh"
-#include "wps.cuh"
+#include "side_paths.cuh"
 
 namespace degpu {
 
@@ -80,6 +80,8 @@ void ensure_registered() {
         register_verner_cross98_parity();
         register_verner_cross6576_fast();
         register_verner_cross8798_fast();
+        register_plain();
+        register_mixed_f64ctrl();
     });
 }
 
@@ -136,14 +138,15 @@ static std::atomic<double>& mixed_bound(int m) {
 }
 
 double mixed_split(const degpu_method_cfg* cfg) {
-    if (cfg->precision != DEGPU_MIXED || cfg->method == DEGPU_RK4) return 0.0;
+    if (!(cfg->precision == DEGPU_MIXED || cfg->precision == DEGPU_MIXED_FP64_CTRL) || cfg->method == DEGPU_RK4)
+        return 0.0;
     // Verner's pairs: their stage sums carry coefficients up to 1.5e4 (RKV877e), whose
     // cancellation FP32 cannot resolve, so every instance of a mixed solve runs in FP64
     if (cfg->method >= DEGPU_RKV655E) return INFINITY;
     return mixed_bound(bound_method(cfg->method)).load();
 }
 
-static bool valid_prec(int p) { return p == DEGPU_FP64_PARITY || p == DEGPU_FP64_FAST || p == DEGPU_MIXED; }
+static bool valid_prec(int p) { return p >= DEGPU_FP64_PARITY && p <= DEGPU_MIXED_FP64_CTRL; }
 
 static void builtin_info(int id, int& dim, int& np) {
     switch (id) {
@@ -247,7 +250,7 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
 
     // ragged (per-instance dimension) problems go to the warp-per-system kernel
     if (pb->rhs_id == DEGPU_RHS_FPU_BETA) {
-        return wps_solve(pb, cfg, a, in->dims, s);
+        return group_solve(pb, cfg, a, in->dims, s);
     }
 
     int kernel_sel = cfg->kernel;
@@ -358,8 +361,8 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
     return DEGPU_OK;
 }
 
-static degpu_status validate(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
-                             const degpu_batch_out* out) {
+degpu_status validate_solve_args(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                 const degpu_batch_out* out) {
     if (!pb || !cfg || !in || !out) return DEGPU_BAD_INPUT;
     if (in->n < 0) return DEGPU_BAD_INPUT;
     if (in->n == 0) return DEGPU_OK;
@@ -583,7 +586,7 @@ template <class Spec>
 static degpu_status crossing_entry(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                                    const Spec* sd, degpu_batch_out* out, degpu_crossing_out* co, cudaStream_t s) {
     if (!sd || !co) return DEGPU_BAD_INPUT;
-    degpu_status v = validate(pb, cfg, in, out);
+    degpu_status v = validate_solve_args(pb, cfg, in, out);
     if (v != DEGPU_OK || in->n == 0) return v;
     CrossSpec cr;
     if (!make_spec(sd, pb->dim, cr)) return DEGPU_BAD_INPUT;
@@ -608,7 +611,7 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
                                         const degpu_batch_in* in, const Spec* sd, degpu_batch_out* out,
                                         degpu_crossing_out* co) {
     if (!sd || !co) return DEGPU_BAD_INPUT;
-    degpu_status v = validate(pb, cfg, in, out);
+    degpu_status v = validate_solve_args(pb, cfg, in, out);
     if (v != DEGPU_OK || in->n == 0) return v;
     CrossSpec cr;
     if (!make_spec(sd, pb->dim, cr)) return DEGPU_BAD_INPUT;
@@ -727,7 +730,7 @@ degpu_status degpu_rhs_info(int32_t rhs_id, int32_t* dim, int32_t* n_params) {
 
 degpu_status degpu_solve_ensemble(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                                   degpu_batch_out* out, void* stream) {
-    degpu_status v = validate(pb, cfg, in, out);
+    degpu_status v = validate_solve_args(pb, cfg, in, out);
     if (v != DEGPU_OK || in->n == 0) return v;
     cudaStream_t s = (cudaStream_t)stream;
     if (pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return nvrtc_solve(pb, cfg, in, out, s);
@@ -787,7 +790,7 @@ degpu_status degpu_solve_ensemble_hyperplane_host(const degpu_problem* pb, const
 
 degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                                        degpu_batch_out* out) {
-    degpu_status v = validate(pb, cfg, in, out);
+    degpu_status v = validate_solve_args(pb, cfg, in, out);
     if (v != DEGPU_OK || in->n == 0) return v;
     cudaStream_t s;
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return DEGPU_CUDA_ERROR;

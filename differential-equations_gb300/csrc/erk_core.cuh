@@ -236,7 +236,7 @@ struct Lane {
     // Mixed form without output: t as an FP32 pair th + tl (about 48 bits), advanced and compared
     // with tf in FP32 arithmetic, so that an accepted step issues no FP64 instruction. A drive
     // phase is advanced as an FP32 pair too; a right-hand side that reads t gets th + tl widened
-    // (tnow). The FP64-controller build (DEGPU_MIXED_F32_CTRL=0) keeps t in FP64 as well.
+    // (tnow). The FP64-controller form (PrecMixedF64Ctrl) keeps t in FP64.
     static constexpr bool FFT = MIX && !DENSE && P::F32_CTRL;
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
     // itself, and the evaluation the crate repeats at the new point on acceptance is that stage.
@@ -397,7 +397,7 @@ struct Lane {
 #pragma unroll
         for (int c = 0; c < D; ++c) {
             double q = ((double)f1[c] - (double)f0[c]) / sk[c];
-            if constexpr (P::ID == PrecMixed::ID) q = (double)(f1[c] - f0[c]) / sk[c];
+            if constexpr (P::KAHAN) q = (double)(f1[c] - f0[c]) / sk[c];
             der2 = der2 + q * q;
         }
         der2 = sqrt(der2) / fabs(hh);

@@ -6,8 +6,9 @@ src/tableau/verner.rs is parsed to the nearest double (Python's float(), like Ru
 parsing) and written as a hexadecimal float. The stage counts S and I, the order O and the FSAL
 flag come from the constructors in src/methods/erk/adaptive/mod.rs.
 
-Usage: python gen_verner_tables.py [path of the crate's source tree]
-(default /root/reference). Writes csrc/verner_tables.inc and oracle/verner_tables.inc.
+Usage: python gen_verner_tables.py CRATE_DIR
+CRATE_DIR is the root of the crate's source tree (the directory holding src/).  Writes
+csrc/verner_tables.inc and oracle/verner_tables.inc.
 """
 import os
 import re
@@ -75,7 +76,9 @@ def emit(name, spec, tab):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python gen_verner_tables.py CRATE_DIR  (the crate's source tree, holding src/)")
+    ref = sys.argv[1]
     src = open(os.path.join(ref, "src", "tableau", "verner.rs")).read()
     specs = constructors(open(os.path.join(ref, "src", "methods", "erk", "adaptive", "mod.rs")).read())
     body = "".join(emit(m, specs[m], parse_block(src, m)) for m in METHODS)

@@ -94,8 +94,8 @@ static GroupChoice choose(int method, int prec, int dense, int d) {
     return {-1, 0, 0};
 }
 
-degpu_status wps_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* dims,
-                       cudaStream_t s) {
+degpu_status group_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* dims,
+                        cudaStream_t s) {
     static bool reg = false;
     if (!reg) {
         reg = true;

@@ -22,7 +22,7 @@
 #include <tuple>
 
 #include "registry.cuh"
-#include "wps.cuh"
+#include "side_paths.cuh"
 
 namespace degpu {
 

@@ -8,13 +8,16 @@
 // device).  Such a caller still provides the inputs and outputs; the few megabytes of work-list
 // space the solve needs come from `noalloc_scratch` below.
 //
-// The array is held by every GPU that loads the library until the process exits.  All calls
+// The array is part of the library's device code.  CUDA loads a library's device code lazily
+// by default (CUDA_MODULE_LOADING=LAZY), so on each device the array and the solve's kernels are
+// loaded by the first call that needs them: that loading is the one device allocation this entry
+// point causes.  A caller that reserves the device's memory for itself makes one call (any small
+// batch) on each device first, before it reserves the pool and before any stream capture; from
+// then on the array stays resident until the process exits and no call allocates.  All calls
 // share it and it keeps the previous call's contents, so each call first clears the part that
 // must start at zero; two calls whose work overlaps on the GPU (different streams, or different
 // host threads) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "registry.cuh"
 
@@ -39,20 +42,13 @@ constexpr size_t NA_BYTES = NA_KEY + (size_t)NA_MAX * 4;
 
 static __device__ __align__(256) unsigned char noalloc_scratch[NA_BYTES];
 
-std::mutex na_mu;
-void* na_ptr[64] = {};  // device address of noalloc_scratch, per device
-
-// The array's device address, looked up once per device with that device current.
+// The array's device address on the current device, looked up on every call: a cached address
+// would outlive a cudaDeviceReset or a new primary context, and once the module is loaded the
+// lookup is a host-side table query.
 degpu_status scratch_address(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEGPU_CUDA_ERROR;
-    std::lock_guard<std::mutex> g(na_mu);
-    if (!na_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress((void**)&p, noalloc_scratch) != cudaSuccess || !p) return DEGPU_CUDA_ERROR;
-        na_ptr[dev] = p;
-    }
-    *out = na_ptr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress((void**)&p, noalloc_scratch) != cudaSuccess || !p) return DEGPU_CUDA_ERROR;
+    *out = p;
     return DEGPU_OK;
 }
 
@@ -66,7 +62,7 @@ __device__ __forceinline__ int na_slot(int id) {
 __global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, const double* rtol,
                                 const double* params, int n_params, const int32_t* family, int fam_const,
                                 double inv_order, double h0, double split, unsigned char* scratch,
-                                int32_t* status) {
+                                int32_t* status, double* y_final, double* t_final, int dmax) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int* cells = (int*)(scratch + NA_CELLS);
@@ -74,7 +70,11 @@ __global__ void na_count_kernel(int64_t n, const double* t0, const double* tf, c
     int* key = (int*)(scratch + NA_KEY);
     int f = na_slot(family ? family[i] : fam_const);
     if (f < 0) {
-        if (status) status[i] = DEGPU_ERR_BAD_INPUT;
+        // not one of the three families of the fixed lists: BadInput, and NaN where a result
+        // would go (status is required whenever a family map is given)
+        status[i] = DEGPU_ERR_BAD_INPUT;
+        for (int c = 0; c < dmax; ++c) y_final[(int64_t)c * n + i] = __longlong_as_double(0x7ff8000000000000ll);
+        if (t_final) t_final[i] = __longlong_as_double(0x7ff8000000000000ll);
         key[i] = -1;
         return;
     }
@@ -125,24 +125,20 @@ using namespace degpu;
 
 extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, const degpu_method_cfg* cfg,
                                                      const degpu_batch_in* in, degpu_batch_out* out, void* stream) {
-    if (!pb || !cfg || !in || !out) return DEGPU_BAD_INPUT;
-    if (in->n < 0) return DEGPU_BAD_INPUT;
+    // the checks degpu_solve_ensemble makes, then the limits of this entry point
+    degpu_status v = validate_solve_args(pb, cfg, in, out);
+    if (v != DEGPU_OK) return v;
     if (in->n > NA_MAX) return DEGPU_BAD_INPUT;  // beyond DEGPU_NOALLOC_MAX_INSTANCES
     if (in->n == 0) return DEGPU_OK;
-    if (cfg->method < DEGPU_RK4 || cfg->method > DEGPU_RKV989E) return DEGPU_BAD_INPUT;
     if (cfg->method > DEGPU_CASH_KARP) return DEGPU_UNSUPPORTED;  // Verner's pairs: not in the fixed lists
-    if (cfg->precision < DEGPU_FP64_PARITY || cfg->precision > DEGPU_MIXED || cfg->max_steps < 0) return DEGPU_BAD_INPUT;
-    if (!in->t0 || !in->tf || !in->y0 || !in->rtol || !in->atol || !out->y_final) return DEGPU_BAD_INPUT;
     if (in->n_eval > 0 || in->dims) return DEGPU_UNSUPPORTED;
     if (in->family) {
-        // the family map is on the device: the rows must have room for every family
-        if (pb->dim < 3 || pb->n_params < 3 || !in->params) return DEGPU_BAD_INPUT;
+        // the family map is on the device: the rows must have room for every family, and the
+        // per-instance status is where an instance of an unsupported family is reported
+        if (pb->dim < 3 || pb->n_params < 3 || !in->params || !out->status) return DEGPU_BAD_INPUT;
     } else {
         const int id = pb->rhs_id;
-        const int need_d = id == DEGPU_RHS_LORENZ ? 3 : (id == DEGPU_RHS_VAN_DER_POL || id == DEGPU_RHS_PENDULUM) ? 2 : 0;
-        const int need_p = id == DEGPU_RHS_VAN_DER_POL ? 1 : 3;
-        if (need_d == 0) return DEGPU_UNSUPPORTED;
-        if (pb->dim < need_d || pb->n_params < need_p || !in->params) return DEGPU_BAD_INPUT;
+        if (id != DEGPU_RHS_LORENZ && id != DEGPU_RHS_VAN_DER_POL && id != DEGPU_RHS_PENDULUM) return DEGPU_UNSUPPORTED;
     }
     ensure_registered();
     auto it = multi_registry().find({cfg->method, cfg->precision, 0});
@@ -167,7 +163,7 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     const unsigned blocks = (unsigned)((n + 255) / 256);
     na_count_kernel<<<blocks, 256, 0, s>>>(n, in->t0, in->tf, in->rtol, in->params, pb->n_params, in->family,
                                            pb->rhs_id, inv_order, cfg->h0 != 0.0 ? cfg->h0 : 1.0, split, scratch,
-                                           out->status);
+                                           out->status, out->y_final, out->t_final, pb->dim);
     na_scan_kernel<<<1, 32, 0, s>>>(scratch);
     na_scatter_kernel<<<blocks, 256, 0, s>>>(n, scratch);
     if (cudaGetLastError() != cudaSuccess) return DEGPU_CUDA_ERROR;

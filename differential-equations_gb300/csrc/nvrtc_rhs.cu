@@ -17,7 +17,7 @@
 #include <string>
 #include <vector>
 
-#include "wps.cuh"
+#include "side_paths.cuh"
 
 namespace degpu {
 int device_sm_count();

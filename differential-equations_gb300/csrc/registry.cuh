@@ -213,6 +213,8 @@ void register_verner_cross87_parity();
 void register_verner_cross98_parity();
 void register_verner_cross6576_fast();
 void register_verner_cross8798_fast();
+void register_plain();
+void register_mixed_f64ctrl();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to
@@ -252,6 +254,11 @@ degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, 
 // instance of a DEGPU_MIXED solve runs the DEGPU_FP64_FAST variant; 0 when cfg asks for another
 // precision or for RK4.
 double mixed_split(const degpu_method_cfg* cfg);
+
+// Argument checks shared by the ensemble entry points (degpu_abi.cu): null pointers, sizes, enum
+// ranges and the problem's dimension and parameter count -> DEGPU_BAD_INPUT.
+degpu_status validate_solve_args(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
+                                 const degpu_batch_out* out);
 
 // Right-hand-side evaluation kernels (degpu_eval_rhs)
 using RhsLaunchFn = cudaError_t (*)(int64_t n, const double* t, const double* y, const double* p, double* dydt,

@@ -20,19 +20,9 @@ namespace degpu {
 #ifndef DEGPU_MIXED_MIN_BLOCKS
 #define DEGPU_MIXED_MIN_BLOCKS 1
 #endif
-// Mixed form of the one-system-per-thread kernels: 1 evaluates the error terms, the norm, the
-// controller's power and the accept decision in FP32 (the terms are FP32 stage data); 0 keeps
-// the norm and the controller in FP64.  t, h and the step-size update are FP64 either way.
-// Measured on the uneven Van der Pol / pendulum / Lorenz ensemble (DOPRI5 and DOP853, rtol
-// 1e-5..1e-11): both settings take the same number of steps to within 0.1% in every rtol decade
-// and reach the same error against FP64; with 1 the solve runs 3.3x faster, because every FP64
-// operation costs as much issue time as 64 FP32 operations on this GPU.
 // Mixed form's sin/cos: 0 uses f32_math.cuh, 1 the CUDA library's sinf/cosf.
 #ifndef DEGPU_MIXED_LIBM_TRIG
 #define DEGPU_MIXED_LIBM_TRIG 0
-#endif
-#ifndef DEGPU_MIXED_F32_CTRL
-#define DEGPU_MIXED_F32_CTRL 1
 #endif
 
 // PhaseOf<R>::value: the family declares PHASE (a drive phase the mixed form advances in FP32,
@@ -81,13 +71,21 @@ struct PrecFast {
     __device__ static __forceinline__ double cos(double x) { return ::cos(x); }
     __device__ static __forceinline__ S from(double x) { return x; }
 };
-// Mixed: stages in FP32, y accumulated with Kahan compensation, t and h in FP64; the error norm
-// and the controller as DEGPU_MIXED_F32_CTRL selects.
+// Plain FP64: FMA contraction, IEEE division and square root, the CUDA math library's sin/cos,
+// and the correctly rounded controller power of the parity path, so that accept and reject
+// follow the crate's decisions; results differ from the crate's only by contraction and the
+// rounding of sin/cos.
+struct PrecPlain : PrecFast {
+    static constexpr int ID = 3;
+    __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl(x, y); }
+};
+// Mixed: stages in FP32, y accumulated with Kahan compensation; the error terms, the norm, the
+// controller's power and the accept decision in FP32, t as an FP32 pair (see Lane).
 struct PrecMixed {
     using S = float;
     static constexpr int ID = 2;
     static constexpr bool KAHAN = true;
-    static constexpr bool F32_CTRL = DEGPU_MIXED_F32_CTRL != 0;
+    static constexpr bool F32_CTRL = true;
     static constexpr int MULTI_MIN_BLOCKS = DEGPU_MIXED_MIN_BLOCKS;
     // x^(-1/order) of the controller: FP64 result from an FP32 log2/exp2 estimate refined by
     // one FP64 Newton step on r^q = x^-1 (q = 5 or 8); general y falls back to FP64 pow.
@@ -114,6 +112,12 @@ struct PrecMixed {
     __device__ static __forceinline__ float cos(float x) { return f32m::cos_f32(x); }
 #endif
     __device__ static __forceinline__ S from(double x) { return (float)x; }
+};
+// Mixed with the FP64 controller: FP32 stages and Kahan-compensated y as in PrecMixed; the error
+// norm over the FP32 error terms, the controller's power, the accept decision, t and h in FP64.
+struct PrecMixedF64Ctrl : PrecMixed {
+    static constexpr int ID = 4;
+    static constexpr bool F32_CTRL = false;
 };
 
 // Families -------------------------------------------------------------------------------------

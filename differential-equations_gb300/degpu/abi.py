@@ -19,7 +19,7 @@ OK, BAD_INPUT, OOM, TIMEOUT, CUDA_ERROR, UNSUPPORTED = range(6)
 RK4, DOPRI5, DOP853, RKF45, CASH_KARP = 0, 1, 2, 3, 4
 RKV655E, RKV656E, RKV766E, RKV767E, RKV877E, RKV878E, RKV988E, RKV989E = range(5, 13)
 # degpu_precision
-FP64_PARITY, FP64_FAST, MIXED = 0, 1, 2
+FP64_PARITY, FP64_FAST, MIXED, FP64_PLAIN, MIXED_FP64_CTRL = 0, 1, 2, 3, 4
 # degpu_kernel
 KERNEL_AUTO, KERNEL_THREAD, KERNEL_WARP, KERNEL_PERSISTENT = 0, 1, 2, 3
 # degpu_dense_mode

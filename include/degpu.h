@@ -84,8 +84,23 @@ typedef enum {
  *                compensation; t as an FP32 pair (about 48 bits, FP64 when output times,
  *                crossings or events need it; RK4: t and h in FP64).
  *                Instances whose rtol is below the method's mixed-precision bound
- *                (degpu_set_mixed_min_rtol) run in FP64_FAST arithmetic instead. */
-typedef enum { DEGPU_FP64_PARITY = 0, DEGPU_FP64_FAST = 1, DEGPU_MIXED = 2 } degpu_precision;
+ *                (degpu_set_mixed_min_rtol) run in FP64_FAST arithmetic instead.
+ *  FP64_PLAIN  — FP64 with FMA contraction, IEEE division and square root, the CUDA library's
+ *                sin/cos, and FP64_PARITY's correctly rounded controller power, so that every
+ *                accept/reject decision follows the crate's unless contraction moves the error
+ *                estimate across 1.  DOPRI5 and DOP853 on the Van der Pol, pendulum and Lorenz
+ *                families, final states and output times.
+ *  MIXED_FP64_CTRL — MIXED's FP32 stages and Kahan-compensated y, with the error norm, the
+ *                controller's power, the accept decision and t in FP64 (the step size is an
+ *                FP32 value, added to t in FP64).  Same families and methods as FP64_PLAIN, and
+ *                the same mixed-precision bound as MIXED. */
+typedef enum {
+    DEGPU_FP64_PARITY = 0,
+    DEGPU_FP64_FAST = 1,
+    DEGPU_MIXED = 2,
+    DEGPU_FP64_PLAIN = 3,
+    DEGPU_MIXED_FP64_CTRL = 4
+} degpu_precision;
 
 /* Kernel layout. AUTO picks by method and dimension. */
 typedef enum {
@@ -223,12 +238,15 @@ degpu_status degpu_solve_ensemble(const degpu_problem* problem, const degpu_meth
  * outputs as for degpu_solve_ensemble; the solve's work lists live in a fixed array of about
  * 4.2 MB inside the library (held by every GPU that loads it, until the process exits).
  *  - n must be <= DEGPU_NOALLOC_MAX_INSTANCES, otherwise DEGPU_BAD_INPUT and nothing runs.
+ *  - The arguments are checked as degpu_solve_ensemble checks them (same DEGPU_BAD_INPUT cases).
  *  - Only the persistent solve of the Van der Pol, pendulum and Lorenz families, without dense
  *    output or per-instance dimensions (DEGPU_UNSUPPORTED otherwise).  With a device family map,
- *    dim and n_params must be >= 3; an instance of another family gets status BadInput and no
- *    other output.
- *  - The first call on a device looks up the array's address on that device; make that first
- *    call before starting any stream capture.
+ *    dim and n_params must be >= 3 and out->status must be given; an instance of another family
+ *    gets status BadInput and a NaN final state and time.
+ *  - CUDA loads the library's device code, this array included, lazily: the first call on a
+ *    device loads it there, and that is the one device allocation this entry point causes.
+ *    Make that first call (any small batch) on each device before reserving the device's memory
+ *    pool and before starting any stream capture; later calls allocate nothing.
  *  - Every call reuses the same array: calls that overlap on the GPU (other streams, other host
  *    threads) race and must be serialised by the caller. */
 degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* problem, const degpu_method_cfg* cfg,

@@ -270,3 +270,66 @@ def test_fpu_chain_fast_and_mixed_accuracy():
         assert np.all(g.status == abi.COMPLETE)
         err = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.max(np.abs(o["y_final"]), axis=0)
         assert np.median(err) < tol, (prec, np.median(err))
+
+
+@pytest.mark.parametrize("kernel", [abi.KERNEL_THREAD, abi.KERNEL_PERSISTENT])
+def test_uneven_ensemble_full_horizon_parity(kernel):
+    """6,000 instances of the uneven ensemble at their drawn horizons (t_end ~ U[5, 50], nothing
+    clipped) and tolerances: the long-horizon regime in which a single rounding difference would
+    flip an accept decision somewhere along the solve.  Bit for bit."""
+    e = W.config1(n=6000)
+    assert e.tf.max() > 45.0
+    cfg = cfg_for(abi.DOPRI5, kernel=kernel)
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    assert_parity(g, o)
+    assert np.all(g.status == abi.COMPLETE)
+    assert np.array_equal(g.y_final, o["y_final"])
+
+
+def test_fpu_chain_full_horizon_parity():
+    """64 FPU-beta chains of the uneven-dimension configuration as drawn (2..128 masses, DOP853
+    rtol 1e-10 atol 1e-12 over [0, 100], 64 uniformly spaced output times)."""
+    e = W.config2(n=64)
+    assert np.all(e.tf == 100.0) and len(e.t_eval) == 64
+    cfg = cfg_for(abi.DOP853)
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    assert_parity(g, o, dense=True)
+    assert np.array_equal(g.y_final, o["y_final"])
+
+
+def status_case(rhs, p, y0, tf, rtol, n=4):
+    d = len(y0)
+    rng = np.random.default_rng(11)
+    y0s = np.array(y0, dtype=float)[:, None] * (1.0 + 1e-6 * rng.standard_normal((d, n)))
+    return W.Ensemble(rhs, abi.DOPRI5, n, d, len(p), np.zeros(n), np.full(n, tf), y0s,
+                      np.array(p, dtype=float).reshape(-1, 1).repeat(n, axis=1), np.full(n, rtol), np.full(n, rtol),
+                      rhs_id=abi.RHS[rhs])
+
+
+@pytest.mark.parametrize("method", [abi.DOPRI5, abi.DOP853])
+@pytest.mark.parametrize("case,expect", [
+    # y' = y: the stiffness quotient's denominator |f(y_new) - y_stage|^2 is rounding noise, so
+    # every 100th step counts as stiff and the 15th detection aborts (ordinary.rs:165-186)
+    (("EXP_GROWTH", [1.0], [1.0], 600.0, 1e-12), "STIFFNESS"),
+    # y' = 1000 y overflows; the step size then shrinks by min_scale per rejection until it is
+    # below 1e-14 of the last accepted one (ordinary.rs:69-80)
+    (("EXP_GROWTH", [1000.0], [1.0], 10.0, 1e-6), "STEP_SIZE"),
+    (("EXP_GROWTH", [1.0], [1e300], 100.0, 1e-6), "STEP_SIZE"),
+], ids=["stiffness", "step_size_growth", "step_size_overflow"])
+def test_stiffness_and_step_size_statuses_parity(method, case, expect):
+    """The crate's Error::Stiffness and Error::StepSize end instances on the device as they end
+    them in the oracle: same status, counters, time and state at the abort."""
+    e = status_case(*case)
+    cfg = cfg_for(method)
+    o = oracle_solve(e, cfg)
+    g = gpu_solve(e, cfg)
+    want = {"STIFFNESS": abi.ERR_STIFFNESS, "STEP_SIZE": abi.ERR_STEP_SIZE}[expect]
+    assert np.all(o["status"] == want)
+    np.testing.assert_array_equal(g.status, o["status"])
+    np.testing.assert_array_equal(g.accepted, o["accepted"])
+    np.testing.assert_array_equal(g.rejected, o["rejected"])
+    np.testing.assert_array_equal(g.fevals, o["fevals"])
+    np.testing.assert_array_equal(g.t_final, o["t_final"])
+    np.testing.assert_array_equal(g.y_final, o["y_final"])

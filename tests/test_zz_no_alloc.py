@@ -5,8 +5,13 @@ run, e.g. an application that has reserved the device memory pool for itself, or
 step cannot absorb an allocator call that may synchronise the device.  It must give the same
 results as the ordinary entry point.  Two calls run back to back, the second on a different,
 smaller batch, because the fixed work-list array keeps the previous call's contents.
+
+CUDA loads the library's device code lazily, so the first call on a device loads the fixed array
+there; a caller makes that call before it reserves its memory pool.  After it, a call must leave
+the device's free memory and the default memory pool's high-water marks where they were.
 """
 import ctypes as C
+import ctypes.util
 
 import numpy as np
 import pytest
@@ -108,3 +113,91 @@ def test_noalloc_rejects_batches_beyond_its_maximum():
     assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), None) == \
         abi.BAD_INPUT
     assert abi_max > 262144
+
+
+def cudart():
+    """The CUDA runtime library, for the default memory pool's attributes."""
+    for name in ("libcudart.so.13", "libcudart.so", ctypes.util.find_library("cudart")):
+        if not name:
+            continue
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    pytest.skip("libcudart not found")
+
+
+POOL_RESERVED_HIGH, POOL_USED_CURRENT, POOL_USED_HIGH = 0x6, 0x7, 0x8  # cudaMemPoolAttr
+
+
+def pool_attr(rt, pool, attr):
+    v = C.c_uint64(0)
+    assert rt.cudaMemPoolGetAttribute(pool, C.c_int(attr), C.byref(v)) == 0
+    return v.value
+
+
+def test_noalloc_call_allocates_nothing_after_the_first():
+    torch = pytest.importorskip("torch")
+    lib = abi.load()
+    rt = cudart()
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.Stream()
+    e = W.config1(n=3 * 1000, first=90_000)
+    e.tf = np.minimum(e.tf, 8.0)
+    cfg = abi.default_cfg(abi.DOPRI5)
+    cfg.precision, cfg.kernel, cfg.max_steps = abi.MIXED, abi.KERNEL_PERSISTENT, 10_000_000
+    prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
+    ins, bi = device_batch(torch, e, dev)
+    out, bo = device_outputs(torch, e.n, dev)
+    h = C.c_void_p(stream.cuda_stream)
+    # the first call on the device loads the array (lazy module loading)
+    assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), h) == abi.OK
+    stream.synchronize()
+    torch.cuda.synchronize()
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), C.c_int(0)) == 0
+    zero = C.c_uint64(0)
+    for attr in (POOL_RESERVED_HIGH, POOL_USED_HIGH):
+        assert rt.cudaMemPoolSetAttribute(pool, C.c_int(attr), C.byref(zero)) == 0
+    used_before = pool_attr(rt, pool, POOL_USED_CURRENT)
+    free_before = torch.cuda.mem_get_info(0)[0]
+    assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), h) == abi.OK
+    stream.synchronize()
+    free_after = torch.cuda.mem_get_info(0)[0]
+    assert free_after == free_before
+    assert pool_attr(rt, pool, POOL_USED_HIGH) <= used_before
+    assert np.all(out["status"].cpu().numpy() == abi.COMPLETE)
+
+
+def test_noalloc_unsupported_family_in_the_map():
+    """An instance whose family is not Van der Pol, pendulum or Lorenz gets BadInput and a NaN
+    final state; the others are solved as the ordinary entry point solves them.  Without a status
+    array such a batch is refused as a whole."""
+    torch = pytest.importorskip("torch")
+    lib = abi.load()
+    stream = torch.cuda.Stream()
+    e = W.config1(n=3 * 100, first=120_000)
+    e.tf = np.minimum(e.tf, 6.0)
+    e.family = e.family.copy()
+    e.family[::7] = abi.RHS["HARMONIC"]
+    dev = torch.device("cuda:0")
+    cfg = abi.default_cfg(abi.DOPRI5)
+    cfg.precision, cfg.kernel, cfg.max_steps = abi.FP64_PARITY, abi.KERNEL_PERSISTENT, 10_000_000
+    prob = abi.Problem(rhs_id=0, dim=3, n_params=3)
+    ins, bi = device_batch(torch, e, dev)
+    got, bo = device_outputs(torch, e.n, dev)
+    h = C.c_void_p(stream.cuda_stream)
+    assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), h) == abi.OK
+    stream.synchronize()
+    g = {k: v.cpu().numpy() for k, v in got.items()}
+    bad = e.family == abi.RHS["HARMONIC"]
+    assert np.all(g["status"][bad] == abi.ERR_BAD_INPUT)
+    assert np.all(np.isnan(g["y_final"][:, bad])) and np.all(np.isnan(g["t_final"][bad]))
+    good = np.nonzero(~bad)[0]
+    ref, got2 = solve_both(torch, lib, e.subset(good), abi.FP64_PARITY, stream)
+    for k in ("status", "accepted", "rejected", "fevals"):
+        assert np.array_equal(g[k][good], ref[k]), k
+    assert np.array_equal(g["y_final"][:, good], ref["y_final"])
+    bo.status = None
+    assert lib.degpu_solve_ensemble_noalloc(C.byref(prob), C.byref(cfg), C.byref(bi), C.byref(bo), h) == \
+        abi.BAD_INPUT
