@@ -417,6 +417,8 @@ extern "C" degpu_status degpu_solve_bvp_host(const degpu_problem* pb, const degp
     if (!pb || !cfg || !in || !bvp || !out || !bo) return DEGPU_BAD_INPUT;
     if (in->n < 0 || !out->y_final || !bo->y_a || !in->t0 || !in->tf || !in->y0 || !in->rtol || !in->atol)
         return DEGPU_BAD_INPUT;
+    // the shots of a Newton pass are assembled with one scalar tolerance per instance
+    if (in->rtol_vec || in->atol_vec) return DEGPU_UNSUPPORTED;
     const int dim = pb->dim;
     if (dim < 1 || dim > DEGPU_HYPERPLANE_MAX_DIM || pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) return DEGPU_BAD_INPUT;
     if (in->family || in->dims || (pb->n_params > 0 && !in->params)) return DEGPU_UNSUPPORTED;

@@ -163,6 +163,7 @@ static void builtin_info(int id, int& dim, int& np) {
         case DEGPU_RHS_BRUSSELATOR: dim = 2; np = 2; return;
         case DEGPU_RHS_CR3BP: dim = 6; np = 1; return;
         case DEGPU_RHS_PIPE_HEAT: dim = 2; np = 2; return;
+        case DEGPU_RHS_DAMPED_QUADRATURE: dim = 3; np = 3; return;
         default: dim = 0; np = -1; return;
     }
 }
@@ -178,6 +179,8 @@ static EnsArgs make_args(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     a.params = in->params;
     a.rtol = in->rtol;
     a.atol = in->atol;
+    a.rtol_vec = in->rtol_vec;
+    a.atol_vec = in->atol_vec;
     a.n_eval = (in->n_eval > 0 && in->t_eval) ? in->n_eval : 0;
     a.dmax = pb->dim;
     a.y_final = out->y_final;
@@ -641,6 +644,8 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
         din.params = np > 0 ? (const double*)up(in->params, np * n * 8) : nullptr;
         din.rtol = (const double*)up(in->rtol, n * 8);
         din.atol = (const double*)up(in->atol, n * 8);
+        din.rtol_vec = (const double*)up(in->rtol_vec, d * n * 8);
+        din.atol_vec = (const double*)up(in->atol_vec, d * n * 8);
         din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
         din.t_eval = ne > 0 ? (const double*)up(in->t_eval, ne * 8) : nullptr;
         din.n_eval = (int32_t)ne;
@@ -655,7 +660,8 @@ static degpu_status crossing_host_entry(const degpu_problem* pb, const degpu_met
         dco.y = m > 0 ? sc.alloc<double>(m * d * n) : nullptr;
         dco.count = sc.alloc<int32_t>(n);
         if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final || !dco.count ||
-            (m > 0 && (!dco.t || !dco.y)) || (ne > 0 && (!din.t_eval || !dout.dense))) {
+            (m > 0 && (!dco.t || !dco.y)) || (ne > 0 && (!din.t_eval || !dout.dense)) ||
+            (in->rtol_vec && !din.rtol_vec) || (in->atol_vec && !din.atol_vec)) {
             st = DEGPU_OOM;
         } else {
             st = crossing_impl(pb, cfg, &din, cr, &dout, &dco, ne > 0 ? in->t_eval : nullptr, s);
@@ -814,6 +820,8 @@ degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_meth
         din.params = np > 0 ? (const double*)up(in->params, (size_t)np * n * 8) : nullptr;
         din.rtol = (const double*)up(in->rtol, n * 8);
         din.atol = (const double*)up(in->atol, n * 8);
+        din.rtol_vec = (const double*)up(in->rtol_vec, (size_t)d * n * 8);
+        din.atol_vec = (const double*)up(in->atol_vec, (size_t)d * n * 8);
         din.dims = in->dims ? (const int32_t*)up(in->dims, n * 4) : nullptr;
         din.family = in->family ? (const int32_t*)up(in->family, n * 4) : nullptr;
         din.t_eval = m > 0 ? (const double*)up(in->t_eval, (size_t)m * 8) : nullptr;
@@ -824,7 +832,8 @@ degpu_status degpu_solve_ensemble_host(const degpu_problem* pb, const degpu_meth
         dout.rejected = out->rejected ? sc.alloc<int64_t>(n) : nullptr;
         dout.fevals = out->fevals ? sc.alloc<int64_t>(n) : nullptr;
         dout.status = out->status ? sc.alloc<int32_t>(n) : nullptr;
-        if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final) {
+        if (!din.t0 || !din.tf || !din.y0 || !din.rtol || !din.atol || !dout.y_final ||
+            (in->rtol_vec && !din.rtol_vec) || (in->atol_vec && !din.atol_vec)) {
             st = DEGPU_OOM;
         } else if (pb->rhs_id >= DEGPU_RHS_NVRTC_BASE) {
             st = nvrtc_solve(pb, cfg, &din, &dout, s);

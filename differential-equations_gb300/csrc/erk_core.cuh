@@ -43,6 +43,8 @@ struct EnsArgs {
     const double* params;
     const double* rtol;
     const double* atol;
+    const double* rtol_vec;  // [dmax][n] per-component tolerances (Tolerance::Vector) or NULL
+    const double* atol_vec;
     const double* t_eval;      // ascending, [n_eval]
     const int32_t* eval_perm;  // ascending position -> caller's index
     int32_t n_eval;
@@ -351,14 +353,29 @@ struct Lane {
     // with the FP32 controller (P::F32_CTRL), whose terms are FP32 stage data.
     using NormT = typename Select<P::F32_CTRL, float, double>::type;
 
-    __device__ __forceinline__ NormT norm_term(S e, S yv, S ynv) const {
+    // Tolerances of component c (src/tolerance.rs:33-40): the batch's per-component value when it
+    // has one (Tolerance::Vector), else the instance's scalar; FP32 copies for the mixed form.
+    __device__ __forceinline__ double rtol_c(int c, const EnsArgs& a) const {
+        return a.rtol_vec ? a.rtol_vec[(int64_t)c * a.n + inst] : rtol;
+    }
+    __device__ __forceinline__ double atol_c(int c, const EnsArgs& a) const {
+        return a.atol_vec ? a.atol_vec[(int64_t)c * a.n + inst] : atol;
+    }
+    __device__ __forceinline__ float rtolf_c(int c, const EnsArgs& a) const {
+        return a.rtol_vec ? (float)a.rtol_vec[(int64_t)c * a.n + inst] : rtolf;
+    }
+    __device__ __forceinline__ float atolf_c(int c, const EnsArgs& a) const {
+        return a.atol_vec ? (float)a.atol_vec[(int64_t)c * a.n + inst] : atolf;
+    }
+
+    __device__ __forceinline__ NormT norm_term(int c, S e, S yv, S ynv, const EnsArgs& a) const {
         // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
         if constexpr (P::F32_CTRL) {
-            float sk = atolf + rtolf * fmaxf(fabsf(yv), fabsf(ynv));
+            float sk = atolf_c(c, a) + rtolf_c(c, a) * fmaxf(fabsf(yv), fabsf(ynv));
             float q = __fdividef(e, sk);
             return q * q;
         } else {
-            double sk = atol + rtol * fmax(fabs((double)yv), fabs((double)ynv));
+            double sk = atol_c(c, a) + rtol_c(c, a) * fmax(fabs((double)yv), fabs((double)ynv));
             double q = (double)e / sk;
             return q * q;
         }
@@ -375,7 +392,7 @@ struct Lane {
         double sk[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            sk[c] = atol + rtol * fabs((double)y[c]);
+            sk[c] = atol_c(c, a) + rtol_c(c, a) * fabs((double)y[c]);
             double q = (double)f0[c] / sk[c];
             dnf = dnf + q * q;
             double r = (double)y[c] / sk[c];
@@ -424,7 +441,7 @@ struct Lane {
         float sk[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            sk[c] = atolf + rtolf * fabsf(y[c]);
+            sk[c] = atolf_c(c, a) + rtolf_c(c, a) * fabsf(y[c]);
             float q = f0[c] / sk[c];
             dnf = dnf + q * q;
             float r = y[c] / sk[c];
@@ -1166,7 +1183,7 @@ struct Lane {
                 }
             });
 #pragma unroll
-            for (int c = 0; c < D; ++c) err = err + norm_term(es[c], y[c], ynew[c]);
+            for (int c = 0; c < D; ++c) err = err + norm_term(c, es[c], y[c], ynew[c], a);
         }
         if constexpr (Tab::HAS_BH) {
             S es[D];
@@ -1180,7 +1197,7 @@ struct Lane {
                 }
             });
 #pragma unroll
-            for (int c = 0; c < D; ++c) err2 = err2 + norm_term(es[c], y[c], ynew[c]);
+            for (int c = 0; c < D; ++c) err2 = err2 + norm_term(c, es[c], y[c], ynew[c], a);
         }
         NormT deno = Tab::HAS_BH ? err + (NormT)0.01 * err2 : err;
         if (deno <= (NormT)0) deno = (NormT)1;
@@ -1516,7 +1533,7 @@ struct Lane {
             float norm = 0.0f;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
-                const float sk = atolf + rtolf * fmaxf(fabsf(y[c]), fabsf(yh[c]));
+                const float sk = atolf_c(c, a) + rtolf_c(c, a) * fmaxf(fabsf(y[c]), fabsf(yh[c]));
                 norm = fmaxf(norm, fabsf(__fdividef(err[c], sk)));
             }
             const float pw = exp2f(__log2f(norm) * (float)(-1.0 / (double)O));
@@ -1526,7 +1543,7 @@ struct Lane {
             double norm = 0.0;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
-                const double sk = atol + rtol * fmax(fabs((double)y[c]), fabs((double)yh[c]));
+                const double sk = atol_c(c, a) + rtol_c(c, a) * fmax(fabs((double)y[c]), fabs((double)yh[c]));
                 norm = fmax(norm, fabs((double)err[c] / sk));
             }
             scale = a.safety * P::pow(norm, -(1.0 / (double)O));

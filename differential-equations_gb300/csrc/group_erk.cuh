@@ -82,6 +82,14 @@ struct GroupLane {
 
     __device__ __forceinline__ void sync() const { __syncwarp(gmask); }
 
+    // Tolerances of component c (src/tolerance.rs:33-40): per component when the batch has them.
+    __device__ __forceinline__ double rtol_c(int c, const EnsArgs& a) const {
+        return a.rtol_vec ? a.rtol_vec[(int64_t)c * a.n + inst] : rtol;
+    }
+    __device__ __forceinline__ double atol_c(int c, const EnsArgs& a) const {
+        return a.atol_vec ? a.atol_vec[(int64_t)c * a.n + inst] : atol;
+    }
+
     // sum of red[0..d) — in component order on the parity path
     __device__ double reduce_terms(const double* terms) {
         if constexpr (P::ID == PrecParity::ID) {
@@ -131,7 +139,8 @@ struct GroupLane {
         double tf_[CPL], ty_[CPL], sk[CPL];
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
-            sk[j] = atol + rtol * fabs((double)y[j]);
+            const int c = lane + G * j < d ? lane + G * j : 0;
+            sk[j] = atol_c(c, a) + rtol_c(c, a) * fabs((double)y[j]);
             double q = (double)f0[j] / sk[j];
             tf_[j] = q * q;
             double r = (double)y[j] / sk[j];
@@ -378,7 +387,7 @@ struct GroupLane {
                 constexpr double ev = Tab::er(jj);
                 if constexpr (ev != 0.0) es = es + (S)ev * k[jj * DG + cc];
             });
-            double sk = atol + rtol * fmax(fabs((double)y[j]), fabs((double)ynew[j]));
+            double sk = atol_c(cc, a) + rtol_c(cc, a) * fmax(fabs((double)y[j]), fabs((double)ynew[j]));
             double q = (double)es / sk;
             e1[j] = live ? q * q : 0.0;
             if constexpr (Tab::HAS_BH) {

@@ -24,5 +24,6 @@ void register_parity_tests() {
     reg_all<RhsBrusselator>();
     reg_all<RhsCr3bp>();
     reg_all<RhsPipeHeat>();
+    reg_all<RhsDampedQuadrature>();
 }
 }  // namespace degpu

@@ -177,6 +177,8 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     a.params = in->params;
     a.rtol = in->rtol;
     a.atol = in->atol;
+    a.rtol_vec = in->rtol_vec;
+    a.atol_vec = in->atol_vec;
     a.dmax = pb->dim;
     a.y_final = out->y_final;
     a.t_final = out->t_final;

@@ -145,6 +145,8 @@ degpu_status nvrtc_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     a.params = in->params;
     a.rtol = in->rtol;
     a.atol = in->atol;
+    a.rtol_vec = in->rtol_vec;
+    a.atol_vec = in->atol_vec;
     a.dmax = pb->dim;
     a.y_final = out->y_final;
     a.t_final = out->t_final;

@@ -288,6 +288,21 @@ struct RhsPipeHeat : BuiltinRhs {
     }
 };
 
+// examples/ode/17_quadrature/main.rs:41-55: damped mass-spring system augmented with the energy
+// dissipated by the damper, y = [x, v, W], p = [k, m, c].
+struct RhsDampedQuadrature : BuiltinRhs {
+    static constexpr int ID = 14, D = 3, NP = 3;
+    template <class P, class PT>
+    __device__ static __forceinline__ void diff(double, const typename P::S* y, typename P::S* dydt, const PT* p) {
+        using S = typename P::S;
+        const S k = (S)p[0], m = (S)p[1], c = (S)p[2];
+        const S x = y[0], v = y[1];
+        dydt[0] = v;
+        dydt[1] = -(k / m) * x - (c / m) * v;
+        dydt[2] = c * v * v;
+    }
+};
+
 // tests/ode/systems.rs:122-153; powi(2) -> x*x, powi(3) -> x*(x*x) as LLVM expands them.
 struct RhsCr3bp : BuiltinRhs {
     static constexpr int ID = 12, D = 6, NP = 1;

@@ -85,6 +85,8 @@ struct ServerImpl {
         const size_t m = (size_t)(r.in.n_eval > 0 ? r.in.n_eval : 0);
         size_t b = align(n * 8) * 6 + align(d * n * 8) * 2 + align(np * n * 8) + align(n * 4) * 3 + align(n * 8) * 3;
         b += align(m * 8) + align(m * d * n * 8);
+        if (r.in.rtol_vec) b += align(d * n * 8);
+        if (r.in.atol_vec) b += align(d * n * 8);
         if (r.resumable && !r.split) b += align(n * r.ops.park_bytes) + 512;
         if (r.split) {
             b += align(r.idx[0].size() * 8) + align(r.idx[1].size() * 8);
@@ -117,6 +119,8 @@ struct ServerImpl {
         r.din.params = r.pb.n_params > 0 ? (const double*)up(r.in.params, np * n * 8) : nullptr;
         r.din.rtol = (const double*)up(r.in.rtol, n * 8);
         r.din.atol = (const double*)up(r.in.atol, n * 8);
+        r.din.rtol_vec = (const double*)up(r.in.rtol_vec, d * n * 8);
+        r.din.atol_vec = (const double*)up(r.in.atol_vec, d * n * 8);
         r.din.dims = r.in.dims ? (const int32_t*)up(r.in.dims, n * 4) : nullptr;
         r.din.family = r.in.family ? (const int32_t*)up(r.in.family, n * 4) : nullptr;
         r.din.t_eval = m ? (const double*)up(r.in.t_eval, m * 8) : nullptr;
@@ -151,6 +155,8 @@ struct ServerImpl {
         a.params = r.din.params;
         a.rtol = r.din.rtol;
         a.atol = r.din.atol;
+        a.rtol_vec = r.din.rtol_vec;
+        a.atol_vec = r.din.atol_vec;
         a.dmax = r.pb.dim;
         a.y_final = r.dout.y_final;
         a.t_final = r.dout.t_final;

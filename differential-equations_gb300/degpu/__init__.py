@@ -196,6 +196,12 @@ class System:
         return System(abi.RHS["PIPE_HEAT"], [heat_loss_rate, ambient], 2)
 
     @staticmethod
+    def damped_quadrature(k, m, c):
+        """Damped mass-spring system with the dissipated energy as a third component,
+        (x, v, W) (examples/ode/17_quadrature/main.rs:41-55)."""
+        return System(abi.RHS["DAMPED_QUADRATURE"], [k, m, c], 3)
+
+    @staticmethod
     def cr3bp(mu):
         """Circular restricted three-body problem, state (x, y, z, vx, vy, vz)."""
         return System(abi.RHS["CR3BP"], [mu], 6)
@@ -411,11 +417,14 @@ def _f64(a, shape=None):
 
 
 def solve_ensemble(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method: ExplicitRungeKutta,
-                   t_eval=None, dims=None, family=None, n_params: Optional[int] = None) -> EnsembleResult:
+                   t_eval=None, dims=None, family=None, n_params: Optional[int] = None, rtol_vec=None,
+                   atol_vec=None) -> EnsembleResult:
     """Solve n IVPs (host arrays) through degpu_solve_ensemble_host.
 
     y0 is [dim, n] (structure of arrays), params [n_params, n]; t0, tf, rtol, atol are [n] or
-    scalars broadcast to n.
+    scalars broadcast to n.  rtol_vec / atol_vec ([dim, n], or [dim] broadcast to every instance)
+    are per-component tolerances, the crate's Tolerance::Vector (`.rtol([..])`, `.atol([..])`);
+    rtol / atol still order the work lists and choose the precision class of a mixed solve.
     """
     lib = abi.load()
     y0 = np.asarray(y0, dtype=np.float64)
@@ -430,13 +439,17 @@ def solve_ensemble(rhs_id: int, dim: int, t0, tf, y0, params, rtol, atol, method
     m = 0 if te is None else len(te)
     dims_a = None if dims is None else np.ascontiguousarray(dims, dtype=np.int32)
     fam_a = None if family is None else np.ascontiguousarray(family, dtype=np.int32)
+    tv = lambda v: None if v is None else _f64(np.broadcast_to(
+        np.asarray(v, dtype=np.float64).reshape(dim, -1), (dim, n)).copy())
+    rtv, atv = tv(rtol_vec), tv(atol_vec)
     out = dict(y_final=np.empty((dim, n)), t_final=np.empty(n), dense=np.empty((m, dim, n)) if m else None,
                accepted=np.empty(n, np.int64), rejected=np.empty(n, np.int64), fevals=np.empty(n, np.int64),
                status=np.empty(n, np.int32))
     prob = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=np_)
     bi = abi.BatchIn(n=n, t0=abi.ptr(t0), tf=abi.ptr(tf), y0=abi.ptr(y0), params=abi.ptr(params),
                      rtol=abi.ptr(rtol), atol=abi.ptr(atol), dims=abi.ptr(dims_a, C.c_int32),
-                     family=abi.ptr(fam_a, C.c_int32), t_eval=abi.ptr(te), n_eval=m)
+                     family=abi.ptr(fam_a, C.c_int32), t_eval=abi.ptr(te), n_eval=m, rtol_vec=abi.ptr(rtv),
+                     atol_vec=abi.ptr(atv))
     bo = abi.BatchOut(y_final=abi.ptr(out["y_final"]), t_final=abi.ptr(out["t_final"]), dense=abi.ptr(out["dense"]),
                       accepted=abi.ptr(out["accepted"], C.c_int64), rejected=abi.ptr(out["rejected"], C.c_int64),
                       fevals=abi.ptr(out["fevals"], C.c_int64), status=abi.ptr(out["status"], C.c_int32))

@@ -29,7 +29,7 @@ COMPLETE, ERR_BAD_INPUT, ERR_MAX_STEPS, ERR_STEP_SIZE, ERR_STIFFNESS, INTERRUPTE
 # degpu_rhs_id
 RHS = dict(
     LORENZ=1, VAN_DER_POL=2, PENDULUM=3, FPU_BETA=4, EXP_GROWTH=5, LINEAR=6, HARMONIC=7,
-    LOGISTIC=8, ROBERTSON=9, HIRES=10, BRUSSELATOR=11, CR3BP=12, PIPE_HEAT=13,
+    LOGISTIC=8, ROBERTSON=9, HIRES=10, BRUSSELATOR=11, CR3BP=12, PIPE_HEAT=13, DAMPED_QUADRATURE=14,
 )
 RHS_NVRTC_BASE = 1000
 
@@ -54,6 +54,7 @@ class BatchIn(C.Structure):
     _fields_ = [
         ("n", C.c_int64), ("t0", DP), ("tf", DP), ("y0", DP), ("params", DP), ("rtol", DP), ("atol", DP),
         ("dims", I32P), ("family", I32P), ("t_eval", DP), ("n_eval", C.c_int32), ("reserved", C.c_int32),
+        ("rtol_vec", DP), ("atol_vec", DP),
     ]
 
 
@@ -154,6 +155,36 @@ class GrayScott(C.Structure):
                 ("Dv", C.c_double), ("F", C.c_double), ("k", C.c_double)]
 
 
+# degpu_mol: the general method-of-lines problem
+PDE_DIFFUSION, PDE_COUPLED_DIFFUSION, PDE_GRAY_SCOTT = 1, 2, 3
+BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = 0, 1, 2
+MOL_MAX_FIELDS, MOL_MAX_PARAMS = 4, 8
+
+
+class Mol(C.Structure):
+    _fields_ = [("pde_id", C.c_int32), ("dims", C.c_int32), ("fields", C.c_int32), ("reserved", C.c_int32),
+                ("nodes", C.c_int32 * 2), ("lower", C.c_double * 2), ("dx", C.c_double * 2),
+                ("bc_kind", (C.c_int32 * 2) * 2), ("bc_value", ((C.c_double * MOL_MAX_FIELDS) * 2) * 2),
+                ("params", C.c_double * MOL_MAX_PARAMS)]
+
+
+def make_mol(pde_id, nodes, lower, dx, faces, params, fields):
+    """A degpu_mol: `faces` is [(lower kind, lower values), (upper kind, upper values)] per axis
+    (values: one per field, the Dirichlet value or Neumann gradient)."""
+    m = Mol(pde_id=pde_id, dims=len(nodes), fields=fields)
+    for a, nd in enumerate(nodes):
+        m.nodes[a] = nd
+        m.lower[a] = lower[a]
+        m.dx[a] = dx[a]
+        for side, (kind, vals) in enumerate(faces[a]):
+            m.bc_kind[a][side] = kind
+            for c, v in enumerate(vals or []):
+                m.bc_value[a][side][c] = v
+    for q, v in enumerate(params):
+        m.params[q] = v
+    return m
+
+
 class ServerCfg(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_active", C.c_int32), ("round_budget", C.c_int32)]
 
@@ -204,6 +235,9 @@ SIGNATURES = {
     "degpu_gray_scott_rk4": (C.c_int, [C.POINTER(GrayScott), C.c_int32, C.c_double, C.c_double, C.c_int64,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
     "degpu_gray_scott_rhs": (C.c_int, [C.POINTER(GrayScott), DP, DP, DP, DP, C.c_void_p]),
+    "degpu_mol_rhs": (C.c_int, [C.POINTER(Mol), C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "degpu_mol_rk4": (C.c_int, [C.POINTER(Mol), C.c_int32, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                C.POINTER(C.c_int64), C.c_void_p]),
     "degpu_server_create": (C.c_int, [C.POINTER(ServerCfg), C.POINTER(C.c_void_p)]),
     "degpu_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(MethodCfg), C.POINTER(BatchIn),
                                       C.POINTER(BatchOut), C.POINTER(C.c_uint64)]),

@@ -31,6 +31,8 @@ pub const DEGPU_RKV989E: i32 = 12;
 pub const DEGPU_FP64_PARITY: i32 = 0;
 pub const DEGPU_FP64_FAST: i32 = 1;
 pub const DEGPU_MIXED: i32 = 2;
+pub const DEGPU_FP64_PLAIN: i32 = 3;
+pub const DEGPU_MIXED_FP64_CTRL: i32 = 4;
 pub const DEGPU_KERNEL_AUTO: i32 = 0;
 pub const DEGPU_KERNEL_THREAD: i32 = 1;
 pub const DEGPU_KERNEL_WARP: i32 = 2;
@@ -59,6 +61,16 @@ pub const DEGPU_BVP_SINGLE: i32 = 0;
 pub const DEGPU_BVP_MULTIPLE: i32 = 1;
 pub const DEGPU_BVP_MAX_UNKNOWNS: usize = 64;
 pub const DEGPU_NOALLOC_MAX_INSTANCES: i64 = 262144;
+
+// degpu_pde_id, degpu_bc_kind
+pub const DEGPU_MOL_MAX_FIELDS: usize = 4;
+pub const DEGPU_MOL_MAX_PARAMS: usize = 8;
+pub const DEGPU_PDE_DIFFUSION: i32 = 1;
+pub const DEGPU_PDE_COUPLED_DIFFUSION: i32 = 2;
+pub const DEGPU_PDE_GRAY_SCOTT: i32 = 3;
+pub const DEGPU_BC_DIRICHLET: i32 = 0;
+pub const DEGPU_BC_NEUMANN: i32 = 1;
+pub const DEGPU_BC_PERIODIC: i32 = 2;
 
 #[repr(C)]
 #[derive(Clone, Copy, Debug)]
@@ -99,6 +111,8 @@ pub struct degpu_batch_in {
     pub t_eval: *const f64,
     pub n_eval: i32,
     pub reserved: i32,
+    pub rtol_vec: *const f64,
+    pub atol_vec: *const f64,
 }
 
 #[repr(C)]
@@ -194,6 +208,21 @@ pub struct degpu_gray_scott {
 }
 
 #[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct degpu_mol {
+    pub pde_id: i32,
+    pub dims: i32,
+    pub fields: i32,
+    pub reserved: i32,
+    pub nodes: [i32; 2],
+    pub lower: [f64; 2],
+    pub dx: [f64; 2],
+    pub bc_kind: [[i32; 2]; 2],
+    pub bc_value: [[[f64; DEGPU_MOL_MAX_FIELDS]; 2]; 2],
+    pub params: [f64; DEGPU_MOL_MAX_PARAMS],
+}
+
+#[repr(C)]
 pub struct degpu_server {
     _private: [u8; 0],
 }
@@ -253,6 +282,10 @@ extern "C" {
                                 u: *mut c_void, v: *mut c_void, stream: *mut c_void) -> degpu_status;
     pub fn degpu_gray_scott_rhs(gs: *const degpu_gray_scott, u: *const f64, v: *const f64, du: *mut f64,
                                 dv: *mut f64, stream: *mut c_void) -> degpu_status;
+    pub fn degpu_mol_rhs(mol: *const degpu_mol, precision: i32, t: f64, y: *const c_void, dydt: *mut c_void,
+                         stream: *mut c_void) -> degpu_status;
+    pub fn degpu_mol_rk4(mol: *const degpu_mol, precision: i32, t0: f64, tf: f64, h: f64, y: *mut c_void,
+                         steps: *mut i64, stream: *mut c_void) -> degpu_status;
     pub fn degpu_server_create(cfg: *const degpu_server_cfg, server: *mut *mut degpu_server) -> degpu_status;
     pub fn degpu_server_submit(server: *mut degpu_server, pb: *const degpu_problem, cfg: *const degpu_method_cfg,
                                inp: *const degpu_batch_in, out: *mut degpu_batch_out,

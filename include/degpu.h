@@ -143,6 +143,7 @@ typedef enum {
     DEGPU_RHS_BRUSSELATOR = 11, /* d=2, p=[a, b]                    tests/ode/systems.rs:103-120  */
     DEGPU_RHS_CR3BP = 12,       /* d=6, p=[mu]                      tests/ode/systems.rs:122-153  */
     DEGPU_RHS_PIPE_HEAT = 13,   /* d=2, p=[heat_loss_rate, ambient] tests/bvp/systems.rs:25-57    */
+    DEGPU_RHS_DAMPED_QUADRATURE = 14, /* d=3, p=[k, m, c]  examples/ode/17_quadrature/main.rs:41-55 */
     DEGPU_RHS_NVRTC_BASE = 1000 /* ids >= this were returned by degpu_register_rhs_nvrtc          */
 } degpu_rhs_id;
 
@@ -183,6 +184,11 @@ typedef struct {
     const double* t_eval;    /* [n_eval] evaluation times shared by all instances, or NULL  */
     int32_t n_eval;          /* number of evaluation times (0 = no dense output)             */
     int32_t reserved;
+    /* Per-component tolerances, Tolerance::Vector (src/tolerance.rs:11-14, indexed per component
+     * by error_norm, src/traits.rs:394-410, and the initial step, src/methods/h_init.rs:76-82):
+     * [dim][n], or NULL to use the scalar rtol[n] / atol[n].  Each may be given alone. */
+    const double* rtol_vec;
+    const double* atol_vec;
 } degpu_batch_in;
 
 typedef struct {
@@ -448,6 +454,51 @@ degpu_status degpu_gray_scott_rk4(const degpu_gray_scott* gs, int32_t precision,
 /* One right-hand-side evaluation of the same semi-discretisation (u, v -> du, dv), FP64. */
 degpu_status degpu_gray_scott_rhs(const degpu_gray_scott* gs, const double* u, const double* v,
                                   double* du, double* dv, void* stream);
+
+/* Method of lines on a structured grid with the crate's faces: the semi-discretisation of
+ * `MethodOfLines::finite_difference(grid).boundary(bc).discretize(&pde)` (SemiDiscretePde::diff,
+ * src/pde/semi_discrete.rs:250-287; StructuredGrid, src/pde/grid.rs:23-145; BoundaryConditions,
+ * src/pde/boundary.rs:11-94) for a built-in PDE, u_t = div(flux(t, x, u, grad u)) + source(t, x, u).
+ * The state holds the fields of a node together, y[node * fields + c], node = i0 + nodes[0] i1
+ * (axis 0 fastest), as the crate's Vec state does.  A node on a Dirichlet face has du/dt = 0.
+ * A periodic face (not in the crate) wraps the neighbour around its axis; both faces of a
+ * periodic axis must be periodic. */
+#define DEGPU_MOL_MAX_FIELDS 4
+#define DEGPU_MOL_MAX_PARAMS 8
+typedef enum {
+    DEGPU_PDE_DIFFUSION = 1,          /* flux_c = p[c] grad_c, no source; fields 1..4
+                                         (HeatEquation, tests/pde/method_of_lines.rs:3-11)        */
+    DEGPU_PDE_COUPLED_DIFFUSION = 2,  /* flux_c = p[c] grad_c, source (u1 - u0, u0 - u1); 2 fields
+                                         (CoupledDiffusion, tests/pde/method_of_lines.rs:13-34)   */
+    DEGPU_PDE_GRAY_SCOTT = 3          /* p = (Du, Dv, F, k); 2 fields (u, v)                    */
+} degpu_pde_id;
+typedef enum { DEGPU_BC_DIRICHLET = 0, DEGPU_BC_NEUMANN = 1, DEGPU_BC_PERIODIC = 2 } degpu_bc_kind;
+
+typedef struct {
+    int32_t pde_id;       /* degpu_pde_id                                                     */
+    int32_t dims;         /* axes: 1 or 2                                                      */
+    int32_t fields;       /* values per node (the PDE's local state length)                    */
+    int32_t reserved;
+    int32_t nodes[2];     /* nodes per axis (>= 2; nodes[1] ignored for one axis)              */
+    double lower[2];      /* grid origin (StructuredGrid::uniform's lower corner)              */
+    double dx[2];         /* node spacing per axis ((upper - lower) / (nodes - 1) for uniform) */
+    int32_t bc_kind[2][2];   /* [axis][0 lower, 1 upper]: degpu_bc_kind                        */
+    double bc_value[2][2][DEGPU_MOL_MAX_FIELDS]; /* Dirichlet value or Neumann gradient per field */
+    double params[DEGPU_MOL_MAX_PARAMS];          /* the PDE's parameters                        */
+} degpu_mol;
+
+/* dydt = f(t, y), the semi-discrete right-hand side, on device arrays of nodes * fields values:
+ * double for DEGPU_FP64_PARITY (the crate's operation order bit for bit), DEGPU_FP64_FAST and
+ * DEGPU_FP64_PLAIN (FMA contraction); float for DEGPU_MIXED. */
+degpu_status degpu_mol_rhs(const degpu_mol* mol, int32_t precision, double t, const void* y, void* dydt,
+                           void* stream);
+
+/* `IVP::pde(..).space(..).method(ExplicitRungeKutta::rk4(h)).solve()` from t0 to tf: the crate's
+ * fixed RK4 steps (src/methods/erk/fixed/ordinary.rs:58-138) under its driver loop
+ * (src/ode/solve_ivp.rs:138-277: the last step is shortened to end at tf), y advanced in place.
+ * *steps receives the number of steps taken.  Precision as degpu_mol_rhs. */
+degpu_status degpu_mol_rk4(const degpu_mol* mol, int32_t precision, double t0, double tf, double h, void* y,
+                           int64_t* steps, void* stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Serving: continuous batching of ensemble solves.

@@ -85,6 +85,17 @@ void oracle_libm_pow_batch(const double* x, const double* y, double* out, int64_
 }
 
 // Solve one instance i of the batch into the outputs.
+// The Tolerance of instance i: the per-component column of `vec` ([d][n]) when given, else the
+// scalar `scalar[i]` (src/tolerance.rs:11-14).
+static Tolerance tolerance_of(const double* scalar, const double* vec, int64_t n, int64_t i, int d) {
+    Tolerance t(scalar[i]);
+    if (vec) {
+        t.vec.resize(d);
+        for (int c = 0; c < d; ++c) t.vec[c] = vec[(int64_t)c * n + i];
+    }
+    return t;
+}
+
 static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg, const degpu_batch_in* in,
                            degpu_batch_out* out, int64_t i, const Math& math, const CrossingSolout* proto = nullptr,
                            int64_t max_points = 0, degpu_crossing_out* co = nullptr,
@@ -102,8 +113,8 @@ static void solve_instance(const degpu_problem* pb, const degpu_method_cfg* cfg,
     for (int q = 0; q < pb->n_params; ++q) p[q] = in->params[(int64_t)q * n + i];
     BuiltinOde ode(rhs, d, p, math);
     Settings set;
-    set.rtol = in->rtol[i];
-    set.atol = in->atol[i];
+    set.rtol = tolerance_of(in->rtol, in->rtol_vec, n, i, d);
+    set.atol = tolerance_of(in->atol, in->atol_vec, n, i, d);
     set.h0 = cfg->h0;
     set.h_min = cfg->h_min;
     set.h_max = cfg->h_max;
@@ -252,8 +263,8 @@ int oracle_solve_bvp(const degpu_problem* pb, const degpu_method_cfg* cfg, const
         for (int q = 0; q < pb->n_params; ++q) p[q] = in->params[(int64_t)q * n + i];
         BuiltinOde ode(pb->rhs_id, dim, p, math);
         BvpSolver sv{cfg->method, ode, Settings{}, math, cfg->dense_mode == DEGPU_DENSE_HAIRER, BvpResult{}};
-        sv.set.rtol = in->rtol[i];
-        sv.set.atol = in->atol[i];
+        sv.set.rtol = tolerance_of(in->rtol, in->rtol_vec, n, i, dim);
+        sv.set.atol = tolerance_of(in->atol, in->atol_vec, n, i, dim);
         sv.set.h0 = cfg->h0;
         sv.set.h_min = cfg->h_min;
         sv.set.h_max = cfg->h_max;
@@ -529,5 +540,78 @@ int oracle_gray_scott_rk4(const degpu_gray_scott* gs, double t0, double dt, int6
         v[i] = s.y[2 * i + 1];
     }
     return 0;
+}
+
+// The general method-of-lines problem of the ABI (degpu_mol): a SemiDiscrete with the built-in PDE.
+struct MolHolder {
+    DiffusionPde diff;
+    CoupledDiffusionPde coupled;
+    GrayScottPde gs;
+    SemiDiscrete sd;
+};
+static bool mol_setup(MolHolder& h, const degpu_mol* m) {
+    const int L = m->fields;
+    switch (m->pde_id) {
+        case DEGPU_PDE_DIFFUSION:
+            h.diff.kappa.assign(m->params, m->params + L);
+            h.sd.pde = &h.diff;
+            break;
+        case DEGPU_PDE_COUPLED_DIFFUSION:
+            if (L != 2) return false;
+            h.coupled.d0 = m->params[0];
+            h.coupled.d1 = m->params[1];
+            h.sd.pde = &h.coupled;
+            break;
+        case DEGPU_PDE_GRAY_SCOTT:
+            if (L != 2) return false;
+            h.gs.Du = m->params[0];
+            h.gs.Dv = m->params[1];
+            h.gs.F = m->params[2];
+            h.gs.k = m->params[3];
+            h.sd.pde = &h.gs;
+            break;
+        default: return false;
+    }
+    h.sd.D = m->dims;
+    h.sd.L = L;
+    h.sd.nodes = {m->nodes[0], m->dims == 2 ? m->nodes[1] : 1};
+    h.sd.lower = {m->lower[0], m->dims == 2 ? m->lower[1] : 0.0};
+    h.sd.dx = {m->dx[0], m->dims == 2 ? m->dx[1] : 1.0};
+    for (int a = 0; a < m->dims; ++a) {
+        h.sd.lo_bc[a] = make_bc(m->bc_kind[a][0], m->bc_value[a][0], L);
+        h.sd.hi_bc[a] = make_bc(m->bc_kind[a][1], m->bc_value[a][1], L);
+    }
+    h.sd.build_mask();
+    return true;
+}
+
+// SemiDiscretePde::diff of a degpu_mol problem; y and dydt hold nodes * fields values.
+int oracle_mol_rhs(const degpu_mol* m, double t, const double* y, double* dydt, int threads) {
+    MolHolder h;
+    if (!mol_setup(h, m)) return 1;
+    size_t E = h.sd.len() * (size_t)m->fields;
+    State yy(y, y + E), dd(E, 0.0);
+    mol_diff_threaded(h.sd, t, yy, dd, threads);
+    for (size_t e = 0; e < E; ++e) dydt[e] = dd[e];
+    return 0;
+}
+
+// IVP::pde(..).method(rk4(h)).solve() from t0 to tf (solve_ode with the fixed RK4 step); y in place.
+int oracle_mol_rk4(const degpu_mol* m, double t0, double tf, double h0, double* y, int64_t* steps, int threads) {
+    MolHolder h;
+    if (!mol_setup(h, m)) return 1;
+    ThreadedOde ode;
+    ode.sd = &h.sd;
+    ode.threads = threads;
+    size_t E = h.sd.len() * (size_t)m->fields;
+    Settings set;
+    set.h0 = h0;
+    set.max_steps = 100000000;
+    Math math;
+    State y0(y, y + E);
+    Result r = solve_one(DEGPU_RK4, ode, t0, tf, y0, set, math, nullptr);
+    for (size_t e = 0; e < E; ++e) y[e] = r.y_final[e];
+    if (steps) *steps = r.accepted;
+    return r.outcome.status;
 }
 }  // extern "C"

@@ -402,11 +402,21 @@ inline double diff_norm_squared(const State& self, const State& other) {  // tra
     }
     return sum;
 }
-// traits.rs:394-410 with scalar Tolerance (src/tolerance.rs:33-40: Scalar indexes to itself).
-inline double error_norm(const State& self, const State& y_new, const State& err, double atol, double rtol) {
+// src/tolerance.rs:11-40: a scalar tolerance (which every index reads) or one per component.
+struct Tolerance {
+    double scalar = 0.0;
+    std::vector<double> vec;
+    Tolerance() = default;
+    Tolerance(double v) : scalar(v) {}  // From<T> (tolerance.rs:52-56)
+    double operator[](size_t i) const { return vec.empty() ? scalar : vec[i]; }  // Index (tolerance.rs:33-40)
+};
+
+// traits.rs:394-410.
+inline double error_norm(const State& self, const State& y_new, const State& err, const Tolerance& atol,
+                         const Tolerance& rtol) {
     double sum = 0.0;
     for (size_t i = 0; i < self.size(); ++i) {
-        double sk = atol + rtol * std::fmax(std::fabs(self[i]), std::fabs(y_new[i]));
+        double sk = atol[i] + rtol[i] * std::fmax(std::fabs(self[i]), std::fabs(y_new[i]));
         double e = err[i] / sk;
         sum += e * e;
     }
@@ -447,6 +457,7 @@ inline void builtin_info(int rhs_id, int& dim, int& np) {
         case DEGPU_RHS_BRUSSELATOR: dim = 2; np = 2; return;
         case DEGPU_RHS_CR3BP: dim = 6; np = 1; return;
         case DEGPU_RHS_PIPE_HEAT: dim = 2; np = 2; return;
+        case DEGPU_RHS_DAMPED_QUADRATURE: dim = 3; np = 3; return;
         default: dim = 0; np = -1; return;
     }
 }
@@ -530,6 +541,13 @@ inline void BuiltinOde::diff(double t, const State& y, State& dydt) const {
             dydt[1] = (b * b) * (y[0] - amb);
             return;
         }
+        case DEGPU_RHS_DAMPED_QUADRATURE: {  // examples/ode/17_quadrature/main.rs:47-55
+            const double k = p[0], m = p[1], c = p[2], x = y[0], v = y[1];
+            dydt[0] = v;
+            dydt[1] = -(k / m) * x - (c / m) * v;
+            dydt[2] = c * v * v;
+            return;
+        }
         case DEGPU_RHS_CR3BP: {                                          // systems.rs:131-152
             // powi(2) and powi(3) lower to x*x and x*(x*x) (LLVM's multiply expansion).
             double mu = p[0];
@@ -602,8 +620,8 @@ inline bool validate_step_size_parameters(double h0, double h_min, double h_max,
 }
 
 struct Settings {  // src/methods/erk/mod.rs:112-159 defaults
-    double rtol = 1.0e-6;
-    double atol = 1.0e-6;
+    Tolerance rtol = 1.0e-6;
+    Tolerance atol = 1.0e-6;
     double h0 = 0.0;
     double h_min = 0.0;
     double h_max = std::numeric_limits<double>::infinity();
@@ -614,8 +632,8 @@ struct Settings {  // src/methods/erk/mod.rs:112-159 defaults
 };
 
 // src/methods/h_init.rs:45-136 (InitialStepSize<Ordinary>::compute).
-inline double h_init(const Ode& ode, double t0, double tf, const State& y0, int order, double rtol, double atol,
-                     double h_min, double h_max, int64_t& fevals, const Math& math) {
+inline double h_init(const Ode& ode, double t0, double tf, const State& y0, int order, const Tolerance& rtol,
+                     const Tolerance& atol, double h_min, double h_max, int64_t& fevals, const Math& math) {
     double posneg = rust_signum(tf - t0);
     size_t n_dim = y0.size();
     State f0(n_dim, 0.0), f1(n_dim, 0.0);
@@ -624,7 +642,7 @@ inline double h_init(const Ode& ode, double t0, double tf, const State& y0, int 
     double dnf = 0.0, dny = 0.0;
     std::vector<double> sk_vec(n_dim);
     for (size_t n = 0; n < n_dim; ++n) {
-        double sk = atol + rtol * std::fabs(y0[n]);
+        double sk = atol[n] + rtol[n] * std::fabs(y0[n]);
         sk_vec[n] = sk;
         double a = f0[n] / sk;
         dnf += a * a;  // powi(2) -> x*x
@@ -1302,7 +1320,7 @@ struct AdaptiveRK : Interpolator {
         // error_norm_inf, traits.rs:413-433 (f64::max keeps the non-NaN operand)
         double err_norm = 0.0;
         for (size_t i = 0; i < y.size(); ++i) {
-            double sk = set.atol + set.rtol * std::fmax(std::fabs(y[i]), std::fabs(y_high[i]));
+            double sk = set.atol[i] + set.rtol[i] * std::fmax(std::fabs(y[i]), std::fabs(y_high[i]));
             err_norm = std::fmax(err_norm, std::fabs(err[i] / sk));
         }
         double error_exponent = 1.0 / (double)tab.order;

@@ -161,6 +161,17 @@ struct HeatPde : Pde {
     }
 };
 
+// Diffusion with one diffusivity per field (HeatEquation is the one-field case): flux_c =
+// kappa_c grad_c along the axis, no source.
+struct DiffusionPde : Pde {
+    std::vector<double> kappa;
+    void flux(double, const double*, const double*, const std::vector<State>& grad,
+              std::vector<State>& fl) const override {
+        for (size_t a = 0; a < grad.size(); ++a)
+            for (size_t c = 0; c < kappa.size(); ++c) fl[a][c] = kappa[c] * grad[a][c];
+    }
+};
+
 // tests/pde/method_of_lines.rs:13-34
 struct CoupledDiffusionPde : Pde {
     double d0, d1;

@@ -72,6 +72,8 @@ def lib():
                                             DP, DP]
         L.oracle_heat1d_solve.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, DP, DP, I64P]
         L.oracle_gray_scott_rhs.argtypes = [C.POINTER(abi.GrayScott), DP, DP, DP, DP, C.c_int]
+        L.oracle_mol_rhs.argtypes = [C.POINTER(abi.Mol), C.c_double, DP, DP, C.c_int]
+        L.oracle_mol_rk4.argtypes = [C.POINTER(abi.Mol), C.c_double, C.c_double, C.c_double, DP, I64P, C.c_int]
         L.oracle_gray_scott_rk4.argtypes = [C.POINTER(abi.GrayScott), C.c_double, C.c_double, C.c_int64, DP, DP,
                                             C.c_int]
         _lib = L
@@ -86,7 +88,7 @@ class Batch:
     """Host-side batch of IVPs in the ABI's structure-of-arrays layout."""
 
     def __init__(self, rhs_id, dim, n_params, t0, tf, y0, params, rtol, atol, t_eval=None, dims=None,
-                 family=None):
+                 family=None, rtol_vec=None, atol_vec=None):
         self.n = len(t0)
         self.problem = abi.Problem(rhs_id=rhs_id, dim=dim, n_params=n_params)
         self.t0 = np.ascontiguousarray(t0, dtype=np.float64)
@@ -99,13 +101,17 @@ class Batch:
         self.t_eval = None if t_eval is None else np.ascontiguousarray(t_eval, dtype=np.float64)
         self.dims = None if dims is None else np.ascontiguousarray(dims, dtype=np.int32)
         self.family = None if family is None else np.ascontiguousarray(family, dtype=np.int32)
+        tv = lambda v: None if v is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(v, dtype=np.float64).reshape(dim, -1), (dim, self.n)))
+        self.rtol_vec, self.atol_vec = tv(rtol_vec), tv(atol_vec)
         self.dim = dim
 
     def batch_in(self):
         return abi.BatchIn(
             n=self.n, t0=p(self.t0), tf=p(self.tf), y0=p(self.y0), params=p(self.params), rtol=p(self.rtol),
             atol=p(self.atol), dims=abi.ptr(self.dims, C.c_int32), family=abi.ptr(self.family, C.c_int32),
-            t_eval=p(self.t_eval), n_eval=0 if self.t_eval is None else len(self.t_eval))
+            t_eval=p(self.t_eval), n_eval=0 if self.t_eval is None else len(self.t_eval),
+            rtol_vec=p(self.rtol_vec), atol_vec=p(self.atol_vec))
 
     def new_outputs(self):
         m = 0 if self.t_eval is None else len(self.t_eval)
