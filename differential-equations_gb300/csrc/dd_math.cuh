@@ -30,6 +30,7 @@
 #if !defined(__CUDACC_RTC__)
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 #endif
 
 #if defined(__CUDACC__)
@@ -258,6 +259,106 @@ DD_HD double pow_ctrl(double x, double y) {
         return (r.hi + t) * post;
     }
     return (r.hi + r.lo) * post;
+}
+
+// Bit-pattern access for host and device builds.
+DD_HD int64_t dd_bits(double x) {
+#if defined(__CUDA_ARCH__)
+    return __double_as_longlong(x);
+#else
+    int64_t b;
+    memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+DD_HD double dd_from_bits(int64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double(b);
+#else
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+DD_HD uint32_t dd_fbits(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    uint32_t b;
+    memcpy(&b, &x, 4);
+    return b;
+#endif
+}
+DD_HD float dd_ffrom(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(b);
+#else
+    float x;
+    memcpy(&x, &b, 4);
+    return x;
+#endif
+}
+
+// The controller's power x^(-0.2) (DOPRI5 and the order-5 pairs) and x^(-0.125) (DOP853),
+// correctly rounded as pow_ctrl, for the contracted FP64 forms: the same double-double Newton
+// finish, with two savings that matter where FP64 runs at 1/64 of the FP32 rate.
+//  - The FP32 starting value is built from the bit pattern of x with integer and FP32
+//    operations only (no FP64 conversion or ldexp).
+//  - The factor exp(-2^-54 ln(x) / 5) that turns 1/5 into binary64 0.2 takes ln(x) from FP32
+//    (absolute error below 2^-14 over the whole range, the FP32 rounding of the exponent sum
+//    included, so the factor is off by less than 2^-69.5 relative).  The result is then the
+//    correctly rounded value unless the computed sum lies within 2^-68 of a rounding boundary
+//    (Ziv's test on the exact remainder of the final addition); only then is ln(x) evaluated in
+//    FP64 (about one call in 2^13).
+// x must be finite and in [2^-800, 2^800] after the caller's scaling; other x go to pow_ctrl.
+DD_HD double pow_ctrl_neg(double x, double y) {
+    const bool fifth = y == -0.2;
+    if (!(fifth || y == -0.125) || !(x >= 0x1p-800 && x <= 0x1p+800)) return pow_ctrl(x, y);
+    const int q = fifth ? 5 : 8;
+    const int64_t b = dd_bits(x);
+    const int ex = (int)((b >> 52) & 0x7ff) - 1023;
+    const float m = dd_ffrom(0x3f800000u | (uint32_t)((b >> 29) & 0x7fffff));  // 1.mantissa, 23 bits
+    const float lx = (float)ex + log2f(m);                                     // log2(x) in FP32
+    const float tq = -lx / (float)q;
+    const float kf = floorf(tq);
+    const uint32_t fb = dd_fbits(exp2f(tq - kf));                              // in [1, 2]
+    const int e2 = (int)((fb >> 23) & 0xff) - 127 + (int)kf;
+    double s = dd_from_bits(((int64_t)(e2 + 1023) << 52) | ((int64_t)(fb & 0x7fffff) << 29));
+    const double q1 = (double)(q + 1), iq = fifth ? 0.2 : 0.125;
+    for (int it = 0; it < 2; ++it) {
+        double s2 = s * s;
+        double s4 = s2 * s2;
+        double sq = fifth ? s4 * s : s4 * s4;
+        s = s * (q1 - x * sq) * iq;
+    }
+    dd s2 = two_prod(s, s);
+    dd s4 = dd_mul(s2, s2);
+    dd sq = fifth ? dd_mul_d(s4, s) : dd_mul(s4, s4);
+    dd xsq = dd_mul_d(sq, x);
+    double e = (1.0 - xsq.hi) - xsq.lo;  // 1 - xsq.hi is exact: xsq.hi is within 2^-50 of 1
+    dd r = fast_two_sum(s, s * e * iq);
+    if (!fifth) return r.hi + r.lo;
+    // binary64 0.2 = (1/5)(1 + 2^-54): multiply by exp(-2^-54 ln(x) / 5) = 1 + g
+    const float gf = lx * -7.6954796e-18f;  // -(2^-54 / 5) ln 2 = -7.69547959e-18
+    const uint32_t gb = dd_fbits(gf);
+    const int ge = (int)((gb >> 23) & 0xff);
+    const double g = ge == 0 ? 0.0
+                             : dd_from_bits(((int64_t)(gb >> 31) << 63) | ((int64_t)(ge + 896) << 52) |
+                                            ((int64_t)(gb & 0x7fffff) << 29));
+    double t = r.lo + r.hi * g;
+    double res = r.hi + t;
+    const double tail = (r.hi - res) + t;  // exact: r.hi + t - res
+    // half an ulp of res, and the error bound 2^-64 res
+    const int64_t rb = dd_bits(res);
+    const int re = (int)((rb >> 52) & 0x7ff);
+    // (below a power of two the spacing halves)
+    const bool below_pow2 = (rb & 0xfffffffffffffll) == 0 && tail < 0.0;
+    const double half_ulp = dd_from_bits((int64_t)(re - (below_pow2 ? 54 : 53)) << 52);
+    const double bound = dd_from_bits((int64_t)(re - 67) << 52);  // > 2^-68 res
+    if (fabs(tail) + bound < half_ulp) return res;
+    const double gx = -1.1102230246251566e-17 /* 2^-54 / 5 */ * log(x);
+    t = r.lo + r.hi * (gx + 0.5 * gx * gx);
+    return r.hi + t;
 }
 
 // sin(u), cos(u) as double-doubles for |u.hi| <= 1/128.

@@ -8,6 +8,9 @@ extern "C" {
 void degpu_host_pow_ctrl(const double* x, double y, double* out, int64_t n) {
     for (int64_t i = 0; i < n; ++i) out[i] = degpu::ddm::pow_ctrl(x[i], y);
 }
+void degpu_host_pow_ctrl_neg(const double* x, double y, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) out[i] = degpu::ddm::pow_ctrl_neg(x[i], y);
+}
 void degpu_host_sincos_f32(const float* x, float* s, float* c, int64_t n) {
     for (int64_t i = 0; i < n; ++i) {
         s[i] = degpu::f32m::sin_f32(x[i]);

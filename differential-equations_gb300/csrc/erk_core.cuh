@@ -217,6 +217,58 @@ __device__ __forceinline__ float narrow_rz(double x) {
     return __uint_as_float(sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
 }
 
+// Comparisons, minima and maxima of non-negative doubles on their bit patterns, for the FP64
+// paths' bookkeeping: an FP64 compare or min/max instruction occupies the FP64 pipe (1/64 of the
+// FP32 rate on this GPU), a 64-bit integer one does not.  The order of doubles >= +0 (with +inf)
+// is the order of their bit patterns, so each helper gives exactly the FP64 result, NaN included
+// as noted.
+__device__ __forceinline__ long long nn_bits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool nn_is_nan(long long b) { return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll; }
+// a < b for a >= +0 or NaN and b >= +0 (false for a NaN, as the FP64 compare)
+__device__ __forceinline__ bool nn_lt(double a, double b) { return nn_bits(a) < nn_bits(b); }
+// a <= b for a >= +0 or NaN and b >= +0 (false for a NaN)
+__device__ __forceinline__ bool nn_le(double a, double b) {
+    const long long x = nn_bits(a);
+    return !nn_is_nan(x) && x <= nn_bits(b);
+}
+// |a| < b for any a and b >= +0 (false for a NaN)
+__device__ __forceinline__ bool abs_lt(double a, double b) { return (nn_bits(a) & 0x7fffffffffffffffll) < nn_bits(b); }
+// fmax(|a|, |b|): the larger magnitude, the other operand when one is NaN
+__device__ __forceinline__ double fmax_abs(double a, double b) {
+    const long long x = nn_bits(a) & 0x7fffffffffffffffll, y = nn_bits(b) & 0x7fffffffffffffffll;
+    if (nn_is_nan(x)) return __longlong_as_double(y);
+    if (nn_is_nan(y)) return __longlong_as_double(x);
+    return __longlong_as_double(x > y ? x : y);
+}
+// fmin(fmax(v, lo), hi) for v >= +0 or NaN and +0 <= lo <= hi (a NaN v gives lo, as fmax does)
+__device__ __forceinline__ double nn_clamp(double v, double lo, double hi) {
+    long long x = nn_bits(v);
+    const long long l = nn_bits(lo), h = nn_bits(hi);
+    if (nn_is_nan(x) || x < l) x = l;
+    if (x > h) x = h;
+    return __longlong_as_double(x);
+}
+// fmin(v, m) for v, m >= +0 (neither NaN)
+__device__ __forceinline__ double nn_min(double v, double m) {
+    const long long x = nn_bits(v), y = nn_bits(m);
+    return __longlong_as_double(x < y ? x : y);
+}
+
+// The earliest stage (>= 1) of a tableau at the same node c as stage i, and the last stage at
+// c = 1 (-1 if none): stages at one time share a time-dependent drive term.
+template <class Tab>
+__host__ __device__ constexpr int first_stage_at_c(int i) {
+    for (int j = 1; j < i; ++j)
+        if (Tab::c(j) == Tab::c(i)) return j;
+    return i;
+}
+template <class Tab>
+__host__ __device__ constexpr int last_stage_at_one() {
+    for (int j = Tab::S - 1; j >= 1; --j)
+        if (Tab::c(j) == 1.0) return j;
+    return -1;
+}
+
 // CROSS: crossing detection instead of output times (needs DENSE for the step's interpolant).
 template <class Tab, class Rhs, class P, bool DENSE, bool CROSS = false>
 struct Lane {
@@ -243,6 +295,9 @@ struct Lane {
     // Mixed form of a first-same-as-last tableau (DOPRI5): the last stage is evaluated at y_new
     // itself, and the evaluation the crate repeats at the new point on acceptance is that stage.
     static constexpr bool FSAL_MIX = MIX && Tab::FSAL;
+    // FP64 forms of a family with a drive term: one drive evaluation per distinct stage time,
+    // shared with the evaluation at the new point (t + h, the time of the c = 1 stage)
+    static constexpr bool DRV = !P::KAHAN && DriveOf<Rhs>::value && Tab::DP;
 
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
@@ -251,6 +306,7 @@ struct Lane {
     float phl, omh, oml;     // FFT with a drive phase: phase = ph0 + phl, rate = omh + oml
     double rem;    // tf - t (mixed form of RK4)
     float h_lim;   // 1e-14 |h_prev| in FP32 (mixed form's step-size guard)
+    double h_lim64;  // 1e-14 |h_prev| (FP64 step-size guard), formed on acceptance
     // Mixed form of the adaptive methods (MIX): the step size, the remaining span used by the
     // overshoot test and the drive phase of time-dependent families are FP32; FP64 is touched
     // only on acceptance (t += h, tf - t, the phase at the new t).
@@ -375,8 +431,8 @@ struct Lane {
             float q = __fdividef(e, sk);
             return q * q;
         } else {
-            double sk = atol_c(c, a) + rtol_c(c, a) * fmax(fabs((double)yv), fabs((double)ynv));
-            double q = (double)e / sk;
+            double sk = atol_c(c, a) + rtol_c(c, a) * fmax_abs((double)yv, (double)ynv);
+            double q = P::quot((double)e, sk);
             return q * q;
         }
     }
@@ -1015,6 +1071,7 @@ struct Lane {
         if constexpr (PHASE) ph0 = Rhs::phase(t0, p);
         t_prev = t0;
         h_prev = 0.0;
+        h_lim64 = 0.0;
         rem = tf - t0;
         h_lim = 0.0f;
         bounded = !(a.h_min == 0.0 && isinf(a.h_max) && a.h_max > 0.0);
@@ -1056,10 +1113,10 @@ struct Lane {
             return;
         }
         h = h0;
+        fwd = dir > 0.0;
         if constexpr (MIX) {
             hf = (float)h0;
             remf = narrow_rz(rem);  // |remf| <= |tf - t|: the overshoot test never lets t pass tf
-            fwd = dir > 0.0;
             last_step = false;
         }
         if constexpr (FFT) {
@@ -1102,7 +1159,7 @@ struct Lane {
                 status = DEGPU_ERR_STEP_SIZE;
                 return 3;
             }
-        } else if (fabs(h) < fabs(h_prev) * 1e-14) {
+        } else if (abs_lt(h, h_lim64)) {  // |h| < |h_prev| 1e-14
             status = DEGPU_ERR_STEP_SIZE;
             return 3;
         }
@@ -1116,6 +1173,7 @@ struct Lane {
 #pragma unroll
         for (int c = 0; c < D; ++c) k[0][c] = k0[c];
         S ys[D];
+        double drv[NS];  // DRV: the drive term at each stage's time
         static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = y[c];
@@ -1127,10 +1185,16 @@ struct Lane {
                     for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
                 }
             });
-            if constexpr (MIX)
+            if constexpr (MIX) {
                 rhs_at((float)Tab::c(i) * hf, ys, k[i]);
-            else
+            } else if constexpr (DRV) {
+                constexpr int i0 = first_stage_at_c<Tab>(decltype(i)::value);
+                if constexpr (i0 == decltype(i)::value)
+                    drv[i0] = Rhs::template drive<P>(t + Tab::c(i) * h, p);
+                Rhs::template diff_drive<P>(drv[i0], ys, k[i], p);
+            } else {
                 rhs(t + Tab::c(i) * h, ys, k[i]);
+            }
         });
         // ys now holds the last stage state (ysti, ordinary.rs:107)
         S yseg[D], ynew[D], ycn[D];
@@ -1200,7 +1264,11 @@ struct Lane {
             for (int c = 0; c < D; ++c) err2 = err2 + norm_term(c, es[c], y[c], ynew[c], a);
         }
         NormT deno = Tab::HAS_BH ? err + (NormT)0.01 * err2 : err;
-        if (deno <= (NormT)0) deno = (NormT)1;
+        if constexpr (P::F32_CTRL) {
+            if (deno <= (NormT)0) deno = (NormT)1;
+        } else if (nn_le(deno, 0.0)) {
+            deno = 1.0;  // deno >= +0: only a zero (or NaN, kept) reaches here
+        }
         double scale = 1.0, errd = 0.0;
         float errf = 0.0f, scalef = 1.0f;
         if constexpr (P::F32_CTRL) {
@@ -1219,12 +1287,12 @@ struct Lane {
             scalef = fminf(fmaxf(a.safety_f * pw, a.min_scale_f), a.max_scale_f);
         } else {
             if constexpr (MIX)
-                errd = (double)fabsf(hf) * err * sqrt(1.0 / (deno * (double)D));
+                errd = (double)fabsf(hf) * err * P::rsqrt(deno * (double)D);
             else
-                errd = fabs(h) * err * sqrt(1.0 / (deno * (double)D));
+                errd = fabs(h) * err * P::rsqrt(deno * (double)D);
             double error_exponent = 1.0 / (double)O;
             scale = a.safety * P::pow(errd, -error_exponent);
-            scale = fmin(fmax(scale, a.min_scale), a.max_scale);
+            scale = nn_clamp(scale, a.min_scale, a.max_scale);
             if constexpr (MIX) scalef = (float)scale;
         }
 
@@ -1234,7 +1302,7 @@ struct Lane {
         if constexpr (P::F32_CTRL)
             accept = errf <= 1.0f;
         else
-            accept = errd <= 1.0;
+            accept = nn_le(errd, 1.0);
         if (accept) {
             double t_new;
             if constexpr (FFT) {
@@ -1252,6 +1320,9 @@ struct Lane {
                 rhs_at(hf, ynew, dydt);
             } else if constexpr (FFT) {
                 rhs(tnow(), ynew, dydt);
+            } else if constexpr (DRV && last_stage_at_one<Tab>() > 0) {
+                // t_new = t + h is the time of the c = 1 stage (t + 1.0 h)
+                Rhs::template diff_drive<P>(drv[first_stage_at_c<Tab>(last_stage_at_one<Tab>())], ynew, dydt, p);
             } else {
                 rhs(t_new, ynew, dydt);
             }
@@ -1309,6 +1380,7 @@ struct Lane {
                 h_lim = fabsf(hf) * 1e-14f;
             } else {
                 h_prev = h;
+                h_lim64 = fabs(h) * 1e-14;
             }
             t = t_new;
             if constexpr (PHASE) {
@@ -1328,7 +1400,7 @@ struct Lane {
                 if constexpr (MIX)
                     scalef = fminf(scalef, 1.0f);
                 else
-                    scale = fmin(scale, 1.0);
+                    scale = nn_min(scale, 1.0);
             }
             result = 1;
         } else {
@@ -1432,7 +1504,7 @@ struct Lane {
                 status = DEGPU_ERR_STEP_SIZE;
                 return 3;
             }
-        } else if (fabs(h) < fabs(h_prev) * 1e-14) {
+        } else if (abs_lt(h, h_lim64)) {  // |h| < |h_prev| 1e-14
             status = DEGPU_ERR_STEP_SIZE;
             return 3;
         }
@@ -1543,12 +1615,12 @@ struct Lane {
             double norm = 0.0;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
-                const double sk = atol_c(c, a) + rtol_c(c, a) * fmax(fabs((double)y[c]), fabs((double)yh[c]));
-                norm = fmax(norm, fabs((double)err[c] / sk));
+                const double sk = atol_c(c, a) + rtol_c(c, a) * fmax_abs((double)y[c], (double)yh[c]);
+                norm = fmax_abs(norm, P::quot((double)err[c], sk));
             }
             scale = a.safety * P::pow(norm, -(1.0 / (double)O));
-            scale = fmin(fmax(scale, a.min_scale), a.max_scale);
-            accept = norm <= 1.0;
+            scale = nn_clamp(scale, a.min_scale, a.max_scale);
+            accept = nn_le(norm, 1.0);
         }
         int result;
         if (accept) {
@@ -1578,6 +1650,7 @@ struct Lane {
                 h_lim = fabsf(hf) * 1e-14f;
             } else {
                 h_prev = h;
+                h_lim64 = fabs(h) * 1e-14;
             }
             if (last_rejected) {
                 last_rejected = false;
@@ -1585,7 +1658,7 @@ struct Lane {
                 if constexpr (MIX)
                     scalef = fminf(scalef, 1.0f);
                 else
-                    scale = fmin(scale, 1.0);
+                    scale = nn_min(scale, 1.0);
             }
             if constexpr (FFT) {
                 ff_advance();
@@ -1737,7 +1810,7 @@ struct Lane {
                 }
                 h = rem;
             }
-        } else if ((t + h - tf) * dir > 0.0) {
+        } else if (fwd ? t + h > tf : t + h < tf) {  // (t + h - tf) dir > 0, exactly
             double h_new = tf - t;
             if (fabs(h_new) < eps10) {
                 done = true;
@@ -1782,7 +1855,7 @@ struct Lane {
             rem = tf - t;
             if (fabs(rem) <= eps10) done = true;
         } else {
-            if (fabs(tf - t) <= eps10) done = true;
+            if (nn_le(fabs(tf - t), eps10)) done = true;
         }
     }
 

@@ -36,6 +36,17 @@ struct PhaseOf {
     static constexpr bool value = test<R>(nullptr);
 };
 
+// DriveOf<R>::value: the family declares DRIVE, a time-dependent term that its FP64 forms
+// evaluate once per distinct stage time (`drive` and `diff_drive`).
+template <class R>
+struct DriveOf {
+    template <class U>
+    __host__ __device__ static constexpr bool test(decltype(U::DRIVE)*) { return U::DRIVE; }
+    template <class U>
+    __host__ __device__ static constexpr bool test(...) { return false; }
+    static constexpr bool value = test<R>(nullptr);
+};
+
 // FloatParamsOf<R>::value: the family's diff accepts FP32 parameters (BuiltinRhs).
 template <class R>
 struct FloatParamsOf {
@@ -45,6 +56,35 @@ struct FloatParamsOf {
     __host__ __device__ static constexpr bool test(...) { return false; }
     static constexpr bool value = test<R>(nullptr);
 };
+
+// Reciprocal and reciprocal square root for the contracted FP64 forms: the hardware estimate
+// (rcp.approx / rsqrt.approx, about 2^-20 relative) refined by two Newton steps (quadratic, to
+// FP64 rounding: within an ulp or two of the IEEE result), five FP64 instructions where the IEEE
+// division and square root take about nine each.  Outside [2^-1000, 2^1000] (where the estimate
+// flushes subnormals) they fall back to the IEEE operations.
+__device__ __forceinline__ bool fp64_mid_range(double x) {
+    const long long e = (__double_as_longlong(x) >> 52) & 0x7ff;
+    return e > 23 && e < 2023;  // 2^-1000 < |x| < 2^1000
+}
+__device__ __forceinline__ double rcp_nr(double x) {
+    if (!fp64_mid_range(x)) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    if (!fp64_mid_range(x) || x < 0.0) return sqrt(1.0 / x);
+    double r;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    // r <- r + r (1 - x r^2) / 2
+    double e = fma(-x * r, r, 1.0);
+    r = fma(0.5 * r, e, r);
+    e = fma(-x * r, r, 1.0);
+    return fma(0.5 * r, e, r);
+}
 
 // Parity: FP64, crate operation order, correctly rounded pow/sin/cos, no FMA contraction (the
 // translation units that instantiate it are compiled with -fmad=false).
@@ -58,6 +98,9 @@ struct PrecParity {
     __device__ static __forceinline__ double sin(double x) { return ddm::sin_cr(x); }
     __device__ static __forceinline__ double cos(double x) { return ddm::cos_cr(x); }
     __device__ static __forceinline__ S from(double x) { return x; }
+    // the error norm's quotients and the controller's sqrt(1/x): IEEE, as the crate computes them
+    __device__ static __forceinline__ double quot(double a, double b) { return a / b; }
+    __device__ static __forceinline__ double rsqrt(double x) { return sqrt(1.0 / x); }
 };
 // Fast FP64: FMA contraction and the CUDA math library.
 struct PrecFast {
@@ -70,14 +113,15 @@ struct PrecFast {
     __device__ static __forceinline__ double sin(double x) { return ::sin(x); }
     __device__ static __forceinline__ double cos(double x) { return ::cos(x); }
     __device__ static __forceinline__ S from(double x) { return x; }
+    __device__ static __forceinline__ double quot(double a, double b) { return a * rcp_nr(b); }
+    __device__ static __forceinline__ double rsqrt(double x) { return rsqrt_nr(x); }
 };
-// Plain FP64: FMA contraction, IEEE division and square root, the CUDA math library's sin/cos,
-// and the correctly rounded controller power of the parity path, so that accept and reject
-// follow the crate's decisions; results differ from the crate's only by contraction and the
-// rounding of sin/cos.
+// Plain FP64: FMA contraction, the refined hardware reciprocal and reciprocal square root in the
+// error norm and the controller, the CUDA math library's sin/cos, and the correctly rounded
+// controller power of the parity path; results differ from the crate's by rounding only.
 struct PrecPlain : PrecFast {
     static constexpr int ID = 3;
-    __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl(x, y); }
+    __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl_neg(x, y); }
 };
 // Mixed: stages in FP32, y accumulated with Kahan compensation; the error terms, the norm, the
 // controller's power and the accept decision in FP32, t as an FP32 pair (see Lane).
@@ -112,6 +156,8 @@ struct PrecMixed {
     __device__ static __forceinline__ float cos(float x) { return f32m::cos_f32(x); }
 #endif
     __device__ static __forceinline__ S from(double x) { return (float)x; }
+    __device__ static __forceinline__ double quot(double a, double b) { return a * rcp_nr(b); }
+    __device__ static __forceinline__ double rsqrt(double x) { return rsqrt_nr(x); }
 };
 // Mixed with the FP64 controller: FP32 stages and Kahan-compensated y as in PrecMixed; the error
 // norm over the FP32 error terms, the controller's power, the accept decision, t and h in FP64.
@@ -174,6 +220,20 @@ struct RhsPendulum : BuiltinRhs {
         float r = ph0 + pf[2] * dt;
         dydt[0] = omega;
         dydt[1] = -pf[0] * omega - P::sin(theta) + pf[1] * P::cos(r);
+    }
+    // FP64 forms: the drive term A cos(Omega t) on its own, so that stages at the same time (the
+    // last two DOPRI5 stages and the new point all sit at t + h) share one evaluation; diff_drive
+    // then forms (-gamma omega - sin theta) + drive, the order of diff.
+    static constexpr bool DRIVE = true;
+    template <class P>
+    __device__ static __forceinline__ double drive(double t, const double* p) {
+        return p[1] * P::cos(p[2] * t);
+    }
+    template <class P>
+    __device__ static __forceinline__ void diff_drive(double drv, const double* y, double* dydt, const double* p) {
+        const double omega = y[1];
+        dydt[0] = omega;
+        dydt[1] = -p[0] * omega - P::sin(y[0]) + drv;
     }
     template <class P, class PT>
     __device__ static __forceinline__ void diff(double t, const typename P::S* y, typename P::S* dydt, const PT* p) {

@@ -175,10 +175,14 @@ struct DiffusionPde : Pde {
 // tests/pde/method_of_lines.rs:13-34
 struct CoupledDiffusionPde : Pde {
     double d0, d1;
+    // the crate's test system is one-dimensional (flux[0] only); on more axes each axis diffuses
+    // alike
     void flux(double, const double*, const double*, const std::vector<State>& grad,
               std::vector<State>& fl) const override {
-        fl[0][0] = d0 * grad[0][0];
-        fl[0][1] = d1 * grad[0][1];
+        for (size_t a = 0; a < grad.size(); ++a) {
+            fl[a][0] = d0 * grad[a][0];
+            fl[a][1] = d1 * grad[a][1];
+        }
     }
     void source(double, const double*, const double* u, double* s, int) const override {
         s[0] = u[1] - u[0];

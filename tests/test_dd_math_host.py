@@ -23,6 +23,7 @@ def H():
         subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", SO, src], check=True)
     h = C.CDLL(SO)
     h.degpu_host_pow_ctrl.argtypes = [O.DP, C.c_double, O.DP, C.c_int64]
+    h.degpu_host_pow_ctrl_neg.argtypes = [O.DP, C.c_double, O.DP, C.c_int64]
     h.degpu_host_sincos_cr.argtypes = [O.DP, O.DP, O.DP, C.c_int64]
     FP = C.POINTER(C.c_float)
     h.degpu_host_sincos_f32.argtypes = [FP, FP, FP, C.c_int64]
@@ -41,6 +42,31 @@ def test_pow_ctrl_correctly_rounded(H, y):
     yy = np.full(n, y)
     O.lib().oracle_cr_pow_batch(O.p(x), O.p(yy), O.p(ref), n)
     assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("y", [-0.2, -0.125])
+def test_pow_ctrl_neg_correctly_rounded(H, y):
+    """The plain path's controller power (FP32 start from the bit pattern, FP32 logarithm in the
+    binary64-exponent factor, Ziv's test with an FP64 logarithm fallback) equals the correctly
+    rounded value, on random inputs, near powers of two and near 1."""
+    rng = np.random.default_rng(21)
+    n = 400_000
+    x = np.exp(rng.uniform(np.log(1e-240), np.log(1e240), n))
+    x[: n // 2] = np.exp(rng.uniform(-12, 12, n // 2))
+    x[:1000] = 2.0 ** rng.integers(-700, 700, 1000)            # results that are powers of two
+    x[1000:2000] = 1.0 + rng.uniform(-1e-12, 1e-12, 1000)      # ln x near 0
+    x[2000:3000] = np.nextafter(2.0 ** (5 * rng.integers(-100, 100, 1000)), 0.0)
+    out = np.empty(n)
+    H.degpu_host_pow_ctrl_neg(O.p(x), y, O.p(out), n)
+    ref = np.empty(n)
+    O.lib().oracle_cr_pow_batch(O.p(x), O.p(np.full(n, y)), O.p(ref), n)
+    assert np.array_equal(out, ref)
+    # outside the direct range it defers to pow_ctrl
+    x2 = np.array([1e-300, 1e300, 0.0, np.inf, np.nan])
+    out2 = np.empty(5)
+    H.degpu_host_pow_ctrl_neg(O.p(x2), y, O.p(out2), 5)
+    ref2 = np.array([O.lib().oracle_cr_pow(v, y) for v in x2])
+    assert np.array_equal(out2, ref2, equal_nan=True)
 
 
 def test_pow_ctrl_special_values(H):
