@@ -262,16 +262,16 @@ DD_HD double pow_ctrl(double x, double y) {
 }
 
 // Bit-pattern access for host and device builds.
-DD_HD int64_t dd_bits(double x) {
+DD_HD long long dd_bits(double x) {
 #if defined(__CUDA_ARCH__)
     return __double_as_longlong(x);
 #else
-    int64_t b;
+    long long b;
     memcpy(&b, &x, 8);
     return b;
 #endif
 }
-DD_HD double dd_from_bits(int64_t b) {
+DD_HD double dd_from_bits(long long b) {
 #if defined(__CUDA_ARCH__)
     return __longlong_as_double(b);
 #else
@@ -280,16 +280,16 @@ DD_HD double dd_from_bits(int64_t b) {
     return x;
 #endif
 }
-DD_HD uint32_t dd_fbits(float x) {
+DD_HD unsigned int dd_fbits(float x) {
 #if defined(__CUDA_ARCH__)
     return __float_as_uint(x);
 #else
-    uint32_t b;
+    unsigned int b;
     memcpy(&b, &x, 4);
     return b;
 #endif
 }
-DD_HD float dd_ffrom(uint32_t b) {
+DD_HD float dd_ffrom(unsigned int b) {
 #if defined(__CUDA_ARCH__)
     return __uint_as_float(b);
 #else
@@ -315,15 +315,15 @@ DD_HD double pow_ctrl_neg(double x, double y) {
     const bool fifth = y == -0.2;
     if (!(fifth || y == -0.125) || !(x >= 0x1p-800 && x <= 0x1p+800)) return pow_ctrl(x, y);
     const int q = fifth ? 5 : 8;
-    const int64_t b = dd_bits(x);
+    const long long b = dd_bits(x);
     const int ex = (int)((b >> 52) & 0x7ff) - 1023;
-    const float m = dd_ffrom(0x3f800000u | (uint32_t)((b >> 29) & 0x7fffff));  // 1.mantissa, 23 bits
+    const float m = dd_ffrom(0x3f800000u | (unsigned int)((b >> 29) & 0x7fffff));  // 1.mantissa, 23 bits
     const float lx = (float)ex + log2f(m);                                     // log2(x) in FP32
     const float tq = -lx / (float)q;
     const float kf = floorf(tq);
-    const uint32_t fb = dd_fbits(exp2f(tq - kf));                              // in [1, 2]
+    const unsigned int fb = dd_fbits(exp2f(tq - kf));                              // in [1, 2]
     const int e2 = (int)((fb >> 23) & 0xff) - 127 + (int)kf;
-    double s = dd_from_bits(((int64_t)(e2 + 1023) << 52) | ((int64_t)(fb & 0x7fffff) << 29));
+    double s = dd_from_bits(((long long)(e2 + 1023) << 52) | ((long long)(fb & 0x7fffff) << 29));
     const double q1 = (double)(q + 1), iq = fifth ? 0.2 : 0.125;
     for (int it = 0; it < 2; ++it) {
         double s2 = s * s;
@@ -340,21 +340,21 @@ DD_HD double pow_ctrl_neg(double x, double y) {
     if (!fifth) return r.hi + r.lo;
     // binary64 0.2 = (1/5)(1 + 2^-54): multiply by exp(-2^-54 ln(x) / 5) = 1 + g
     const float gf = lx * -7.6954796e-18f;  // -(2^-54 / 5) ln 2 = -7.69547959e-18
-    const uint32_t gb = dd_fbits(gf);
+    const unsigned int gb = dd_fbits(gf);
     const int ge = (int)((gb >> 23) & 0xff);
     const double g = ge == 0 ? 0.0
-                             : dd_from_bits(((int64_t)(gb >> 31) << 63) | ((int64_t)(ge + 896) << 52) |
-                                            ((int64_t)(gb & 0x7fffff) << 29));
+                             : dd_from_bits(((long long)(gb >> 31) << 63) | ((long long)(ge + 896) << 52) |
+                                            ((long long)(gb & 0x7fffff) << 29));
     double t = r.lo + r.hi * g;
     double res = r.hi + t;
     const double tail = (r.hi - res) + t;  // exact: r.hi + t - res
     // half an ulp of res, and the error bound 2^-64 res
-    const int64_t rb = dd_bits(res);
+    const long long rb = dd_bits(res);
     const int re = (int)((rb >> 52) & 0x7ff);
     // (below a power of two the spacing halves)
     const bool below_pow2 = (rb & 0xfffffffffffffll) == 0 && tail < 0.0;
-    const double half_ulp = dd_from_bits((int64_t)(re - (below_pow2 ? 54 : 53)) << 52);
-    const double bound = dd_from_bits((int64_t)(re - 67) << 52);  // > 2^-68 res
+    const double half_ulp = dd_from_bits((long long)(re - (below_pow2 ? 54 : 53)) << 52);
+    const double bound = dd_from_bits((long long)(re - 67) << 52);  // > 2^-68 res
     if (fabs(tail) + bound < half_ulp) return res;
     const double gx = -1.1102230246251566e-17 /* 2^-54 / 5 */ * log(x);
     t = r.lo + r.hi * (gx + 0.5 * gx * gx);

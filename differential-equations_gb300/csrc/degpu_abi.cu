@@ -82,6 +82,7 @@ void ensure_registered() {
         register_verner_cross8798_fast();
         register_plain();
         register_mixed_f64ctrl();
+        register_mixed_pair();
     });
 }
 
@@ -105,36 +106,37 @@ struct Scratch {
 
 static bool valid_method(int m) { return m >= DEGPU_RK4 && m <= DEGPU_RKV989E; }
 
-// The mixed-precision bound a method uses: the order-5 embedded pairs share DOPRI5's.
-static int bound_method(int m) { return m == DEGPU_DOP853 ? DEGPU_DOP853 : DEGPU_DOPRI5; }
+// Slot of the mixed-precision bound a method uses: DOPRI5, DOP853, or the other order-5 pairs.
+static int bound_slot(int m) { return m == DEGPU_DOPRI5 ? 0 : (m == DEGPU_DOP853 ? 1 : 2); }
 
-// Mixed-precision bounds of DOPRI5 [0] and DOP853 [1]: the rtol below which an instance of a
-// mixed solve runs in FP64.  Below the FP32 rounding level of the stage states the error
-// estimate has a noise floor and the step count climbs.  Measured per rtol decade on the uneven
-// Van der Pol / pendulum / Lorenz ensemble (t_end ~ U[5,50], the crate's 10 000-step cap), as
-// FP32-stage steps / FP64 steps and the share of instances ending in MaxSteps:
-//   DOPRI5  1e-8: 1.03-1.18x, none    1e-9: 1.6-3.2x, up to 39%    1e-10: 1.7-11x, 53-96%
-//   DOP853  1e-7: 1.14-1.46x, none    1e-8: 4.8-21x, up to 53%     1e-9: 10-76x, 82-100%
-// The bound is the lowest decade at which every family still finishes in the majority; there
-// the FP32-stage form is still 3.7-5x faster than FP64.  Callers that want FP64-like step counts
-// raise it (DOPRI5 1e-8, DOP853 1e-6).
-static constexpr double MIXED_MIN_RTOL_DOPRI5 = 1e-9;
-static constexpr double MIXED_MIN_RTOL_DOP853 = 1e-7;
+// Mixed-precision bounds, by slot (DOPRI5, DOP853, RKF45 / Cash-Karp): the rtol below which an
+// instance of a mixed solve leaves the FP32 stages.
+//  - DOPRI5 1e-6, and below it FP32-pair stages.  FP32 stage rounding puts a floor of about 5e-7
+//    (Van der Pol) under the error against an rtol = atol = 1e-13 solution, whatever the
+//    tolerance; measured per rtol decade on the uneven Van der Pol / pendulum / Lorenz ensemble,
+//    the FP32 stages match FP64's error at rtol >= 1e-6 (Van der Pol median 1.26e-5 against
+//    1.16e-5, pendulum 5.2e-6 against 6.0e-6) and miss it below (1e-7..1e-6: 1.7e-6 against 1.0e-6;
+//    1e-9..1e-8: 5.2e-7 against 6.1e-9).  Pair stages carry 48 bits.
+//  - DOP853 1e-7 and RKF45 / Cash-Karp 1e-9, and below them FP64.  Below the FP32 rounding level
+//    of the stage states the error estimate has a noise floor and the step count climbs
+//    (FP32-stage steps / FP64 steps, share of instances ending in MaxSteps at the crate's
+//    10 000-step cap): DOPRI5 1e-8: 1.03-1.18x, none; 1e-9: 1.6-3.2x, up to 39%; 1e-10: 1.7-11x,
+//    53-96%; DOP853 1e-7: 1.14-1.46x, none; 1e-8: 4.8-21x, up to 53%.
+static constexpr double MIXED_MIN_RTOL[3] = {1e-6, 1e-7, 1e-9};
 
-static std::atomic<double>& mixed_bound(int m) {
-    static std::atomic<double> b[2];
+static std::atomic<double>& mixed_bound(int slot) {
+    static std::atomic<double> b[3];
     static std::once_flag once;
     std::call_once(once, []() {
-        double d5 = MIXED_MIN_RTOL_DOPRI5, d8 = MIXED_MIN_RTOL_DOP853;
+        double v[3] = {MIXED_MIN_RTOL[0], MIXED_MIN_RTOL[1], MIXED_MIN_RTOL[2]};
         if (const char* e = getenv("DEGPU_MIXED_MIN_RTOL")) {
             char* end = nullptr;
-            double v = strtod(e, &end);
-            if (end != e && std::isfinite(v) && v >= 0.0) d5 = d8 = v;
+            double x = strtod(e, &end);
+            if (end != e && std::isfinite(x) && x >= 0.0) v[0] = v[1] = v[2] = x;
         }
-        b[0].store(d5);
-        b[1].store(d8);
+        for (int q = 0; q < 3; ++q) b[q].store(v[q]);
     });
-    return b[m == DEGPU_DOP853 ? 1 : 0];
+    return b[slot];
 }
 
 double mixed_split(const degpu_method_cfg* cfg) {
@@ -143,7 +145,12 @@ double mixed_split(const degpu_method_cfg* cfg) {
     // Verner's pairs: their stage sums carry coefficients up to 1.5e4 (RKV877e), whose
     // cancellation FP32 cannot resolve, so every instance of a mixed solve runs in FP64
     if (cfg->method >= DEGPU_RKV655E) return INFINITY;
-    return mixed_bound(bound_method(cfg->method)).load();
+    return mixed_bound(bound_slot(cfg->method)).load();
+}
+
+int mixed_low_precision(const degpu_method_cfg* cfg) {
+    const bool mixed = cfg->precision == DEGPU_MIXED || cfg->precision == DEGPU_MIXED_FP64_CTRL;
+    return (mixed && cfg->method == DEGPU_DOPRI5) ? PrecMixedPair::ID : DEGPU_FP64_FAST;
 }
 
 static bool valid_prec(int p) { return p >= DEGPU_FP64_PARITY && p <= DEGPU_MIXED_FP64_CTRL; }
@@ -315,7 +322,11 @@ static degpu_status solve_impl(const degpu_problem* pb, const degpu_method_cfg* 
         std::map<std::pair<int, int>, std::vector<int64_t>> by;
         for (int64_t i = 0; i < n; ++i) {
             const int fam = family_host ? family_host[i] : pb->rhs_id;
-            const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
+            int prec = cfg->precision;
+            if (split > 0.0 && rtol_host[i] < split) {
+                prec = mixed_low_precision(cfg);
+                if (!ens_registry().count(VariantKey{cfg->method, fam, prec, dense ? 1 : 0})) prec = DEGPU_FP64_FAST;
+            }
             by[{fam, prec}].push_back(i);
         }
         for (auto& kv : by) groups.push_back(WorkList{kv.first.first, kv.first.second, false, std::move(kv.second)});
@@ -710,16 +721,17 @@ void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method) {
 }
 
 degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol) {
-    if (method != DEGPU_DOPRI5 && method != DEGPU_DOP853) return DEGPU_BAD_INPUT;
+    if (method != DEGPU_DOPRI5 && method != DEGPU_DOP853 && method != DEGPU_RKF45 && method != DEGPU_CASH_KARP)
+        return DEGPU_BAD_INPUT;
     if (!std::isfinite(min_rtol) || min_rtol < 0.0) return DEGPU_BAD_INPUT;
-    mixed_bound(method).store(min_rtol);
+    mixed_bound(bound_slot(method)).store(min_rtol);
     return DEGPU_OK;
 }
 
 double degpu_mixed_min_rtol(int32_t method) {
     if (!valid_method(method) || method == DEGPU_RK4) return 0.0;
     if (method >= DEGPU_RKV655E) return INFINITY;
-    return mixed_bound(bound_method(method)).load();
+    return mixed_bound(bound_slot(method)).load();
 }
 
 degpu_status degpu_rhs_info(int32_t rhs_id, int32_t* dim, int32_t* n_params) {

@@ -1,0 +1,26 @@
+// Host build of df_math.cuh so that the pair arithmetic and its sin/cos can be tested without a
+// GPU.  Compiled with -ffp-contract=off: every fused multiply-add is an explicit fmaf, as on the
+// device.
+#include <stdint.h>
+
+#include "df_math.cuh"
+
+extern "C" {
+// sin and cos of the pairs (hi[i], lo[i])
+void degpu_host_df_sincos(const float* hi, const float* lo, double* s, double* c, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        const degpu::df x(hi[i], lo[i]);
+        s[i] = degpu::to_f64(degpu::df_sin(x));
+        c[i] = degpu::to_f64(degpu::df_cos(x));
+    }
+}
+// a * b + c on pairs, and a - b
+void degpu_host_df_ops(const float* ah, const float* al, const float* bh, const float* bl, const float* ch,
+                       const float* cl, double* fma_out, double* sub_out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        const degpu::df a(ah[i], al[i]), b(bh[i], bl[i]), c(ch[i], cl[i]);
+        fma_out[i] = degpu::to_f64(a * b + c);
+        sub_out[i] = degpu::to_f64(a - b);
+    }
+}
+}

@@ -318,7 +318,7 @@ struct Lane {
     bool last_step;  // this attempt was clamped to end at tf
     bool bounded;  // h_min / h_max differ from the defaults 0 / +inf
     double p[NPP];
-    float pf[NPP];  // mixed form: FP32 copies of p, made once per instance
+    typename P::PS pf[NPP];  // mixed form: FP32 (or FP32-pair) copies of p, made once per instance
     S y[D];
     S yc[D];  // Kahan compensation of y (mixed precision only)
     S k0[D];  // derivative at (t, y): k[0] of the next step
@@ -355,10 +355,14 @@ struct Lane {
     // Right-hand side at t + dt in the mixed form: a family with a drive phase adds Omega dt to
     // the phase at t in FP32; the others get the stage time t + dt (unused by autonomous ones).
     __device__ __forceinline__ void rhs_at(float dt, const S* yy, S* dd) const {
-        if constexpr (PHASE)
-            Rhs::template diff_phase<P>(ph0, dt, yy, dd, pf);
-        else
+        if constexpr (PHASE) {
+            if constexpr (P::PAIR)
+                Rhs::template diff_phase<P>(df(ph0, phl), dt, yy, dd, pf);  // the phase pair
+            else
+                Rhs::template diff_phase<P>(ph0, dt, yy, dd, pf);
+        } else {
             rhs(tnow() + (double)dt, yy, dd);
+        }
     }
 
     // FFT: t += hf as an FP32 pair (TwoSum, then FastTwoSum), or t = tf after a clamped last step
@@ -411,27 +415,40 @@ struct Lane {
 
     // Tolerances of component c (src/tolerance.rs:33-40): the batch's per-component value when it
     // has one (Tolerance::Vector), else the instance's scalar; FP32 copies for the mixed form.
+    // The element offset of component c of this instance, formed where it is used: the empty asm
+    // keeps the compiler from hoisting the D offsets out of the solve loop into registers, which
+    // every solve would pay for, per-component tolerances or not.
+    __device__ __forceinline__ int64_t comp_offset(int c, const EnsArgs& a) const {
+        int64_t off = (int64_t)c * a.n + inst;
+        asm volatile("" : "+l"(off));
+        return off;
+    }
     __device__ __forceinline__ double rtol_c(int c, const EnsArgs& a) const {
-        return a.rtol_vec ? a.rtol_vec[(int64_t)c * a.n + inst] : rtol;
+        return a.rtol_vec ? a.rtol_vec[comp_offset(c, a)] : rtol;
     }
     __device__ __forceinline__ double atol_c(int c, const EnsArgs& a) const {
-        return a.atol_vec ? a.atol_vec[(int64_t)c * a.n + inst] : atol;
+        return a.atol_vec ? a.atol_vec[comp_offset(c, a)] : atol;
     }
     __device__ __forceinline__ float rtolf_c(int c, const EnsArgs& a) const {
-        return a.rtol_vec ? (float)a.rtol_vec[(int64_t)c * a.n + inst] : rtolf;
+        return a.rtol_vec ? (float)a.rtol_vec[comp_offset(c, a)] : rtolf;
     }
     __device__ __forceinline__ float atolf_c(int c, const EnsArgs& a) const {
-        return a.atol_vec ? (float)a.atol_vec[(int64_t)c * a.n + inst] : atolf;
+        return a.atol_vec ? (float)a.atol_vec[comp_offset(c, a)] : atolf;
     }
 
+    // TV: the batch has per-component tolerances (a uniform branch: the scalar path keeps its
+    // registers)
+    template <bool TV>
     __device__ __forceinline__ NormT norm_term(int c, S e, S yv, S ynv, const EnsArgs& a) const {
         // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
         if constexpr (P::F32_CTRL) {
-            float sk = atolf_c(c, a) + rtolf_c(c, a) * fmaxf(fabsf(yv), fabsf(ynv));
+            const float at = TV ? atolf_c(c, a) : atolf, rt = TV ? rtolf_c(c, a) : rtolf;
+            float sk = at + rt * fmaxf(fabsf(yv), fabsf(ynv));
             float q = __fdividef(e, sk);
             return q * q;
         } else {
-            double sk = atol_c(c, a) + rtol_c(c, a) * fmax_abs((double)yv, (double)ynv);
+            const double at = TV ? atol_c(c, a) : atol, rt = TV ? rtol_c(c, a) : rtol;
+            double sk = at + rt * fmax_abs((double)yv, (double)ynv);
             double q = P::quot((double)e, sk);
             return q * q;
         }
@@ -1060,7 +1077,7 @@ struct Lane {
         for (int q = 0; q < Rhs::NP; ++q) p[q] = a.params[(int64_t)q * n + inst];
         if constexpr (PF) {
 #pragma unroll
-            for (int q = 0; q < Rhs::NP; ++q) pf[q] = (float)p[q];
+            for (int q = 0; q < Rhs::NP; ++q) pf[q] = (typename P::PS)p[q];
         }
 #pragma unroll
         for (int c = 0; c < D; ++c) {
@@ -1214,7 +1231,7 @@ struct Lane {
             hs = P::from(h);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            if constexpr (P::KAHAN) {
+            if constexpr (P::KAHAN && !P::PAIR) {  // pairs carry 48 bits: no compensation
                 S inc = hs * yseg[c];
                 S yk = inc - yc[c];
                 S ts = y[c] + yk;
@@ -1236,18 +1253,25 @@ struct Lane {
 
         NormT err = (NormT)0, err2 = (NormT)0;
         {
-            S es[D];
+            // the embedded error estimate; FP32 for pair stages (it only feeds the FP32 norm)
+            using ES = typename PickT<P::PAIR, float, S>::type;
+            ES es[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) es[c] = (S)0;
+            for (int c = 0; c < D; ++c) es[c] = (ES)0;
             static_for<0, NS>([&](auto j) {
                 constexpr double e_ = Tab::er(decltype(j)::value);
                 if constexpr (e_ != 0.0) {
 #pragma unroll
-                    for (int c = 0; c < D; ++c) es[c] = es[c] + (S)e_ * k[j][c];
+                    for (int c = 0; c < D; ++c) es[c] = es[c] + (ES)e_ * (ES)k[j][c];
                 }
             });
+            if (a.rtol_vec || a.atol_vec) {
 #pragma unroll
-            for (int c = 0; c < D; ++c) err = err + norm_term(c, es[c], y[c], ynew[c], a);
+                for (int c = 0; c < D; ++c) err = err + norm_term<true>(c, es[c], y[c], ynew[c], a);
+            } else {
+#pragma unroll
+                for (int c = 0; c < D; ++c) err = err + norm_term<false>(c, es[c], y[c], ynew[c], a);
+            }
         }
         if constexpr (Tab::HAS_BH) {
             S es[D];
@@ -1260,8 +1284,13 @@ struct Lane {
                     for (int c = 0; c < D; ++c) es[c] = es[c] + (S)(-bh_) * k[j][c];
                 }
             });
+            if (a.rtol_vec || a.atol_vec) {
 #pragma unroll
-            for (int c = 0; c < D; ++c) err2 = err2 + norm_term(c, es[c], y[c], ynew[c], a);
+                for (int c = 0; c < D; ++c) err2 = err2 + norm_term<true>(c, es[c], y[c], ynew[c], a);
+            } else {
+#pragma unroll
+                for (int c = 0; c < D; ++c) err2 = err2 + norm_term<false>(c, es[c], y[c], ynew[c], a);
+            }
         }
         NormT deno = Tab::HAS_BH ? err + (NormT)0.01 * err2 : err;
         if constexpr (P::F32_CTRL) {
@@ -1433,7 +1462,7 @@ struct Lane {
 
     __device__ __forceinline__ S stage_coef(double aij) const {
         if constexpr (MIX)
-            return (float)aij * hf;
+            return P::from(aij) * hf;  // FP32, or the pair nearest to a_ij
         else if constexpr (P::KAHAN)
             return (float)aij * (float)h;
         else
@@ -1862,7 +1891,7 @@ struct Lane {
     __device__ void finish(const EnsArgs& a) const {
         const int64_t n = a.n;
 #pragma unroll
-        for (int c = 0; c < D; ++c) a.y_final[(int64_t)c * n + inst] = (double)y[c] - (double)yc[c];
+        for (int c = 0; c < D; ++c) a.y_final[(int64_t)c * n + inst] = to_f64(y[c]) - to_f64(yc[c]);
         for (int c = D; c < a.dmax; ++c) a.y_final[(int64_t)c * n + inst] = 0.0;
         if (a.t_final) {
             if constexpr (FFT)

@@ -146,7 +146,8 @@ extern "C" degpu_status degpu_solve_ensemble_noalloc(const degpu_problem* pb, co
     const double split = mixed_split(cfg);
     MultiLaunchFn fp64_launch = nullptr;
     if (split > 0.0) {
-        auto it64 = multi_registry().find({cfg->method, DEGPU_FP64_FAST, 0});
+        auto it64 = multi_registry().find({cfg->method, mixed_low_precision(cfg), 0});
+        if (it64 == multi_registry().end()) it64 = multi_registry().find({cfg->method, DEGPU_FP64_FAST, 0});
         if (it64 == multi_registry().end()) return DEGPU_UNSUPPORTED;
         fp64_launch = it64->second;
     }

@@ -119,7 +119,9 @@ degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const in
     const double split = mixed_split(cfg);
     MultiLaunchFn fp64_launch = nullptr;
     if (split > 0.0) {
-        auto it64 = multi_registry().find({cfg->method, DEGPU_FP64_FAST, d});
+        // the tight class: FP32-pair stages where built, else FP64
+        auto it64 = multi_registry().find({cfg->method, mixed_low_precision(cfg), d});
+        if (it64 == multi_registry().end()) it64 = multi_registry().find({cfg->method, DEGPU_FP64_FAST, d});
         if (it64 == multi_registry().end()) return DEGPU_UNSUPPORTED;
         fp64_launch = it64->second;
     }
@@ -157,8 +159,12 @@ degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, 
         st = DEGPU_CUDA_ERROR;
     for (int l = NLISTS - 1; l >= 0 && st == DEGPU_OK; --l) {  // FP64 class first
         if (hc[l] == 0) continue;
-        const int prec = l >= 3 ? DEGPU_FP64_FAST : cfg->precision;
+        int prec = l >= 3 ? mixed_low_precision(cfg) : cfg->precision;
         auto it = reg.find(VariantKey{cfg->method, ids[l % 3], prec, dense ? 1 : 0});
+        if (l >= 3 && it == reg.end()) {
+            prec = DEGPU_FP64_FAST;
+            it = reg.find(VariantKey{cfg->method, ids[l % 3], prec, dense ? 1 : 0});
+        }
         if (it == reg.end()) {
             st = DEGPU_UNSUPPORTED;
             break;

@@ -215,6 +215,7 @@ void register_verner_cross6576_fast();
 void register_verner_cross8798_fast();
 void register_plain();
 void register_mixed_f64ctrl();
+void register_mixed_pair();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to
@@ -254,6 +255,11 @@ degpu_status sorted_thread_solve(const degpu_method_cfg* cfg, const EnsArgs& a, 
 // instance of a DEGPU_MIXED solve runs the DEGPU_FP64_FAST variant; 0 when cfg asks for another
 // precision or for RK4.
 double mixed_split(const degpu_method_cfg* cfg);
+
+// The arithmetic of the instances below the split of a mixed solve: FP32-pair stages
+// (PrecMixedPair) where they are built (DOPRI5), else DEGPU_FP64_FAST.  Callers fall back to
+// DEGPU_FP64_FAST when the layout they launch has no pair kernel.
+int mixed_low_precision(const degpu_method_cfg* cfg);
 
 // Argument checks shared by the ensemble entry points (degpu_abi.cu): null pointers, sizes, enum
 // ranges and the problem's dimension and parameter count -> DEGPU_BAD_INPUT.

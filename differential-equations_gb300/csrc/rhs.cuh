@@ -10,6 +10,7 @@
 #pragma once
 
 #include "dd_math.cuh"
+#include "df_math.cuh"
 #include "f32_math.cuh"
 
 namespace degpu {
@@ -90,6 +91,8 @@ __device__ __forceinline__ double rsqrt_nr(double x) {
 // translation units that instantiate it are compiled with -fmad=false).
 struct PrecParity {
     using S = double;
+    using PS = double;             // parameter copies of the mixed forms (unused here)
+    static constexpr bool PAIR = false;  // stages in FP32 pairs (PrecMixedPair)
     static constexpr int ID = 0;
     static constexpr bool KAHAN = false;
     static constexpr bool F32_CTRL = false;
@@ -105,6 +108,8 @@ struct PrecParity {
 // Fast FP64: FMA contraction and the CUDA math library.
 struct PrecFast {
     using S = double;
+    using PS = double;
+    static constexpr bool PAIR = false;
     static constexpr int ID = 1;
     static constexpr bool KAHAN = false;
     static constexpr bool F32_CTRL = false;
@@ -127,6 +132,8 @@ struct PrecPlain : PrecFast {
 // controller's power and the accept decision in FP32, t as an FP32 pair (see Lane).
 struct PrecMixed {
     using S = float;
+    using PS = float;
+    static constexpr bool PAIR = false;
     static constexpr int ID = 2;
     static constexpr bool KAHAN = true;
     static constexpr bool F32_CTRL = true;
@@ -164,6 +171,21 @@ struct PrecMixed {
 struct PrecMixedF64Ctrl : PrecMixed {
     static constexpr int ID = 4;
     static constexpr bool F32_CTRL = false;
+};
+// Mixed with FP32-pair stages (df_math.cuh, about 48 bits): the state, the stage states, the
+// right-hand sides and the stage combinations in pairs, everything else (the step size, the error
+// norm, the controller, the accept decision, t as an FP32 pair) as in PrecMixed.  A DEGPU_MIXED
+// solve runs the instances whose rtol is below the FP32 stages' bound with it: they keep FP64-like
+// accuracy, and every pair operation costs 6 to 11 FP32 instructions where an FP64 instruction
+// costs the issue time of 64.
+struct PrecMixedPair : PrecMixed {
+    using S = df;
+    using PS = df;
+    static constexpr bool PAIR = true;
+    static constexpr int ID = 5;
+    __device__ static __forceinline__ df sin(df x) { return df_sin(x); }
+    __device__ static __forceinline__ df cos(df x) { return df_cos(x); }
+    __device__ static __forceinline__ S from(double x) { return df(x); }
 };
 
 // Families -------------------------------------------------------------------------------------
@@ -213,11 +235,13 @@ struct RhsPendulum : BuiltinRhs {
         double k = rint(ph * 0.15915494309189535);
         return (float)fma(-k, 6.283185307179586, ph);
     }
-    template <class P>
-    __device__ static __forceinline__ void diff_phase(float ph0, float dt, const float* y, float* dydt,
-                                                      const float* pf) {
-        float theta = y[0], omega = y[1];
-        float r = ph0 + pf[2] * dt;
+    // PH: float, or an FP32 pair (the phase and its low part) for pair stages
+    template <class P, class PH>
+    __device__ static __forceinline__ void diff_phase(PH ph0, float dt, const typename P::S* y, typename P::S* dydt,
+                                                      const typename P::PS* pf) {
+        using S = typename P::S;
+        S theta = y[0], omega = y[1];
+        PH r = ph0 + pf[2] * dt;
         dydt[0] = omega;
         dydt[1] = -pf[0] * omega - P::sin(theta) + pf[1] * P::cos(r);
     }

@@ -355,9 +355,11 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
             r->ops = it->second;
         }
         // a mixed request whose rtol values straddle the mixed-precision bound: the instances
-        // below it run the FP64_FAST round kernels
+        // below it run the FP32-pair round kernels where built, else the FP64_FAST ones
         const double bound = mixed_split(cfg);
-        auto it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, DEGPU_FP64_FAST, 0});
+        auto it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, mixed_low_precision(cfg), 0});
+        if (it64 == round_registry().end())
+            it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, DEGPU_FP64_FAST, 0});
         if (r->resumable && bound > 0.0) {
             if (it64 == round_registry().end()) return DEGPU_UNSUPPORTED;
             for (int64_t i = 0; i < in->n; ++i) r->idx[in->rtol[i] < bound ? 1 : 0].push_back(i);

@@ -84,7 +84,10 @@ typedef enum {
  *                compensation; t as an FP32 pair (about 48 bits, FP64 when output times,
  *                crossings or events need it; RK4: t and h in FP64).
  *                Instances whose rtol is below the method's mixed-precision bound
- *                (degpu_set_mixed_min_rtol) run in FP64_FAST arithmetic instead.
+ *                (degpu_set_mixed_min_rtol) leave the FP32 stages: DOPRI5 on the Van der Pol,
+ *                pendulum and Lorenz families runs them with FP32-pair stages (about 48 bits:
+ *                the state, stage states, right-hand sides and stage sums as unevaluated sums of
+ *                two FP32 numbers, the step machinery as above), everything else in FP64_FAST.
  *  FP64_PLAIN  — FP64 with FMA contraction, IEEE division and square root, the CUDA library's
  *                sin/cos, and FP64_PARITY's correctly rounded controller power, so that every
  *                accept/reject decision follows the crate's unless contraction moves the error
@@ -205,20 +208,22 @@ typedef struct {
 void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method);
 
 /* Mixed-precision bound of an adaptive method (no counterpart in the crate, which is FP64 only).
- * FP32 stages cannot meet tolerances near their own rounding level: the embedded error estimate
- * stalls at the FP32 noise floor, the controller keeps rejecting and the instance ends in
- * MaxSteps.  So in a DEGPU_MIXED solve an instance with rtol < min_rtol runs in DEGPU_FP64_FAST
- * arithmetic; the choice depends on the instance's own rtol only, so a result does not depend on
- * the batch it is solved in.  min_rtol = 0 disables the split.  The setting is process-wide and
- * applies to solves launched after the call; the environment variable DEGPU_MIXED_MIN_RTOL, read
- * at the first solve, replaces the defaults of both methods.  RK4 (fixed step) has no bound.
- * Returns DEGPU_BAD_INPUT for RK4, an unknown method, or a negative or non-finite min_rtol. */
+ * FP32 stage rounding puts a floor under the error: about 5e-7 relative on long Van der Pol
+ * solves whatever the tolerance, and below rtol ~1e-9 the embedded error estimate stalls on the
+ * noise and the controller keeps rejecting.  So in a DEGPU_MIXED solve an instance with
+ * rtol < min_rtol leaves the FP32 stages: DOPRI5 (default bound 1e-6) runs it with FP32-pair
+ * stages, DOP853 (1e-7), RKF45 and Cash-Karp (1e-9) in DEGPU_FP64_FAST arithmetic.  The choice
+ * depends on the instance's own rtol only, so a result does not depend on the batch it is solved
+ * in.  min_rtol = 0 disables the split.  RKF45 and Cash-Karp share one setting.  The setting is
+ * process-wide and applies to solves launched after the call; the environment variable
+ * DEGPU_MIXED_MIN_RTOL, read at the first solve, replaces every default.  RK4 (fixed step) has
+ * no bound.  Returns DEGPU_BAD_INPUT for RK4, Verner's pairs, an unknown method, or a negative or
+ * non-finite min_rtol. */
 degpu_status degpu_set_mixed_min_rtol(int32_t method, double min_rtol);
 
-/* The bound in force for `method` (0 for RK4 and unknown methods).  RKF45 and Cash-Karp (order-5
- * pairs) use DOPRI5's bound.  Verner's pairs return +infinity: their stage sums carry coefficients
- * up to 1.5e4, whose cancellation FP32 cannot resolve, so a DEGPU_MIXED solve runs all their
- * instances in DEGPU_FP64_FAST arithmetic. */
+/* The bound in force for `method` (0 for RK4 and unknown methods).  Verner's pairs return
+ * +infinity: their stage sums carry coefficients up to 1.5e4, whose cancellation FP32 cannot
+ * resolve, so a DEGPU_MIXED solve runs all their instances in DEGPU_FP64_FAST arithmetic. */
 double degpu_mixed_min_rtol(int32_t method);
 
 /* Dimension and parameter count of a built-in family (dim = -1 for variable-size families).

@@ -1,0 +1,69 @@
+"""The double-float (FP32 pair) arithmetic of the mixed form's tight-tolerance stages
+(df_math.cuh), compiled for the host: products, sums and sin/cos against exact references.
+A pair carries about 48 bits; sin and cos are within 1e-11 of the correctly rounded value
+(absolute, for arguments up to 1e3), far below any tolerance the stages serve."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+
+CSRC = os.path.join(O.REPO, "differential-equations_gb300", "csrc")
+SO = os.path.join(CSRC, "libdfmath_host.so")
+FP = C.POINTER(C.c_float)
+
+
+@pytest.fixture(scope="module")
+def H():
+    src = os.path.join(CSRC, "df_math_host.cpp")
+    deps = [src, os.path.join(CSRC, "df_math.cuh")]
+    if not os.path.exists(SO) or any(os.path.getmtime(d) > os.path.getmtime(SO) for d in deps):
+        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", SO, src], check=True)
+    h = C.CDLL(SO)
+    h.degpu_host_df_sincos.argtypes = [FP, FP, O.DP, O.DP, C.c_int64]
+    h.degpu_host_df_ops.argtypes = [FP, FP, FP, FP, FP, FP, O.DP, O.DP, C.c_int64]
+    return h
+
+
+def pairs(x):
+    hi = x.astype(np.float32)
+    lo = (x - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo, hi.astype(np.float64) + lo.astype(np.float64)
+
+
+def fp(a):
+    return a.ctypes.data_as(FP)
+
+
+def test_pair_products_and_sums(H):
+    rng = np.random.default_rng(3)
+    n = 200_000
+    a, b, c = (rng.uniform(-4, 4, n) * 10.0 ** rng.integers(-3, 3, n) for _ in range(3))
+    (ah, al, av), (bh, bl, bv), (ch, cl, cv) = pairs(a), pairs(b), pairs(c)
+    f, s = np.empty(n), np.empty(n)
+    H.degpu_host_df_ops(fp(ah), fp(al), fp(bh), fp(bl), fp(ch), fp(cl), O.p(f), O.p(s), n)
+    ref_f = (np.longdouble(av) * np.longdouble(bv) + np.longdouble(cv)).astype(np.float64)
+    scale = np.abs(av * bv) + np.abs(cv)
+    assert np.max(np.abs(f - ref_f) / scale) < 2.0 ** -44
+    ref_s = av - bv
+    assert np.max(np.abs(s - ref_s) / (np.abs(av) + np.abs(bv))) < 2.0 ** -46
+
+
+@pytest.mark.parametrize("lo_,hi_", [(-4.0, 4.0), (-60.0, 60.0), (-1e3, 1e3), (-1e-3, 1e-3)])
+def test_pair_sin_cos(H, lo_, hi_):
+    rng = np.random.default_rng(4)
+    n = 100_000
+    x = rng.uniform(lo_, hi_, n)
+    xh, xl, xv = pairs(x)
+    s, c = np.empty(n), np.empty(n)
+    H.degpu_host_df_sincos(fp(xh), fp(xl), O.p(s), O.p(c), n)
+    rs, rc = np.empty(n), np.empty(n)
+    O.lib().oracle_cr_sincos_batch(O.p(xv), O.p(rs), O.p(rc), n)
+    assert np.max(np.abs(s - rs)) < 1e-11
+    assert np.max(np.abs(c - rc)) < 1e-11
+    small = np.abs(xv) < 1e-2  # near zero sin keeps its relative accuracy
+    if small.any():
+        assert np.max(np.abs(s[small] - rs[small]) / np.abs(rs[small])) < 1e-12

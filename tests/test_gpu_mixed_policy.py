@@ -1,7 +1,9 @@
 """Mixed-precision bound (degpu_set_mixed_min_rtol): in a MIXED solve, instances with rtol below
-the bound run the FP64_FAST arithmetic and the others the FP32-stage form.  Each instance's result
-must equal, bit for bit, the same instance solved by the arithmetic its rtol selects, on every
-kernel layout (persistent multi-family, one system per thread, group per system)."""
+the bound leave the FP32 stages (DOPRI5: FP32-pair stages; DOP853: the FP64_FAST arithmetic) and
+the others run the FP32-stage form.  Each instance's result must equal, bit for bit, the same
+instance solved by the arithmetic its rtol selects, on every kernel layout (persistent
+multi-family, one system per thread, group per system).  The pair stages keep FP64-like accuracy
+where the FP32 stages cannot."""
 import numpy as np
 import pytest
 
@@ -51,14 +53,18 @@ def test_split_matches_the_selected_arithmetic(bound, method, kernel):
     assert 0 < tight.sum() < e.n
     degpu.set_mixed_min_rtol(method, BOUND)
     split = run(e, method, abi.MIXED, kernel)
-    fast = run(e, method, abi.FP64_FAST, kernel)
+    if method == abi.DOPRI5:
+        degpu.set_mixed_min_rtol(method, 1.0)  # every instance below the bound: pair stages
+        low = run(e, method, abi.MIXED, kernel)
+    else:
+        low = run(e, method, abi.FP64_FAST, kernel)
     degpu.set_mixed_min_rtol(method, 0.0)
     mixed = run(e, method, abi.MIXED, kernel)
-    same(split, fast, tight)
+    same(split, low, tight)
     same(split, mixed, ~tight)
     # the FP32-stage form below the bound is what the split avoids: it needs more steps there
     steps = lambda r: (r.accepted + r.rejected)[tight].mean()
-    assert steps(mixed) > steps(fast)
+    assert steps(mixed) > steps(low)
 
 
 def test_split_on_ragged_group_kernel(bound):
@@ -109,3 +115,30 @@ def test_mixed_time_pair_ends_at_tf_and_tracks_fp64(method, kernel):
         errs.append(np.median(rel))
     assert errs[0] < 1e-4 and errs[1] < 1e-4
     assert errs[1] < 10 * errs[0] + 1e-6
+
+
+@pytest.mark.parametrize("kernel", [abi.KERNEL_PERSISTENT, abi.KERNEL_THREAD])
+def test_pair_stages_track_fp64(bound, kernel):
+    """DOPRI5's FP32-pair stages (the tight class of a mixed solve) against FP64 at the same
+    tolerances on the non-chaotic families (Van der Pol, the damped driven pendulum), over the
+    ensemble's full horizons: the FP32 stages' error floor (about 5e-7) is gone."""
+    e = W.config1(n=3 * 1500, first=20_000)
+    keep = e.family != abi.RHS["LORENZ"]
+    e = e.subset(np.nonzero(keep)[0])
+    e.rtol = W.logU(9, np.arange(e.n), 1, 1e-10, 1e-7)
+    e.atol = 1e-2 * e.rtol
+    degpu.set_mixed_min_rtol(abi.DOPRI5, 1.0)
+    pair = run(e, abi.DOPRI5, abi.MIXED, kernel)
+    degpu.set_mixed_min_rtol(abi.DOPRI5, 0.0)
+    f32 = run(e, abi.DOPRI5, abi.MIXED, kernel)
+    fast = run(e, abi.DOPRI5, abi.FP64_FAST, kernel)
+    ok = (pair.status == abi.COMPLETE) & (fast.status == abi.COMPLETE)
+    assert ok.mean() > 0.999
+    rel = lambda r: np.max(np.abs(r.y_final[:, ok] - fast.y_final[:, ok]), axis=0) / \
+        np.maximum(np.max(np.abs(fast.y_final[:, ok]), axis=0), 1e-300)
+    # the pair stages follow FP64 to the rounding-driven spread of the step sequence
+    assert np.median(rel(pair)) < 1e-9
+    assert np.median(rel(pair)) < 0.05 * np.median(rel(f32))
+    # the step counts of FP64
+    steps = lambda r: (r.accepted + r.rejected)[ok].astype(float)
+    assert abs(steps(pair).mean() / steps(fast).mean() - 1.0) < 0.01

@@ -36,11 +36,11 @@ def requests():
         dim = 3 if fam == abi.RHS["LORENZ"] else 2
         reqs.append(dict(rhs=fam, dim=dim, e=e, m=method(m, prec, 1e-3 if m == abi.RK4 else 0.0)))
     # a mixed request whose rtol values straddle the mixed-precision bound: its instances run in
-    # two round kernels (FP32 stages above the bound, FP64 below)
+    # two round kernels (FP32 stages above the bound, FP32-pair stages below)
     e = W.config1(n=1500, first=123_000)
     e = e.subset(np.nonzero(e.family == abi.RHS["VAN_DER_POL"])[0])
     e.tf = np.minimum(e.tf, 6.0)
-    e.rtol = W.logU(9, np.arange(e.n), 1, 1e-11, 1e-7)
+    e.rtol = W.logU(9, np.arange(e.n), 1, 1e-9, 1e-5)
     e.atol = 1e-2 * e.rtol
     assert 0 < (e.rtol < degpu.mixed_min_rtol(abi.DOPRI5)).sum() < e.n
     reqs.append(dict(rhs=abi.RHS["VAN_DER_POL"], dim=2, e=e, m=method(abi.DOPRI5, abi.MIXED)))
