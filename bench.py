@@ -737,100 +737,168 @@ def run_gray_scott(args, torch, dev, lib, emit=True):
     return line
 
 
-def serving_requests(count, seed_base=7_000_000):
-    """Requests of the serving configuration, from the seed: ensemble size ~ int logU[1,65536],
+def serving_specs(count):
+    """The serving configuration's requests, from the seed: ensemble size ~ int logU[1,65536],
     family uniform over {Van der Pol, pendulum, Lorenz, FPU-beta chain with <= 64 masses},
-    method uniform over {RK4 h=1e-3, DOPRI5, DOP853} (DOPRI5/DOP853 for chains),
-    rtol ~ logU[1e-10,1e-5], atol = 1e-2 rtol.  Horizons are t_end ~ U[1,10] (shorter than the
-    ensemble benchmark's so that a sweep of arrival rates fits in minutes)."""
+    method uniform over {RK4 h=1e-3, DOPRI5, DOP853} (DOPRI5 / DOP853 / DOP853 for chains),
+    rtol ~ logU[1e-10,1e-5] per request, atol = 1e-2 rtol; horizons per instance t_end ~ U[5,50]
+    as in the uneven ensemble."""
     r = np.arange(count)
     size = np.floor(np.exp(W.U(4, r, 0, 0.0, math.log(65537.0)))).astype(np.int64).clip(1, 65536)
     fam = np.floor(W.U(4, r, 1, 0.0, 4.0)).astype(int).clip(0, 3)
     meth = np.floor(W.U(4, r, 2, 0.0, 3.0)).astype(int).clip(0, 2)
     rtol = W.logU(4, r, 3, 1e-10, 1e-5)
-    reqs = []
-    for k in range(count):
-        n = int(size[k])
-        if fam[k] < 3:
-            fid = W.FAMILIES_C1[fam[k]]
-            base = W.config1(n=3 * n, first=seed_base + 3 * 65536 * k)
-            e = base.subset(np.nonzero(base.family == fid)[0][:n])
-            e.rhs_id = fid
-            e.family = None
-            e.dim = 3 if fid == abi.RHS["LORENZ"] else 2
-            e.y0 = np.ascontiguousarray(e.y0[:e.dim])
-            m = [abi.RK4, abi.DOPRI5, abi.DOP853][meth[k]]
-        else:
-            e = W.config2(n=n, first=seed_base + 65536 * k)
-            masses = np.minimum(e.dims // 2, 64)
-            e.dims = (2 * masses).astype(np.int32)
-            e.dim = 128
-            y = np.zeros((128, n))
-            rows = min(128, e.y0.shape[0])
-            mask = np.arange(rows)[:, None] < masses[None, :]
-            y[:rows] = np.where(mask, e.y0[:rows], 0.0)
-            e.y0 = y
-            e.t_eval = None
-            m = [abi.DOPRI5, abi.DOP853, abi.DOP853][meth[k]]
-        e.n = len(e.t0)
-        e.tf = W.U(4, np.arange(e.n) + 1000 * k, 5, 1.0, 10.0)
-        e.rtol = np.full(e.n, rtol[k])
-        e.atol = 1e-2 * e.rtol
-        reqs.append((e, m))
-    return reqs
+    return size, fam, meth, rtol
+
+
+def serving_request(k, size, fam, meth, rtol, seed_base=7_000_000):
+    """Request k of the serving configuration: (Ensemble, method)."""
+    n = int(size[k])
+    first = seed_base + 3 * 65536 * k
+    if fam[k] < 3:
+        e = W.config1_family(int(fam[k]), n, first=first)
+        m = [abi.RK4, abi.DOPRI5, abi.DOP853][meth[k]]
+    else:
+        e = W.config2(n=n, first=first, max_masses=64)
+        e.t_eval = None
+        m = [abi.DOPRI5, abi.DOP853, abi.DOP853][meth[k]]
+    e.tf = W.U(4, np.arange(first, first + n), 5, 5.0, 50.0)
+    e.rtol = np.full(n, rtol[k])
+    e.atol = 1e-2 * e.rtol
+    return e, m
 
 
 def run_serving(args, torch, dev, lib):
-    """Continuous-batching server under Poisson arrivals: saturated capacity first, then a sweep of
-    arrival rates (fractions of capacity); p50/p99 latency and solves/s, mixed vs FP64."""
+    """Continuous-batching server under Poisson arrivals on the serving configuration
+    (--requests, 10,000 by default): the saturated capacity first (every request queued at once,
+    at most 512 outstanding), then arrival rates as fractions of it until p99 saturates; p50/p99
+    latency and solves/s, mixed vs FP64 (fast); error of the mixed results against the FP64 oracle
+    at the same tolerances on a sample of requests."""
+    import queue
     import degpu
     from degpu.serving import Server
 
-    reqs = serving_requests(args.requests)
-    total_inst = sum(e.n for e, _ in reqs)
+    size, fam, meth, rtol = serving_specs(args.requests)
+    total_inst = int(size.sum())
+    # host memory of the pre-generated requests (the chains' states are padded to 128 rows):
+    # generate them once if they fit three times over in the available memory, else per request
+    est = int(np.sum(np.where(fam == 3, 128 + 8, 10) * size * 8))
+    avail = 0
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable:"):
+                avail = int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    t = time.perf_counter()
+    if avail > 3 * est:
+        cache = [serving_request(k, size, fam, meth, rtol) for k in range(args.requests)]
+        reqs = cache.__getitem__
+    else:
+        reqs = lambda k: serving_request(k, size, fam, meth, rtol)
+    gen_s = time.perf_counter() - t
+    sample = set(range(0, args.requests, max(1, args.requests // 24)))
     out = {}
-    for prec_name, prec in (("mixed", abi.MIXED), ("fp64", abi.FP64_PARITY)):
-        def run(rate):
-            srv = Server(memory_budget_gb=150.0, max_active=64, round_budget=512)
-            rng = np.random.default_rng(11)
-            gaps = rng.exponential(1.0 / rate, len(reqs)) if rate > 0 else np.zeros(len(reqs))
-            ids = []
-            t0 = time.perf_counter()
-            next_t = t0
-            for (e, m), g in zip(reqs, gaps):
-                next_t += g
-                while time.perf_counter() < next_t:
-                    time.sleep(min(0.0005, max(0.0, next_t - time.perf_counter())))
-                meth = degpu.ExplicitRungeKutta(m, h0=1e-3 if m == abi.RK4 else 0.0)
-                meth.cfg.precision, meth.cfg.max_steps = prec, 10_000_000
-                ids.append(srv.submit(e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, meth,
-                                      dims=e.dims))
-            lats = [srv.wait(i)[1] for i in ids]
-            wall = time.perf_counter() - t0
-            srv.close()
-            lats = np.array(lats)
-            return {"rate_req_per_s": rate, "p50_ms": float(np.percentile(lats, 50)),
-                    "p99_ms": float(np.percentile(lats, 99)), "solves_per_s": total_inst / wall,
-                    "requests_per_s": len(reqs) / wall}
 
-        sat = run(0.0)
+    def run(prec, rate, keep=False):
+        srv = Server(memory_budget_gb=150.0, max_active=64, round_budget=512)
+        rng = np.random.default_rng(11)
+        gaps = rng.exponential(1.0 / rate, args.requests) if rate > 0 else np.zeros(args.requests)
+        ids = queue.Queue()
+        lats, kept = [], {}
+        slots = threading.Semaphore(512)
+
+        def waiter():
+            while True:
+                item = ids.get()
+                if item is None:
+                    return
+                k, rid = item
+                res, lat = srv.wait(rid)
+                lats.append(lat)
+                if keep and k in sample:
+                    kept[k] = res
+                slots.release()
+
+        th = threading.Thread(target=waiter, daemon=True)
+        th.start()
+        t0 = time.perf_counter()
+        next_t = t0
+        for k, g in enumerate(gaps):
+            e, m = reqs(k)
+            next_t += g
+            while time.perf_counter() < next_t:
+                time.sleep(min(0.0005, max(0.0, next_t - time.perf_counter())))
+            slots.acquire()
+            meth_ = degpu.ExplicitRungeKutta(m, h0=1e-3 if m == abi.RK4 else 0.0)
+            meth_.cfg.precision, meth_.cfg.max_steps = prec, 10_000_000
+            ids.put((k, srv.submit(e.rhs_id, e.dim, e.t0, e.tf, e.y0, e.params, e.rtol, e.atol, meth_,
+                                   dims=e.dims)))
+        ids.put(None)
+        th.join()
+        wall = time.perf_counter() - t0
+        srv.close()
+        lats = np.array(lats)
+        r = {"rate_req_per_s": rate, "p50_ms": float(np.percentile(lats, 50)),
+             "p99_ms": float(np.percentile(lats, 99)), "solves_per_s": total_inst / wall,
+             "requests_per_s": args.requests / wall, "wall_s": wall}
+        print(json.dumps({"serving_run": prec, **r}), flush=True)
+        return r, kept
+
+    for prec_name, prec, fracs in (("mixed", abi.MIXED, args.serving_fracs_mixed),
+                                   ("fp64", abi.FP64_FAST, args.serving_fracs_fp64)):
+        sat, kept = run(prec, 0.0, keep=prec == abi.MIXED)
         cap = sat["requests_per_s"]
-        fracs = (0.25, 0.5, 0.75, 0.9) if prec == abi.MIXED else (0.5, 0.9)
-        sweep = [run(f * cap) for f in fracs]
-        # highest swept rate whose p99 stays within 3x the lightest load's p99
-        ok = [s for s in sweep if s["p99_ms"] <= 3.0 * sweep[0]["p99_ms"]]
-        out[prec_name] = {"saturated": sat, "sweep": sweep, "sustainable": ok[-1] if ok else sweep[0]}
+        sweep = []
+        for f in [float(x) for x in fracs.split(",") if x]:
+            sweep.append(run(prec, f * cap)[0])
+            if sweep[-1]["p99_ms"] > 3.0 * sweep[0]["p99_ms"]:
+                break  # p99 has saturated
+        ok = [s for s in sweep if s["p99_ms"] <= 3.0 * sweep[0]["p99_ms"]] if sweep else []
+        out[prec_name] = {"saturated": sat, "sweep": sweep, "sustainable": ok[-1] if ok else sat}
+        if prec == abi.MIXED:
+            out["mixed"]["error_vs_fp64_oracle"] = serving_accuracy(reqs, kept)
     line = {"metric": "serving p50/p99 latency and solves/s (continuous batching)",
             "value": out["mixed"]["sustainable"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
-            "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 beside)",
+            "higher_is_better": True, "dtype": "f32/f64 mixed (fp64 fast beside)",
             "data": "synthetic (seeded SplitMix64)",
-            "config": {"workload": f"{len(reqs)} requests, size int-logU[1,65536] ({total_inst} instances), "
+            "config": {"workload": f"{args.requests} requests, size int-logU[1,65536] ({total_inst} instances), "
                                    f"VdP/pendulum/Lorenz/FPU(<=64 masses), RK4 h=1e-3 / DOPRI5 / DOP853, "
-                                   f"rtol logU[1e-10,1e-5], t_end U[1,10], 150 GB budget",
+                                   f"rtol logU[1e-10,1e-5], t_end U[5,50], 150 GB budget, Poisson arrivals",
                        "mixed_min_rtol": {"dopri5": lib.degpu_mixed_min_rtol(abi.DOPRI5),
-                                          "dop853": lib.degpu_mixed_min_rtol(abi.DOP853)}},
+                                          "dop853": lib.degpu_mixed_min_rtol(abi.DOP853)},
+                       "generation_s": gen_s, "host_bytes_requests": est, "host_bytes_available": avail},
             "results": out}
     print(json.dumps(line))
+
+
+def serving_accuracy(reqs, kept, per_request=32):
+    """Median relative final-state error of kept mixed results against the FP64 oracle at the same
+    tolerances (host libm), on up to `per_request` instances of each kept request, by kind."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib as O
+
+    errs = {}
+    for k, res in kept.items():
+        e, m = reqs(k)
+        idx = np.arange(min(e.n, per_request))
+        s = e.subset(idx)
+        s.dim = e.dim
+        b = O.Batch(s.rhs_id, s.dim, s.n_params, s.t0, s.tf, s.y0, s.params, s.rtol, s.atol, dims=s.dims)
+        cfg = abi.default_cfg(m)
+        cfg.max_steps = 10_000_000
+        cfg.h0 = 1e-3 if m == abi.RK4 else 0.0
+        o = O.solve(b, cfg, math_mode=0)
+        ok = (o["status"] == abi.COMPLETE) & (res.status[idx] == abi.COMPLETE)
+        if not ok.any():
+            continue
+        yo, yg = o["y_final"][:, ok], res.y_final[:, idx][:, ok]
+        rel = np.max(np.abs(yg - yo), axis=0) / np.maximum(np.max(np.abs(yo), axis=0), 1e-300)
+        kind = ("lorenz" if s.rhs_id == abi.RHS["LORENZ"] else "fpu" if s.rhs_id == abi.RHS["FPU_BETA"]
+                else "vdp_pendulum")
+        errs.setdefault(kind, []).extend(rel.tolist())
+    return {k: {"median": float(np.median(v)), "p90": float(np.percentile(v, 90)), "instances": len(v)}
+            for k, v in errs.items()}
 
 
 def run_profile_case(args):
@@ -910,7 +978,10 @@ def main():
     ap.add_argument("--fpu-mixed-max-steps", type=int, default=200_000)
     ap.add_argument("--gs-n", type=int, default=4096)
     ap.add_argument("--gs-steps", type=int, default=1000)
-    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--requests", type=int, default=10000)
+    ap.add_argument("--serving-fracs-mixed", default="0.25,0.5,0.75,0.9,1.0",
+                    help="arrival rates of the serving sweep as fractions of the saturated capacity")
+    ap.add_argument("--serving-fracs-fp64", default="0.5,0.9")
     ap.add_argument("--profile-family", default="", choices=["", "VAN_DER_POL", "PENDULUM", "LORENZ"],
                     help="with --profile-case: keep only this family's instances")
     ap.add_argument("--profile-case", type=int, default=0,

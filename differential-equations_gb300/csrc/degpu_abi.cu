@@ -83,6 +83,8 @@ void ensure_registered() {
         register_plain();
         register_mixed_f64ctrl();
         register_mixed_pair();
+        register_round_dense_parity();
+        register_round_dense_fast_mixed();
     });
 }
 

@@ -12,9 +12,7 @@
 // Muller and Popescu ("Tight and rigorous error bounds for basic building blocks of
 // double-word arithmetic", ACM TOMS 2017).  Additions are the "sloppy" form: its error is below
 // 2^-46 of the larger operand, which is what an ODE stage needs (the state's magnitude sets the
-// scale).  sin and cos reduce by multiples of pi/2 (split in three FP32 parts, the products
-// formed exactly), then evaluate the Taylor series with the leading terms in pairs and the tail
-// in FP32 (relative error about 1e-11 on the reduced range).
+// scale).  sin and cos are table-driven (see df_sin below).
 #pragma once
 
 #if !defined(__CUDACC_RTC__)
@@ -24,13 +22,34 @@
 
 #if defined(__CUDACC__)
 #define DF_HD __host__ __device__ __forceinline__
+#define DF_DEV __device__ __forceinline__
 #define DF_CTOR __host__ __device__ constexpr
 #else
 #define DF_HD static inline
+#define DF_DEV static inline
 #define DF_CTOR constexpr
 #endif
 
+#include "df_tables.inc"
+
+// A product that the compiler must not fuse into a following addition: the error-free
+// transformations below rely on the rounded product, and every build (ahead of time or at run
+// time) then evaluates a pair expression identically.
+#if defined(__CUDA_ARCH__)
+#define DF_MUL(a, b) __fmul_rn((a), (b))
+#else
+#define DF_MUL(a, b) ((a) * (b))
+#endif
+
 namespace degpu {
+
+// sin and cos of j pi/64, j = 0..127, as pairs: one 16-byte row per j (sin hi, sin lo, cos hi,
+// cos lo), read through the read-only data cache
+#if defined(__CUDACC__)
+static __device__ __align__(16) const float kDfTrigTab[128][4] = {DF_TRIG_TAB_ROWS};
+#else
+alignas(16) static const float kDfTrigTab[128][4] = {DF_TRIG_TAB_ROWS};
+#endif
 
 struct df {
     float hi, lo;
@@ -68,14 +87,14 @@ DF_HD df operator-(df a, df b) { return a + (-b); }
 DF_HD df operator-(df a, float b) { return a + (-b); }
 DF_HD df operator-(float a, df b) { return (-b) + a; }
 DF_HD df operator*(df a, df b) {
-    const float p = a.hi * b.hi;
+    const float p = DF_MUL(a.hi, b.hi);
     float e = fmaf(a.hi, b.hi, -p);
     e = fmaf(a.hi, b.lo, e);
     e = fmaf(a.lo, b.hi, e);
     return df_fast_two_sum(p, e);
 }
 DF_HD df operator*(df a, float b) {
-    const float p = a.hi * b;
+    const float p = DF_MUL(a.hi, b);
     float e = fmaf(a.hi, b, -p);
     e = fmaf(a.lo, b, e);
     return df_fast_two_sum(p, e);
@@ -83,66 +102,136 @@ DF_HD df operator*(df a, float b) {
 DF_HD df operator*(float a, df b) { return b * a; }
 DF_HD df& operator+=(df& a, df b) { return a = a + b; }
 
+// Stage sums y + sum_j a_j k_j.  For pairs the sum is kept unnormalised: each product is formed
+// as a pair (TwoProduct plus the cross terms), its leading part is added to the running leading
+// part with TwoSum, and every low-order part goes into the running low part; one FastTwoSum
+// normalises at the end.  12 FP32 instructions per term instead of 18 for a pair product followed
+// by a pair addition, with the same error bound (a few units of 2^-48 of the largest term).  For
+// FP32 and FP64 the accumulator is the number itself and a term is `s + a * b`, the expression
+// the stage sums have always used.
+struct dfacc {
+    float hi, lo;
+};
+template <class S>
+struct AccOf {
+    using type = S;
+};
+template <>
+struct AccOf<df> {
+    using type = dfacc;
+};
+DF_HD float acc_begin(float y) { return y; }
+DF_HD double acc_begin(double y) { return y; }
+DF_HD dfacc acc_begin(df y) { return dfacc{y.hi, y.lo}; }
+DF_HD void acc_fma(float& s, float a, float b) { s = s + a * b; }
+DF_HD void acc_fma(double& s, double a, double b) { s = s + a * b; }
+DF_HD void acc_add_pair(dfacc& s, float p, float e) {
+    const float t = s.hi + p;
+    const float bb = t - s.hi;
+    const float err = (s.hi - (t - bb)) + (p - bb);
+    s.hi = t;
+    s.lo = s.lo + (e + err);
+}
+DF_HD void acc_fma(dfacc& s, df a, df b) {
+    const float p = DF_MUL(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    acc_add_pair(s, p, e);
+}
+DF_HD void acc_fma(dfacc& s, df a, float b) {
+    const float p = DF_MUL(a.hi, b);
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    acc_add_pair(s, p, e);
+}
+DF_HD float acc_end(float s) { return s; }
+DF_HD double acc_end(double s) { return s; }
+DF_HD df acc_end(dfacc s) { return df_fast_two_sum(s.hi, s.lo); }
+
 // The value of a pair as a double (exact: the sum of two FP32 numbers fits in 53 bits)
 DF_HD double to_f64(df x) { return (double)x.hi + (double)x.lo; }
 DF_HD double to_f64(float x) { return (double)x; }
 DF_HD double to_f64(double x) { return x; }
 
-// sin and cos of a pair.  x = k pi/2 + r with |r| <= pi/4; pi/2 = C1 + C2 + C3 (FP32 parts).
-DF_HD df df_reduce_pio2(df x, float& kq) {
-    const float C1 = 0x1.921fb6p+0f, C2 = -0x1.777a5cp-25f, C3 = -0x1.ee59dap-50f;
-    const float k = rintf(x.hi * 0x1.45f306p-1f);  // x / (pi/2)
-    kq = k;
-    // x - k C1 - k C2 - k C3, each product exact as a pair (TwoProduct)
-    const float p1 = k * C1, e1 = fmaf(k, C1, -p1);
-    df r = df_two_sum(x.hi, -p1);          // cancels most of x.hi
-    r = r + (x.lo - e1);
-    const float p2 = k * C2, e2 = fmaf(k, C2, -p2);
-    r = r - df(p2, e2);
-    r = r - k * C3;
-    return r;
+// sin and cos of a pair, table-driven (the method of Tang's table-driven elementary functions,
+// ACM TOMS 1989-1992): x = j pi/64 + d with |d| <= about pi/128, then
+//     sin x = S cos d + C sin d,   cos x = C cos d - S sin d,
+// S, C = sin, cos(j pi/64) from a 128-row table of pairs, and the Taylor series of the small d:
+//     cos d = 1 - h + h q,  h = d^2/2 (a pair), q = d^2/12 - d^4/360 (FP32, |q| < 5.1e-5)
+//     sin d = d + s,        s = -d^3/6 + d^5/120 (FP32, |s| < 2.5e-6)
+// The neglected terms are below 4e-16.  The sums run through the stage-sum accumulator, so a
+// call costs about 60 FP32 instructions and one 16-byte table load.  Absolute error about 1e-12
+// (the FP32 parts s and h q), plus 2^-47 |x| from the reduction's FP32 tail.
+DF_DEV df df_reduce_pio64(df x, int& j) {
+    const float kf = rintf(x.hi * DF_64_OVER_PI);
+    j = (int)kf & 127;  // the table row of kf mod 128 (two's complement for kf < 0)
+    const float p1 = DF_MUL(kf, DF_PIO64_1), e1 = fmaf(kf, DF_PIO64_1, -p1);
+    const float p2 = DF_MUL(kf, DF_PIO64_2), e2 = fmaf(kf, DF_PIO64_2, -p2);
+    const df r = df_two_sum(x.hi, -p1);  // exact
+    // the parts below ulp(x.hi): x.lo, the low part of kf C1, kf C2 and kf C3
+    const float b = (((r.lo + x.lo) - e1) - p2) - fmaf(kf, DF_PIO64_3, e2);
+    return df_fast_two_sum(r.hi, b);
 }
 
-// sin r and cos r for |r| <= pi/4 (z = r^2): the terms through r^7 (r^6) in pairs, the tail in FP32
-DF_HD df df_sin_poly(df r, df z) {
-    const float zf = z.hi;
-    float t = fmaf(zf, 0x1.952c78p-49f, -0x1.ae7f3ep-41f);  //  1/17!, -1/15!
-    t = fmaf(t, zf, 0x1.612462p-33f);                       //  1/13!
-    t = fmaf(t, zf, -0x1.ae6456p-26f);                      // -1/11!
-    t = fmaf(t, zf, 0x1.71de3ap-19f);                       //  1/9!
-    // -1/7! + z t, 1/5! + z (..), -1/3! + z (..) in pairs
-    df s = z * t + df(-0x1.a01a02p-13f, 0x1.7f97fap-39f);   // -1/5040
-    s = z * s + df(0x1.111112p-7f, -0x1.dddddep-32f);       //  1/120
-    s = z * s + df(-0x1.555556p-3f, 0x1.555556p-28f);       // -1/6
-    return r + (r * z) * s;
+DF_DEV void df_trig_row(int j, df& S, df& C) {
+#if defined(__CUDACC__)
+    const float4 row = __ldg(reinterpret_cast<const float4*>(&kDfTrigTab[j][0]));
+    S = df(row.x, row.y);
+    C = df(row.z, row.w);
+#else
+    S = df(kDfTrigTab[j][0], kDfTrigTab[j][1]);
+    C = df(kDfTrigTab[j][2], kDfTrigTab[j][3]);
+#endif
 }
-DF_HD df df_cos_poly(df z) {
-    const float zf = z.hi;
-    float t = fmaf(zf, -0x1.682786p-53f, 0x1.ae7f3ep-45f);  // -1/18!, 1/16!
-    t = fmaf(t, zf, -0x1.93974ap-37f);                      // -1/14!
-    t = fmaf(t, zf, 0x1.1eed8ep-29f);                       //  1/12!
-    t = fmaf(t, zf, -0x1.27e4fcp-22f);                      // -1/10!
-    df s = z * t + df(0x1.a01a02p-16f, -0x1.7f97fap-42f);   //  1/40320
-    s = z * s + df(-0x1.6c16c2p-10f, 0x1.27d27ep-35f);      // -1/720
-    s = z * s + df(0x1.555556p-5f, -0x1.555556p-30f);       //  1/24
-    s = z * s + df(-0.5f);
-    return z * s + df(1.0f);
+
+// d^2/2 as a pair (hh, hl), h q and s of the series above.  s is formed from d^3 to about
+// 2^-40 (its leading product exact, the low parts of d and d^2 folded in) and 1/6 as a pair, so
+// that its one final rounding is its only sizeable error.
+DF_DEV void df_small_series(df d, float& hh, float& hl, float& hq, float& s) {
+    const float p = DF_MUL(d.hi, d.hi);
+    float e = fmaf(d.hi, d.hi, -p);
+    e = fmaf(2.0f * d.hi, d.lo, e);  // d^2 = p + e
+    hh = 0.5f * p;
+    hl = 0.5f * e;
+    hq = hh * (p * fmaf(p, -1.0f / 360.0f, 1.0f / 12.0f));
+    const float t = DF_MUL(d.hi, p);
+    float tl = fmaf(d.hi, p, -t);
+    tl = fmaf(d.hi, e, tl);
+    tl = fmaf(p, d.lo, tl);  // d^3 = t + tl (d.hi e already carries 2 d.hi^2 d.lo of the 3)
+    const float C6H = 0x1.555556p-3f, C6L = -0x1.555556p-28f;  // 1/6 = C6H + C6L
+    const float inner = fmaf(t, C6L, tl * C6H);
+    s = fmaf(t, -C6H, -inner);                    // -d^3/6
+    s = fmaf(t * p, 1.0f / 120.0f, s);            // + d^5/120
 }
-DF_HD df df_sin(df x) {
-    float k;
-    const df r = df_reduce_pio2(x, k);
-    const df z = r * r;
-    const int q = (int)k & 3;
-    df v = (q & 1) ? df_cos_poly(z) : df_sin_poly(r, z);
-    return (q & 2) ? -v : v;
+
+DF_DEV df df_sin(df x) {
+    int j;
+    const df d = df_reduce_pio64(x, j);
+    df S, C;
+    df_trig_row(j, S, C);
+    float hh, hl, hq, s;
+    df_small_series(d, hh, hl, hq, s);
+    dfacc a = acc_begin(S);
+    acc_fma(a, C, d);
+    acc_fma(a, -S, df(hh, hl));
+    a.lo = fmaf(S.hi, hq, a.lo);
+    a.lo = fmaf(C.hi, s, a.lo);
+    return acc_end(a);
 }
-DF_HD df df_cos(df x) {
-    float k;
-    const df r = df_reduce_pio2(x, k);
-    const df z = r * r;
-    const int q = (int)k & 3;
-    df v = (q & 1) ? df_sin_poly(r, z) : df_cos_poly(z);
-    return (q == 1 || q == 2) ? -v : v;
+DF_DEV df df_cos(df x) {
+    int j;
+    const df d = df_reduce_pio64(x, j);
+    df S, C;
+    df_trig_row(j, S, C);
+    float hh, hl, hq, s;
+    df_small_series(d, hh, hl, hq, s);
+    dfacc a = acc_begin(C);
+    acc_fma(a, -S, d);
+    acc_fma(a, -C, df(hh, hl));
+    a.lo = fmaf(C.hi, hq, a.lo);
+    a.lo = fmaf(-S.hi, s, a.lo);
+    return acc_end(a);
 }
 
 }  // namespace degpu

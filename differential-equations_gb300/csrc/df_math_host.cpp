@@ -23,4 +23,20 @@ void degpu_host_df_ops(const float* ah, const float* al, const float* bh, const 
         sub_out[i] = degpu::to_f64(a - b);
     }
 }
+// y + sum_j a_j k_j over m terms through the lazily normalised accumulator (the stage sums);
+// a, k: [m][n], the last term's factor is FP32 (the step size) when last_f32 is set
+void degpu_host_df_stage_sum(const float* yh, const float* yl, const float* ah, const float* al, const float* kh,
+                             const float* kl, int32_t m, int32_t last_f32, double* out, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        degpu::dfacc s = degpu::acc_begin(degpu::df(yh[i], yl[i]));
+        for (int32_t j = 0; j < m; ++j) {
+            const degpu::df k(kh[j * n + i], kl[j * n + i]);
+            if (last_f32 && j == m - 1)
+                degpu::acc_fma(s, k, ah[j * n + i]);
+            else
+                degpu::acc_fma(s, degpu::df(ah[j * n + i], al[j * n + i]), k);
+        }
+        out[i] = degpu::to_f64(degpu::acc_end(s));
+    }
+}
 }

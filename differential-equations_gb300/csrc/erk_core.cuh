@@ -284,6 +284,7 @@ struct Lane {
     static constexpr int KN = (DENSE && Tab::HAS_BI) ? I : NS;
     static constexpr int NPP = Rhs::NP > 0 ? Rhs::NP : 1;
     using S = typename P::S;
+    using AccT = typename AccOf<S>::type;  // stage sums: S itself, or a lazily normalised pair
     static constexpr bool MIX = P::KAHAN && Tab::ADAPTIVE;
     static constexpr bool PHASE = MIX && PhaseOf<Rhs>::value;
     static constexpr bool PF = MIX && FloatParamsOf<Rhs>::value;  // FP32 parameter copies
@@ -303,7 +304,7 @@ struct Lane {
     double t, tf, h, h_prev, t_prev, dir, rtol, atol;
     float th, tl, tfh, tfl;  // FFT: t = th + tl, tf = tfh + tfl
     bool at_tf;              // FFT: the last step ended exactly at tf
-    float phl, omh, oml;     // FFT with a drive phase: phase = ph0 + phl, rate = omh + oml
+    float phl, omh, oml;     // drive phase = ph0 + phl (FFT or pair stages), rate = omh + oml (FFT)
     double rem;    // tf - t (mixed form of RK4)
     float h_lim;   // 1e-14 |h_prev| in FP32 (mixed form's step-size guard)
     double h_lim64;  // 1e-14 |h_prev| (FP64 step-size guard), formed on acceptance
@@ -365,6 +366,18 @@ struct Lane {
         }
     }
 
+    // The drive phase at tt outside FFT: reduced to [-pi, pi] in FP64; pair stages keep it as an
+    // FP32 pair (ph0 + phl), the FP32 stages its leading part.
+    __device__ __forceinline__ void set_phase(double tt) {
+        if constexpr (P::PAIR) {
+            const double ph = p[Rhs::PHASE_RATE] * tt;
+            const double r = fma(-rint(ph * 0.15915494309189535), 6.283185307179586, ph);
+            ph0 = (float)r;
+            phl = (float)(r - (double)ph0);
+        } else {
+            ph0 = Rhs::phase(tt, p);
+        }
+    }
     // FFT: t += hf as an FP32 pair (TwoSum, then FastTwoSum), or t = tf after a clamped last step
     __device__ __forceinline__ void ff_advance() {
         if (last_step) {
@@ -576,7 +589,7 @@ struct Lane {
         int slot = eval_slot(idx, a);
         double* out = a.dense + ((int64_t)slot * a.dmax) * a.n + inst;
 #pragma unroll
-        for (int c = 0; c < D; ++c) out[(int64_t)c * a.n] = (double)v[c];
+        for (int c = 0; c < D; ++c) out[(int64_t)c * a.n] = to_f64(v[c]);
     }
     __device__ void interpolate(double te, S* out, const EnsArgs& a) const {
         if constexpr (DENSE) {
@@ -862,7 +875,7 @@ struct Lane {
                         a.cross_t[(int64_t)ncross * n + inst] = tc;
                         double* out = a.cross_y + ((int64_t)ncross * a.dmax) * n + inst;
 #pragma unroll
-                        for (int c = 0; c < D; ++c) out[(int64_t)c * n] = (double)v[c];
+                        for (int c = 0; c < D; ++c) out[(int64_t)c * n] = to_f64(v[c]);
                     }
                     ncross += 1;
                 }
@@ -998,7 +1011,7 @@ struct Lane {
                         a.cross_t[(int64_t)ncross * n + inst] = te;
                         double* out = a.cross_y + ((int64_t)ncross * a.dmax) * n + inst;
 #pragma unroll
-                        for (int c = 0; c < D; ++c) out[(int64_t)c * n] = (double)v[c];
+                        for (int c = 0; c < D; ++c) out[(int64_t)c * n] = to_f64(v[c]);
                     }
                     ncross += 1;
                     have_push = true;
@@ -1085,7 +1098,7 @@ struct Lane {
             yc[c] = (S)0;
         }
         t = t0;
-        if constexpr (PHASE) ph0 = Rhs::phase(t0, p);
+        if constexpr (PHASE) set_phase(t0);
         t_prev = t0;
         h_prev = 0.0;
         h_lim64 = 0.0;
@@ -1193,15 +1206,19 @@ struct Lane {
         double drv[NS];  // DRV: the drive term at each stage's time
         static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
 #pragma unroll
-            for (int c = 0; c < D; ++c) ys[c] = y[c];
+            AccT acc[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
             static_for<0, decltype(i)::value>([&](auto j) {
                 constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                 if constexpr (aij != 0.0) {
                     S ah = stage_coef(aij);
 #pragma unroll
-                    for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                    for (int c = 0; c < D; ++c) acc_fma(acc[c], ah, k[j][c]);
                 }
             });
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
             if constexpr (MIX) {
                 rhs_at((float)Tab::c(i) * hf, ys, k[i]);
             } else if constexpr (DRV) {
@@ -1215,15 +1232,20 @@ struct Lane {
         });
         // ys now holds the last stage state (ysti, ordinary.rs:107)
         S yseg[D], ynew[D], ycn[D];
+        {
+            AccT acc[D];
 #pragma unroll
-        for (int c = 0; c < D; ++c) yseg[c] = (S)0;
-        static_for<0, NS>([&](auto i) {
-            constexpr double bi_ = Tab::b(decltype(i)::value);
-            if constexpr (bi_ != 0.0) {
+            for (int c = 0; c < D; ++c) acc[c] = acc_begin((S)0);
+            static_for<0, NS>([&](auto i) {
+                constexpr double bi_ = Tab::b(decltype(i)::value);
+                if constexpr (bi_ != 0.0) {
 #pragma unroll
-                for (int c = 0; c < D; ++c) yseg[c] = yseg[c] + (S)bi_ * k[i][c];
-            }
-        });
+                    for (int c = 0; c < D; ++c) acc_fma(acc[c], (S)bi_, k[i][c]);
+                }
+            });
+#pragma unroll
+            for (int c = 0; c < D; ++c) yseg[c] = acc_end(acc[c]);
+        }
         S hs;
         if constexpr (MIX)
             hs = hf;
@@ -1237,6 +1259,11 @@ struct Lane {
                 S ts = y[c] + yk;
                 ycn[c] = (ts - y[c]) - yk;
                 ynew[c] = ts;
+            } else if constexpr (P::PAIR) {
+                AccT acc = acc_begin(y[c]);
+                acc_fma(acc, yseg[c], hf);  // hs = hf: the product of a pair and an FP32 number
+                ynew[c] = acc_end(acc);
+                ycn[c] = (S)0;
             } else {
                 ynew[c] = y[c] + hs * yseg[c];
                 ycn[c] = (S)0;
@@ -1253,18 +1280,26 @@ struct Lane {
 
         NormT err = (NormT)0, err2 = (NormT)0;
         {
-            // the embedded error estimate; FP32 for pair stages (it only feeds the FP32 norm)
+            // the embedded error estimate.  Pair stages sum it in pairs too: its terms are of the
+            // size of h k while the estimate is of the size of the tolerance, and an FP32 sum's
+            // rounding (about 6e-8 h |k|) would exceed a 1e-10 tolerance and reject good steps.
+            // The FP32 norm then reads its leading part.
             using ES = typename PickT<P::PAIR, float, S>::type;
             ES es[D];
+            {
+                AccT ea[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) es[c] = (ES)0;
-            static_for<0, NS>([&](auto j) {
-                constexpr double e_ = Tab::er(decltype(j)::value);
-                if constexpr (e_ != 0.0) {
+                for (int c = 0; c < D; ++c) ea[c] = acc_begin((S)0);
+                static_for<0, NS>([&](auto j) {
+                    constexpr double e_ = Tab::er(decltype(j)::value);
+                    if constexpr (e_ != 0.0) {
 #pragma unroll
-                    for (int c = 0; c < D; ++c) es[c] = es[c] + (ES)e_ * (ES)k[j][c];
-                }
-            });
+                        for (int c = 0; c < D; ++c) acc_fma(ea[c], (S)e_, k[j][c]);
+                    }
+                });
+#pragma unroll
+                for (int c = 0; c < D; ++c) es[c] = (ES)acc_end(ea[c]);
+            }
             if (a.rtol_vec || a.atol_vec) {
 #pragma unroll
                 for (int c = 0; c < D; ++c) err = err + norm_term<true>(c, es[c], y[c], ynew[c], a);
@@ -1416,7 +1451,7 @@ struct Lane {
                 if constexpr (FFT)
                     ff_phase_advance();
                 else
-                    ph0 = Rhs::phase(t, p);
+                    set_phase(t);
             }
 #pragma unroll
             for (int c = 0; c < D; ++c) {
@@ -1495,15 +1530,19 @@ struct Lane {
                 S ys[D];
                 static_for<NS + 1, I>([&](auto i) {
 #pragma unroll
-                    for (int c = 0; c < D; ++c) ys[c] = y[c];
+                    AccT acc[D];
+#pragma unroll
+                    for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
                     static_for<0, decltype(i)::value>([&](auto j) {
                         constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                         if constexpr (aij != 0.0) {
                             S ah = stage_coef(aij);
 #pragma unroll
-                            for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                            for (int c = 0; c < D; ++c) acc_fma(acc[c], ah, k[j][c]);
                         }
                     });
+#pragma unroll
+                    for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
                     if constexpr (MIX)
                         rhs_at((float)Tab::c(i) * hf, ys, k[i]);
                     else
@@ -1549,15 +1588,19 @@ struct Lane {
         // stage i from the step's start: y + sum_j (a_ij h) k_j in order (add_scaled)
         auto stage = [&](auto i) {
 #pragma unroll
-            for (int c = 0; c < D; ++c) ys[c] = y[c];
+            AccT acc[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
             static_for<0, decltype(i)::value>([&](auto j) {
                 constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                 if constexpr (aij != 0.0) {
                     S ah = stage_coef(aij);
 #pragma unroll
-                    for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                    for (int c = 0; c < D; ++c) acc_fma(acc[c], ah, k[j][c]);
                 }
             });
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
             if constexpr (MIX)
                 rhs_at((float)Tab::c(i) * hf, ys, k[i]);
             else
@@ -1694,7 +1737,7 @@ struct Lane {
                 if constexpr (PHASE) ff_phase_advance();
             } else if constexpr (MIX) {
                 t = last_step ? tf : t + widen_f32(hf);  // a clamped last step ends exactly at tf
-                if constexpr (PHASE) ph0 = Rhs::phase(t, p);
+                if constexpr (PHASE) set_phase(t);
             } else {
                 t = t + h;
             }
@@ -1759,15 +1802,19 @@ struct Lane {
         S ys[D];
         static_for<1, NS>([&](auto i) {
 #pragma unroll
-            for (int c = 0; c < D; ++c) ys[c] = y[c];
+            AccT acc[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
             static_for<0, decltype(i)::value>([&](auto j) {
                 constexpr double aij = Tab::a(decltype(i)::value, decltype(j)::value);
                 if constexpr (aij != 0.0) {
                     S ah = stage_coef(aij);
 #pragma unroll
-                    for (int c = 0; c < D; ++c) ys[c] = ys[c] + ah * k[j][c];
+                    for (int c = 0; c < D; ++c) acc_fma(acc[c], ah, k[j][c]);
                 }
             });
+#pragma unroll
+            for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
             rhs(t + Tab::c(i) * h, ys, k[i]);
         });
         fev += NS - 1;

@@ -4,8 +4,11 @@
 //     template <class R> __device__ void NAME(R t, const R* y, R* dydt, const double* p);
 // the CUDA twin of `ODE::diff(&self, t, &y, &mut dydt)` (src/ode/ode.rs:20-44) with the
 // system's fields in p[0..n_params).  Registration compiles the integrator headers plus that
-// source with NVRTC for this GPU twice — once with -fmad=false (the parity variants) and once
-// with contraction (FP64_FAST / MIXED) — and loads the kernels through the driver API.
+// source with NVRTC for this GPU: once with -fmad=false (the parity variants), once with
+// contraction (FP64_FAST / MIXED), and once more for DOPRI5's FP32-pair stages (the tight class
+// of a MIXED solve) with R = degpu::df.  The last build is optional: a source that does not
+// compile for pairs (it calls a function with no pair overload) runs its tight class in
+// FP64_FAST.  The kernels load through the runtime's library API.
 
 #include <cuda_runtime.h>
 #include <dlfcn.h>
@@ -21,15 +24,16 @@
 
 namespace degpu {
 int device_sm_count();
+double mixed_split(const degpu_method_cfg* cfg);
 }
 
 namespace degpu {
 
 struct NvrtcRhs {
     int dim, n_params;
-    cudaLibrary_t mod[2] = {nullptr, nullptr};  // [0] parity build, [1] contracted build
-    // [method][prec][dense][kernel: 0 thread, 1 persistent]
-    cudaKernel_t fn[3][3][2][2] = {};
+    cudaLibrary_t mod[3] = {nullptr, nullptr, nullptr};  // parity, contracted and pair builds
+    // [method][prec: parity, fast, mixed, pair][dense][kernel: 0 thread, 1 persistent]
+    cudaKernel_t fn[3][4][2][2] = {};
 };
 
 static std::mutex g_mu;
@@ -46,21 +50,24 @@ static std::string csrc_dir() {
 }
 
 static const char* kMethods[3] = {"TabRK4", "TabDopri5", "TabDop853"};
-static const char* kPrecs[3] = {"PrecParity", "PrecFast", "PrecMixed"};
+static const char* kPrecs[4] = {"PrecParity", "PrecFast", "PrecMixed", "PrecMixedPair"};
+// the build that holds (method m, precision slot p): 0 parity, 1 contracted, 2 pair stages
+static int build_of(int m, int p) { return p == 0 ? 0 : p == 3 ? (m == 1 ? 2 : -1) : 1; }
 
 static std::string kernel_name(int m, int p, int dense, int persistent) {
     return std::string("degpu::") + (persistent ? "erk_persistent_kernel<" : "erk_thread_kernel<") + "degpu::" +
            kMethods[m] + ", degpu::RhsUser, degpu::" + kPrecs[p] + ", " + (dense ? "true" : "false") + ">";
 }
 
-static degpu_status compile_module(const std::string& src, bool parity, NvrtcRhs* r, std::string& log) {
+static degpu_status compile_module(const std::string& src, int build, NvrtcRhs* r, std::string& log) {
+    const bool parity = build == 0;
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, src.c_str(), "degpu_user_rhs.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
         return DEGPU_CUDA_ERROR;
     std::vector<std::string> names;
     for (int m = 0; m < 3; ++m)
-        for (int p = 0; p < 3; ++p) {
-            if (parity != (p == 0)) continue;
+        for (int p = 0; p < 4; ++p) {
+            if (build_of(m, p) != build) continue;
             for (int d = 0; d < 2; ++d)
                 for (int k = 0; k < 2; ++k) {
                     names.push_back(kernel_name(m, p, d, k));
@@ -97,10 +104,10 @@ static degpu_status compile_module(const std::string& src, bool parity, NvrtcRhs
         nvrtcDestroyProgram(&prog);
         return DEGPU_CUDA_ERROR;
     }
-    r->mod[parity ? 0 : 1] = mod;
+    r->mod[build] = mod;
     for (int m = 0; m < 3; ++m)
-        for (int p = 0; p < 3; ++p) {
-            if (parity != (p == 0)) continue;
+        for (int p = 0; p < 4; ++p) {
+            if (build_of(m, p) != build) continue;
             for (int d = 0; d < 2; ++d)
                 for (int k = 0; k < 2; ++k) {
                     std::string nm = kernel_name(m, p, d, k);
@@ -167,29 +174,87 @@ degpu_status nvrtc_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     a.dense_mode = cfg->dense_mode;
     a.n_params = pb->n_params;
     if (in->n_eval > 0) return DEGPU_UNSUPPORTED;  // dense output for run-time systems: not built
-    const int persistent = cfg->kernel == DEGPU_KERNEL_PERSISTENT ? 1 : 0;
-    cudaKernel_t f = r->fn[cfg->method][cfg->precision][0][persistent];
-    if (!f) return DEGPU_UNSUPPORTED;
-    unsigned long long* tk = nullptr;
-    if (persistent) {
-        if (cudaMallocAsync((void**)&tk, sizeof(unsigned long long), s) != cudaSuccess) return DEGPU_OOM;
-        cudaMemsetAsync(tk, 0, sizeof(unsigned long long), s);
-        a.ticket = tk;
-    }
-    void* args[] = {&a};
-    unsigned grid;
-    if (persistent) {
-        int bps = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)f, 128, 0);
-        long long g = (long long)(bps > 0 ? bps : 1) * device_sm_count();
-        long long need = (n + 127) / 128;
-        grid = (unsigned)(g < need ? g : need);
+    // run-time systems have RK4, DOPRI5 and DOP853 in the parity, FP64_FAST and MIXED forms
+    if (cfg->method < DEGPU_RK4 || cfg->method > DEGPU_DOP853) return DEGPU_UNSUPPORTED;
+    if (cfg->precision != DEGPU_FP64_PARITY && cfg->precision != DEGPU_FP64_FAST && cfg->precision != DEGPU_MIXED)
+        return DEGPU_UNSUPPORTED;
+    const int m = cfg->method, persistent = cfg->kernel == DEGPU_KERNEL_PERSISTENT ? 1 : 0;
+    // a MIXED solve sends the instances with rtol below the bound to the pair stages (DOPRI5,
+    // when the source built for pairs) or to FP64_FAST, like a built-in system's
+    struct Part {
+        int prec;
+        std::vector<int64_t> idx;
+    };
+    std::vector<Part> parts;
+    const double split = mixed_split(cfg);
+    if (split > 0.0) {
+        std::vector<double> rt(n);
+        if (cudaMemcpyAsync(rt.data(), in->rtol, n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return DEGPU_CUDA_ERROR;
+        const int low = r->fn[m][3][0][persistent] ? 3 : DEGPU_FP64_FAST;
+        parts.push_back(Part{low, {}});
+        parts.push_back(Part{DEGPU_MIXED, {}});
+        for (int64_t i = 0; i < n; ++i) parts[rt[i] < split ? 0 : 1].idx.push_back(i);
     } else {
-        grid = (unsigned)((n + 127) / 128);
+        parts.push_back(Part{cfg->precision, {}});
     }
-    cudaError_t cr = cudaLaunchKernel((const void*)f, dim3(grid), dim3(128), args, 0, s);
-    if (tk) cudaFreeAsync(tk, s);
-    return cr == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
+    std::vector<void*> scratch;
+    degpu_status st = DEGPU_OK;
+    for (const Part& pt : parts) {
+        if (split > 0.0 && pt.idx.empty()) continue;
+        cudaKernel_t f = r->fn[m][pt.prec][0][persistent];
+        if (!f) {
+            st = DEGPU_UNSUPPORTED;
+            break;
+        }
+        EnsArgs ga = a;
+        if (split > 0.0) {
+            int64_t* d_idx = nullptr;
+            if (cudaMallocAsync((void**)&d_idx, pt.idx.size() * sizeof(int64_t), s) != cudaSuccess) {
+                st = DEGPU_OOM;
+                break;
+            }
+            scratch.push_back(d_idx);
+            if (cudaMemcpyAsync(d_idx, pt.idx.data(), pt.idx.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s) !=
+                cudaSuccess) {
+                st = DEGPU_CUDA_ERROR;
+                break;
+            }
+            ga.index = d_idx;
+            ga.count = (int64_t)pt.idx.size();
+        }
+        unsigned grid;
+        if (persistent) {
+            unsigned long long* tk = nullptr;
+            if (cudaMallocAsync((void**)&tk, sizeof(unsigned long long), s) != cudaSuccess) {
+                st = DEGPU_OOM;
+                break;
+            }
+            scratch.push_back(tk);
+            if (cudaMemsetAsync(tk, 0, sizeof(unsigned long long), s) != cudaSuccess) {
+                st = DEGPU_CUDA_ERROR;
+                break;
+            }
+            ga.ticket = tk;
+            int bps = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)f, 128, 0);
+            long long g = (long long)(bps > 0 ? bps : 1) * device_sm_count();
+            long long need = (ga.count + 127) / 128;
+            grid = (unsigned)(g < need ? g : need);
+        } else {
+            grid = (unsigned)((ga.count + 127) / 128);
+        }
+        void* args[] = {&ga};
+        if (cudaLaunchKernel((const void*)f, dim3(grid), dim3(128), args, 0, s) != cudaSuccess) {
+            st = DEGPU_CUDA_ERROR;
+            break;
+        }
+    }
+    // the index lists come from host vectors that die with this call
+    if (split > 0.0 && cudaStreamSynchronize(s) != cudaSuccess && st == DEGPU_OK) st = DEGPU_CUDA_ERROR;
+    for (void* q : scratch) cudaFreeAsync(q, s);
+    return st;
 }
 
 }  // namespace degpu
@@ -212,8 +277,20 @@ extern "C" degpu_status degpu_register_rhs_nvrtc(const char* source, const char*
     r->dim = dim;
     r->n_params = n_params;
     std::string lg;
-    degpu_status st = compile_module(src, true, r, lg);
-    if (st == DEGPU_OK) st = compile_module(src, false, r, lg);
+    degpu_status st = compile_module(src, 0, r, lg);
+    if (st == DEGPU_OK) st = compile_module(src, 1, r, lg);
+    if (st == DEGPU_OK) {
+        std::string plog;
+        if (compile_module(src, 2, r, plog) != DEGPU_OK) {
+            // optional: the tight class of a MIXED solve then runs in FP64_FAST
+            if (r->mod[2]) cudaLibraryUnload(r->mod[2]);
+            r->mod[2] = nullptr;
+            for (auto& fm : r->fn)
+                for (auto& fd : fm[3])
+                    for (auto& fk : fd) fk = nullptr;
+            lg += "note: no FP32-pair build of this source (the tight class of MIXED solves runs in FP64_FAST)\n";
+        }
+    }
     if (log && log_size) {
         size_t k = lg.size() < log_size - 1 ? lg.size() : log_size - 1;
         memcpy(log, lg.data(), k);

@@ -111,7 +111,8 @@ void register_cross_embedded_methods() {
     cross_registry()[VariantKey{DEGPU_CASH_KARP, Rhs::ID, P::ID, 1}] = &launch_cross<TabCashKarp, Rhs, P>;
 }
 
-// Resumable round kernels of the serving path (no dense output).
+// Resumable round kernels of the serving path, keyed with dense = 1 for the kernels that also
+// write output times.
 struct RoundOps {
     size_t park_bytes;  // resident state per instance
     cudaError_t (*launch)(const EnsArgs& a, void* park, int budget, unsigned long long* done, int max_blocks,
@@ -119,15 +120,15 @@ struct RoundOps {
 };
 std::map<VariantKey, RoundOps>& round_registry();
 
-template <class Tab, class Rhs, class P>
+template <class Tab, class Rhs, class P, bool DENSE = false>
 cudaError_t launch_round(const EnsArgs& a, void* park, int budget, unsigned long long* done, int max_blocks,
                          cudaStream_t s) {
-    using L = Lane<Tab, Rhs, P, false>;
+    using L = Lane<Tab, Rhs, P, DENSE>;
     if (a.count <= 0) return cudaSuccess;
     static int blocks_per_sm = -1;
     if (blocks_per_sm < 0) {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm,
-                                                                      erk_round_kernel<Tab, Rhs, P, false>, 128, 0);
+                                                                      erk_round_kernel<Tab, Rhs, P, DENSE>, 128, 0);
         if (e != cudaSuccess) return e;
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
@@ -135,21 +136,21 @@ cudaError_t launch_round(const EnsArgs& a, void* park, int budget, unsigned long
     long long need = (a.count + 127) / 128;
     if (grid > need) grid = need;
     if (max_blocks > 0 && grid > max_blocks) grid = max_blocks;
-    erk_round_kernel<Tab, Rhs, P, false><<<(unsigned)grid, 128, 0, s>>>(a, (Parked<L>*)park, budget, done);
+    erk_round_kernel<Tab, Rhs, P, DENSE><<<(unsigned)grid, 128, 0, s>>>(a, (Parked<L>*)park, budget, done);
     return cudaGetLastError();
 }
 
-template <class Tab, class Rhs, class P>
+template <class Tab, class Rhs, class P, bool DENSE = false>
 void register_round() {
-    round_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, 0}] =
-        RoundOps{sizeof(Parked<Lane<Tab, Rhs, P, false>>), &launch_round<Tab, Rhs, P>};
+    round_registry()[VariantKey{method_id<Tab>(), Rhs::ID, P::ID, DENSE ? 1 : 0}] =
+        RoundOps{sizeof(Parked<Lane<Tab, Rhs, P, DENSE>>), &launch_round<Tab, Rhs, P, DENSE>};
 }
 
-template <class Rhs, class P>
+template <class Rhs, class P, bool DENSE = false>
 void register_round_all_methods() {
-    register_round<TabRK4, Rhs, P>();
-    register_round<TabDopri5, Rhs, P>();
-    register_round<TabDop853, Rhs, P>();
+    register_round<TabRK4, Rhs, P, DENSE>();
+    register_round<TabDopri5, Rhs, P, DENSE>();
+    register_round<TabDop853, Rhs, P, DENSE>();
 }
 
 // Multi-family persistent kernels: families Van der Pol (slot 0), pendulum (1), Lorenz (2).
@@ -216,6 +217,8 @@ void register_verner_cross8798_fast();
 void register_plain();
 void register_mixed_f64ctrl();
 void register_mixed_pair();
+void register_round_dense_parity();
+void register_round_dense_fast_mixed();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to

@@ -11,10 +11,13 @@
 //      (Parked lanes: t, h, y, derivative, counters, controller state) never leaves the device.
 // Rounds are bounded (`round_budget` driver iterations per instance), so the GPU is shared
 // between the requests in flight and a new request starts within one round of being admitted.
-// Requests the round kernels do not cover (dense output, ragged FPU chains, run-time families)
-// are solved with one degpu_solve_ensemble call on the request's stream.
+// Requests with output times run round kernels that also write them (the times sorted once, as
+// TEvalSolout::new sorts them).  Requests the round kernels do not cover (ragged FPU chains,
+// run-time families, family maps) are solved with one degpu_solve_ensemble call on the request's
+// stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -62,6 +65,9 @@ struct SrvRequest {
     unsigned long long* ticket = nullptr;
     unsigned long long* done_dev = nullptr;
     unsigned long long* done_host = nullptr;  // pinned
+    // output times of a resumable request: ascending, with the permutation to the caller's order
+    std::vector<double> te_sorted;
+    std::vector<int32_t> te_perm;
 };
 
 struct ServerImpl {
@@ -84,7 +90,7 @@ struct ServerImpl {
         const size_t n = (size_t)r.in.n, d = (size_t)r.pb.dim, np = (size_t)(r.pb.n_params > 0 ? r.pb.n_params : 1);
         const size_t m = (size_t)(r.in.n_eval > 0 ? r.in.n_eval : 0);
         size_t b = align(n * 8) * 6 + align(d * n * 8) * 2 + align(np * n * 8) + align(n * 4) * 3 + align(n * 8) * 3;
-        b += align(m * 8) + align(m * d * n * 8);
+        b += align(m * 8) + align(m * d * n * 8) + align(m * 4);
         if (r.in.rtol_vec) b += align(d * n * 8);
         if (r.in.atol_vec) b += align(d * n * 8);
         if (r.resumable && !r.split) b += align(n * r.ops.park_bytes) + 512;
@@ -177,6 +183,15 @@ struct ServerImpl {
         a.dense_mode = r.cfg.dense_mode;
         a.n_params = r.pb.n_params;
         a.ticket = r.ticket;
+        if (!r.te_sorted.empty()) {
+            // the sorted output times over the caller's copy, their permutation, NaN outputs
+            a.n_eval = (int32_t)m;
+            a.t_eval = (const double*)r.din.t_eval;
+            cudaMemcpyAsync((void*)a.t_eval, r.te_sorted.data(), m * 8, cudaMemcpyHostToDevice, s);
+            a.eval_perm = (const int32_t*)up(r.te_perm.data(), m * 4);
+            a.dense = r.dout.dense;
+            cudaMemsetAsync(a.dense, 0xFF, m * d * n * 8, s);  // 0xFF bytes form a quiet NaN
+        }
         if (r.split) {
             const size_t n1 = r.idx[1].size();
             a.index = (const int64_t*)up(r.idx[0].data(), n0 * 8);
@@ -347,9 +362,10 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
     r->in = *in;
     r->out = *out;
     r->t_submit = Clock::now();
-    const bool plain = !in->family && !in->dims && in->n_eval <= 0 && pb->rhs_id < DEGPU_RHS_NVRTC_BASE;
+    const bool plain = !in->family && !in->dims && pb->rhs_id < DEGPU_RHS_NVRTC_BASE;
+    const int dense = (in->n_eval > 0 && in->t_eval && out->dense) ? 1 : 0;
     if (plain) {
-        auto it = round_registry().find(VariantKey{cfg->method, pb->rhs_id, cfg->precision, 0});
+        auto it = round_registry().find(VariantKey{cfg->method, pb->rhs_id, cfg->precision, dense});
         if (it != round_registry().end()) {
             r->resumable = true;
             r->ops = it->second;
@@ -357,9 +373,9 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
         // a mixed request whose rtol values straddle the mixed-precision bound: the instances
         // below it run the FP32-pair round kernels where built, else the FP64_FAST ones
         const double bound = mixed_split(cfg);
-        auto it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, mixed_low_precision(cfg), 0});
+        auto it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, mixed_low_precision(cfg), dense});
         if (it64 == round_registry().end())
-            it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, DEGPU_FP64_FAST, 0});
+            it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, DEGPU_FP64_FAST, dense});
         if (r->resumable && bound > 0.0) {
             if (it64 == round_registry().end()) return DEGPU_UNSUPPORTED;
             for (int64_t i = 0; i < in->n; ++i) r->idx[in->rtol[i] < bound ? 1 : 0].push_back(i);
@@ -373,6 +389,16 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
                 r->ops64 = it64->second;
             }
         }
+    }
+    if (r->resumable && dense) {
+        // TEvalSolout::new's stable ascending sort (src/solout/t_eval.rs:154-171), done once
+        const int32_t m = in->n_eval;
+        r->te_perm.resize(m);
+        for (int32_t e = 0; e < m; ++e) r->te_perm[e] = e;
+        std::stable_sort(r->te_perm.begin(), r->te_perm.end(),
+                         [&](int32_t x, int32_t y) { return in->t_eval[x] < in->t_eval[y]; });
+        r->te_sorted.resize(m);
+        for (int32_t e = 0; e < m; ++e) r->te_sorted[e] = in->t_eval[r->te_perm[e]];
     }
     r->bytes = I.footprint(*r);
     if (cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming) != cudaSuccess) return DEGPU_CUDA_ERROR;

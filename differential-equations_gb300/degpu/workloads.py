@@ -100,6 +100,26 @@ def config0(n: int = 4096) -> Ensemble:
 FAMILIES_C1 = (abi.RHS["VAN_DER_POL"], abi.RHS["PENDULUM"], abi.RHS["LORENZ"])
 
 
+def _family_draws(slot: int, i: np.ndarray):
+    """(y0 [3, len(i)], params [3, len(i)]) of instances `i` of one family of the uneven ensemble
+    (slot 0 Van der Pol, 1 pendulum, 2 Lorenz)."""
+    y0 = np.zeros((3, len(i)))
+    p = np.zeros((3, len(i)))
+    if slot == 0:  # Van der Pol: mu ~ logU[0.1,5], y0 ~ U[-2,2]^2
+        p[0] = logU(1, i, 10, 0.1, 5.0)
+        y0[0] = U(1, i, 11, -2.0, 2.0)
+        y0[1] = U(1, i, 12, -2.0, 2.0)
+    elif slot == 1:  # pendulum: gamma ~ U[0.05,0.5], A ~ U[0.5,1.5], Omega ~ U[0.5,1], y0 ~ U[-2,2]^2
+        p[0] = U(1, i, 20, 0.05, 0.5)
+        p[1] = U(1, i, 21, 0.5, 1.5)
+        p[2] = U(1, i, 22, 0.5, 1.0)
+        y0[0] = U(1, i, 23, -2.0, 2.0)
+        y0[1] = U(1, i, 24, -2.0, 2.0)
+    else:  # Lorenz as config 0
+        y0[:], p[:] = lorenz_draws(1, i)
+    return y0, p
+
+
 def config1(n: int = 1 << 20, first: int = 0) -> Ensemble:
     """Uneven ensemble: instance index mod 3 -> Van der Pol / damped driven pendulum / Lorenz;
     t_end ~ U[5,50], rtol ~ logU[1e-9,1e-5], atol = 1e-2 rtol, DOPRI5."""
@@ -108,39 +128,38 @@ def config1(n: int = 1 << 20, first: int = 0) -> Ensemble:
     family = np.array(FAMILIES_C1, dtype=np.int32)[fam_idx]
     y0 = np.zeros((3, n))
     p = np.zeros((3, n))
-    # Van der Pol: mu ~ logU[0.1,5], y0 ~ U[-2,2]^2
-    m = fam_idx == 0
-    i = inst[m]
-    p[0, m] = logU(1, i, 10, 0.1, 5.0)
-    y0[0, m] = U(1, i, 11, -2.0, 2.0)
-    y0[1, m] = U(1, i, 12, -2.0, 2.0)
-    # pendulum: gamma ~ U[0.05,0.5], A ~ U[0.5,1.5], Omega ~ U[0.5,1], y0 ~ U[-2,2]^2
-    m = fam_idx == 1
-    i = inst[m]
-    p[0, m] = U(1, i, 20, 0.05, 0.5)
-    p[1, m] = U(1, i, 21, 0.5, 1.5)
-    p[2, m] = U(1, i, 22, 0.5, 1.0)
-    y0[0, m] = U(1, i, 23, -2.0, 2.0)
-    y0[1, m] = U(1, i, 24, -2.0, 2.0)
-    # Lorenz as config 0
-    m = fam_idx == 2
-    i = inst[m]
-    ly, lp = lorenz_draws(1, i)
-    y0[:, m] = ly
-    p[:, m] = lp
+    for slot in range(3):
+        m = fam_idx == slot
+        y0[:, m], p[:, m] = _family_draws(slot, inst[m])
     tf = U(1, inst, 30, 5.0, 50.0)
     rtol = logU(1, inst, 31, 1e-9, 1e-5)
     return Ensemble("uneven-dopri5", abi.DOPRI5, n, 3, 3, np.zeros(n), tf, y0, p, rtol, 1e-2 * rtol,
                     family=family)
 
 
-def config2(n: int = 131072, first: int = 0) -> Ensemble:
+def config1_family(slot: int, n: int, first: int = 0) -> Ensemble:
+    """n instances of one family of the uneven ensemble (slot 0 Van der Pol, 1 pendulum, 2 Lorenz):
+    the instances first + 3 j + r (r the residue that gives the slot), with the draws config1 gives
+    them, generated without the other families.  Single-family batch: rhs_id set, no family map,
+    state and parameter rows of that family only."""
+    inst = first + 3 * np.arange(n) + ((slot - first) % 3)
+    y0, p = _family_draws(slot, inst)
+    fid = FAMILIES_C1[slot]
+    d = 3 if fid == abi.RHS["LORENZ"] else 2
+    tf = U(1, inst, 30, 5.0, 50.0)
+    rtol = logU(1, inst, 31, 1e-9, 1e-5)
+    return Ensemble("uneven-family", abi.DOPRI5, n, d, 3, np.zeros(n), tf, np.ascontiguousarray(y0[:d]), p, rtol,
+                    1e-2 * rtol, rhs_id=fid)
+
+
+def config2(n: int = 131072, first: int = 0, max_masses: int = 128) -> Ensemble:
     """FPU-beta chains with fixed ends: masses ~ int log-uniform [2,128] (d = 2 masses),
     beta ~ U[0.1,1], x ~ N(0,0.1^2), p = 0; DOP853 rtol=1e-10 atol=1e-12, t in [0,100],
-    64 output times 100 k / 63."""
+    64 output times 100 k / 63.  `max_masses` caps the draw (the serving configuration's
+    chains have at most 64 masses)."""
     inst = np.arange(first, first + n)
     masses = np.floor(np.exp(U(2, inst, 0, math.log(2.0), math.log(129.0)))).astype(np.int32)
-    masses = np.clip(masses, 2, 128)
+    masses = np.clip(masses, 2, max_masses)
     dims = 2 * masses
     dmax = int(dims.max()) if n else 2
     y0 = np.zeros((dmax, n))

@@ -133,7 +133,10 @@ def test_pair_stages_track_fp64(bound, kernel):
     f32 = run(e, abi.DOPRI5, abi.MIXED, kernel)
     fast = run(e, abi.DOPRI5, abi.FP64_FAST, kernel)
     ok = (pair.status == abi.COMPLETE) & (fast.status == abi.COMPLETE)
-    assert ok.mean() > 0.999
+    # at rtol 1e-10 over horizons up to 50 a few Van der Pol instances end on the crate's
+    # stiffness test or the step limit in either arithmetic; the pairs must not end more often
+    assert ok.mean() > 0.99
+    assert (pair.status == abi.COMPLETE).sum() >= (fast.status == abi.COMPLETE).sum() - 0.002 * e.n
     rel = lambda r: np.max(np.abs(r.y_final[:, ok] - fast.y_final[:, ok]), axis=0) / \
         np.maximum(np.max(np.abs(fast.y_final[:, ok]), axis=0), 1e-300)
     # the pair stages follow FP64 to the rounding-driven spread of the step sequence
