@@ -72,6 +72,31 @@ def flops_of(family, accepted, rejected):
     return tot
 
 
+# FP32 operations (FMA = 2) of one attempted step with FP32-pair stages, the emulation's own
+# instruction counts: a stage-sum term (pair product accumulated: 1 mul, 3 FMA, 8 add) = 15, a
+# pair times FP32 coefficient (1 mul, 2 FMA, 3 add) = 8, a pair product (1 mul, 3 FMA, 3 add) =
+# 10, a pair sum (11 add) = 11, a normalisation = 3.
+#   15 stage coefficients 8 each; per component: 15 stage-sum terms + 5 normalisations, 5 terms
+#   of y_seg + 1, y_new 16, 6 terms of the error estimate + 1, the FP32 norm 5; controller and
+#   pair time 18; 6 right-hand sides in pairs (sin/cos not counted, as in the FP64 model).
+PAIR_RHS_FLOPS = {abi.RHS["LORENZ"]: 4 * 10 + 4 * 11, abi.RHS["VAN_DER_POL"]: 3 * 10 + 2 * 11,
+                  abi.RHS["PENDULUM"]: 2 * 10 + 2 * 11 + 8 + 11}
+
+
+def pair_step_flops(rhs_id):
+    d = RHS_FLOPS[rhs_id][0]
+    return 15 * 8 + (15 * 15 + 5 * 3 + 5 * 15 + 3 + 16 + 6 * 15 + 3 + 5) * d + 18 + 6 * PAIR_RHS_FLOPS[rhs_id]
+
+
+def pair_flops_of(family, accepted, rejected, mask):
+    """FP32 operations of the pair-stage instances (`mask`) of a mixed solve."""
+    tot = 0.0
+    for rid in RHS_FLOPS:
+        m = (family == rid) & mask
+        tot += pair_step_flops(rid) * float((accepted[m] + rejected[m]).sum())
+    return tot
+
+
 def fp64_ops_mixed(family, accepted, rejected):
     """FP64 operations of the mixed form's final-state solve: none.  Its time is an FP32 pair and
     its step size, norm and controller are FP32; FP64 appears only once per instance (setting up
@@ -218,17 +243,26 @@ class AccuracySample:
             out[names[f]] = rows
         return out
 
-    def meets_fp64_floor(self, tab):
+    def meets_fp64_floor(self, tab, median_ratio=1.25, share_gap=0.03):
         """The decades (family, rtol decade) where the FP64 result itself reaches 1e-6 against the
-        tight oracle on the median, and whether the variant does there too."""
-        qual, ok = [], True
+        tight oracle on the median, and whether the variant is as accurate there: its median
+        error at most `median_ratio` times FP64's and its share of instances within 1e-6 at most
+        `share_gap` below FP64's.  (Comparing the two medians with 1e-6 directly would turn on
+        sampling noise where FP64's median sits at 1e-6 itself.)"""
+        qual, ok, worst_ratio, worst_gap = [], True, 0.0, 0.0
         for fam, rows in tab.items():
             for dec, row in rows.items():
                 fl = row.get("fp64_floor")
                 if fl and fl["median"] <= 1e-6:
                     qual.append(f"{fam} {dec}")
-                    ok = ok and row["median"] <= 1e-6
-        return {"decades_where_fp64_meets_1e-6": qual, "variant_meets_1e-6_there": ok}
+                    ratio = row["median"] / max(fl["median"], 1e-300)
+                    gap = fl["frac_le_1e-6"] - row["frac_le_1e-6"]
+                    worst_ratio, worst_gap = max(worst_ratio, ratio), max(worst_gap, gap)
+                    ok = ok and ratio <= median_ratio and gap <= share_gap
+        return {"decades_where_fp64_meets_1e-6": qual,
+                "rule": f"median <= {median_ratio} x FP64's and share <= 1e-6 at most {share_gap} below FP64's",
+                "worst_median_ratio": worst_ratio, "worst_share_gap": worst_gap,
+                "variant_meets_1e-6_there": ok}
 
 
 def agreement(acc, rej, y, acc_ref, rej_ref, y_ref, conditioned):
@@ -958,7 +992,7 @@ def main():
     ap.add_argument("--compare", default="fp64-plain,fp64plain-persistent,fp64fast-persistent,fp64parity-persistent,"
                                          "mixedf64ctrl-persistent,mixed-persistent-nosplit",
                     help="comma list of extra variants timed once each")
-    ap.add_argument("--accuracy-per-family", type=int, default=1000)
+    ap.add_argument("--accuracy-per-family", type=int, default=3000)
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the 4096-Lorenz, Gray-Scott and FPU-chain lines of the default run")
     ap.add_argument("--fpu-slice", type=int, default=16384,
@@ -1105,13 +1139,17 @@ def main():
     def split_ops(variant, a_, r_):
         """(FP64, FP32) algorithmic operations of a variant's solve.  In the mixed forms both the
         FP32 stages (rtol above the bound) and the FP32-pair stages (below it, DOPRI5) run on the
-        FP32 pipe; only the per-step bookkeeping that stays FP64 is counted there."""
+        FP32 pipe: the FP32 stages count the FP64 model's operations, the pair stages the
+        emulation's FP32 operations (pair_step_flops); only the per-step bookkeeping that stays
+        FP64 is counted on the FP64 pipe."""
         p_ = VARIANTS[variant][0]
-        total = flops_of(fam, a_, r_)
         if p_ not in MIXED_PRECISIONS:
-            return total, 0.0
+            return flops_of(fam, a_, r_), 0.0
+        pair = e.rtol < bound if variant not in NOSPLIT else np.zeros(e.n, bool)
+        keep = ~pair
+        f32 = flops_of(fam[keep], a_[keep], r_[keep]) + pair_flops_of(fam, a_, r_, pair)
         f64 = fp64_ops_mixed(fam, a_, r_)
-        return f64, total - f64
+        return f64, f32 - f64
 
     fp64_ops, fp32_ops = split_ops(args.variant, acc, rej)
     t_s = ms * 1e-3 / world
@@ -1126,7 +1164,8 @@ def main():
             "fp64": {"achieved": a64, "peak": fp64_peak, "frac": f64},
             "fp32": {"achieved": a32, "peak": fp32_peak, "frac": f32},
             "peak_source": "self-measured FMA probe (MEASURED_PEAKS.json has no FP64/FP32 figure); FMA = 2 ops",
-            "note": "algorithmic ops of the whole ensemble solve / solve time (one kernel launch per solve)"}
+            "note": "algorithmic ops of the whole ensemble solve / solve time (one kernel launch per solve); "
+                    "pair-stage instances count the FP32 operations of the pair emulation"}
 
     # end-to-end through the host-pointer entry point (pinned buffers, copies inside the timing)
     pin = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).pin_memory()

@@ -1,9 +1,10 @@
-// Host build of df_math.cuh so that the pair arithmetic and its sin/cos can be tested without a
-// GPU.  Compiled with -ffp-contract=off: every fused multiply-add is an explicit fmaf, as on the
+// Host build of df_math.cuh and f64_tab_math.cuh so that the pair arithmetic and the pair and
+// FP64 table-driven sin/cos can be tested without a GPU.  Compiled with -ffp-contract=off: every fused multiply-add is an explicit fmaf, as on the
 // device.
 #include <stdint.h>
 
 #include "df_math.cuh"
+#include "f64_tab_math.cuh"
 
 extern "C" {
 // sin and cos of the pairs (hi[i], lo[i])
@@ -21,6 +22,13 @@ void degpu_host_df_ops(const float* ah, const float* al, const float* bh, const 
         const degpu::df a(ah[i], al[i]), b(bh[i], bl[i]), c(ch[i], cl[i]);
         fma_out[i] = degpu::to_f64(a * b + c);
         sub_out[i] = degpu::to_f64(a - b);
+    }
+}
+// the plain FP64 form's table-driven sin and cos
+void degpu_host_f64t_sincos(const double* x, double* s, double* c, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        s[i] = degpu::f64t::sin(x[i]);
+        c[i] = degpu::f64t::cos(x[i]);
     }
 }
 // y + sum_j a_j k_j over m terms through the lazily normalised accumulator (the stage sums);

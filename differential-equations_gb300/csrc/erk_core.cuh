@@ -1205,7 +1205,6 @@ struct Lane {
         S ys[D];
         double drv[NS];  // DRV: the drive term at each stage's time
         static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
-#pragma unroll
             AccT acc[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
@@ -1529,7 +1528,6 @@ struct Lane {
                 for (int c = 0; c < D; ++c) k[NS][c] = dydt[c];
                 S ys[D];
                 static_for<NS + 1, I>([&](auto i) {
-#pragma unroll
                     AccT acc[D];
 #pragma unroll
                     for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
@@ -1587,7 +1585,6 @@ struct Lane {
         S ys[D];
         // stage i from the step's start: y + sum_j (a_ij h) k_j in order (add_scaled)
         auto stage = [&](auto i) {
-#pragma unroll
             AccT acc[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
@@ -1801,7 +1798,6 @@ struct Lane {
         for (int c = 0; c < D; ++c) k[0][c] = k0[c];
         S ys[D];
         static_for<1, NS>([&](auto i) {
-#pragma unroll
             AccT acc[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);

@@ -7,6 +7,11 @@ Contents
                   remainder by a fraction of an ulp of it)
   DF_TRIG_TAB     sin(j pi/64), cos(j pi/64) for j = 0..127 as (hi, lo) FP32 pairs, one
                   16-byte row per j: sin hi, sin lo, cos hi, cos lo
+and for the plain FP64 sin and cos (f64_tab_math.cuh):
+  F64_PIO64_1, _2 pi/64 as two doubles
+  F64_64_OVER_PI  64/pi rounded to a double
+  F64_TRIG_TAB    sin(j pi/64), cos(j pi/64) for j = 0..127 as double-double values, one
+                  32-byte row per j: sin hi, cos hi, sin lo, cos lo
 """
 import os
 
@@ -47,7 +52,7 @@ def main(out_dir):
     c1 = f32_exact(pio64)
     c2 = f32_exact(pio64 - c1)
     c3 = f32_exact(pio64 - c1 - c2)
-    lines = ["// Generated by gen_df_tables.py — do not edit.",
+    lines = ["// Generated by gen_df_tables.py — do not edit.", "#pragma once",
              f"#define DF_PIO64_1 {_hexf(c1)}",
              f"#define DF_PIO64_2 {_hexf(c2)}",
              f"#define DF_PIO64_3 {_hexf(c3)}",
@@ -58,6 +63,19 @@ def main(out_dir):
         sh, sl = pair(mp.sin(j * pio64))
         ch, cl = pair(mp.cos(j * pio64))
         rows.append("    {" + ", ".join(_hexf(v) for v in (sh, sl, ch, cl)) + "}")
+    lines.append(", \\\n".join(rows))
+    d1 = float(pio64)
+    d2 = float(pio64 - mp.mpf(d1))
+    lines += [f"#define F64_PIO64_1 {float.hex(d1)}", f"#define F64_PIO64_2 {float.hex(d2)}",
+              f"#define F64_64_OVER_PI {float.hex(float(64 / mp.pi))}", "#define F64_TRIG_TAB_ROWS \\"]
+    rows = []
+    for j in range(128):
+        vals = []
+        for v in (mp.sin(j * pio64), mp.cos(j * pio64)):
+            hi = float(v) if abs(v) >= mp.mpf(2) ** -1000 else 0.0
+            lo = float(v - mp.mpf(hi)) if hi != 0.0 else 0.0
+            vals += [hi, lo]
+        rows.append("    {" + ", ".join(float.hex(x) for x in (vals[0], vals[2], vals[1], vals[3])) + "}")
     lines.append(", \\\n".join(rows))
     with open(os.path.join(out_dir, "df_tables.inc"), "w") as f:
         f.write("\n".join(lines) + "\n")

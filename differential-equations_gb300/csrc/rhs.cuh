@@ -12,6 +12,7 @@
 #include "dd_math.cuh"
 #include "df_math.cuh"
 #include "f32_math.cuh"
+#include "f64_tab_math.cuh"
 
 namespace degpu {
 
@@ -122,11 +123,14 @@ struct PrecFast {
     __device__ static __forceinline__ double rsqrt(double x) { return rsqrt_nr(x); }
 };
 // Plain FP64: FMA contraction, the refined hardware reciprocal and reciprocal square root in the
-// error norm and the controller, the CUDA math library's sin/cos, and the correctly rounded
-// controller power of the parity path; results differ from the crate's by rounding only.
+// error norm and the controller, the table-driven sin/cos of f64_tab_math.cuh (within one unit in
+// the last place, about 16 FP64 instructions), and the correctly rounded controller power of the
+// parity path; results differ from the crate's by rounding only.
 struct PrecPlain : PrecFast {
     static constexpr int ID = 3;
     __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl_neg(x, y); }
+    __device__ static __forceinline__ double sin(double x) { return f64t::sin(x); }
+    __device__ static __forceinline__ double cos(double x) { return f64t::cos(x); }
 };
 // Mixed: stages in FP32, y accumulated with Kahan compensation; the error terms, the norm, the
 // controller's power and the accept decision in FP32, t as an FP32 pair (see Lane).

@@ -19,12 +19,13 @@ FP = C.POINTER(C.c_float)
 @pytest.fixture(scope="module")
 def H():
     src = os.path.join(CSRC, "df_math_host.cpp")
-    deps = [src, os.path.join(CSRC, "df_math.cuh")]
+    deps = [src] + [os.path.join(CSRC, f) for f in ("df_math.cuh", "f64_tab_math.cuh", "df_tables.inc")]
     if not os.path.exists(SO) or any(os.path.getmtime(d) > os.path.getmtime(SO) for d in deps):
         subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", SO, src], check=True)
     h = C.CDLL(SO)
     h.degpu_host_df_sincos.argtypes = [FP, FP, O.DP, O.DP, C.c_int64]
     h.degpu_host_df_ops.argtypes = [FP, FP, FP, FP, FP, FP, O.DP, O.DP, C.c_int64]
+    h.degpu_host_f64t_sincos.argtypes = [O.DP, O.DP, O.DP, C.c_int64]
     h.degpu_host_df_stage_sum.argtypes = [FP, FP, FP, FP, FP, FP, C.c_int32, C.c_int32, O.DP, C.c_int64]
     return h
 
@@ -100,3 +101,19 @@ def test_pair_sin_cos(H, lo_, hi_):
     small = np.abs(xv) < 1e-2  # near zero sin keeps its relative accuracy
     if small.any():
         assert np.max(np.abs(s[small] - rs[small]) / np.abs(rs[small])) < 5e-12
+
+
+@pytest.mark.parametrize("lo_,hi_", [(-4.0, 4.0), (-60.0, 60.0), (-1e6, 1e6), (-1e-3, 1e-3)])
+def test_f64_table_sin_cos(H, lo_, hi_):
+    """The plain FP64 form's table-driven sin and cos: within one unit in the last place of the
+    correctly rounded value, and equal to it on at least 97 % of arguments."""
+    rng = np.random.default_rng(8)
+    n = 200_000
+    x = rng.uniform(lo_, hi_, n)
+    s, c = np.empty(n), np.empty(n)
+    H.degpu_host_f64t_sincos(O.p(x), O.p(s), O.p(c), n)
+    rs, rc = np.empty(n), np.empty(n)
+    O.lib().oracle_cr_sincos_batch(O.p(x), O.p(rs), O.p(rc), n)
+    for got, ref in ((s, rs), (c, rc)):
+        assert np.all(np.abs(got - ref) <= np.spacing(np.abs(ref)))
+        assert np.mean(got == ref) >= 0.97
