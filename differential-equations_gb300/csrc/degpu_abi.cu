@@ -85,6 +85,7 @@ void ensure_registered() {
         register_mixed_pair();
         register_round_dense_parity();
         register_round_dense_fast_mixed();
+        register_group_rounds();
     });
 }
 

@@ -59,8 +59,9 @@ struct df {
     DF_CTOR df(int x) : hi((float)x), lo(0.0f) {}
     // nearest pair to a double (a compile-time constant in the stage loops)
     DF_CTOR df(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
-    // FP32 bookkeeping (the norm, the controller, stiffness detection) reads the leading part
-    DF_CTOR operator float() const { return hi; }
+    // FP32 bookkeeping (the norm, the controller, stiffness detection) reads the leading part.
+    // Explicit, so that a function without a pair overload never takes a pair silently.
+    DF_CTOR explicit operator float() const { return hi; }
 };
 
 DF_HD df df_fast_two_sum(float a, float b) {
@@ -149,6 +150,10 @@ DF_HD float acc_end(float s) { return s; }
 DF_HD double acc_end(double s) { return s; }
 DF_HD df acc_end(dfacc s) { return df_fast_two_sum(s.hi, s.lo); }
 
+// The leading FP32 part (the FP32 bookkeeping's view of a stage value)
+DF_HD float lead(df x) { return x.hi; }
+DF_HD float lead(float x) { return x; }
+
 // The value of a pair as a double (exact: the sum of two FP32 numbers fits in 53 bits)
 DF_HD double to_f64(df x) { return (double)x.hi + (double)x.lo; }
 DF_HD double to_f64(float x) { return (double)x; }
@@ -232,6 +237,24 @@ DF_DEV df df_cos(df x) {
     a.lo = fmaf(C.hi, hq, a.lo);
     a.lo = fmaf(-S.hi, s, a.lo);
     return acc_end(a);
+}
+
+// sin and cos under their usual names for pairs only (a run-time right-hand side written as
+// `sin(y[0])` finds them by argument-dependent lookup when R is a pair).  They are templates that
+// accept nothing but a pair, so no other argument is ever converted to one.
+template <class T>
+struct df_only {};
+template <>
+struct df_only<df> {
+    using type = df;
+};
+template <class T>
+DF_DEV typename df_only<T>::type sin(T x) {
+    return df_sin(x);
+}
+template <class T>
+DF_DEV typename df_only<T>::type cos(T x) {
+    return df_cos(x);
 }
 
 }  // namespace degpu

@@ -64,6 +64,7 @@ struct EnsArgs {
     int32_t n_params;
     const int32_t* family;           // per-instance family id (multi-family persistent kernel)
     unsigned long long* ticket;      // persistent queue head
+    const int32_t* dims;             // per-instance dimension (ragged systems, serving rounds)
     // crossing and event detection (erk_cross_kernel), by cross_mode:
     //  0 component crossing: y[cross_comp] - cross_value changes sign;
     //  1 hyperplane crossing: sum_j (y[term_comp[j]] - term_a[j]) term_w[j], j < n_terms, with
@@ -456,8 +457,8 @@ struct Lane {
         // sk = atol + rtol * max(|y|, |y_new|); e/sk squared (traits.rs:402-407)
         if constexpr (P::F32_CTRL) {
             const float at = TV ? atolf_c(c, a) : atolf, rt = TV ? rtolf_c(c, a) : rtolf;
-            float sk = at + rt * fmaxf(fabsf(yv), fabsf(ynv));
-            float q = __fdividef(e, sk);
+            float sk = at + rt * fmaxf(fabsf(lead(yv)), fabsf(lead(ynv)));
+            float q = __fdividef(lead(e), sk);
             return q * q;
         } else {
             const double at = TV ? atol_c(c, a) : atol, rt = TV ? rtol_c(c, a) : rtol;
@@ -469,7 +470,9 @@ struct Lane {
 
     // ----- h_init: src/methods/h_init.rs:45-136 --------------------------------------------
     __device__ double initial_step(double t0, const EnsArgs& a) {
-        if constexpr (MIX) return initial_step_f32(t0, a);
+        if constexpr (MIX) {
+            return initial_step_f32(t0, a);
+        } else {
         double posneg = rs_signum(tf - t0);
         S f0[D], f1[D], y1[D];
         rhs(t0, y, f0);
@@ -513,6 +516,7 @@ struct Lane {
         double interval = fabs(tf - t0);
         hh = fmin(fmax(fmin(fmin(fabs(hh) * 100.0, h1), a.h_max), a.h_min), interval);
         return hh * posneg;
+        }
     }
 
     // The same heuristic in FP32 for the mixed form (the stage data are FP32; an FP64 version
@@ -527,10 +531,10 @@ struct Lane {
         float sk[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            sk[c] = atolf_c(c, a) + rtolf_c(c, a) * fabsf(y[c]);
-            float q = f0[c] / sk[c];
+            sk[c] = atolf_c(c, a) + rtolf_c(c, a) * fabsf(lead(y[c]));
+            float q = lead(f0[c]) / sk[c];
             dnf = dnf + q * q;
-            float r = y[c] / sk[c];
+            float r = lead(y[c]) / sk[c];
             dny = dny + r * r;
         }
         float hh;
@@ -548,7 +552,7 @@ struct Lane {
         float der2 = 0.0f;
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            float q = (f1[c] - f0[c]) / sk[c];
+            float q = lead(f1[c] - f0[c]) / sk[c];
             der2 = der2 + q * q;
         }
         der2 = sqrtf(der2) / fabsf(hh);
@@ -1204,7 +1208,8 @@ struct Lane {
         for (int c = 0; c < D; ++c) k[0][c] = k0[c];
         S ys[D];
         double drv[NS];  // DRV: the drive term at each stage's time
-        static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
+        // ys = y + sum_j (a_ij h) k_j for stage i
+        auto stage_state = [&](auto i) {
             AccT acc[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) acc[c] = acc_begin(y[c]);
@@ -1218,6 +1223,9 @@ struct Lane {
             });
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
+        };
+        static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
+            stage_state(i);
             if constexpr (MIX) {
                 rhs_at((float)Tab::c(i) * hf, ys, k[i]);
             } else if constexpr (DRV) {
@@ -1399,9 +1407,9 @@ struct Lane {
                     float sn = 0.0f, sd = 0.0f;
 #pragma unroll
                     for (int c = 0; c < D; ++c) {
-                        float d1 = yseg[c] - k[NS - 1][c];
+                        float d1 = lead(yseg[c] - k[NS - 1][c]);
                         sn = sn + d1 * d1;
-                        float d2 = dydt[c] - ys[c];
+                        float d2 = lead(dydt[c] - ys[c]);
                         sd = sd + d2 * d2;
                     }
                     den_pos = sd > 0.0f;
@@ -1989,7 +1997,13 @@ __global__ void __launch_bounds__(128, P::MULTI_MIN_BLOCKS) erk_multi_kernel(Ens
     int fam = cnt[2] >= cnt[1] && cnt[2] >= cnt[0] ? 2 : (cnt[1] >= cnt[0] ? 1 : 0);
     bool active = false, exhausted = false;
     for (;;) {
-        if (!active && !exhausted) {
+        // Lanes refill together: a lane's set-up (the initial-step heuristic, two right-hand
+        // sides and the norms) costs the warp the same issue time for one lane as for all, so
+        // finished lanes wait until DEGPU_REFILL_BATCH of them are idle (or the warp is) and then
+        // start their next instances in one pass.
+        const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
+        const bool refill = __popc(idle) >= DEGPU_REFILL_BATCH || __ballot_sync(0xffffffffu, active) == 0u;
+        if (refill && !active && !exhausted) {
             unsigned long long w = atomicAdd(&q.head[fam], 1ULL);
             if (w < (unsigned long long)cnt[fam]) {
                 int64_t inst = q.items[st[fam] + (int64_t)w];

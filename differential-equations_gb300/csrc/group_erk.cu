@@ -15,6 +15,10 @@ std::map<GroupKey, GroupLaunch>& group_registry() {
     static std::map<GroupKey, GroupLaunch> m;
     return m;
 }
+std::map<GroupKey, GroupRoundOps>& group_round_registry() {
+    static std::map<GroupKey, GroupRoundOps> m;
+    return m;
+}
 
 void register_group_fast() {
     reg_group<TabDop853, PrecFast, 8, 1>();
@@ -171,6 +175,38 @@ degpu_status group_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     if (cudaStreamSynchronize(s) != cudaSuccess && st == DEGPU_OK) st = DEGPU_CUDA_ERROR;
     for (void* p : to_free) cudaFreeAsync(p, s);
     return st;
+}
+
+}  // namespace degpu
+
+namespace degpu {
+
+degpu_status group_round_parts(const degpu_problem* pb, const degpu_method_cfg* cfg, const int32_t* dims_host,
+                               const double* rtol_host, int64_t n, int dense, std::vector<GroupRoundPart>& parts) {
+    parts.clear();
+    if (!dims_host || cfg->method == DEGPU_RK4) return DEGPU_UNSUPPORTED;
+    const double split = mixed_split(cfg);
+    std::map<std::tuple<int, int, int>, size_t> slot;
+    for (int64_t i = 0; i < n; ++i) {
+        const int d = dims_host[i];
+        if (d <= 0 || d > pb->dim || (d & 1)) return DEGPU_BAD_INPUT;
+        const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
+        const GroupChoice c = choose(cfg->method, prec, dense, d);
+        if (c.dmax < 0) return DEGPU_UNSUPPORTED;
+        const auto key = std::make_tuple(prec, c.g, c.cpl);
+        auto it = slot.find(key);
+        if (it == slot.end()) {
+            auto r = group_round_registry().find(GroupKey{cfg->method, prec, dense, c.g, c.cpl});
+            if (r == group_round_registry().end()) return DEGPU_UNSUPPORTED;
+            it = slot.emplace(key, parts.size()).first;
+            parts.push_back(GroupRoundPart{r->second, {}});
+        }
+        parts[it->second].idx.push_back(i);
+    }
+    // the largest systems first inside a part, as in group_solve
+    for (auto& p : parts)
+        std::stable_sort(p.idx.begin(), p.idx.end(), [&](int64_t x, int64_t y) { return dims_host[x] > dims_host[y]; });
+    return DEGPU_OK;
 }
 
 }  // namespace degpu

@@ -20,6 +20,7 @@
 
 #include <map>
 #include <tuple>
+#include <vector>
 
 #include "registry.cuh"
 #include "side_paths.cuh"
@@ -54,6 +55,15 @@ __device__ __forceinline__ void fpu_rhs(const typename P::S* sy, typename P::S* 
         }
     }
 }
+
+// Scalars of a group-per-system solve parked between serving rounds; the slot continues with the
+// lane-distributed vectors (GroupLane::park).
+struct GroupPark {
+    int32_t phase;  // 0 not started, 1 in progress, 2 finished
+    int32_t d, stiff, nonstiff, next_eval, status, last_rejected, pad;
+    int64_t inst, steps, acc, rej, fev;
+    double t, tf, h, h_prev, t_prev, dir, rtol, atol, beta;
+};
 
 template <class Tab, class P, int G, int CPL, bool DENSE>
 struct GroupLane {
@@ -538,6 +548,74 @@ struct GroupLane {
         if (fabs(tf - t) <= eps10) done = true;
     }
 
+    // Serving rounds: the state that lives across driver iterations — the scalars (written by
+    // lane 0) and, per component, y, its compensation and the derivative k0 at t (k[0] in shared
+    // memory).  Everything else a step reads is rebuilt inside the step.
+    __device__ void park(GroupPark& pk, S* vec) const {
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) {
+            const int c = lane + G * j;
+            if (c < d) {
+                vec[c] = y[j];
+                vec[DG + c] = yc[j];
+                vec[2 * DG + c] = k[c];
+            }
+        }
+        if (lane == 0) {
+            pk.d = d;
+            pk.stiff = stiff;
+            pk.nonstiff = nonstiff;
+            pk.next_eval = next_eval;
+            pk.status = status;
+            pk.last_rejected = last_rejected ? 1 : 0;
+            pk.inst = inst;
+            pk.steps = steps;
+            pk.acc = acc;
+            pk.rej = rej;
+            pk.fev = fev;
+            pk.t = t;
+            pk.tf = tf;
+            pk.h = h;
+            pk.h_prev = h_prev;
+            pk.t_prev = t_prev;
+            pk.dir = dir;
+            pk.rtol = rtol;
+            pk.atol = atol;
+            pk.beta = beta;
+        }
+    }
+    __device__ void resume(const GroupPark& pk, const S* vec) {
+        d = pk.d;
+        stiff = pk.stiff;
+        nonstiff = pk.nonstiff;
+        next_eval = pk.next_eval;
+        status = pk.status;
+        last_rejected = pk.last_rejected != 0;
+        done = false;
+        inst = pk.inst;
+        steps = pk.steps;
+        acc = pk.acc;
+        rej = pk.rej;
+        fev = pk.fev;
+        t = pk.t;
+        tf = pk.tf;
+        h = pk.h;
+        h_prev = pk.h_prev;
+        t_prev = pk.t_prev;
+        dir = pk.dir;
+        rtol = pk.rtol;
+        atol = pk.atol;
+        beta = pk.beta;
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) {
+            const int c = lane + G * j;
+            y[j] = c < d ? vec[c] : (S)0;
+            yc[j] = c < d ? vec[DG + c] : (S)0;
+            if (c < d) k[c] = vec[2 * DG + c];
+        }
+        sync();
+    }
+
     __device__ void finish(const EnsArgs& a) const {
         const int64_t n = a.n;
 #pragma unroll
@@ -593,6 +671,94 @@ __global__ void __launch_bounds__(128) erk_group_kernel(GroupArgs ga) {
     }
 }
 
+// Bytes of one parked system: the scalars, then y, its compensation and k0 over DG components.
+template <class Tab, class P, int G, int CPL>
+__host__ __device__ constexpr size_t group_park_bytes() {
+    return ((sizeof(GroupPark) + 15) / 16) * 16 + (size_t)3 * G * CPL * sizeof(typename P::S);
+}
+
+// Resumable form of erk_group_kernel for the server: every work item is visited once per round;
+// a visit starts the system (phase 0) or resumes its parked state, runs at most `budget` driver
+// iterations, then parks it again or finishes it.  `done_count` counts finished systems across
+// rounds.  Slot w of `park` holds work item w (instance a.index[w] when an index list is given).
+template <class Tab, class P, int G, int CPL, bool DENSE>
+__global__ void __launch_bounds__(128) erk_group_round_kernel(GroupArgs ga, unsigned char* park, int budget,
+                                                              unsigned long long* done_count) {
+    using GL = GroupLane<Tab, P, G, CPL, DENSE>;
+    using S = typename P::S;
+    constexpr int DG = G * CPL;
+    constexpr size_t slot_bytes = group_park_bytes<Tab, P, G, CPL>();
+    constexpr size_t scal_bytes = ((sizeof(GroupPark) + 15) / 16) * 16;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int gid = threadIdx.x / G;
+    constexpr size_t per = group_smem_per_system<Tab, P, G, CPL, DENSE>();
+    unsigned char* base = smem + per * gid;
+    GL L;
+    L.k = (S*)base;
+    L.sy = L.k + Tab::I * DG;
+    L.cont = L.sy + DG;
+    L.red = (double*)(base + (size_t)(Tab::I + 1 + (DENSE ? Tab::ORDER : 0)) * DG * sizeof(S));
+    L.lane = threadIdx.x % G;
+    const int wlane = threadIdx.x % 32;
+    L.gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (wlane / G * G));
+    const EnsArgs& a = ga.a;
+    for (;;) {
+        unsigned long long w = 0;
+        if (L.lane == 0) w = atomicAdd(a.ticket, 1ULL);
+        w = __shfl_sync(L.gmask, w, 0, G);
+        if (w >= (unsigned long long)a.count) break;
+        GroupPark& pk = *reinterpret_cast<GroupPark*>(park + w * slot_bytes);
+        S* vec = reinterpret_cast<S*>(park + w * slot_bytes + scal_bytes);
+        const int phase = pk.phase;
+        __syncwarp(L.gmask);  // every lane has read the phase before lane 0 may rewrite it
+        if (phase == 2) continue;
+        if (phase == 0)
+            L.begin(a.index ? a.index[w] : (int64_t)w, ga);
+        else
+            L.resume(pk, vec);
+        for (int it = 0; it < budget && !L.done; ++it) L.iterate(a);
+        if (L.done) {
+            L.finish(a);
+            if (L.lane == 0) {
+                pk.phase = 2;
+                atomicAdd(done_count, 1ULL);
+            }
+        } else {
+            L.park(pk, vec);
+            if (L.lane == 0) pk.phase = 1;
+        }
+        __syncwarp(L.gmask);
+    }
+}
+
+template <class Tab, class P, int G, int CPL, bool DENSE>
+cudaError_t launch_group_round(const EnsArgs& a, void* park, int budget, unsigned long long* done, int max_blocks,
+                               cudaStream_t s) {
+    auto kern = erk_group_round_kernel<Tab, P, G, CPL, DENSE>;
+    constexpr size_t per = group_smem_per_system<Tab, P, G, CPL, DENSE>();
+    const int threads = 128;
+    const size_t smem = per * (threads / G);
+    if (a.count <= 0) return cudaSuccess;
+    static int blocks_per_sm = -1;
+    if (blocks_per_sm < 0) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, threads, smem);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
+    }
+    long long grid = (long long)blocks_per_sm * device_sm_count();
+    long long need = (a.count * G + threads - 1) / threads;
+    if (grid > need) grid = need;
+    if (max_blocks > 0 && grid > max_blocks) grid = max_blocks;
+    if (grid < 1) grid = 1;
+    GroupArgs ga;
+    ga.a = a;
+    ga.dims = a.dims;
+    kern<<<(unsigned)grid, threads, smem, s>>>(ga, (unsigned char*)park, budget, done);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------------------------
@@ -635,7 +801,35 @@ void reg_group() {
     group_registry()[GroupKey{method_id<Tab>(), P::ID, 1, G, CPL}] = &launch_group<Tab, P, G, CPL, true>;
 }
 
+// Resumable group kernels of the server, keyed like group_registry: bytes per parked system and
+// the round launcher (the signature of the other round kernels, dims in EnsArgs).
+struct GroupRoundOps {
+    size_t park_bytes;
+    cudaError_t (*launch)(const EnsArgs& a, void* park, int budget, unsigned long long* done, int max_blocks,
+                          cudaStream_t s);
+};
+std::map<GroupKey, GroupRoundOps>& group_round_registry();
+
+template <class Tab, class P, int G, int CPL>
+void reg_group_round() {
+    group_round_registry()[GroupKey{method_id<Tab>(), P::ID, 0, G, CPL}] =
+        GroupRoundOps{group_park_bytes<Tab, P, G, CPL>(), &launch_group_round<Tab, P, G, CPL, false>};
+    group_round_registry()[GroupKey{method_id<Tab>(), P::ID, 1, G, CPL}] =
+        GroupRoundOps{group_park_bytes<Tab, P, G, CPL>(), &launch_group_round<Tab, P, G, CPL, true>};
+}
+
+// The work of a ragged request split for the resumable group kernels: one part per (precision,
+// G, CPL) bucket, with its instances (the host copies of dims and rtol are read).  DEGPU_OK when
+// every bucket has a round kernel.
+struct GroupRoundPart {
+    GroupRoundOps ops;
+    std::vector<int64_t> idx;
+};
+degpu_status group_round_parts(const degpu_problem* pb, const degpu_method_cfg* cfg, const int32_t* dims_host,
+                               const double* rtol_host, int64_t n, int dense, std::vector<GroupRoundPart>& parts);
+
 void register_group_parity();
 void register_group_fast();
+void register_group_rounds();
 
 }  // namespace degpu

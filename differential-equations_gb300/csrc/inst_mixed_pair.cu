@@ -11,5 +11,8 @@ void register_mixed_pair() {
     register_round<TabDopri5, RhsLorenz, PrecMixedPair>();
     register_round<TabDopri5, RhsVanDerPol, PrecMixedPair>();
     register_round<TabDopri5, RhsPendulum, PrecMixedPair>();
+    register_round<TabDopri5, RhsLorenz, PrecMixedPair, true>();
+    register_round<TabDopri5, RhsVanDerPol, PrecMixedPair, true>();
+    register_round<TabDopri5, RhsPendulum, PrecMixedPair, true>();
 }
 }  // namespace degpu

@@ -22,6 +22,14 @@ namespace degpu {
 #ifndef DEGPU_MIXED_MIN_BLOCKS
 #define DEGPU_MIXED_MIN_BLOCKS 1
 #endif
+// The same for the FP32-pair stage kernels (PrecMixedPair).
+#ifndef DEGPU_PAIR_MIN_BLOCKS
+#define DEGPU_PAIR_MIN_BLOCKS 1
+#endif
+// Lanes of the multi-family persistent kernel refill in batches of at least this many.
+#ifndef DEGPU_REFILL_BATCH
+#define DEGPU_REFILL_BATCH 4
+#endif
 // Mixed form's sin/cos: 0 uses f32_math.cuh, 1 the CUDA library's sinf/cosf.
 #ifndef DEGPU_MIXED_LIBM_TRIG
 #define DEGPU_MIXED_LIBM_TRIG 0
@@ -187,6 +195,7 @@ struct PrecMixedPair : PrecMixed {
     using PS = df;
     static constexpr bool PAIR = true;
     static constexpr int ID = 5;
+    static constexpr int MULTI_MIN_BLOCKS = DEGPU_PAIR_MIN_BLOCKS;
     __device__ static __forceinline__ df sin(df x) { return df_sin(x); }
     __device__ static __forceinline__ df cos(df x) { return df_cos(x); }
     __device__ static __forceinline__ S from(double x) { return df(x); }

@@ -12,9 +12,10 @@
 // Rounds are bounded (`round_budget` driver iterations per instance), so the GPU is shared
 // between the requests in flight and a new request starts within one round of being admitted.
 // Requests with output times run round kernels that also write them (the times sorted once, as
-// TEvalSolout::new sorts them).  Requests the round kernels do not cover (ragged FPU chains,
-// run-time families, family maps) are solved with one degpu_solve_ensemble call on the request's
-// stream.
+// TEvalSolout::new sorts them).  Ragged FPU-beta requests run the resumable group kernels, one
+// round kernel per (precision, layout) bucket.  Requests the round kernels do not cover (run-time
+// families, family maps, parity-form chains) are solved with one degpu_solve_ensemble call on the
+// request's stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,6 +29,7 @@
 #include <thread>
 #include <vector>
 
+#include "group_erk.cuh"
 #include "registry.cuh"
 
 namespace degpu {
@@ -45,24 +47,25 @@ struct SrvRequest {
     degpu_status result = DEGPU_OK;
     size_t bytes = 0;
     bool resumable = false;
-    RoundOps ops{};
-    // mixed request split by rtol (degpu_set_mixed_min_rtol): idx[0] runs `ops`, idx[1] the
-    // FP64_FAST round kernels `ops64`, each with its own resident state and work ticket
-    bool split = false;
-    std::vector<int64_t> idx[2];
-    RoundOps ops64{};
-    EnsArgs args64{};
-    void* park64 = nullptr;
-    unsigned long long* ticket64 = nullptr;
+    // The round kernels of a resumable request, each over its own instances with its own
+    // resident state and work ticket: one part for a plain request; a mixed request whose rtol
+    // values straddle the mixed-precision bound has a second part (the tight class); a ragged
+    // request has one part per (precision, layout) bucket of the group kernels.  An empty index
+    // list means every instance.
+    struct Part {
+        RoundOps ops{};
+        std::vector<int64_t> idx;
+        EnsArgs args{};
+        void* park = nullptr;
+        unsigned long long* ticket = nullptr;
+    };
+    std::vector<Part> parts;
     // device side
     cudaStream_t stream = nullptr;
     cudaEvent_t ev = nullptr;
     char* dblock = nullptr;
     degpu_batch_in din{};
     degpu_batch_out dout{};
-    EnsArgs args{};
-    void* park = nullptr;
-    unsigned long long* ticket = nullptr;
     unsigned long long* done_dev = nullptr;
     unsigned long long* done_host = nullptr;  // pinned
     // output times of a resumable request: ascending, with the permutation to the caller's order
@@ -93,10 +96,12 @@ struct ServerImpl {
         b += align(m * 8) + align(m * d * n * 8) + align(m * 4);
         if (r.in.rtol_vec) b += align(d * n * 8);
         if (r.in.atol_vec) b += align(d * n * 8);
-        if (r.resumable && !r.split) b += align(n * r.ops.park_bytes) + 512;
-        if (r.split) {
-            b += align(r.idx[0].size() * 8) + align(r.idx[1].size() * 8);
-            b += align(r.idx[0].size() * r.ops.park_bytes) + align(r.idx[1].size() * r.ops64.park_bytes) + 1024;
+        if (r.resumable) {
+            b += 512;  // done counter
+            for (const auto& pt : r.parts) {
+                const size_t cnt = pt.idx.empty() ? n : pt.idx.size();
+                b += align(pt.idx.size() * 8) + align(cnt * pt.ops.park_bytes) + 256;
+            }
         }
         return b;
     }
@@ -145,14 +150,9 @@ struct ServerImpl {
             }
             return true;
         }
-        const size_t n0 = r.split ? r.idx[0].size() : n;
-        r.park = take(n0 * r.ops.park_bytes);
-        r.ticket = (unsigned long long*)take(16);
         r.done_dev = (unsigned long long*)take(16);
-        cudaMemsetAsync(r.park, 0, n0 * r.ops.park_bytes, s);  // phase 0: not started
         cudaMemsetAsync(r.done_dev, 0, 8, s);
-        EnsArgs& a = r.args;
-        a = EnsArgs{};
+        EnsArgs a{};
         a.n = (int64_t)n;
         a.count = (int64_t)n;
         a.t0 = r.din.t0;
@@ -182,7 +182,7 @@ struct ServerImpl {
         a.max_scale_f = (float)a.max_scale;
         a.dense_mode = r.cfg.dense_mode;
         a.n_params = r.pb.n_params;
-        a.ticket = r.ticket;
+        a.dims = r.din.dims;
         if (!r.te_sorted.empty()) {
             // the sorted output times over the caller's copy, their permutation, NaN outputs
             a.n_eval = (int32_t)m;
@@ -192,29 +192,25 @@ struct ServerImpl {
             a.dense = r.dout.dense;
             cudaMemsetAsync(a.dense, 0xFF, m * d * n * 8, s);  // 0xFF bytes form a quiet NaN
         }
-        if (r.split) {
-            const size_t n1 = r.idx[1].size();
-            a.index = (const int64_t*)up(r.idx[0].data(), n0 * 8);
-            a.count = (int64_t)n0;
-            r.args64 = a;
-            r.args64.index = (const int64_t*)up(r.idx[1].data(), n1 * 8);
-            r.args64.count = (int64_t)n1;
-            r.park64 = take(n1 * r.ops64.park_bytes);
-            r.ticket64 = (unsigned long long*)take(16);
-            r.args64.ticket = r.ticket64;
-            cudaMemsetAsync(r.park64, 0, n1 * r.ops64.park_bytes, s);
+        for (auto& pt : r.parts) {
+            const size_t cnt = pt.idx.empty() ? n : pt.idx.size();
+            pt.args = a;
+            if (!pt.idx.empty()) pt.args.index = (const int64_t*)up(pt.idx.data(), cnt * 8);
+            pt.args.count = (int64_t)cnt;
+            pt.park = take(cnt * pt.ops.park_bytes);
+            pt.ticket = (unsigned long long*)take(16);
+            pt.args.ticket = pt.ticket;
+            cudaMemsetAsync(pt.park, 0, cnt * pt.ops.park_bytes, s);  // phase 0: not started
         }
         return launch_round(r);
     }
 
     bool launch_round(SrvRequest& r) {
         cudaStream_t s = r.stream;
-        if (r.split) {
-            if (cudaMemsetAsync(r.ticket64, 0, 8, s) != cudaSuccess) return false;
-            if (r.ops64.launch(r.args64, r.park64, cfg.round_budget, r.done_dev, 0, s) != cudaSuccess) return false;
+        for (auto& pt : r.parts) {
+            if (cudaMemsetAsync(pt.ticket, 0, 8, s) != cudaSuccess) return false;
+            if (pt.ops.launch(pt.args, pt.park, cfg.round_budget, r.done_dev, 0, s) != cudaSuccess) return false;
         }
-        if (cudaMemsetAsync(r.ticket, 0, 8, s) != cudaSuccess) return false;
-        if (r.ops.launch(r.args, r.park, cfg.round_budget, r.done_dev, 0, s) != cudaSuccess) return false;
         cudaMemcpyAsync(r.done_host, r.done_dev, 8, cudaMemcpyDeviceToHost, s);
         cudaEventRecord(r.ev, s);
         return true;
@@ -363,12 +359,14 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
     r->out = *out;
     r->t_submit = Clock::now();
     const bool plain = !in->family && !in->dims && pb->rhs_id < DEGPU_RHS_NVRTC_BASE;
+    const bool ragged = !in->family && in->dims && pb->rhs_id == DEGPU_RHS_FPU_BETA;
     const int dense = (in->n_eval > 0 && in->t_eval && out->dense) ? 1 : 0;
     if (plain) {
         auto it = round_registry().find(VariantKey{cfg->method, pb->rhs_id, cfg->precision, dense});
         if (it != round_registry().end()) {
             r->resumable = true;
-            r->ops = it->second;
+            r->parts.resize(1);
+            r->parts[0].ops = it->second;
         }
         // a mixed request whose rtol values straddle the mixed-precision bound: the instances
         // below it run the FP32-pair round kernels where built, else the FP64_FAST ones
@@ -378,15 +376,28 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
             it64 = round_registry().find(VariantKey{cfg->method, pb->rhs_id, DEGPU_FP64_FAST, dense});
         if (r->resumable && bound > 0.0) {
             if (it64 == round_registry().end()) return DEGPU_UNSUPPORTED;
-            for (int64_t i = 0; i < in->n; ++i) r->idx[in->rtol[i] < bound ? 1 : 0].push_back(i);
-            if (r->idx[1].empty()) {
-                r->idx[0].clear();
-            } else if (r->idx[0].empty()) {
-                r->ops = it64->second;  // every instance below the bound: a plain FP64_FAST request
-                r->idx[1].clear();
-            } else {
-                r->split = true;
-                r->ops64 = it64->second;
+            std::vector<int64_t> idx[2];
+            for (int64_t i = 0; i < in->n; ++i) idx[in->rtol[i] < bound ? 1 : 0].push_back(i);
+            if (idx[0].empty()) {
+                r->parts[0].ops = it64->second;  // every instance below the bound
+            } else if (!idx[1].empty()) {
+                r->parts[0].idx = std::move(idx[0]);
+                r->parts.push_back(SrvRequest::Part{});
+                r->parts[1].ops = it64->second;
+                r->parts[1].idx = std::move(idx[1]);
+            }
+        }
+    } else if (ragged && in->n_eval >= 0) {
+        // FPU-beta chains: resumable group kernels, one part per (precision, layout) bucket;
+        // anything the round kernels do not cover is solved in one piece instead
+        std::vector<GroupRoundPart> gp;
+        if (group_round_parts(pb, cfg, in->dims, in->rtol, in->n, dense, gp) == DEGPU_OK) {
+            r->resumable = true;
+            for (auto& g : gp) {
+                SrvRequest::Part pt;
+                pt.ops = RoundOps{g.ops.park_bytes, g.ops.launch};
+                if (gp.size() > 1 || g.idx.size() != (size_t)in->n) pt.idx = std::move(g.idx);
+                r->parts.push_back(std::move(pt));
             }
         }
     }

@@ -54,6 +54,28 @@ def requests():
     f.tf[:] = 5.0
     reqs.append(dict(rhs=abi.RHS["FPU_BETA"], dim=f.dim, e=f, m=method(abi.DOP853, abi.FP64_PARITY), dims=f.dims,
                      t_eval=np.linspace(0, 5, 6)))
+    # ragged FPU-chain requests on the resumable group kernels: FP64 fast with output times, and
+    # mixed with rtol values straddling the bounds of DOP853 (FP32 stages / FP64 fast parts) and
+    # DOPRI5, so that one request runs several round kernels (one per precision and layout)
+    for k, (m, prec, te) in enumerate(((abi.DOP853, abi.FP64_FAST, np.linspace(0, 5, 6)),
+                                       (abi.DOP853, abi.MIXED, None),
+                                       (abi.DOPRI5, abi.MIXED, np.linspace(0, 4, 5)))):
+        f = W.config2(n=48, first=500 * (k + 1))
+        f.tf[:] = 4.0 + k
+        if prec == abi.MIXED:
+            f.rtol = W.logU(11, np.arange(f.n), 1, 1e-9, 1e-5)
+            f.atol = 1e-2 * f.rtol
+            assert 0 < (f.rtol < degpu.mixed_min_rtol(m)).sum() < f.n
+        reqs.append(dict(rhs=abi.RHS["FPU_BETA"], dim=f.dim, e=f, m=method(m, prec), dims=f.dims, t_eval=te))
+    # mixed requests with output times that straddle the DOPRI5 bound (the dense round kernels,
+    # FP32 stages above the bound and FP32-pair stages below)
+    for fam, dim in ((abi.RHS["PENDULUM"], 2), (abi.RHS["LORENZ"], 3)):
+        e = W.config1(n=900, first=77_000)
+        e = e.subset(np.nonzero(e.family == fam)[0])
+        e.tf = np.minimum(e.tf, 5.0)
+        e.rtol = W.logU(12, np.arange(e.n), 1, 1e-9, 1e-5)
+        e.atol = 1e-2 * e.rtol
+        reqs.append(dict(rhs=fam, dim=dim, e=e, m=method(abi.DOPRI5, abi.MIXED), t_eval=np.linspace(5, 0, 11)))
     return reqs
 
 
