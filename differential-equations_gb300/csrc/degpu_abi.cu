@@ -514,7 +514,12 @@ static degpu_status crossing_impl(const degpu_problem* pb, const degpu_method_cf
     std::map<std::pair<int, int>, std::vector<int64_t>> lists;
     for (int64_t i = 0; i < n; ++i) {
         const int fam = in->family ? fam_host[i] : pb->rhs_id;
-        const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
+        int prec = cfg->precision;
+        if (split > 0.0 && rtol_host[i] < split) {
+            // the tight class: FP32-pair stages where built for this family, else FP64 fast
+            prec = mixed_low_precision(cfg);
+            if (!cross_registry().count(VariantKey{cfg->method, fam, prec, 1})) prec = DEGPU_FP64_FAST;
+        }
         lists[{fam, prec}].push_back(i);
     }
     for (auto& kv : lists) {

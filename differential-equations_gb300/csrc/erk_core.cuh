@@ -828,13 +828,13 @@ struct Lane {
     // The mixed form's offset at the step's end in FP32: (y - compensation) against the FP32 copies
     // of the threshold or plane.
     __device__ __forceinline__ float state_offset_f32(const EnsArgs& a) const {
-        if (a.cross_mode == 0) return (comp_s(y, a.cross_comp) - a.cross_value_f) - comp_s(yc, a.cross_comp);
+        if (a.cross_mode == 0) return lead((comp_s(y, a.cross_comp) - a.cross_value_f) - comp_s(yc, a.cross_comp));
         float sum = 0.0f;
 #pragma unroll
         for (int j = 0; j < DEGPU_HYPERPLANE_MAX_DIM; ++j)
             if (j < a.n_terms) {
                 const int c = a.term_comp[j];
-                sum += ((comp_s(y, c) - a.term_a_f[j]) - comp_s(yc, c)) * a.term_w_f[j];
+                sum += lead((comp_s(y, c) - a.term_a_f[j]) - comp_s(yc, c)) * a.term_w_f[j];
             }
         return sum;
     }
