@@ -11,6 +11,7 @@
 // the mixed kernel after it; or, for the run-to-completion layout, one launch per list.
 // Ordering inside a bucket follows the atomics and is not deterministic; every instance's result
 // is independent of the order in which instances are taken, so solutions are deterministic.
+#include <mutex>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -109,6 +110,19 @@ static degpu_status run_plan(const degpu_method_cfg* cfg, const EnsArgs& a, cons
     return cudaGetLastError() == cudaSuccess ? DEGPU_OK : DEGPU_CUDA_ERROR;
 }
 
+// One non-blocking helper stream per device (created on first use) for the second class of a
+// split solve.
+static cudaStream_t helper_stream() {
+    static std::mutex mu;
+    static cudaStream_t per_dev[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> g(mu);
+    if (!per_dev[dev] && cudaStreamCreateWithFlags(&per_dev[dev], cudaStreamNonBlocking) != cudaSuccess)
+        per_dev[dev] = nullptr;
+    return per_dev[dev];
+}
+
 // Plans and launches one multi-family persistent solve (two launches when a mixed solve splits
 // by rtol).  Returns DEGPU_UNSUPPORTED when no kernel is registered for the combination.
 degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* family_dev, int fam_const,
@@ -128,12 +142,34 @@ degpu_status multi_solve(const degpu_method_cfg* cfg, const EnsArgs& a, const in
     const int64_t n = a.n;
     Plan pl;
     degpu_status st = run_plan(cfg, a, family_dev, fam_const, split, pl, s);
-    // class 1 (FP64) lists: start/count/head [3..6); class 0: [0..3)
+    // class 1 (tight) lists: start/count/head [3..6); class 0: [0..3)
     if (st == DEGPU_OK && fp64_launch) {
-        MultiQueue q{pl.items, pl.start + 3, pl.count + 3, pl.head + 3};
-        if (fp64_launch(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
-    }
-    if (st == DEGPU_OK) {
+        // The two classes run concurrently: the second launch goes to a helper stream that waits
+        // for the plan, so its blocks take the SMs the first launch frees at its tail; the
+        // caller's stream then waits for both.
+        cudaStream_t s2 = helper_stream();
+        cudaEvent_t planned = nullptr, second = nullptr;
+        if (!s2 || cudaEventCreateWithFlags(&planned, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&second, cudaEventDisableTiming) != cudaSuccess) {
+            s2 = s;  // no helper: one after the other on the caller's stream
+        } else if (cudaEventRecord(planned, s) != cudaSuccess || cudaStreamWaitEvent(s2, planned, 0) != cudaSuccess) {
+            st = DEGPU_CUDA_ERROR;
+        }
+        if (st == DEGPU_OK) {
+            MultiQueue q{pl.items, pl.start + 3, pl.count + 3, pl.head + 3};
+            if (fp64_launch(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
+        }
+        if (st == DEGPU_OK) {
+            MultiQueue q{pl.items, pl.start, pl.count, pl.head};
+            if (it->second(a, q, n, s2) != cudaSuccess) st = DEGPU_CUDA_ERROR;
+        }
+        if (s2 != s && second) {
+            if (cudaEventRecord(second, s2) != cudaSuccess || cudaStreamWaitEvent(s, second, 0) != cudaSuccess)
+                st = DEGPU_CUDA_ERROR;
+        }
+        if (planned) cudaEventDestroy(planned);
+        if (second) cudaEventDestroy(second);
+    } else if (st == DEGPU_OK) {
         MultiQueue q{pl.items, pl.start, pl.count, pl.head};
         if (it->second(a, q, n, s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
     }
