@@ -356,15 +356,25 @@ struct Lane {
     }
     // Right-hand side at t + dt in the mixed form: a family with a drive phase adds Omega dt to
     // the phase at t in FP32; the others get the stage time t + dt (unused by autonomous ones).
-    __device__ __forceinline__ void rhs_at(float dt, const S* yy, S* dd) const {
+    // DT: FP32, or for pair stages the stage's offset c_i h as a pair (so that a time-dependent
+    // right-hand side sees the stage time to the pairs' accuracy, not to FP32 rounding).
+    template <class DT>
+    __device__ __forceinline__ void rhs_at(DT dt, const S* yy, S* dd) const {
         if constexpr (PHASE) {
             if constexpr (P::PAIR)
                 Rhs::template diff_phase<P>(df(ph0, phl), dt, yy, dd, pf);  // the phase pair
             else
                 Rhs::template diff_phase<P>(ph0, dt, yy, dd, pf);
         } else {
-            rhs(tnow() + (double)dt, yy, dd);
+            rhs(tnow() + to_f64(dt), yy, dd);
         }
+    }
+    // c_i h of a stage: FP32 for the FP32 stages, a pair for the pair stages
+    __device__ __forceinline__ auto stage_offset(double ci) const {
+        if constexpr (P::PAIR)
+            return df(ci) * hf;
+        else
+            return (float)ci * hf;
     }
 
     // The drive phase at tt outside FFT: reduced to [-pi, pi] in FP64; pair stages keep it as an
@@ -1227,7 +1237,7 @@ struct Lane {
         static_for<1, (FSAL_MIX ? NS - 1 : NS)>([&](auto i) {
             stage_state(i);
             if constexpr (MIX) {
-                rhs_at((float)Tab::c(i) * hf, ys, k[i]);
+                rhs_at(stage_offset(Tab::c(i)), ys, k[i]);
             } else if constexpr (DRV) {
                 constexpr int i0 = first_stage_at_c<Tab>(decltype(i)::value);
                 if constexpr (i0 == decltype(i)::value)
@@ -1550,7 +1560,7 @@ struct Lane {
 #pragma unroll
                     for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
                     if constexpr (MIX)
-                        rhs_at((float)Tab::c(i) * hf, ys, k[i]);
+                        rhs_at(stage_offset(Tab::c(i)), ys, k[i]);
                     else
                         rhs(t + Tab::c(i) * h, ys, k[i]);
                     fev += 1;
@@ -1607,7 +1617,7 @@ struct Lane {
 #pragma unroll
             for (int c = 0; c < D; ++c) ys[c] = acc_end(acc[c]);
             if constexpr (MIX)
-                rhs_at((float)Tab::c(i) * hf, ys, k[i]);
+                rhs_at(stage_offset(Tab::c(i)), ys, k[i]);
             else
                 rhs(t + Tab::c(i) * h, ys, k[i]);
         };

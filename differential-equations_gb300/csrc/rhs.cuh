@@ -22,9 +22,10 @@ namespace degpu {
 #ifndef DEGPU_MIXED_MIN_BLOCKS
 #define DEGPU_MIXED_MIN_BLOCKS 1
 #endif
-// The same for the FP32-pair stage kernels (PrecMixedPair).
+// The same for the FP32-pair stage kernels (PrecMixedPair): three blocks of 128 per SM fit the
+// register file without spills (measured: four blocks gained nothing, five spill).
 #ifndef DEGPU_PAIR_MIN_BLOCKS
-#define DEGPU_PAIR_MIN_BLOCKS 1
+#define DEGPU_PAIR_MIN_BLOCKS 3
 #endif
 // Lanes of the multi-family persistent kernel refill in batches of at least this many.
 #ifndef DEGPU_REFILL_BATCH
@@ -248,9 +249,10 @@ struct RhsPendulum : BuiltinRhs {
         double k = rint(ph * 0.15915494309189535);
         return (float)fma(-k, 6.283185307179586, ph);
     }
-    // PH: float, or an FP32 pair (the phase and its low part) for pair stages
-    template <class P, class PH>
-    __device__ static __forceinline__ void diff_phase(PH ph0, float dt, const typename P::S* y, typename P::S* dydt,
+    // PH: float, or an FP32 pair (the phase and its low part) for pair stages; DT: the stage offset
+    // c_i h, FP32 or a pair
+    template <class P, class PH, class DT>
+    __device__ static __forceinline__ void diff_phase(PH ph0, DT dt, const typename P::S* y, typename P::S* dydt,
                                                       const typename P::PS* pf) {
         using S = typename P::S;
         S theta = y[0], omega = y[1];
