@@ -628,8 +628,8 @@ def fpu_step_ops(dims, accepted, rejected):
 def run_fpu(args, torch, dev, lib, n=None, emit=True):
     """FPU-beta chains (2..128 masses), DOP853 rtol=1e-10 atol=1e-12 on [0,100] with 64 output
     times: group-per-system kernel, FP64 parity, FP64 fast and the library's mixed form (whose
-    precision bound runs rtol 1e-10 in FP64); energy drift from the dense output; CPU oracle on a
-    sample.  With `n`, the first n chains of the 131,072."""
+    precision bound runs rtol 1e-10 in its tight class, FP32-pair stages); energy drift from the
+    dense output; CPU oracle on a sample.  With `n`, the first n chains of the 131,072."""
     n = n or args.fpu_n
     e = W.config2(n=n)
     stream = torch.cuda.Stream(device=dev)
@@ -669,7 +669,7 @@ def run_fpu(args, torch, dev, lib, n=None, emit=True):
                      "step_attempts": int((out["accepted"] + out["rejected"]).sum().item()),
                      "fp64_algorithmic_frac": ops / (ms * 1e-3) / 1e12 / fp64_peak if name != "mixed-nosplit" else None,
                      "status_counts": {str(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}}
-        res[name]["fp64_chains"] = int((e.rtol < (0.0 if nosplit else bound)).sum()) if prec == abi.MIXED else n
+        res[name]["tight_class_chains"] = int((e.rtol < (0.0 if nosplit else bound)).sum()) if prec == abi.MIXED else 0
         if emit:
             print(json.dumps({"fpu_variant": name, **res[name]}), flush=True)
         if name == "fp64":
@@ -879,8 +879,10 @@ def run_serving(args, torch, dev, lib):
         print(json.dumps({"serving_run": prec, **r}), flush=True)
         return r, kept
 
-    for prec_name, prec, fracs in (("mixed", abi.MIXED, args.serving_fracs_mixed),
-                                   ("fp64", abi.FP64_FAST, args.serving_fracs_fp64)):
+    runs = [("mixed", abi.MIXED, args.serving_fracs_mixed)]
+    if args.serving_fracs_fp64 != "skip":
+        runs.append(("fp64", abi.FP64_FAST, args.serving_fracs_fp64))
+    for prec_name, prec, fracs in runs:
         sat, kept = run(prec, 0.0, keep=prec == abi.MIXED)
         cap = sat["requests_per_s"]
         sweep = []
@@ -1015,7 +1017,7 @@ def main():
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--serving-fracs-mixed", default="0.25,0.5,0.75,0.9,1.0",
                     help="arrival rates of the serving sweep as fractions of the saturated capacity")
-    ap.add_argument("--serving-fracs-fp64", default="0.5,0.9")
+    ap.add_argument("--serving-fracs-fp64", default="0.5,0.9", help='"skip": the mixed server only')
     ap.add_argument("--profile-family", default="", choices=["", "VAN_DER_POL", "PENDULUM", "LORENZ"],
                     help="with --profile-case: keep only this family's instances")
     ap.add_argument("--profile-case", type=int, default=0,

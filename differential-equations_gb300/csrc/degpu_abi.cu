@@ -85,7 +85,8 @@ void ensure_registered() {
         register_mixed_pair();
         register_round_dense_parity();
         register_round_dense_fast_mixed();
-        register_group_rounds();
+        register_groups();
+        register_mixed_pair853();
     });
 }
 
@@ -153,7 +154,8 @@ double mixed_split(const degpu_method_cfg* cfg) {
 
 int mixed_low_precision(const degpu_method_cfg* cfg) {
     const bool mixed = cfg->precision == DEGPU_MIXED || cfg->precision == DEGPU_MIXED_FP64_CTRL;
-    return (mixed && cfg->method == DEGPU_DOPRI5) ? PrecMixedPair::ID : DEGPU_FP64_FAST;
+    return (mixed && (cfg->method == DEGPU_DOPRI5 || cfg->method == DEGPU_DOP853)) ? PrecMixedPair::ID
+                                                                                 : DEGPU_FP64_FAST;
 }
 
 static bool valid_prec(int p) { return p >= DEGPU_FP64_PARITY && p <= DEGPU_MIXED_FP64_CTRL; }

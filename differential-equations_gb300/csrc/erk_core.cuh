@@ -1327,15 +1327,20 @@ struct Lane {
         }
         if constexpr (Tab::HAS_BH) {
             S es[D];
+            {
+                AccT ea[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) es[c] = yseg[c];
-            static_for<0, NS>([&](auto j) {
-                constexpr double bh_ = Tab::bh(decltype(j)::value);
-                if constexpr (bh_ != 0.0) {
+                for (int c = 0; c < D; ++c) ea[c] = acc_begin(yseg[c]);
+                static_for<0, NS>([&](auto j) {
+                    constexpr double bh_ = Tab::bh(decltype(j)::value);
+                    if constexpr (bh_ != 0.0) {
 #pragma unroll
-                    for (int c = 0; c < D; ++c) es[c] = es[c] + (S)(-bh_) * k[j][c];
-                }
-            });
+                        for (int c = 0; c < D; ++c) acc_fma(ea[c], (S)(-bh_), k[j][c]);
+                    }
+                });
+#pragma unroll
+                for (int c = 0; c < D; ++c) es[c] = acc_end(ea[c]);
+            }
             if (a.rtol_vec || a.atol_vec) {
 #pragma unroll
                 for (int c = 0; c < D; ++c) err2 = err2 + norm_term<true>(c, es[c], y[c], ynew[c], a);

@@ -4,6 +4,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -18,6 +19,18 @@ std::map<GroupKey, GroupLaunch>& group_registry() {
 std::map<GroupKey, GroupRoundOps>& group_round_registry() {
     static std::map<GroupKey, GroupRoundOps> m;
     return m;
+}
+
+void register_groups() {
+    static std::once_flag once;
+    std::call_once(once, []() {
+        register_group_parity();
+        register_group_fast();
+        register_group_pair853();
+        register_group_pair853_rounds();
+        register_group_pair5();
+        register_group_rounds();
+    });
 }
 
 void register_group_fast() {
@@ -100,12 +113,7 @@ static GroupChoice choose(int method, int prec, int dense, int d) {
 
 degpu_status group_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, const EnsArgs& a, const int32_t* dims,
                         cudaStream_t s) {
-    static bool reg = false;
-    if (!reg) {
-        reg = true;
-        register_group_parity();
-        register_group_fast();
-    }
+    register_groups();
     if (!dims) return DEGPU_BAD_INPUT;
     if (cfg->method == DEGPU_RK4) return DEGPU_UNSUPPORTED;
     const int64_t n = a.n;
@@ -114,7 +122,7 @@ degpu_status group_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
         cudaStreamSynchronize(s) != cudaSuccess)
         return DEGPU_CUDA_ERROR;
     const int dense = a.n_eval > 0 ? 1 : 0;
-    // a mixed solve sends instances with rtol below the mixed-precision bound to FP64_FAST
+    // a mixed solve sends instances with rtol below the mixed-precision bound to its tight class
     const double split = mixed_split(cfg);
     std::vector<double> rtol_host;
     if (split > 0.0) {
@@ -128,8 +136,16 @@ degpu_status group_solve(const degpu_problem* pb, const degpu_method_cfg* cfg, c
     for (int64_t i = 0; i < n; ++i) {
         int d = hd[i];
         if (d <= 0 || d > pb->dim || (d & 1)) return DEGPU_BAD_INPUT;
-        const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
-        GroupChoice c = choose(cfg->method, prec, dense, d);
+        int prec = cfg->precision;
+        GroupChoice c{};
+        if (split > 0.0 && rtol_host[i] < split) {
+            // the tight class: FP32-pair stages where built for this layout, else FP64 fast
+            prec = mixed_low_precision(cfg);
+            c = choose(cfg->method, prec, dense, d);
+            if (c.dmax < 0 || !group_registry().count(GroupKey{cfg->method, prec, dense, c.g, c.cpl}))
+                prec = DEGPU_FP64_FAST;
+        }
+        if (prec != PrecMixedPair::ID) c = choose(cfg->method, prec, dense, d);
         if (c.dmax < 0) return DEGPU_UNSUPPORTED;
         buckets[{prec, c.g, c.cpl}].push_back(i);
     }
@@ -190,8 +206,16 @@ degpu_status group_round_parts(const degpu_problem* pb, const degpu_method_cfg* 
     for (int64_t i = 0; i < n; ++i) {
         const int d = dims_host[i];
         if (d <= 0 || d > pb->dim || (d & 1)) return DEGPU_BAD_INPUT;
-        const int prec = (split > 0.0 && rtol_host[i] < split) ? DEGPU_FP64_FAST : cfg->precision;
-        const GroupChoice c = choose(cfg->method, prec, dense, d);
+        int prec = cfg->precision;
+        GroupChoice c{};
+        if (split > 0.0 && rtol_host[i] < split) {
+            prec = mixed_low_precision(cfg);  // as in group_solve
+            c = choose(cfg->method, prec, dense, d);
+            if (c.dmax < 0 || !group_round_registry().count(GroupKey{cfg->method, prec, dense, c.g, c.cpl}) ||
+                !group_registry().count(GroupKey{cfg->method, prec, dense, c.g, c.cpl}))
+                prec = DEGPU_FP64_FAST;
+        }
+        if (prec != PrecMixedPair::ID) c = choose(cfg->method, prec, dense, d);
         if (c.dmax < 0) return DEGPU_UNSUPPORTED;
         const auto key = std::make_tuple(prec, c.g, c.cpl);
         auto it = slot.find(key);

@@ -73,6 +73,7 @@ struct GroupLane {
     static constexpr int O = Tab::ORDER;
     static constexpr int NC = DENSE ? O : 1;
     using S = typename P::S;
+    using AccT = typename AccOf<S>::type;  // stage sums: S itself, or a lazily normalised pair
 
     // shared memory of this system
     S* k;     // [I][DG]
@@ -130,7 +131,9 @@ struct GroupLane {
     __device__ __forceinline__ void rhs(S* out) { fpu_rhs<P, G, CPL>(sy, out, d, lane, beta); }
 
     __device__ __forceinline__ S stage_coef(double aij) const {
-        if constexpr (P::KAHAN)
+        if constexpr (P::PAIR)
+            return df(aij) * df(h);  // the pairs nearest to a_ij and h
+        else if constexpr (P::KAHAN)
             return (float)aij * (float)h;
         else
             return aij * h;
@@ -150,10 +153,10 @@ struct GroupLane {
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
             const int c = lane + G * j < d ? lane + G * j : 0;
-            sk[j] = atol_c(c, a) + rtol_c(c, a) * fabs((double)y[j]);
-            double q = (double)f0[j] / sk[j];
+            sk[j] = atol_c(c, a) + rtol_c(c, a) * fabs(to_f64(y[j]));
+            double q = to_f64(f0[j]) / sk[j];
             tf_[j] = q * q;
-            double r = (double)y[j] / sk[j];
+            double r = to_f64(y[j]) / sk[j];
             ty_[j] = r * r;
         }
         double dnf = reduce_terms(tf_);
@@ -177,7 +180,7 @@ struct GroupLane {
         double q2[CPL];
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
-            double q = ((double)f1[j] - (double)f0[j]) / sk[j];
+            double q = (to_f64(f1[j]) - to_f64(f0[j])) / sk[j];
             q2[j] = q * q;
         }
         double der2 = reduce_terms(q2);
@@ -205,7 +208,7 @@ struct GroupLane {
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
             int c = lane + G * j;
-            if (c < d) out[(int64_t)c * a.n] = (double)v[j];
+            if (c < d) out[(int64_t)c * a.n] = to_f64(v[j]);
         }
     }
     __device__ void interpolate(double te, S* out, const EnsArgs& a) const {
@@ -336,12 +339,12 @@ struct GroupLane {
         for (int j = 0; j < CPL; ++j) {
             int c = lane + G * j;
             if (c >= d) break;
-            S ys = y[j];
+            AccT ys = acc_begin(y[j]);
             static_for<0, Ii>([&](auto jj) {
                 constexpr double aij = Tab::a(Ii, jj);
-                if constexpr (aij != 0.0) ys = ys + stage_coef(aij) * k[jj * DG + c];
+                if constexpr (aij != 0.0) acc_fma(ys, stage_coef(aij), k[jj * DG + c]);
             });
-            sy[c] = ys;
+            sy[c] = acc_end(ys);
         }
         sync();
         S o[CPL];
@@ -376,13 +379,14 @@ struct GroupLane {
             bool live = c < d;
             int cc = live ? c : 0;
             ysti[j] = sy[cc];
-            S s = (S)0;
+            AccT sa = acc_begin((S)0);
             static_for<0, NS>([&](auto i) {
                 constexpr double bv = Tab::b(i);
-                if constexpr (bv != 0.0) s = s + (S)bv * k[i * DG + cc];
+                if constexpr (bv != 0.0) acc_fma(sa, (S)bv, k[i * DG + cc]);
             });
+            const S s = acc_end(sa);
             yseg[j] = s;
-            if constexpr (P::KAHAN) {
+            if constexpr (P::KAHAN && !P::PAIR) {  // pairs carry 48 bits: no compensation
                 S inc = hs * s;
                 S yk = inc - yc[j];
                 S ts = y[j] + yk;
@@ -392,21 +396,23 @@ struct GroupLane {
                 ynew[j] = y[j] + hs * s;
                 ycn[j] = (S)0;
             }
-            S es = (S)0;
+            AccT ea = acc_begin((S)0);
             static_for<0, NS>([&](auto jj) {
                 constexpr double ev = Tab::er(jj);
-                if constexpr (ev != 0.0) es = es + (S)ev * k[jj * DG + cc];
+                if constexpr (ev != 0.0) acc_fma(ea, (S)ev, k[jj * DG + cc]);
             });
-            double sk = atol_c(cc, a) + rtol_c(cc, a) * fmax(fabs((double)y[j]), fabs((double)ynew[j]));
-            double q = (double)es / sk;
+            const S es = acc_end(ea);
+            double sk = atol_c(cc, a) + rtol_c(cc, a) * fmax(fabs(to_f64(y[j])), fabs(to_f64(ynew[j])));
+            double q = to_f64(es) / sk;
             e1[j] = live ? q * q : 0.0;
             if constexpr (Tab::HAS_BH) {
-                S es2 = s;
+                AccT e2a = acc_begin(s);
                 static_for<0, NS>([&](auto jj) {
                     constexpr double bhv = Tab::bh(jj);
-                    if constexpr (bhv != 0.0) es2 = es2 + (S)(-bhv) * k[jj * DG + cc];
+                    if constexpr (bhv != 0.0) acc_fma(e2a, (S)(-bhv), k[jj * DG + cc]);
                 });
-                double q2 = (double)es2 / sk;
+                const S es2 = acc_end(e2a);
+                double q2 = to_f64(es2) / sk;
                 e2[j] = live ? q2 * q2 : 0.0;
             }
         }
@@ -437,8 +443,8 @@ struct GroupLane {
                 for (int j = 0; j < CPL; ++j) {
                     int c = lane + G * j;
                     int cc = c < d ? c : 0;
-                    double a1 = (double)yseg[j] - (double)k[(NS - 1) * DG + cc];
-                    double a2 = (double)dydt[j] - (double)ysti[j];
+                    double a1 = to_f64(yseg[j]) - to_f64(k[(NS - 1) * DG + cc]);
+                    double a2 = to_f64(dydt[j]) - to_f64(ysti[j]);
                     n1[j] = c < d ? a1 * a1 : 0.0;
                     n2[j] = c < d ? a2 * a2 : 0.0;
                 }
@@ -621,7 +627,7 @@ struct GroupLane {
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
             int c = lane + G * j;
-            if (c < d) a.y_final[(int64_t)c * n + inst] = (double)y[j] - (double)yc[j];
+            if (c < d) a.y_final[(int64_t)c * n + inst] = to_f64(y[j]) - to_f64(yc[j]);
         }
         for (int c = d + lane; c < a.dmax; c += G) a.y_final[(int64_t)c * n + inst] = 0.0;
         if (lane == 0) {
@@ -831,5 +837,10 @@ degpu_status group_round_parts(const degpu_problem* pb, const degpu_method_cfg* 
 void register_group_parity();
 void register_group_fast();
 void register_group_rounds();
+void register_group_pair853();
+void register_group_pair853_rounds();
+void register_group_pair5();
+// every group kernel (run to completion and resumable), once
+void register_groups();
 
 }  // namespace degpu

@@ -1,0 +1,14 @@
+// FP32-pair stage group-per-system kernels (DOP853), resumable: the server's rounds of the tight
+// class of a mixed request of FPU-beta chains, every layout of the default dimension buckets.
+#include "group_erk.cuh"
+
+namespace degpu {
+void register_group_pair853_rounds() {
+    reg_group_round<TabDop853, PrecMixedPair, 8, 1>();
+    reg_group_round<TabDop853, PrecMixedPair, 16, 1>();
+    reg_group_round<TabDop853, PrecMixedPair, 32, 1>();
+    reg_group_round<TabDop853, PrecMixedPair, 32, 2>();
+    reg_group_round<TabDop853, PrecMixedPair, 32, 4>();
+    reg_group_round<TabDop853, PrecMixedPair, 32, 8>();
+}
+}  // namespace degpu

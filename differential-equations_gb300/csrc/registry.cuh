@@ -219,7 +219,8 @@ void register_mixed_f64ctrl();
 void register_mixed_pair();
 void register_round_dense_parity();
 void register_round_dense_fast_mixed();
-void register_group_rounds();
+void register_groups();
+void register_mixed_pair853();
 void ensure_registered();
 
 // Estimated log2 cost of one instance, the sort key of the longest-first work lists.  Fitted to

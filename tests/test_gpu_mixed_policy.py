@@ -1,6 +1,6 @@
 """Mixed-precision bound (degpu_set_mixed_min_rtol): in a MIXED solve, instances with rtol below
-the bound leave the FP32 stages (DOPRI5: FP32-pair stages; DOP853: the FP64_FAST arithmetic) and
-the others run the FP32-stage form.  Each instance's result must equal, bit for bit, the same
+the bound leave the FP32 stages for FP32-pair stages (DOPRI5, DOP853; other methods: the FP64_FAST
+arithmetic) and the others run the FP32-stage form.  Each instance's result must equal, bit for bit, the same
 instance solved by the arithmetic its rtol selects, on every kernel layout (persistent
 multi-family, one system per thread, group per system).  The pair stages keep FP64-like accuracy
 where the FP32 stages cannot."""
@@ -53,11 +53,8 @@ def test_split_matches_the_selected_arithmetic(bound, method, kernel):
     assert 0 < tight.sum() < e.n
     degpu.set_mixed_min_rtol(method, BOUND)
     split = run(e, method, abi.MIXED, kernel)
-    if method == abi.DOPRI5:
-        degpu.set_mixed_min_rtol(method, 1.0)  # every instance below the bound: pair stages
-        low = run(e, method, abi.MIXED, kernel)
-    else:
-        low = run(e, method, abi.FP64_FAST, kernel)
+    degpu.set_mixed_min_rtol(method, 1.0)  # every instance below the bound: pair stages
+    low = run(e, method, abi.MIXED, kernel)
     degpu.set_mixed_min_rtol(method, 0.0)
     mixed = run(e, method, abi.MIXED, kernel)
     same(split, low, tight)
@@ -76,11 +73,18 @@ def test_split_on_ragged_group_kernel(bound):
     assert 0 < tight.sum() < f.n
     degpu.set_mixed_min_rtol(abi.DOP853, BOUND)
     split = run(f, abi.DOP853, abi.MIXED, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
-    fast = run(f, abi.DOP853, abi.FP64_FAST, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
+    degpu.set_mixed_min_rtol(abi.DOP853, 1.0)  # every chain in the tight class: pair stages
+    pair = run(f, abi.DOP853, abi.MIXED, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
     degpu.set_mixed_min_rtol(abi.DOP853, 0.0)
     mixed = run(f, abi.DOP853, abi.MIXED, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
-    same(split, fast, tight)
+    same(split, pair, tight)
     same(split, mixed, ~tight)
+    # the pair stages follow FP64 at the same tolerances
+    fast = run(f, abi.DOP853, abi.FP64_FAST, abi.KERNEL_WARP, rhs=abi.RHS["FPU_BETA"], dims=f.dims)
+    ok = (pair.status == abi.COMPLETE) & (fast.status == abi.COMPLETE)
+    assert ok.all()
+    rel = np.max(np.abs(pair.y_final - fast.y_final), axis=0) / np.max(np.abs(fast.y_final), axis=0)
+    assert np.median(rel[tight]) < 1e-9
 
 
 def test_rk4_has_no_bound(bound):
@@ -117,9 +121,10 @@ def test_mixed_time_pair_ends_at_tf_and_tracks_fp64(method, kernel):
     assert errs[1] < 10 * errs[0] + 1e-6
 
 
+@pytest.mark.parametrize("method", [abi.DOPRI5, abi.DOP853])
 @pytest.mark.parametrize("kernel", [abi.KERNEL_PERSISTENT, abi.KERNEL_THREAD])
-def test_pair_stages_track_fp64(bound, kernel):
-    """DOPRI5's FP32-pair stages (the tight class of a mixed solve) against FP64 at the same
+def test_pair_stages_track_fp64(bound, kernel, method):
+    """The FP32-pair stages (the tight class of a mixed solve) against FP64 at the same
     tolerances on the non-chaotic families (Van der Pol, the damped driven pendulum), over the
     ensemble's full horizons: the FP32 stages' error floor (about 5e-7) is gone."""
     e = W.config1(n=3 * 1500, first=20_000)
@@ -127,11 +132,11 @@ def test_pair_stages_track_fp64(bound, kernel):
     e = e.subset(np.nonzero(keep)[0])
     e.rtol = W.logU(9, np.arange(e.n), 1, 1e-10, 1e-7)
     e.atol = 1e-2 * e.rtol
-    degpu.set_mixed_min_rtol(abi.DOPRI5, 1.0)
-    pair = run(e, abi.DOPRI5, abi.MIXED, kernel)
-    degpu.set_mixed_min_rtol(abi.DOPRI5, 0.0)
-    f32 = run(e, abi.DOPRI5, abi.MIXED, kernel)
-    fast = run(e, abi.DOPRI5, abi.FP64_FAST, kernel)
+    degpu.set_mixed_min_rtol(method, 1.0)
+    pair = run(e, method, abi.MIXED, kernel)
+    degpu.set_mixed_min_rtol(method, 0.0)
+    f32 = run(e, method, abi.MIXED, kernel)
+    fast = run(e, method, abi.FP64_FAST, kernel)
     ok = (pair.status == abi.COMPLETE) & (fast.status == abi.COMPLETE)
     # at rtol 1e-10 over horizons up to 50 a few Van der Pol instances end on the crate's
     # stiffness test or the step limit in either arithmetic; the pairs must not end more often
