@@ -34,10 +34,10 @@ struct GroupArgs {
 
 // FPU-beta right-hand side for the components this lane owns; `sy` is the stage state.
 template <class P, int G, int CPL>
-__device__ __forceinline__ void fpu_rhs(const typename P::S* sy, typename P::S* out, int d, int lane, double beta) {
+__device__ __forceinline__ void fpu_rhs(const typename P::S* sy, typename P::S* out, int d, int lane,
+                                        typename P::S b) {
     using S = typename P::S;
     const int m = d / 2;
-    S b = (S)beta;
 #pragma unroll
     for (int j = 0; j < CPL; ++j) {
         int c = lane + G * j;
@@ -86,6 +86,11 @@ struct GroupLane {
     int d;
     int64_t inst;
     double t, tf, h, h_prev, t_prev, dir, rtol, atol, beta;
+    // pair stages: h as a pair, formed once per step attempt, and FP32 copies of the tolerances
+    // (their error terms, norm terms and stiffness terms are FP32, widened for the FP64 sums)
+    S hc;
+    float rtolf, atolf;
+    S betas;  // beta in the stage arithmetic, converted once per instance
     S y[CPL], yc[CPL];
     int64_t steps, acc, rej, fev;
     int stiff, nonstiff, next_eval, status;
@@ -128,11 +133,20 @@ struct GroupLane {
     }
 
     // dydt of the lane's components at state sy (all lanes of the group call it together)
-    __device__ __forceinline__ void rhs(S* out) { fpu_rhs<P, G, CPL>(sy, out, d, lane, beta); }
+    // the per-instance values derived from rtol, atol and beta
+    __device__ __forceinline__ void set_derived() {
+        betas = (S)beta;
+        if constexpr (P::PAIR) {
+            rtolf = narrow_rz(rtol);
+            atolf = narrow_rz(atol);
+        }
+    }
+
+    __device__ __forceinline__ void rhs(S* out) { fpu_rhs<P, G, CPL>(sy, out, d, lane, betas); }
 
     __device__ __forceinline__ S stage_coef(double aij) const {
         if constexpr (P::PAIR)
-            return df(aij) * df(h);  // the pairs nearest to a_ij and h
+            return df(aij) * hc;  // the pairs nearest to a_ij and h
         else if constexpr (P::KAHAN)
             return (float)aij * (float)h;
         else
@@ -274,6 +288,7 @@ struct GroupLane {
         rtol = a.rtol[inst];
         atol = a.atol[inst];
         beta = a.params[inst];
+        set_derived();
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
             int c = lane + G * j;
@@ -368,6 +383,7 @@ struct GroupLane {
             return 3;
         }
         steps += 1;
+        if constexpr (P::PAIR) hc = P::from(h);
         static_for<1, NS>([&](auto i) { stage<i>(k + i * DG); });
         // sy holds the last stage state (ysti)
         S ysti[CPL], yseg[CPL], ynew[CPL], ycn[CPL];
@@ -402,9 +418,19 @@ struct GroupLane {
                 if constexpr (ev != 0.0) acc_fma(ea, (S)ev, k[jj * DG + cc]);
             });
             const S es = acc_end(ea);
-            double sk = atol_c(cc, a) + rtol_c(cc, a) * fmax(fabs(to_f64(y[j])), fabs(to_f64(ynew[j])));
-            double q = to_f64(es) / sk;
-            e1[j] = live ? q * q : 0.0;
+            double sk = 0.0;
+            if constexpr (P::PAIR) {
+                // FP32 norm terms: the estimate's leading part against an FP32 scale
+                const float skf = (a.atol_vec ? narrow_rz(atol_c(cc, a)) : atolf) +
+                                  (a.rtol_vec ? narrow_rz(rtol_c(cc, a)) : rtolf) *
+                                      fmaxf(fabsf(lead(y[j])), fabsf(lead(ynew[j])));
+                const float qf = __fdividef(lead(es), skf);
+                e1[j] = live ? widen_f32(qf * qf) : 0.0;
+            } else {
+                sk = atol_c(cc, a) + rtol_c(cc, a) * fmax(fabs(to_f64(y[j])), fabs(to_f64(ynew[j])));
+                double q = to_f64(es) / sk;
+                e1[j] = live ? q * q : 0.0;
+            }
             if constexpr (Tab::HAS_BH) {
                 AccT e2a = acc_begin(s);
                 static_for<0, NS>([&](auto jj) {
@@ -412,8 +438,16 @@ struct GroupLane {
                     if constexpr (bhv != 0.0) acc_fma(e2a, (S)(-bhv), k[jj * DG + cc]);
                 });
                 const S es2 = acc_end(e2a);
-                double q2 = to_f64(es2) / sk;
-                e2[j] = live ? q2 * q2 : 0.0;
+                if constexpr (P::PAIR) {
+                    const float skf = (a.atol_vec ? narrow_rz(atol_c(cc, a)) : atolf) +
+                                      (a.rtol_vec ? narrow_rz(rtol_c(cc, a)) : rtolf) *
+                                          fmaxf(fabsf(lead(y[j])), fabsf(lead(ynew[j])));
+                    const float q2 = __fdividef(lead(es2), skf);
+                    e2[j] = live ? widen_f32(q2 * q2) : 0.0;
+                } else {
+                    double q2 = to_f64(es2) / sk;
+                    e2[j] = live ? q2 * q2 : 0.0;
+                }
             }
         }
         double t_new = t + h;
@@ -443,10 +477,17 @@ struct GroupLane {
                 for (int j = 0; j < CPL; ++j) {
                     int c = lane + G * j;
                     int cc = c < d ? c : 0;
-                    double a1 = to_f64(yseg[j]) - to_f64(k[(NS - 1) * DG + cc]);
-                    double a2 = to_f64(dydt[j]) - to_f64(ysti[j]);
-                    n1[j] = c < d ? a1 * a1 : 0.0;
-                    n2[j] = c < d ? a2 * a2 : 0.0;
+                    if constexpr (P::PAIR) {
+                        const float a1 = lead(yseg[j] - k[(NS - 1) * DG + cc]);
+                        const float a2 = lead(dydt[j] - ysti[j]);
+                        n1[j] = c < d ? widen_f32(a1 * a1) : 0.0;
+                        n2[j] = c < d ? widen_f32(a2 * a2) : 0.0;
+                    } else {
+                        double a1 = to_f64(yseg[j]) - to_f64(k[(NS - 1) * DG + cc]);
+                        double a2 = to_f64(dydt[j]) - to_f64(ysti[j]);
+                        n1[j] = c < d ? a1 * a1 : 0.0;
+                        n2[j] = c < d ? a2 * a2 : 0.0;
+                    }
                 }
                 double stdnum = reduce_terms(n1);
                 double stden = reduce_terms(n2);
@@ -612,6 +653,7 @@ struct GroupLane {
         rtol = pk.rtol;
         atol = pk.atol;
         beta = pk.beta;
+        set_derived();
 #pragma unroll
         for (int j = 0; j < CPL; ++j) {
             const int c = lane + G * j;

@@ -84,12 +84,14 @@ typedef enum {
  *                compensation; t as an FP32 pair (about 48 bits, FP64 when output times,
  *                crossings or events need it; RK4: t and h in FP64).
  *                Instances whose rtol is below the method's mixed-precision bound
- *                (degpu_set_mixed_min_rtol) leave the FP32 stages: DOPRI5 on the Van der Pol,
- *                pendulum and Lorenz families runs them with FP32-pair stages (about 48 bits:
- *                the state, stage states, right-hand sides and stage sums as unevaluated sums of
- *                two FP32 numbers, the step machinery as above), everything else in FP64_FAST.
- *  FP64_PLAIN  — FP64 with FMA contraction, IEEE division and square root, the CUDA library's
- *                sin/cos, and FP64_PARITY's correctly rounded controller power, so that every
+ *                (degpu_set_mixed_min_rtol) leave the FP32 stages: DOPRI5 and DOP853 on the Van
+ *                der Pol, pendulum and Lorenz families and on FPU-beta chains run them with
+ *                FP32-pair stages (about 48 bits: the state, stage states, right-hand sides and
+ *                stage sums as unevaluated sums of two FP32 numbers, the step machinery as
+ *                above), everything else in FP64_FAST.
+ *  FP64_PLAIN  — FP64 with FMA contraction, refined hardware reciprocal and reciprocal square
+ *                root, table-driven sin/cos (within one unit in the last place), and
+ *                FP64_PARITY's correctly rounded controller power, so that every
  *                accept/reject decision follows the crate's unless contraction moves the error
  *                estimate across 1.  DOPRI5 and DOP853 on the Van der Pol, pendulum and Lorenz
  *                families, final states and output times.
@@ -211,8 +213,8 @@ void degpu_default_cfg(degpu_method_cfg* cfg, int32_t method);
  * FP32 stage rounding puts a floor under the error: about 5e-7 relative on long Van der Pol
  * solves whatever the tolerance, and below rtol ~1e-9 the embedded error estimate stalls on the
  * noise and the controller keeps rejecting.  So in a DEGPU_MIXED solve an instance with
- * rtol < min_rtol leaves the FP32 stages: DOPRI5 (default bound 1e-6) runs it with FP32-pair
- * stages, DOP853 (1e-7), RKF45 and Cash-Karp (1e-9) in DEGPU_FP64_FAST arithmetic.  The choice
+ * rtol < min_rtol leaves the FP32 stages: DOPRI5 (default bound 1e-6) and DOP853 (1e-7) run it
+ * with FP32-pair stages, RKF45 and Cash-Karp (1e-9) in DEGPU_FP64_FAST arithmetic.  The choice
  * depends on the instance's own rtol only, so a result does not depend on the batch it is solved
  * in.  min_rtol = 0 disables the split.  RKF45 and Cash-Karp share one setting.  The setting is
  * process-wide and applies to solves launched after the call; the environment variable

@@ -144,8 +144,9 @@ def test_pair_stages_track_fp64(bound, kernel, method):
     assert (pair.status == abi.COMPLETE).sum() >= (fast.status == abi.COMPLETE).sum() - 0.002 * e.n
     rel = lambda r: np.max(np.abs(r.y_final[:, ok] - fast.y_final[:, ok]), axis=0) / \
         np.maximum(np.max(np.abs(fast.y_final[:, ok]), axis=0), 1e-300)
-    # the pair stages follow FP64 to the rounding-driven spread of the step sequence
-    assert np.median(rel(pair)) < 1e-9
+    # the pair stages follow FP64 to the rounding-driven spread of the step sequence (wider for
+    # DOP853, whose longer steps amplify a rounding-level difference more)
+    assert np.median(rel(pair)) < (1e-9 if method == abi.DOPRI5 else 3e-9)
     assert np.median(rel(pair)) < 0.05 * np.median(rel(f32))
     # the step counts of FP64
     steps = lambda r: (r.accepted + r.rejected)[ok].astype(float)
