@@ -1011,7 +1011,7 @@ def main():
     ap.add_argument("--bvp-cpu-sample", type=int, default=2000)
     ap.add_argument("--fpu-n", type=int, default=131072)
     ap.add_argument("--fpu-cpu-sample", type=int, default=200)
-    ap.add_argument("--fpu-mixed-max-steps", type=int, default=200_000)
+    ap.add_argument("--fpu-mixed-max-steps", type=int, default=20_000)
     ap.add_argument("--gs-n", type=int, default=4096)
     ap.add_argument("--gs-steps", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=10000)

@@ -849,6 +849,13 @@ void reg_group() {
     group_registry()[GroupKey{method_id<Tab>(), P::ID, 1, G, CPL}] = &launch_group<Tab, P, G, CPL, true>;
 }
 
+// Only the kernel without output times: the layouts where the pair form with output times holds
+// too many registers to beat FP64 (measured on FPU-beta chains of 66..128 components).
+template <class Tab, class P, int G, int CPL>
+void reg_group_final() {
+    group_registry()[GroupKey{method_id<Tab>(), P::ID, 0, G, CPL}] = &launch_group<Tab, P, G, CPL, false>;
+}
+
 // Resumable group kernels of the server, keyed like group_registry: bytes per parked system and
 // the round launcher (the signature of the other round kernels, dims in EnsArgs).
 struct GroupRoundOps {
@@ -864,6 +871,11 @@ void reg_group_round() {
         GroupRoundOps{group_park_bytes<Tab, P, G, CPL>(), &launch_group_round<Tab, P, G, CPL, false>};
     group_round_registry()[GroupKey{method_id<Tab>(), P::ID, 1, G, CPL}] =
         GroupRoundOps{group_park_bytes<Tab, P, G, CPL>(), &launch_group_round<Tab, P, G, CPL, true>};
+}
+template <class Tab, class P, int G, int CPL>
+void reg_group_round_final() {
+    group_round_registry()[GroupKey{method_id<Tab>(), P::ID, 0, G, CPL}] =
+        GroupRoundOps{group_park_bytes<Tab, P, G, CPL>(), &launch_group_round<Tab, P, G, CPL, false>};
 }
 
 // The work of a ragged request split for the resumable group kernels: one part per (precision,
