@@ -387,7 +387,7 @@ degpu_status degpu_server_submit(degpu_server* server, const degpu_problem* pb, 
                 r->parts[1].idx = std::move(idx[1]);
             }
         }
-    } else if (ragged && in->n_eval >= 0) {
+    } else if (ragged) {
         // FPU-beta chains: resumable group kernels, one part per (precision, layout) bucket;
         // anything the round kernels do not cover is solved in one piece instead
         std::vector<GroupRoundPart> gp;
