@@ -85,21 +85,21 @@ static std::vector<GroupChoice> default_choices() {
 }
 
 static void load_tune_file() {
-    static bool loaded = false;
-    if (loaded) return;
-    loaded = true;
-    const char* path = getenv("DEGPU_TUNE_FILE");
-    if (!path) return;
-    FILE* f = fopen(path, "r");
-    if (!f) return;
-    int m, p, dn, dmax, g, cpl;
-    while (fscanf(f, "%d %d %d %d %d %d", &m, &p, &dn, &dmax, &g, &cpl) == 6) {
-        auto& v = tune_table()[{m, p, dn}];
-        if (v.empty()) v = default_choices();
-        for (auto& c : v)
-            if (c.dmax == dmax) c = {dmax, g, cpl};
-    }
-    fclose(f);
+    static std::once_flag once;
+    std::call_once(once, []() {
+        const char* path = getenv("DEGPU_TUNE_FILE");
+        if (!path) return;
+        FILE* f = fopen(path, "r");
+        if (!f) return;
+        int m, p, dn, dmax, g, cpl;
+        while (fscanf(f, "%d %d %d %d %d %d", &m, &p, &dn, &dmax, &g, &cpl) == 6) {
+            auto& v = tune_table()[{m, p, dn}];
+            if (v.empty()) v = default_choices();
+            for (auto& c : v)
+                if (c.dmax == dmax) c = {dmax, g, cpl};
+        }
+        fclose(f);
+    });
 }
 
 static GroupChoice choose(int method, int prec, int dense, int d) {
