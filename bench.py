@@ -1292,6 +1292,9 @@ def main():
         "clocks": ck,
         "variants": extra,
         "agreement_with_crate": agree,
+        # the headline variant's accuracy against FP64 where FP64 meets 1e-6 (accuracy.*.rule)
+        "headline_meets_accuracy_rule": (accuracy["variants"][args.variant]["rule"]["variant_meets_1e-6_there"]
+                                         if accuracy and args.variant in accuracy["variants"] else None),
         "accuracy": accuracy,
         "configs": configs,
     }
