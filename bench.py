@@ -74,18 +74,18 @@ def flops_of(family, accepted, rejected):
 
 # FP32 operations (FMA = 2) of one attempted step with FP32-pair stages, the emulation's own
 # instruction counts: a stage-sum term (pair product accumulated: 1 mul, 3 FMA, 8 add) = 15, a
-# pair times FP32 coefficient (1 mul, 2 FMA, 3 add) = 8, a pair product (1 mul, 3 FMA, 3 add) =
-# 10, a pair sum (11 add) = 11, a normalisation = 3.
-#   15 stage coefficients 8 each; per component: 15 stage-sum terms + 5 normalisations, 5 terms
+# pair times an FP32 coefficient (1 mul, 2 FMA; left unnormalised) = 5, a pair product (1 mul,
+# 3 FMA) = 7, a pair sum (11 add) = 11, a normalisation = 3.
+#   15 stage coefficients 5 each; per component: 15 stage-sum terms + 5 normalisations, 5 terms
 #   of y_seg + 1, y_new 16, 6 terms of the error estimate + 1, the FP32 norm 5; controller and
 #   pair time 18; 6 right-hand sides in pairs (sin/cos not counted, as in the FP64 model).
-PAIR_RHS_FLOPS = {abi.RHS["LORENZ"]: 4 * 10 + 4 * 11, abi.RHS["VAN_DER_POL"]: 3 * 10 + 2 * 11,
-                  abi.RHS["PENDULUM"]: 2 * 10 + 2 * 11 + 8 + 11}
+PAIR_RHS_FLOPS = {abi.RHS["LORENZ"]: 4 * 7 + 4 * 11, abi.RHS["VAN_DER_POL"]: 3 * 7 + 2 * 11,
+                  abi.RHS["PENDULUM"]: 2 * 7 + 2 * 11 + 7 + 11}
 
 
 def pair_step_flops(rhs_id):
     d = RHS_FLOPS[rhs_id][0]
-    return 15 * 8 + (15 * 15 + 5 * 3 + 5 * 15 + 3 + 16 + 6 * 15 + 3 + 5) * d + 18 + 6 * PAIR_RHS_FLOPS[rhs_id]
+    return 15 * 5 + (15 * 15 + 5 * 3 + 5 * 15 + 3 + 16 + 6 * 15 + 3 + 5) * d + 18 + 6 * PAIR_RHS_FLOPS[rhs_id]
 
 
 def pair_flops_of(family, accepted, rejected, mask):

@@ -87,18 +87,21 @@ DF_HD df operator-(df a) { return df(-a.hi, -a.lo); }
 DF_HD df operator-(df a, df b) { return a + (-b); }
 DF_HD df operator-(df a, float b) { return a + (-b); }
 DF_HD df operator-(float a, df b) { return (-b) + a; }
+// Products are left as (p, e) without the final FastTwoSum: e is the product's rounding error plus
+// the cross terms, within about 1.5 units of p's last place, a pair every operation here accepts
+// (sums re-split the leading parts with TwoSum; products only need |lo| small against |hi|).
 DF_HD df operator*(df a, df b) {
     const float p = DF_MUL(a.hi, b.hi);
     float e = fmaf(a.hi, b.hi, -p);
     e = fmaf(a.hi, b.lo, e);
     e = fmaf(a.lo, b.hi, e);
-    return df_fast_two_sum(p, e);
+    return df(p, e);
 }
 DF_HD df operator*(df a, float b) {
     const float p = DF_MUL(a.hi, b);
     float e = fmaf(a.hi, b, -p);
     e = fmaf(a.lo, b, e);
-    return df_fast_two_sum(p, e);
+    return df(p, e);
 }
 DF_HD df operator*(float a, df b) { return b * a; }
 DF_HD df& operator+=(df& a, df b) { return a = a + b; }
