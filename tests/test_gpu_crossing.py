@@ -162,3 +162,20 @@ def test_ivp_builder_crossing_and_host_entry():
     assert np.array_equal(cc, g["cross_count"])
     assert np.array_equal(ct, g["cross_t"], equal_nan=True) and np.array_equal(cy, g["cross_y"], equal_nan=True)
     assert np.array_equal(r.accepted, g["accepted"]) and np.array_equal(r.y_final, g["y_final"])
+
+
+@pytest.mark.parametrize("fam", ["VAN_DER_POL", "PENDULUM"])
+def test_crossing_pair_stages_track_oracle(fam):
+    """Mixed DOPRI5 below its bound (rtol 1e-9): the FP32-pair detecting lanes find the crate's
+    crossings, at times within the FP32 search's resolution (1e-6 of a step) of the oracle's."""
+    e = family_ensemble(fam, 400, first=31000)
+    e.rtol[:] = 1e-9
+    e.atol[:] = 1e-11
+    g = gpu_crossing(e, cfg_for(abi.DOPRI5, abi.MIXED), 0, 0.0, abi.CROSS_BOTH, 10)
+    o = oracle_crossing(e, cfg_for(abi.DOPRI5), 0, 0.0, abi.CROSS_BOTH, 10)
+    assert np.all(g["status"] == abi.COMPLETE)
+    same = g["cross_count"] == o["cross_count"]
+    assert same.mean() > 0.99
+    m = ~np.isnan(o["cross_t"][:, same])
+    dt = np.abs(g["cross_t"][:, same][m] - o["cross_t"][:, same][m])
+    assert np.median(dt) < 1e-7 and np.max(dt) < 1e-4

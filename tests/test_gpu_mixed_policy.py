@@ -151,3 +151,25 @@ def test_pair_stages_track_fp64(bound, kernel, method):
     # the step counts of FP64
     steps = lambda r: (r.accepted + r.rejected)[ok].astype(float)
     assert abs(steps(pair).mean() / steps(fast).mean() - 1.0) < 0.01
+
+
+@pytest.mark.parametrize("method", [abi.DOPRI5, abi.DOP853])
+@pytest.mark.parametrize("kernel", [abi.KERNEL_PERSISTENT, abi.KERNEL_THREAD])
+def test_pair_dense_output_tracks_fp64(bound, method, kernel):
+    """Output times through the pair stages' interpolants (the tight class with dense output):
+    the interpolated states follow FP64 at the same tolerances, on both kernel layouts."""
+    e = W.config1(n=3 * 600, first=41_000)
+    e = e.subset(np.nonzero(e.family != abi.RHS["LORENZ"])[0])
+    e.tf = np.minimum(e.tf, 10.0)
+    e.rtol = W.logU(14, np.arange(e.n), 1, 1e-10, 1e-7)
+    e.atol = 1e-2 * e.rtol
+    te = np.linspace(10.0, 0.0, 21)
+    pair = run(e, method, abi.MIXED, kernel, t_eval=te)
+    fast = run(e, method, abi.FP64_FAST, kernel, t_eval=te)
+    ok = (pair.status == abi.COMPLETE) & (fast.status == abi.COMPLETE)
+    assert ok.mean() > 0.99
+    a, b = pair.dense[:, :, ok], fast.dense[:, :, ok]
+    fin = np.isfinite(b)
+    assert np.array_equal(np.isfinite(a), fin)
+    rel = np.abs(a[fin] - b[fin]) / np.maximum(np.abs(b[fin]), 1e-3)
+    assert np.median(rel) < (1e-9 if method == abi.DOPRI5 else 3e-9)
