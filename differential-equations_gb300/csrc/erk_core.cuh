@@ -331,7 +331,10 @@ struct Lane {
     int next_eval;
     int status;
     // crossing detection: previous offset (events: previous g); FP32 in the mixed form
-    using OffT = typename PickT<P::KAHAN, float, double>::type;
+    // FP32-stage lanes search in FP32; pair lanes, like FP64 ones, run the crate's FP64 search on
+    // their (pair) interpolant
+    static constexpr bool F32_SEARCH = P::KAHAN && !P::PAIR;
+    using OffT = typename PickT<F32_SEARCH, float, double>::type;
     OffT last_off;
     bool have_last_off;
     int ncross;          // crossings / events recorded
@@ -735,7 +738,7 @@ struct Lane {
             if (c == comp) r = v[c];
         return r;
     }
-    __device__ __forceinline__ double comp_value(const S* v, int comp) const { return (double)comp_s(v, comp); }
+    __device__ __forceinline__ double comp_value(const S* v, int comp) const { return to_f64(comp_s(v, comp)); }
     // The monitored offset of a state given component by component: y[comp] - threshold
     // (crossing.rs:207), or the hyperplane's signed distance (pos - point) . normal
     // (hyperplane.rs signed_distance), the dot product folded from zero in component order
@@ -851,7 +854,7 @@ struct Lane {
 
     __device__ void crossing_solout(const EnsArgs& a) {
         OffT offset;
-        if constexpr (P::KAHAN)
+        if constexpr (F32_SEARCH)
             offset = state_offset_f32(a);
         else
             offset = offset_by([&](int c) { return comp_value(y, c); }, a);
@@ -872,7 +875,7 @@ struct Lane {
                 if (record) {
                     double tc;
                     S v[D];
-                    if constexpr (P::KAHAN) {
+                    if constexpr (F32_SEARCH) {
                         // mixed: the same search in the step's normalised coordinate, in FP32
                         const float sg = find_crossing_sigma(last_off, offset, a);
                         tc = t_prev + (double)sg * (t - t_prev);
@@ -940,7 +943,7 @@ struct Lane {
     }
     __device__ void event_solout(const EnsArgs& a) {
         OffT g_curr;
-        if constexpr (P::KAHAN) {
+        if constexpr (F32_SEARCH) {
             // mixed: g at the step's end in FP32 on y - compensation; the time term in FP64 once
             S sv[D];
 #pragma unroll
@@ -977,7 +980,7 @@ struct Lane {
             }
             double te;
             bool found;
-            if constexpr (P::KAHAN) {
+            if constexpr (F32_SEARCH) {
                 // mixed: the same search on sg in [0, 1] (t_prev to t) in FP32 on the FP32
                 // interpolant, stopping at 1e-6 of the step; a backward step locates nothing, as
                 // the crate's interpolator refuses every time inside it
