@@ -214,19 +214,39 @@ def test_fast_fp64_accuracy():
 
 
 def test_mixed_precision_error_vs_oracle():
-    """Mixed form (FP32 stages, Kahan-compensated y, FP64 controller): error against the FP64
-    oracle at tolerances the FP32 stages can meet."""
-    e = W.config1(n=3 * 300)
-    keep = e.family == abi.RHS["VAN_DER_POL"]
-    e = e.subset(np.nonzero(keep)[0])
+    """The default mixed form (FP32 stages with Kahan-compensated y above the DOPRI5 bound,
+    FP32-pair stages below it; the error norm, controller and accept decision in FP32, t as an
+    FP32 pair) against a tight FP64 oracle (DOP853, rtol = atol = 1e-13), per rtol decade of the
+    uneven ensemble's Van der Pol and pendulum instances.  In every decade where FP64 at the same
+    tolerances reaches a median error of 1e-6, the mixed median may be at most 1.25 x FP64's and its
+    share of instances within 1e-6 at most 3 points below FP64's (the accuracy rule of the
+    benchmark's headline)."""
+    e = W.config1(n=3 * 1600)
+    e = e.subset(np.nonzero(e.family != abi.RHS["LORENZ"])[0])
     e.tf = np.minimum(e.tf, 10.0)
-    e.rtol[:] = 1e-6
-    e.atol[:] = 1e-8
-    o = oracle_solve(e, cfg_for(abi.DOPRI5))
-    g = gpu_solve(e, cfg_for(abi.DOPRI5, precision=abi.MIXED))
-    assert np.all(g.status == abi.COMPLETE)
-    err = np.max(np.abs(g.y_final - o["y_final"]), axis=0) / np.maximum(1.0, np.max(np.abs(o["y_final"]), axis=0))
-    assert np.median(err) < 1e-5
+    tight = O.Batch(0, e.dim, e.n_params, e.t0, e.tf, e.y0, e.params, np.full(e.n, 1e-13), np.full(e.n, 1e-13),
+                    family=e.family)
+    c8 = cfg_for(abi.DOP853, max_steps=50_000_000)
+    y_tight = O.solve(tight, c8, math_mode=1)["y_final"]
+    g64 = gpu_solve(e, cfg_for(abi.DOPRI5, precision=abi.FP64_FAST, kernel=abi.KERNEL_PERSISTENT))
+    gm = gpu_solve(e, cfg_for(abi.DOPRI5, precision=abi.MIXED, kernel=abi.KERNEL_PERSISTENT))
+    assert np.all(g64.status == abi.COMPLETE) and np.all(gm.status == abi.COMPLETE)
+
+    def rel(y):
+        return np.max(np.abs(y - y_tight), axis=0) / np.maximum(np.max(np.abs(y_tight), axis=0), 1e-300)
+
+    r64, rm = rel(g64.y_final), rel(gm.y_final)
+    checked = 0
+    for fam in (abi.RHS["VAN_DER_POL"], abi.RHS["PENDULUM"]):
+        for lo, hi in ((1e-9, 1e-8), (1e-8, 1e-7), (1e-7, 1e-6), (1e-6, 1e-5)):
+            m = (e.family == fam) & (e.rtol >= lo) & (e.rtol < hi)
+            if m.sum() < 100 or np.median(r64[m]) > 1e-6:
+                continue
+            checked += 1
+            assert np.median(rm[m]) <= 1.25 * np.median(r64[m]), (fam, lo, np.median(rm[m]), np.median(r64[m]))
+            gap = np.mean(r64[m] <= 1e-6) - np.mean(rm[m] <= 1e-6)
+            assert gap <= 0.03, (fam, lo, gap)
+    assert checked >= 4
 
 
 @pytest.mark.parametrize("precision", [abi.FP64_PARITY])
