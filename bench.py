@@ -539,8 +539,7 @@ def run_adaptive(args, torch, dev, lib):
 
 def fp64_peak_of(lib):
     pk = C.c_double(0.0)
-    lib.degpu_internal_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
-    lib.degpu_internal_fma_peak(1, C.byref(pk))
+    abi.load_probe().degpu_internal_fma_peak(1, C.byref(pk))
     return pk.value
 
 
@@ -1132,10 +1131,10 @@ def main():
     # time.  Algorithmic operations are split by the pipe that executes them.
     pk = C.c_double(0.0)
     prec = VARIANTS[args.variant][0]
-    lib.degpu_internal_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
-    lib.degpu_internal_fma_peak(1, C.byref(pk))
+    probe = abi.load_probe()
+    probe.degpu_internal_fma_peak(1, C.byref(pk))
     fp64_peak = pk.value
-    lib.degpu_internal_fma_peak(0, C.byref(pk))
+    probe.degpu_internal_fma_peak(0, C.byref(pk))
     fp32_peak = pk.value
 
     def split_ops(variant, a_, r_):

@@ -1,4 +1,6 @@
-"""Builds libdegpu.so in place: every CUDA translation unit for sm_103a, in parallel.
+"""Builds libdegpu.so in place: every CUDA translation unit for sm_103a, in parallel; and
+libdegpu_probe.so from probe/ (the FMA peak probe and device self-checks used by the benchmark and
+the tests, kept out of the integrator library).
 
 Usage: python build.py [--jobs N] [--verbose]
 The parity translation units (inst_parity_*.cu) and the shooting Newton kernels (bvp.cu) are
@@ -13,6 +15,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "libdegpu.so")
+PROBE_OUT = os.path.join(HERE, "libdegpu_probe.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction (gcc contracts by default on aarch64), so host-side FP64
@@ -60,10 +63,11 @@ def needs(obj, src):
 
 
 def compile_one(src, verbose):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    probe = os.path.basename(os.path.dirname(src)) == "probe"
+    obj = os.path.join(BUILD, ("probe_" if probe else "") + os.path.basename(src) + ".o")
     if not needs(obj, src):
         return obj, ""
-    cmd = [nvcc()] + flags_for(src) + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + flags_for(src) + (["-I", HERE] if probe else []) + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -75,14 +79,19 @@ def compile_one(src, verbose):
 def build(jobs=None, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
-    jobs = jobs or min(len(srcs), os.cpu_count() or 4)
+    probe_srcs = sorted(glob.glob(os.path.join(HERE, "probe", "*.cu")))
+    jobs = jobs or min(len(srcs) + len(probe_srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(jobs) as ex:
-        objs = [f.result()[0] for f in [ex.submit(compile_one, s, verbose) for s in srcs]]
-    if not os.path.exists(OUT) or any(os.path.getmtime(o) > os.path.getmtime(OUT) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", OUT] + objs + ["-lcudart", "-lnvrtc"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        futs = [ex.submit(compile_one, s, verbose) for s in srcs]
+        probe_futs = [ex.submit(compile_one, s, verbose) for s in probe_srcs]
+        objs = [f.result()[0] for f in futs]
+        probe_objs = [f.result()[0] for f in probe_futs]
+    for out, os_, libs in ((OUT, objs, ["-lcudart", "-lnvrtc"]), (PROBE_OUT, probe_objs, ["-lcudart"])):
+        if not os.path.exists(out) or any(os.path.getmtime(o) > os.path.getmtime(out) for o in os_):
+            cmd = [nvcc()] + ARCH + ["-shared", "-o", out] + os_ + libs
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     return OUT
 
 

@@ -299,17 +299,33 @@ DD_HD float dd_ffrom(unsigned int b) {
 #endif
 }
 
+// a * b rounded on its own: never contracted with a later addition into an FMA, in device code
+// compiled with contraction as on the host.
+DD_HD double dd_mul_nc(double a, double b) {
+#if defined(__CUDA_ARCH__)
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+
 // The controller's power x^(-0.2) (DOPRI5 and the order-5 pairs) and x^(-0.125) (DOP853),
-// correctly rounded as pow_ctrl, for the contracted FP64 forms: the same double-double Newton
-// finish, with two savings that matter where FP64 runs at 1/64 of the FP32 rate.
-//  - The FP32 starting value is built from the bit pattern of x with integer and FP32
-//    operations only (no FP64 conversion or ldexp).
-//  - The factor exp(-2^-54 ln(x) / 5) that turns 1/5 into binary64 0.2 takes ln(x) from FP32
-//    (absolute error below 2^-14 over the whole range, the FP32 rounding of the exponent sum
-//    included, so the factor is off by less than 2^-69.5 relative).  The result is then the
-//    correctly rounded value unless the computed sum lies within 2^-68 of a rounding boundary
-//    (Ziv's test on the exact remainder of the final addition); only then is ln(x) evaluated in
-//    FP64 (about one call in 2^13).
+// correctly rounded as pow_ctrl, for the contracted FP64 forms, with as few FP64 instructions as
+// possible (FP64 runs at 1/64 of the FP32 rate on this GPU):
+//  - Start: x = 2^e m with e = q k + r, 0 <= r < q, so x^(-1/q) = 2^-k (2^r m)^(-1/q).  The
+//    second factor lies in (1/2, 1] and comes from FP32 log2/exp2 of 2^r m (relative error near
+//    2^-22); the exponent -k is put into the bit pattern with integer operations.
+//  - One correction from the exact residual instead of Newton steps: x s^q = H + L is formed with
+//    error-free products (TwoProduct by FMA, Ogita-Rump-Oishi 2005) to about 2^-100, without
+//    renormalising the intermediate pairs; with e = 1 - x s^q (|e| < 2^-19),
+//    x^(-1/q) = s (1 - e)^(-1/q) = s (1 + e/q + c2 e^2 + c3 e^3 + c4 e^4 + ...), the binomial
+//    series truncated after e^4 (the rest is below 2^-90).
+//  - For 1/5, the factor exp(-2^-54 ln(x) / 5) that turns 1/5 into binary64 0.2 takes ln(x) from
+//    FP32 (off by less than 2^-69.5 relative).
+//  - Ziv's test on the exact remainder of the final addition: the total error is below 2^-69 of
+//    the result, so the rounded sum is the correctly rounded value unless it lies within 2^-68 of
+//    a rounding boundary; only then (about one call in 2^13) does pow_ctrl evaluate it again in
+//    double-double arithmetic.
 // x must be finite and in [2^-800, 2^800] after the caller's scaling; other x go to pow_ctrl.
 DD_HD double pow_ctrl_neg(double x, double y) {
     const bool fifth = y == -0.2;
@@ -317,48 +333,60 @@ DD_HD double pow_ctrl_neg(double x, double y) {
     const int q = fifth ? 5 : 8;
     const long long b = dd_bits(x);
     const int ex = (int)((b >> 52) & 0x7ff) - 1023;
-    const float m = dd_ffrom(0x3f800000u | (unsigned int)((b >> 29) & 0x7fffff));  // 1.mantissa, 23 bits
-    const float lx = (float)ex + log2f(m);                                     // log2(x) in FP32
-    const float tq = -lx / (float)q;
-    const float kf = floorf(tq);
-    const unsigned int fb = dd_fbits(exp2f(tq - kf));                              // in [1, 2]
-    const int e2 = (int)((fb >> 23) & 0xff) - 127 + (int)kf;
-    double s = dd_from_bits(((long long)(e2 + 1023) << 52) | ((long long)(fb & 0x7fffff) << 29));
-    const double q1 = (double)(q + 1), iq = fifth ? 0.2 : 0.125;
-    for (int it = 0; it < 2; ++it) {
-        double s2 = s * s;
-        double s4 = s2 * s2;
-        double sq = fifth ? s4 * s : s4 * s4;
-        s = s * (q1 - x * sq) * iq;
+    const int k = (ex + 1000) / q - 1000 / q;  // floor(ex / q): ex + 1000 > 0
+    const int r = ex - q * k;                  // in [0, q)
+    const float lm = log2f(dd_ffrom(0x3f800000u | (unsigned int)((b >> 29) & 0x7fffff)));  // log2 m, m in [1, 2)
+    const unsigned int fb = dd_fbits(exp2f(-((float)r + lm) * (fifth ? 0.2f : 0.125f)));   // in [1/2, 1]
+    const int e2 = (int)((fb >> 23) & 0xff) - 127 - k;
+    const double s = dd_from_bits(((long long)(e2 + 1023) << 52) | ((long long)(fb & 0x7fffff) << 29));
+    // x s^q = H + L
+    const double s2h = s * s;
+    const double s2l = fma(s, s, -s2h);
+    const double s4h = s2h * s2h;
+    const double s4l = fma(2.0, s2h * s2l, fma(s2h, s2h, -s4h));
+    double H, L;
+    if (fifth) {
+        const double ph = x * s;
+        const double pl = fma(x, s, -ph);
+        H = dd_mul_nc(ph, s4h);
+        L = fma(pl, s4h, fma(ph, s4l, fma(ph, s4h, -H)));
+    } else {
+        const double s8h = s4h * s4h;
+        const double s8l = fma(2.0, s4h * s4l, fma(s4h, s4h, -s8h));
+        H = dd_mul_nc(x, s8h);
+        L = fma(x, s8l, fma(x, s8h, -H));
     }
-    dd s2 = two_prod(s, s);
-    dd s4 = dd_mul(s2, s2);
-    dd sq = fifth ? dd_mul_d(s4, s) : dd_mul(s4, s4);
-    dd xsq = dd_mul_d(sq, x);
-    double e = (1.0 - xsq.hi) - xsq.lo;  // 1 - xsq.hi is exact: xsq.hi is within 2^-50 of 1
-    dd r = fast_two_sum(s, s * e * iq);
-    if (!fifth) return r.hi + r.lo;
-    // binary64 0.2 = (1/5)(1 + 2^-54): multiply by exp(-2^-54 ln(x) / 5) = 1 + g
-    const float gf = lx * -7.6954796e-18f;  // -(2^-54 / 5) ln 2 = -7.69547959e-18
-    const unsigned int gb = dd_fbits(gf);
-    const int ge = (int)((gb >> 23) & 0xff);
-    const double g = ge == 0 ? 0.0
-                             : dd_from_bits(((long long)(gb >> 31) << 63) | ((long long)(ge + 896) << 52) |
-                                            ((long long)(gb & 0x7fffff) << 29));
-    double t = r.lo + r.hi * g;
-    double res = r.hi + t;
-    const double tail = (r.hi - res) + t;  // exact: r.hi + t - res
-    // half an ulp of res, and the error bound 2^-64 res
+    // e = eh + el; 1 - H is exact (H is within 2^-18 of 1)
+    const double eh = 1.0 - H, el = -L;
+    double P;
+    if (fifth)  // (1 - e)^(-1/5) - 1: 1/5, 6/50, 66/750, 1056/15000
+        P = eh * fma(eh, fma(eh, fma(eh, 0.0704, 0.088), 0.12), 0.2);
+    else        // (1 - e)^(-1/8) - 1: 1/8, 9/128, 51/1024, 1275/32768
+        P = eh * fma(eh, fma(eh, fma(eh, 0.038909912109375, 0.0498046875), 0.0703125), 0.125);
+    P = fma(fifth ? 0.2 : 0.125, el, P);
+    const double c = dd_mul_nc(s, P);
+    const double hi = s + c;
+    double lo = c - (hi - s);  // exact: |c| < 2^-17 |s|
+    if (fifth) {
+        // binary64 0.2 = (1/5)(1 + 2^-54): multiply by exp(-2^-54 ln(x) / 5) = 1 + g
+        const float gf = ((float)ex + lm) * -7.6954796e-18f;  // -(2^-54 / 5) ln 2 log2(x)
+        const unsigned int gb = dd_fbits(gf);
+        const int ge = (int)((gb >> 23) & 0xff);
+        const double g = ge == 0 ? 0.0
+                                 : dd_from_bits(((long long)(gb >> 31) << 63) | ((long long)(ge + 896) << 52) |
+                                                ((long long)(gb & 0x7fffff) << 29));
+        lo = fma(hi, g, lo);
+    }
+    const double res = hi + lo;
+    const double tail = (hi - res) + lo;  // exact: hi + lo - res
+    // half an ulp of res (below a power of two the spacing halves) against the error bound 2^-68 res
     const long long rb = dd_bits(res);
     const int re = (int)((rb >> 52) & 0x7ff);
-    // (below a power of two the spacing halves)
     const bool below_pow2 = (rb & 0xfffffffffffffll) == 0 && tail < 0.0;
     const double half_ulp = dd_from_bits((long long)(re - (below_pow2 ? 54 : 53)) << 52);
     const double bound = dd_from_bits((long long)(re - 67) << 52);  // > 2^-68 res
     if (fabs(tail) + bound < half_ulp) return res;
-    const double gx = -1.1102230246251566e-17 /* 2^-54 / 5 */ * log(x);
-    t = r.lo + r.hi * (gx + 0.5 * gx * gx);
-    return r.hi + t;
+    return pow_ctrl(x, y);
 }
 
 // sin(u), cos(u) as double-doubles for |u.hi| <= 1/128.

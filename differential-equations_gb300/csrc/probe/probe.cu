@@ -1,8 +1,15 @@
-// peak_probe.cu — FP64 / FP32 FMA throughput probe used as the roofline denominator of the
-// ALU-bound ensemble kernels.  Each thread runs 8 independent FMA chains; the grid covers every
-// SM several times over.  Not part of the public ABI.
+// probe.cu — libdegpu_probe.so: measurement and device self-checks, kept out of the integrator
+// library.  Not part of the public ABI.
+//  - degpu_internal_fma_peak: FP64 / FP32 FMA throughput, the roofline denominator of the
+//    ALU-bound ensemble kernels.  Each thread runs 8 independent FMA chains; the grid covers every
+//    SM several times over.
+//  - degpu_internal_conv_check: the mixed form's integer-op conversions on the device.
+//  - degpu_internal_pow_ctrl_neg_check: the plain FP64 form's controller power on the device,
+//    compiled as the plain form is (FMA contraction on, CUDA's FP32 log2f/exp2f in its start).
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "erk_core.cuh"
 
 template <class T>
 __global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
@@ -51,10 +58,7 @@ extern "C" int degpu_internal_fma_peak(int fp64, double* tflops) {
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
-// Checks of the mixed form's integer-op conversions (widen_f32, narrow_rz in erk_core.cuh) on
-// device: wide[i] = widen_f32(f[i]), narrow[i] = narrow_rz(d[i]).  Device pointers, n elements.
-#include "erk_core.cuh"
-
+// wide[i] = widen_f32(f[i]), narrow[i] = narrow_rz(d[i]) (erk_core.cuh).  Device pointers.
 __global__ void conv_check_kernel(int64_t n, const float* f, double* wide, const double* d, float* narrow) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -65,5 +69,18 @@ __global__ void conv_check_kernel(int64_t n, const float* f, double* wide, const
 extern "C" int degpu_internal_conv_check(int64_t n, const float* f, double* wide, const double* d, float* narrow) {
     if (n <= 0) return 0;
     conv_check_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, f, wide, d, narrow);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+
+// out[i] = x[i]^y through the plain form's controller power (PrecPlain::pow).  Device pointers.
+__global__ void pow_check_kernel(int64_t n, const double* x, double y, double* out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = degpu::PrecPlain::pow(x[i], y);
+}
+
+extern "C" int degpu_internal_pow_ctrl_neg_check(int64_t n, const double* x, double y, double* out) {
+    if (n <= 0) return 0;
+    pow_check_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, x, y, out);
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
 }

@@ -12,6 +12,9 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 PKG_ROOT = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(PKG_ROOT, "csrc", "libdegpu.so")
+# measurement and device self-checks (FMA peak probe, conversion and controller-power checks),
+# built beside libdegpu.so and used by the benchmark and the tests only
+PROBE_PATH = os.path.join(PKG_ROOT, "csrc", "libdegpu_probe.so")
 
 # degpu_status
 OK, BAD_INPUT, OOM, TIMEOUT, CUDA_ERROR, UNSUPPORTED = range(6)
@@ -267,6 +270,27 @@ def load(path: str = LIB_PATH):
         fn.argtypes = args
     if path == LIB_PATH:
         _lib = lib
+    return lib
+
+
+_probe = None
+
+
+def load_probe():
+    """Open libdegpu_probe.so (the benchmark's FMA peak probe and the tests' device checks)."""
+    global _probe
+    if _probe is not None:
+        return _probe
+    if not os.path.exists(PROBE_PATH):
+        raise RuntimeError(f"libdegpu_probe.so is not built ({PROBE_PATH}); run __graft_entry__.build()")
+    lib = C.CDLL(PROBE_PATH)
+    lib.degpu_internal_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    lib.degpu_internal_fma_peak.restype = C.c_int
+    lib.degpu_internal_conv_check.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.degpu_internal_conv_check.restype = C.c_int
+    lib.degpu_internal_pow_ctrl_neg_check.argtypes = [C.c_int64, C.c_void_p, C.c_double, C.c_void_p]
+    lib.degpu_internal_pow_ctrl_neg_check.restype = C.c_int
+    _probe = lib
     return lib
 
 

@@ -1,6 +1,5 @@
 """Integer-op FP32<->FP64 conversions of the mixed form's per-step bookkeeping, checked on the
 device against numpy: widening is exact; narrowing rounds toward zero."""
-import ctypes as C
 
 import numpy as np
 import pytest
@@ -12,10 +11,7 @@ pytestmark = pytest.mark.gpu
 
 def test_widen_exact_and_narrow_toward_zero():
     torch = pytest.importorskip("torch")
-    lib = abi.load()
-    fn = lib.degpu_internal_conv_check
-    fn.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
-    fn.restype = C.c_int
+    fn = abi.load_probe().degpu_internal_conv_check
     rng = np.random.default_rng(3)
     n = 1 << 20
     f = (rng.standard_normal(n) * 10.0 ** rng.integers(-37, 38, n)).astype(np.float32)
