@@ -309,23 +309,73 @@ DD_HD double dd_mul_nc(double a, double b) {
 #endif
 }
 
+// 128-bit fixed-point helpers for the controller power's residual (integer pipe only).
+typedef unsigned long long dd_u64;
+DD_HD dd_u64 dd_umulhi(dd_u64 a, dd_u64 b) {
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (dd_u64)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+DD_HD int dd_clz64(dd_u64 a) {  // a != 0
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)a);
+#else
+    return __builtin_clzll(a);
+#endif
+}
+// A positive number M 2^(E - 127) with the 128-bit mantissa M = (h, l) in [2^127, 2^128).
+struct dd_fx {
+    dd_u64 h, l;
+    int e;
+};
+DD_HD dd_fx dd_fx_norm(dd_u64 h, dd_u64 l, int e) {
+    if (!(h >> 63)) {
+        h = (h << 1) | (l >> 63);
+        l <<= 1;
+        e -= 1;
+    }
+    return {h, l, e};
+}
+// a times the 64-bit mantissa m in [2^63, 2^64) (the number m 2^-63): the top 128 bits of the
+// product, truncated (below 2^-126 relative)
+DD_HD dd_fx dd_fx_mul64(dd_fx a, dd_u64 m) {
+    dd_u64 h = dd_umulhi(a.h, m), l = a.h * m;
+    const dd_u64 c = dd_umulhi(a.l, m);
+    l += c;
+    h += (l < c);
+    return dd_fx_norm(h, l, a.e + 1);
+}
+// a squared: the top 128 bits, truncated (below 2^-125 relative)
+DD_HD dd_fx dd_fx_sqr(dd_fx a) {
+    dd_u64 h = dd_umulhi(a.h, a.h), l = a.h * a.h;
+    const dd_u64 m = dd_umulhi(a.h, a.l);  // 2 a.h a.l / 2^64, less its low bit
+    const dd_u64 t = m << 1;
+    l += t;
+    h += (m >> 63) + (l < t);
+    return dd_fx_norm(h, l, 2 * a.e + 1);
+}
+
 // The controller's power x^(-0.2) (DOPRI5 and the order-5 pairs) and x^(-0.125) (DOP853),
 // correctly rounded as pow_ctrl, for the contracted FP64 forms, with as few FP64 instructions as
-// possible (FP64 runs at 1/64 of the FP32 rate on this GPU):
+// possible (FP64 runs at 1/64 of the FP32 rate on this GPU, integer and FP32 work issues in its
+// shadow):
 //  - Start: x = 2^e m with e = q k + r, 0 <= r < q, so x^(-1/q) = 2^-k (2^r m)^(-1/q).  The
 //    second factor lies in (1/2, 1] and comes from FP32 log2/exp2 of 2^r m (relative error near
 //    2^-22); the exponent -k is put into the bit pattern with integer operations.
-//  - One correction from the exact residual instead of Newton steps: x s^q = H + L is formed with
-//    error-free products (TwoProduct by FMA, Ogita-Rump-Oishi 2005) to about 2^-100, without
-//    renormalising the intermediate pairs; with e = 1 - x s^q (|e| < 2^-19),
-//    x^(-1/q) = s (1 - e)^(-1/q) = s (1 + e/q + c2 e^2 + c3 e^3 + c4 e^4 + ...), the binomial
-//    series truncated after e^4 (the rest is below 2^-90).
+//  - The residual e = 1 - x s^q (|e| < 2^-18) in 128-bit fixed point on the integer pipe: the
+//    mantissas of s and x multiplied out with truncated 128-bit products (relative error below
+//    2^-120), e converted to binary64 by truncation (absolute error below 2^-70).
+//  - One correction instead of Newton steps: x^(-1/q) = s (1 - e)^(-1/q)
+//    = s (1 + e/q + c2 e^2 + c3 e^3 + c4 e^4 + ...), the binomial series truncated after e^4 (the
+//    rest is below 2^-88).
 //  - For 1/5, the factor exp(-2^-54 ln(x) / 5) that turns 1/5 into binary64 0.2 takes ln(x) from
 //    FP32 (off by less than 2^-69.5 relative).
-//  - Ziv's test on the exact remainder of the final addition: the total error is below 2^-69 of
-//    the result, so the rounded sum is the correctly rounded value unless it lies within 2^-68 of
-//    a rounding boundary; only then (about one call in 2^13) does pow_ctrl evaluate it again in
-//    double-double arithmetic.
+//  - Ziv's test on the exact remainder of the final addition, in integer arithmetic: the total
+//    error is below 2^-68.9 of the result, so the rounded sum is the correctly rounded value
+//    unless it lies within 2^-68 of a rounding boundary; only then (about one call in 2^13) does
+//    pow_ctrl evaluate it again in double-double arithmetic.
 // x must be finite and in [2^-800, 2^800] after the caller's scaling; other x go to pow_ctrl.
 DD_HD double pow_ctrl_neg(double x, double y) {
     const bool fifth = y == -0.2;
@@ -337,33 +387,46 @@ DD_HD double pow_ctrl_neg(double x, double y) {
     const int r = ex - q * k;                  // in [0, q)
     const float lm = log2f(dd_ffrom(0x3f800000u | (unsigned int)((b >> 29) & 0x7fffff)));  // log2 m, m in [1, 2)
     const unsigned int fb = dd_fbits(exp2f(-((float)r + lm) * (fifth ? 0.2f : 0.125f)));   // in [1/2, 1]
-    const int e2 = (int)((fb >> 23) & 0xff) - 127 - k;
-    const double s = dd_from_bits(((long long)(e2 + 1023) << 52) | ((long long)(fb & 0x7fffff) << 29));
-    // x s^q = H + L
-    const double s2h = s * s;
-    const double s2l = fma(s, s, -s2h);
-    const double s4h = s2h * s2h;
-    const double s4l = fma(2.0, s2h * s2l, fma(s2h, s2h, -s4h));
-    double H, L;
-    if (fifth) {
-        const double ph = x * s;
-        const double pl = fma(x, s, -ph);
-        H = dd_mul_nc(ph, s4h);
-        L = fma(pl, s4h, fma(ph, s4l, fma(ph, s4h, -H)));
+    const int es = (int)((fb >> 23) & 0xff) - 127 - k;
+    const long long sb = ((long long)(es + 1023) << 52) | ((long long)(fb & 0x7fffff) << 29);
+    const double s = dd_from_bits(sb);
+    // x s^q = W 2^(ex + q es) with W = v u^q, u and v the mantissas of s and x in [1, 2)
+    const dd_u64 U = ((dd_u64)sb << 11) | (1ull << 63), V = ((dd_u64)b << 11) | (1ull << 63);
+    dd_fx w = dd_fx_norm(dd_umulhi(U, U), U * U, 1);  // u^2
+    w = dd_fx_sqr(w);                                 // u^4
+    w = fifth ? dd_fx_mul64(w, U) : dd_fx_sqr(w);     // u^5 or u^8
+    w = dd_fx_mul64(w, V);
+    const int T = w.e + ex + q * es;  // x s^q = M 2^(T - 127): 0 (x s^q in [1, 2)) or -1
+    if (T != 0 && T != -1) return pow_ctrl(x, y);
+    // D = |1 - x s^q| 2^(127 - T) as a 128-bit integer
+    dd_u64 dh, dl;
+    if (T == 0) {
+        dh = w.h & 0x7fffffffffffffffull;
+        dl = w.l;
     } else {
-        const double s8h = s4h * s4h;
-        const double s8l = fma(2.0, s4h * s4l, fma(s4h, s4h, -s8h));
-        H = dd_mul_nc(x, s8h);
-        L = fma(x, s8l, fma(x, s8h, -H));
+        dl = 0ull - w.l;
+        dh = ~w.h + (w.l == 0);
     }
-    // e = eh + el; 1 - H is exact (H is within 2^-18 of 1)
-    const double eh = 1.0 - H, el = -L;
+    double e = 0.0;
+    if (dh | dl) {
+        // leading bit p, the 53 bits from it (truncated) and e = +-D 2^(T - 127)
+        const int p = dh ? 127 - dd_clz64(dh) : 63 - dd_clz64(dl);
+        const int n = p - 52;
+        dd_u64 mnt;
+        if (n >= 64)
+            mnt = dh >> (n - 64);
+        else if (n > 0)
+            mnt = (dl >> n) | (dh << (64 - n));
+        else
+            mnt = dl << (-n);
+        const long long eb = ((long long)(p + T - 127 + 1023) << 52) | (long long)(mnt & 0xfffffffffffffull);
+        e = dd_from_bits(T == 0 ? (eb | (long long)0x8000000000000000ull) : eb);
+    }
     double P;
     if (fifth)  // (1 - e)^(-1/5) - 1: 1/5, 6/50, 66/750, 1056/15000
-        P = eh * fma(eh, fma(eh, fma(eh, 0.0704, 0.088), 0.12), 0.2);
+        P = e * fma(e, fma(e, fma(e, 0.0704, 0.088), 0.12), 0.2);
     else        // (1 - e)^(-1/8) - 1: 1/8, 9/128, 51/1024, 1275/32768
-        P = eh * fma(eh, fma(eh, fma(eh, 0.038909912109375, 0.0498046875), 0.0703125), 0.125);
-    P = fma(fifth ? 0.2 : 0.125, el, P);
+        P = e * fma(e, fma(e, fma(e, 0.038909912109375, 0.0498046875), 0.0703125), 0.125);
     const double c = dd_mul_nc(s, P);
     const double hi = s + c;
     double lo = c - (hi - s);  // exact: |c| < 2^-17 |s|
@@ -379,13 +442,15 @@ DD_HD double pow_ctrl_neg(double x, double y) {
     }
     const double res = hi + lo;
     const double tail = (hi - res) + lo;  // exact: hi + lo - res
-    // half an ulp of res (below a power of two the spacing halves) against the error bound 2^-68 res
-    const long long rb = dd_bits(res);
+    // |tail| against half an ulp of res less the error bound 2^-68 res, compared as bit patterns
+    // (both non-negative): half_ulp = 2^(re - 53) (2^(re - 54) just below a power of two, where
+    // the spacing halves), bound = 2^(re - 67), biased exponents
+    const long long rb = dd_bits(res), tb = dd_bits(tail);
     const int re = (int)((rb >> 52) & 0x7ff);
-    const bool below_pow2 = (rb & 0xfffffffffffffll) == 0 && tail < 0.0;
-    const double half_ulp = dd_from_bits((long long)(re - (below_pow2 ? 54 : 53)) << 52);
-    const double bound = dd_from_bits((long long)(re - 67) << 52);  // > 2^-68 res
-    if (fabs(tail) + bound < half_ulp) return res;
+    const int hu = re - (((rb & 0xfffffffffffffll) == 0 && tb < 0) ? 54 : 53);
+    const int kk = hu - (re - 67);  // 14 or 13: half_ulp - bound = 2^(hu - 1) (2 - 2^(1 - kk))
+    const long long lim = ((long long)(hu - 1) << 52) | ((1ll << 52) - (1ll << (53 - kk)));
+    if ((tb & 0x7fffffffffffffffll) < lim) return res;
     return pow_ctrl(x, y);
 }
 
