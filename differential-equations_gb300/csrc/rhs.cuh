@@ -107,7 +107,9 @@ struct PrecParity {
     static constexpr bool KAHAN = false;
     static constexpr bool F32_CTRL = false;
     static constexpr int MULTI_MIN_BLOCKS = 1;
-    __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl(x, y); }
+    // the controller's x^(-0.2) and x^(-0.125) through pow_ctrl_neg (fixed-point residual, Ziv's
+    // test, pow_ctrl behind it): the same correctly rounded values with far fewer FP64 instructions
+    __device__ static __forceinline__ double pow(double x, double y) { return ddm::pow_ctrl_neg(x, y); }
     __device__ static __forceinline__ double sin(double x) { return ddm::sin_cr(x); }
     __device__ static __forceinline__ double cos(double x) { return ddm::cos_cr(x); }
     __device__ static __forceinline__ S from(double x) { return x; }
