@@ -345,9 +345,14 @@ def _oracle_solve(e, method, threads, math_mode=0):
     return o, time.perf_counter() - t
 
 
-# DRAM bytes (read + write) of the four FP32 Gray-Scott passes of one RK4 step at 4096^2, from an
-# ncu capture of gs_pass_vec_kernel<float>
+# DRAM bytes (read + write) of one FP32 Gray-Scott RK4 step at 4096^2 from ncu captures: the four
+# passes of gs_pass_vec_kernel<float>, and the fused step gs_step_fused_kernel (None until captured)
 GS_NCU_TRAFFIC_FP32 = 1.84e9
+GS_NCU_TRAFFIC_FP32_FUSED = None
+# FP32 operations per node and RK4 step (FMA = 2): four evaluations of f (44 each: u v^2, the two
+# sources, two flux differences per axis and field), three stage states (4) and the four
+# accumulation terms (4)
+GS_FLOPS_PER_NODE_STEP = 4 * 44 + 3 * 4 + 4 * 4
 
 # the hyperplane workload's plane: pos = (y0, y1) through (0.1, -0.2) with normal (1, 1)
 PLANE = ([0, 1], [0.1, -0.2], [1.0, 1.0])
@@ -706,10 +711,17 @@ def run_fpu(args, torch, dev, lib, n=None, emit=True):
 
 def run_gray_scott(args, torch, dev, lib, emit=True):
     """2-D Gray-Scott, 4096 x 4096 periodic, RK4 dt = 0.2 dx^2/Du, 1000 steps, FP64 and FP32:
-    time per step and algorithmic HBM bandwidth against the measured copy bandwidth, on two byte
-    models per node and RK4 step: this build's passes (15 arrays of 2 fields: 240 / 120 B FP64 /
-    FP32) and the minimal one (13 arrays: 208 / 104 B).  The inputs (134 / 268 MB) are larger
-    than L2; the 1000 steps are one timed call."""
+    time per step and HBM bandwidth against the measured copy bandwidth.  FP32 runs the fused step
+    (one launch per RK4 step: y and k0 in, y_next and k0 out, 32 B per node and step) and, beside
+    it, the four passes (15 arrays of 2 fields: 120 B; the survey's minimal pass model counts 13
+    arrays, 104 B); FP64 runs the passes (240 / 208 B).  The inputs (134 / 268 MB) are larger than
+    L2; the 1000 steps are one timed call."""
+    fused_fn = lib.degpu_internal_gs_fused_step
+    fused_fn.argtypes = [C.c_int]
+    fused_fn.restype = C.c_int
+    fp32_peak = C.c_double(0.0)
+    abi.load_probe().degpu_internal_fma_peak(0, C.byref(fp32_peak))
+    fp32_peak = fp32_peak.value
     nx = ny = args.gs_n
     dx = 1.0 / 4096
     p = W.GRAY_SCOTT
@@ -723,24 +735,34 @@ def run_gray_scott(args, torch, dev, lib, emit=True):
         peak = json.load(open(mp)).get("hbm_gbs")
     res, ck = {}, None
     steps = args.gs_steps
-    for name, prec, tdt, bpn in (("fp32", abi.MIXED, torch.float32, 120), ("fp64", abi.FP64_FAST, torch.float64, 240),
+    for name, prec, tdt, bpn in (("fp32", abi.MIXED, torch.float32, 32), ("fp32-passes", abi.MIXED, torch.float32, 120),
+                                 ("fp64", abi.FP64_FAST, torch.float64, 240),
                                  ("fp64-parity", abi.FP64_PARITY, torch.float64, 240)):
         u = torch.as_tensor(u0, dtype=tdt, device=dev)
         v = torch.as_tensor(v0, dtype=tdt, device=dev)
         f = lambda: lib.degpu_gray_scott_rk4(C.byref(gs), prec, 0.0, dt, steps, C.c_void_p(u.data_ptr()),
                                              C.c_void_p(v.data_ptr()), C.c_void_p(stream.cuda_stream))
-        if name == "fp32":
-            ms, ck = _clock_ms(f, stream, torch, 1, clocks=Clocks())
-        else:
-            ms = _clock_ms(f, stream, torch, 1)
+        prev = fused_fn(0 if name == "fp32-passes" else 1)
+        try:
+            if name == "fp32":
+                ms, ck = _clock_ms(f, stream, torch, 1, clocks=Clocks())
+            else:
+                ms = _clock_ms(f, stream, torch, 1)
+        finally:
+            fused_fn(prev)
         per_step = ms / steps
         gbs = bpn * nx * ny / (per_step * 1e-3) / 1e9
-        gbs_min = (bpn * 13 // 15) * nx * ny / (per_step * 1e-3) / 1e9
-        res[name] = {"ms_per_step": per_step, "algorithmic_GBps": gbs,
+        res[name] = {"ms_per_step": per_step, "bytes_per_node_step": bpn, "algorithmic_GBps": gbs,
                      "frac_of_measured_hbm": (gbs / peak) if peak else None,
-                     "algorithmic_GBps_13_arrays": gbs_min,
-                     "frac_of_measured_hbm_13_arrays": (gbs_min / peak) if peak else None,
                      "node_steps_per_s": nx * ny / (per_step * 1e-3)}
+        if name != "fp32":
+            gbs_min = (bpn * 13 // 15) * nx * ny / (per_step * 1e-3) / 1e9
+            res[name]["algorithmic_GBps_13_arrays"] = gbs_min
+            res[name]["frac_of_measured_hbm_13_arrays"] = (gbs_min / peak) if peak else None
+        if tdt == torch.float32:
+            tf = GS_FLOPS_PER_NODE_STEP * nx * ny / (per_step * 1e-3) / 1e12
+            res[name]["fp32_algorithmic"] = {"achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                                             "frac": tf / fp32_peak if fp32_peak else None}
     # CPU baseline: the oracle's restatement of SemiDiscretePde::diff on a 256x256 grid, 4 steps
     sys.path.insert(0, os.path.join(REPO, "tests"))
     import oracle_lib as O
@@ -759,10 +781,12 @@ def run_gray_scott(args, torch, dev, lib, emit=True):
             "ms_per_step": res["fp32"]["ms_per_step"],
             "variants": res, "hbm_peak_GBps": peak, "clocks": ck,
             "roofline": {"bound": "hbm", "achieved": res["fp32"]["algorithmic_GBps"], "peak": peak, "unit": "GB/s",
-                         "frac": res["fp32"]["frac_of_measured_hbm"], "kernel": "gs_pass_vec_kernel<float>",
-                         "traffic": GS_NCU_TRAFFIC_FP32, "traffic_unit": "bytes per RK4 step (4 launches)",
-                         "bytes_per_node_step": 120,
-                         "frac_13_arrays": res["fp32"]["frac_of_measured_hbm_13_arrays"]},
+                         "frac": res["fp32"]["frac_of_measured_hbm"], "kernel": "gs_step_fused_kernel<64x32>",
+                         "traffic": GS_NCU_TRAFFIC_FP32_FUSED, "traffic_unit": "bytes per RK4 step (1 launch)",
+                         "bytes_per_node_step": 32, "fp32": res["fp32"]["fp32_algorithmic"],
+                         "note": "fused step: y and k0 in, y_next and k0 out; the four-pass form (120 B per "
+                                 "node and step, ncu traffic %.3g B per step) is variant fp32-passes"
+                                 % GS_NCU_TRAFFIC_FP32},
             "cpu_baseline": {"value": cn * cn * 4 / cdt, "unit": "node-steps/s", "cores": threads, "kind": "port",
                              "sample": "256x256 grid, 4 RK4 steps, FP64 (restated SemiDiscretePde::diff)"}}
     if emit:

@@ -18,12 +18,46 @@ static bool is_pow2(double x) {
     return m == 0.5;
 }
 
+// The fused FP32 step (one launch per RK4 step, gs_step_fused_kernel) replaces the four passes
+// where the grid divides into its tiles (nx % 64 == 0, ny % 32 == 0); degpu_internal_gs_fused_step(0) turns it off (the tests
+// compare the two).
+// tiles of 64 x 32 nodes, 512 threads, two blocks (2 x 92 KB of shared memory) per SM: measured
+// on 4096^2, 0.239 ms per step against 0.246 ms for 32 x 32 tiles with 256 threads, 0.251 ms for
+// 32 x 32 with 512 and 0.300 ms for 64 x 32 with 256 (the four passes: 0.317 ms)
+#ifndef DEGPU_GS_TX
+#define DEGPU_GS_TX 64
+#define DEGPU_GS_TY 32
+#endif
+constexpr int GS_TX = DEGPU_GS_TX, GS_TY = DEGPU_GS_TY;
+static int g_gs_fused = 1;
+
+// the kernel's shared-memory opt-in (51 KB), set once before its first launch (and so outside any
+// stream capture)
+template <bool POW2>
+static cudaError_t gs_fused_prepare() {
+    static cudaError_t attr = cudaFuncSetAttribute(gs_step_fused_kernel<POW2, GS_TX, GS_TY>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)gs_fused_smem<GS_TX, GS_TY>());
+    return attr;
+}
+
+template <bool POW2>
+static cudaError_t gs_fused_launch(const GsFusedPlanes& P, const GsParams<float>& p, const GsFusedCoef& cf,
+                                   cudaStream_t s) {
+    constexpr size_t smem = gs_fused_smem<GS_TX, GS_TY>();
+    dim3 grd(p.nx / GS_TX, p.ny / GS_TY);
+    gs_step_fused_kernel<POW2, GS_TX, GS_TY><<<grd, GS_FUSED_THREADS, smem, s>>>(P, p, cf);
+    return cudaGetLastError();
+}
+
 template <class T>
 struct GsRun {
     using Fn = cudaError_t (*)(int, const GsPlanes&, const GsParams<T>&, cudaStream_t);
     Fn fn;
     GsParams<T> p;
     double h;
+    bool fused = false;  // FP32 only: one fused launch per step, k0 alternating between buf[0..1] and buf[2..3]
+    bool pow2 = true;
     T* buf[10];  // k0u k0v k1u k1v k2u k2v accu accv ybu ybv
 
     cudaError_t pass4(const void* yu, const void* yv, cudaStream_t s) {
@@ -34,9 +68,27 @@ struct GsRun {
         P.ov = buf[1];
         return fn(4, P, p, s);
     }
-    // one RK4 step from (yu, yv) into (nu, nv); k0 in buf[0..1] on entry and exit
-    cudaError_t step(const void* yu, const void* yv, void* nu, void* nv, cudaStream_t s) {
+    // one RK4 step from (yu, yv) into (nu, nv); k0 in buf[0..1] on entry and exit (the fused
+    // form: in buf[2 kin .. 2 kin + 1] on entry, in the other pair on exit)
+    cudaError_t step(const void* yu, const void* yv, void* nu, void* nv, cudaStream_t s, int kin = 0) {
         const double b0 = 1.0 / 6.0, b1 = 1.0 / 3.0, b2 = 1.0 / 3.0, b3 = 1.0 / 6.0;
+        if constexpr (sizeof(T) == 4) {
+            if (fused) {
+                GsFusedPlanes F{};
+                F.yu = (const float*)yu;
+                F.yv = (const float*)yv;
+                F.ku = (const float*)buf[2 * kin];
+                F.kv = (const float*)buf[2 * kin + 1];
+                F.nu = (float*)nu;
+                F.nv = (float*)nv;
+                F.knu = (float*)buf[2 - 2 * kin];
+                F.knv = (float*)buf[3 - 2 * kin];
+                // the passes' coefficients, rounded the same way
+                GsFusedCoef cf{(T)(0.5 * h), (T)(0.5 * h), (T)(1.0 * h), (T)(b0 * h), (T)(b1 * h), (T)(b2 * h),
+                               (T)(b3 * h)};
+                return pow2 ? gs_fused_launch<true>(F, p, cf, s) : gs_fused_launch<false>(F, p, cf, s);
+            }
+        }
         GsPlanes P{};
         P.yu = yu;
         P.yv = yv;
@@ -66,11 +118,15 @@ struct GsRun {
 
 template <class T>
 static degpu_status gs_run(const degpu_gray_scott* gs, typename GsRun<T>::Fn fn, double dt, int64_t steps, T* u, T* v,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool pow2 = true) {
     const size_t N = (size_t)gs->nx * gs->ny;
     GsRun<T> R;
     R.fn = fn;
     R.h = dt;
+    R.pow2 = pow2;
+    R.fused = sizeof(T) == 4 && g_gs_fused && gs->nx % GS_TX == 0 && gs->ny % GS_TY == 0;
+    if (R.fused && (pow2 ? gs_fused_prepare<true>() : gs_fused_prepare<false>()) != cudaSuccess)
+        return DEGPU_CUDA_ERROR;
     R.p.nx = gs->nx;
     R.p.ny = gs->ny;
     R.p.Du = (T)gs->Du;
@@ -79,6 +135,8 @@ static degpu_status gs_run(const degpu_gray_scott* gs, typename GsRun<T>::Fn fn,
     R.p.k = (T)gs->k;
     R.p.dx = (T)gs->dx;
     R.p.inv_dx = (T)(1.0 / gs->dx);
+    R.p.cu = (T)(gs->Du / (gs->dx * gs->dx));
+    R.p.cv = (T)(gs->Dv / (gs->dx * gs->dx));
     void* block = nullptr;
     if (cudaMallocAsync(&block, 10 * N * sizeof(T), s) != cudaSuccess) return DEGPU_OOM;
     for (int q = 0; q < 10; ++q) R.buf[q] = (T*)block + q * N;
@@ -97,8 +155,8 @@ static degpu_status gs_run(const degpu_gray_scott* gs, typename GsRun<T>::Fn fn,
         if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) st = DEGPU_CUDA_ERROR;
         if (st == DEGPU_OK) {
             cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-            cudaError_t e1 = R.step(ya[0], yb[0], ya[1], yb[1], cs);
-            cudaError_t e2 = R.step(ya[1], yb[1], ya[0], yb[0], cs);
+            cudaError_t e1 = R.step(ya[0], yb[0], ya[1], yb[1], cs, 0);
+            cudaError_t e2 = R.step(ya[1], yb[1], ya[0], yb[0], cs, 1);
             cudaError_t ec = cudaStreamEndCapture(cs, &g);
             if (e1 != cudaSuccess || e2 != cudaSuccess || ec != cudaSuccess ||
                 cudaGraphInstantiate(&ge, g, 0) != cudaSuccess)
@@ -111,7 +169,7 @@ static degpu_status gs_run(const degpu_gray_scott* gs, typename GsRun<T>::Fn fn,
         if (g) cudaGraphDestroy(g);
     }
     if (st == DEGPU_OK && done < steps) {
-        if (R.step(ya[0], yb[0], ya[1], yb[1], s) != cudaSuccess) st = DEGPU_CUDA_ERROR;
+        if (R.step(ya[0], yb[0], ya[1], yb[1], s, 0) != cudaSuccess) st = DEGPU_CUDA_ERROR;
         cur = 1;
         done += 1;
     }
@@ -145,10 +203,17 @@ degpu_status degpu_gray_scott_rk4(const degpu_gray_scott* gs, int32_t precision,
             return gs_run<double>(gs, p2 ? &gs_launch_pass<double, true> : &gs_launch_pass<double, false>, dt, steps,
                                   (double*)u, (double*)v, s);
         case DEGPU_MIXED:
-            return gs_run<float>(gs, &gs_launch_pass<float, true>, dt, steps, (float*)u, (float*)v, s);
+            return gs_run<float>(gs, &gs_launch_pass<float, true>, dt, steps, (float*)u, (float*)v, s, true);
         default:
             return DEGPU_BAD_INPUT;
     }
+}
+
+// Internal: the fused FP32 step on (1) or off (0); returns the previous setting.
+int degpu_internal_gs_fused_step(int on) {
+    const int prev = g_gs_fused;
+    g_gs_fused = on ? 1 : 0;
+    return prev;
 }
 
 degpu_status degpu_gray_scott_rhs(const degpu_gray_scott* gs, const double* u, const double* v, double* du, double* dv,

@@ -19,10 +19,14 @@
 // stencil: horizontal neighbours share the cache line, vertical ones hit L1/L2), so DRAM sees
 // each array once per pass.  Algorithmic bytes per node per step: 4 + 5 + 4 + 2 arrays read/written
 // of 2 fields -> (8 + 10 + 8 + 4) * sizeof(T) = 240 B (FP64), 120 B (FP32).
+// FP32 runs the same four stages in one launch per step where the grid divides into 64 x 32
+// tiles (gs_step_fused_kernel, below): 32 B per node and step, the same values bit for bit.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 namespace degpu {
 
@@ -30,16 +34,69 @@ template <class T>
 struct GsParams {
     int nx, ny;
     T Du, Dv, F, k, dx, inv_dx;
+    T cu, cv;   // FP32 form: Du / dx^2, Dv / dx^2
     T ah;       // stage coefficient a_{i,i-1} * h
     T bh0, bh1; // accumulation coefficients b_i * h of the pass
 };
 
+// Explicit rounding of every operation, so that the passes and the fused step (different kernels,
+// different surrounding code) compute the same values whatever the compiler would contract: gs_m
+// and gs_a are a single rounded multiply and add, gs_f a fused multiply-add, except in the parity
+// build (-fmad=false, DEGPU_NO_FMAD), where gs_f is a multiply then an add as the crate computes.
+__device__ __forceinline__ float gs_m(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double gs_m(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float gs_a(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double gs_a(double a, double b) { return __dadd_rn(a, b); }
+#if defined(DEGPU_NO_FMAD)
+template <class T>
+__device__ __forceinline__ T gs_f(T a, T b, T c) { return gs_a(gs_m(a, b), c); }
+#else
+__device__ __forceinline__ float gs_f(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double gs_f(double a, double b, double c) { return __fma_rn(a, b, c); }
+#endif
+
 template <class T, bool POW2>
 __device__ __forceinline__ T gs_ddx(T a, const GsParams<T>& p) {
     if constexpr (POW2)
-        return a * p.inv_dx;
+        return gs_m(a, p.inv_dx);
     else
         return a / p.dx;
+}
+
+// one node's f from its stage state and its four neighbours (l, r: x -+ 1; d, u: y -+ 1), in the
+// crate's order: der = source; for axis x then y: der = der + (F_hi - F_lo) / dx with
+// F_lo = D ((c - c_lo) / dx), F_hi = D ((c_hi - c) / dx)
+template <class T, bool POW2>
+__device__ __forceinline__ void gs_node(const GsParams<T>& p, T u, T v, T ul, T vl, T ur, T vr, T ud, T vd, T uu,
+                                        T vu, T& du, T& dv) {
+    if constexpr (sizeof(T) == 4) {
+        // FP32 (this build's own form, not the crate's order): the 5-point Laplacian as a sum of
+        // the four neighbour differences (each exact where neighbours lie within a factor of two)
+        // times D / dx^2, fused into the source term
+        const T uvv = gs_m(gs_m(u, v), v);
+        const T lu = gs_a(gs_a(gs_a(ur, -u), gs_a(ul, -u)), gs_a(gs_a(uu, -u), gs_a(ud, -u)));
+        const T lv = gs_a(gs_a(gs_a(vr, -v), gs_a(vl, -v)), gs_a(gs_a(vu, -v), gs_a(vd, -v)));
+        du = gs_f(p.cu, lu, gs_f(p.F, gs_a((T)1, -u), -uvv));
+        dv = gs_f(p.cv, lv, gs_f(-gs_a(p.F, p.k), v, uvv));
+        return;
+    }
+    const T uvv = gs_m(gs_m(u, v), v);
+    T a_u = gs_f(p.F, gs_a((T)1, -u), -uvv);     // -u v^2 + F (1 - u)
+    T a_v = gs_f(-gs_a(p.F, p.k), v, uvv);       //  u v^2 - (F + k) v
+    auto flux = [&](T a, T c, T lo, T hi, T D) {  // a + (F_hi - F_lo) / dx
+        const T flo = gs_m(D, gs_ddx<T, POW2>(gs_a(c, -lo), p));
+        const T fhi = gs_m(D, gs_ddx<T, POW2>(gs_a(hi, -c), p));
+        if constexpr (POW2)
+            return gs_f(gs_a(fhi, -flo), p.inv_dx, a);
+        else
+            return gs_a(a, gs_a(fhi, -flo) / p.dx);
+    };
+    a_u = flux(a_u, u, ul, ur, p.Du);
+    a_v = flux(a_v, v, vl, vr, p.Dv);
+    a_u = flux(a_u, u, ud, uu, p.Du);
+    a_v = flux(a_v, v, vd, vu, p.Dv);
+    du = a_u;
+    dv = a_v;
 }
 
 // f at node (i, j); `get(i, j, u, v)` returns the stage state at a node.
@@ -47,35 +104,13 @@ template <class T, bool POW2, class Get>
 __device__ __forceinline__ void gs_rhs_at(int i, int j, const GsParams<T>& p, Get get, T& du, T& dv) {
     const int im = i == 0 ? p.nx - 1 : i - 1, ip = i == p.nx - 1 ? 0 : i + 1;
     const int jm = j == 0 ? p.ny - 1 : j - 1, jp = j == p.ny - 1 ? 0 : j + 1;
-    T u, v;
+    T u, v, ul, vl, ur, vr, ud, vd, uu, vu;
     get(i, j, u, v);
-    T uvv = u * v * v;
-    T a_u = -uvv + p.F * ((T)1 - u);
-    T a_v = uvv - (p.F + p.k) * v;
-    T ul, vl, ur, vr;
     get(im, j, ul, vl);
     get(ip, j, ur, vr);
-    {
-        T flo_u = p.Du * gs_ddx<T, POW2>(u - ul, p);
-        T fhi_u = p.Du * gs_ddx<T, POW2>(ur - u, p);
-        a_u = a_u + gs_ddx<T, POW2>(fhi_u - flo_u, p);
-        T flo_v = p.Dv * gs_ddx<T, POW2>(v - vl, p);
-        T fhi_v = p.Dv * gs_ddx<T, POW2>(vr - v, p);
-        a_v = a_v + gs_ddx<T, POW2>(fhi_v - flo_v, p);
-    }
-    T ud, vd, uu, vu;
     get(i, jm, ud, vd);
     get(i, jp, uu, vu);
-    {
-        T flo_u = p.Du * gs_ddx<T, POW2>(u - ud, p);
-        T fhi_u = p.Du * gs_ddx<T, POW2>(uu - u, p);
-        a_u = a_u + gs_ddx<T, POW2>(fhi_u - flo_u, p);
-        T flo_v = p.Dv * gs_ddx<T, POW2>(v - vd, p);
-        T fhi_v = p.Dv * gs_ddx<T, POW2>(vu - v, p);
-        a_v = a_v + gs_ddx<T, POW2>(fhi_v - flo_v, p);
-    }
-    du = a_u;
-    dv = a_v;
+    gs_node<T, POW2>(p, u, v, ul, vl, ur, vr, ud, vd, uu, vu, du, dv);
 }
 
 struct GsPlanes {
@@ -119,31 +154,31 @@ __global__ void __launch_bounds__(256) gs_pass_kernel(GsPlanes P, GsParams<T> p)
         const T ah = p.ah;
         auto get = [&](int ii, int jj, T& u, T& v) {
             int64_t q = (int64_t)jj * nx + ii;
-            u = __ldg(yu + q) + ah * __ldg(ku + q);
-            v = __ldg(yv + q) + ah * __ldg(kv + q);
+            u = gs_f(ah, __ldg(ku + q), __ldg(yu + q));
+            v = gs_f(ah, __ldg(kv + q), __ldg(yv + q));
         };
         gs_rhs_at<T, POW2>(i, j, p, get, du, dv);
         if constexpr (PASS == 1) {
             const T* k0u = (const T*)P.k0u;
             const T* k0v = (const T*)P.k0v;
-            T au = yu[c] + p.bh0 * k0u[c];
-            T av = yv[c] + p.bh0 * k0v[c];
-            ((T*)P.accu)[c] = au + p.bh1 * du;
-            ((T*)P.accv)[c] = av + p.bh1 * dv;
+            T au = gs_f(p.bh0, k0u[c], yu[c]);
+            T av = gs_f(p.bh0, k0v[c], yv[c]);
+            ((T*)P.accu)[c] = gs_f(p.bh1, du, au);
+            ((T*)P.accv)[c] = gs_f(p.bh1, dv, av);
             ((T*)P.ou)[c] = du;
             ((T*)P.ov)[c] = dv;
         } else if constexpr (PASS == 2) {
             T* accu = (T*)P.accu;
             T* accv = (T*)P.accv;
-            accu[c] = accu[c] + p.bh0 * du;
-            accv[c] = accv[c] + p.bh0 * dv;
+            accu[c] = gs_f(p.bh0, du, accu[c]);
+            accv[c] = gs_f(p.bh0, dv, accv[c]);
             ((T*)P.ou)[c] = du;
             ((T*)P.ov)[c] = dv;
         } else {
             const T* accu = (const T*)P.accu;
             const T* accv = (const T*)P.accv;
-            ((T*)P.ynu)[c] = accu[c] + p.bh0 * du;
-            ((T*)P.ynv)[c] = accv[c] + p.bh0 * dv;
+            ((T*)P.ynu)[c] = gs_f(p.bh0, du, accu[c]);
+            ((T*)P.ynv)[c] = gs_f(p.bh0, dv, accv[c]);
         }
     }
 }
@@ -183,33 +218,6 @@ __device__ __forceinline__ void st4(T* p, const Vec4<T>& r) {
     }
 }
 
-// one node's f from its stage state and its four neighbours (gs_rhs_at's operation order)
-template <class T, bool POW2>
-__device__ __forceinline__ void gs_node(const GsParams<T>& p, T u, T v, T ul, T vl, T ur, T vr, T ud, T vd, T uu,
-                                        T vu, T& du, T& dv) {
-    T uvv = u * v * v;
-    T a_u = -uvv + p.F * ((T)1 - u);
-    T a_v = uvv - (p.F + p.k) * v;
-    {
-        T flo_u = p.Du * gs_ddx<T, POW2>(u - ul, p);
-        T fhi_u = p.Du * gs_ddx<T, POW2>(ur - u, p);
-        a_u = a_u + gs_ddx<T, POW2>(fhi_u - flo_u, p);
-        T flo_v = p.Dv * gs_ddx<T, POW2>(v - vl, p);
-        T fhi_v = p.Dv * gs_ddx<T, POW2>(vr - v, p);
-        a_v = a_v + gs_ddx<T, POW2>(fhi_v - flo_v, p);
-    }
-    {
-        T flo_u = p.Du * gs_ddx<T, POW2>(u - ud, p);
-        T fhi_u = p.Du * gs_ddx<T, POW2>(uu - u, p);
-        a_u = a_u + gs_ddx<T, POW2>(fhi_u - flo_u, p);
-        T flo_v = p.Dv * gs_ddx<T, POW2>(v - vd, p);
-        T fhi_v = p.Dv * gs_ddx<T, POW2>(vu - v, p);
-        a_v = a_v + gs_ddx<T, POW2>(fhi_v - flo_v, p);
-    }
-    du = a_u;
-    dv = a_v;
-}
-
 template <class T, bool POW2, int PASS>
 __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T> p) {
     constexpr int R = 4;  // rows per thread
@@ -238,8 +246,8 @@ __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T
             Vec4<T> c = ld4(ku + o), d = ld4(kv + o);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                su[r][q] = a.v[q] + ah * c.v[q];
-                sv[r][q] = b.v[q] + ah * d.v[q];
+                su[r][q] = gs_f(ah, c.v[q], a.v[q]);
+                sv[r][q] = gs_f(ah, d.v[q], b.v[q]);
             }
         } else {
 #pragma unroll
@@ -268,8 +276,8 @@ __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T
             const int64_t o = (int64_t)(j0 + r) * nx + xe;
             T eu = __ldg(yu + o), ev = __ldg(yv + o);
             if (has_k) {
-                eu = eu + ah * __ldg(ku + o);
-                ev = ev + ah * __ldg(kv + o);
+                eu = gs_f(ah, __ldg(ku + o), eu);
+                ev = gs_f(ah, __ldg(kv + o), ev);
             }
             if (lane == 0) {
                 lu[r] = eu;
@@ -302,8 +310,8 @@ __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T
             Vec4<T> au, av;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                au.v[q] = (y_u.v[q] + p.bh0 * k_u.v[q]) + p.bh1 * du.v[q];
-                av.v[q] = (y_v.v[q] + p.bh0 * k_v.v[q]) + p.bh1 * dv.v[q];
+                au.v[q] = gs_f(p.bh1, du.v[q], gs_f(p.bh0, k_u.v[q], y_u.v[q]));
+                av.v[q] = gs_f(p.bh1, dv.v[q], gs_f(p.bh0, k_v.v[q], y_v.v[q]));
             }
             st4((T*)P.accu + o, au);
             st4((T*)P.accv + o, av);
@@ -313,8 +321,8 @@ __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T
             Vec4<T> au = ld4((const T*)P.accu + o), av = ld4((const T*)P.accv + o);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                au.v[q] = au.v[q] + p.bh0 * du.v[q];
-                av.v[q] = av.v[q] + p.bh0 * dv.v[q];
+                au.v[q] = gs_f(p.bh0, du.v[q], au.v[q]);
+                av.v[q] = gs_f(p.bh0, dv.v[q], av.v[q]);
             }
             st4((T*)P.accu + o, au);
             st4((T*)P.accv + o, av);
@@ -324,12 +332,123 @@ __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T
             Vec4<T> au = ld4((const T*)P.accu + o), av = ld4((const T*)P.accv + o);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                au.v[q] = au.v[q] + p.bh0 * du.v[q];
-                av.v[q] = av.v[q] + p.bh0 * dv.v[q];
+                au.v[q] = gs_f(p.bh0, du.v[q], au.v[q]);
+                av.v[q] = gs_f(p.bh0, dv.v[q], av.v[q]);
             }
             st4((T*)P.ynu + o, au);
             st4((T*)P.ynv + o, av);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fused FP32 RK4 step (temporal blocking): one launch per step instead of four passes.  A block
+// owns a TX x TY tile of nodes and stages the tile plus a 4-node halo of y and k0 in shared memory
+// (both fields of a node side by side, one 8-byte word); the four stages then run on shrinking
+// regions (tile + 3, + 2, + 1 and the tile itself), so no stage result goes through HBM.  Per step
+// HBM sees y and k0 in and y_next and k0 out: 32 B per node against the passes' 120 B.  The cost
+// is the halo: f is evaluated on (TX+6)(TY+6) + (TX+4)(TY+4) + (TX+2)(TY+2) + TX TY nodes per
+// tile (1.15 x the tile's four evaluations at 64 x 32).  The stage state is double-buffered in
+// shared memory, so each stage's derivative goes straight into the accumulator and the next
+// stage state, and one barrier separates the stages.
+// Per node the arithmetic is the passes', in the same order (stage states y + (a h) k, gs_node,
+// the accumulation ((y + (b0 h) k0) + (b1 h) k1) + (b2 h) k2 + (b3 h) k3), so the results equal
+// the four-pass kernels' bit for bit.  Requires nx % TX == 0 and ny % TY == 0.
+// ---------------------------------------------------------------------------------------------
+struct GsFusedPlanes {
+    const float* yu;
+    const float* yv;
+    const float* ku;  // k0 = f(y) of this step's start
+    const float* kv;
+    float* nu;        // y_next
+    float* nv;
+    float* knu;       // k0 of the next step, f(y_next)
+    float* knv;
+};
+struct GsFusedCoef {
+    float ah1, ah2, ah3;       // stage coefficients a_{i,i-1} h
+    float bh0, bh1, bh2, bh3;  // weights b_i h
+};
+
+#ifndef DEGPU_GS_THREADS
+#define DEGPU_GS_THREADS 512
+#endif
+constexpr int GS_FUSED_THREADS = DEGPU_GS_THREADS;
+
+template <int TX, int TY>
+constexpr size_t gs_fused_smem() {
+    return 4 * (size_t)(TX + 8) * (TY + 8) * sizeof(float2);
+}
+
+template <bool POW2, int TX, int TY>
+__global__ void __launch_bounds__(GS_FUSED_THREADS) gs_step_fused_kernel(GsFusedPlanes P, GsParams<float> p,
+                                                                         GsFusedCoef cf) {
+    constexpr int HALO = 4, W = TX + 2 * HALO, HH = TY + 2 * HALO, N = W * HH;
+    extern __shared__ float2 gs_sm[];
+    float2* Ys = gs_sm;          // y on the tile + 4
+    float2* S0 = gs_sm + N;      // stage states, alternating
+    float2* S1 = gs_sm + 2 * N;
+    float2* As = gs_sm + 3 * N;  // accumulator (tile + 1)
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int nx = p.nx, ny = p.ny;
+    auto inner = [](int r, int c) { return r >= HALO - 1 && r < HH - HALO + 1 && c >= HALO - 1 && c < W - HALO + 1; };
+    // y and k0 on the tile + 4 (periodic wrap); s1 = y + (a10 h) k0 there, the accumulator's
+    // first term y + (b0 h) k0 on the tile + 1
+    for (int q = threadIdx.x; q < N; q += GS_FUSED_THREADS) {
+        const int r = q / W, c = q - r * W;
+        int gx = x0 - HALO + c;
+        gx += gx < 0 ? nx : (gx >= nx ? -nx : 0);
+        int gy = y0 - HALO + r;
+        gy += gy < 0 ? ny : (gy >= ny ? -ny : 0);
+        const int64_t g = (int64_t)gy * nx + gx;
+        const float yu = __ldg(P.yu + g), yv = __ldg(P.yv + g);
+        const float ku = __ldg(P.ku + g), kv = __ldg(P.kv + g);
+        Ys[q] = make_float2(yu, yv);
+        S0[q] = make_float2(gs_f(cf.ah1, ku, yu), gs_f(cf.ah1, kv, yv));
+        if (inner(r, c)) As[q] = make_float2(gs_f(cf.bh0, ku, yu), gs_f(cf.bh0, kv, yv));
+    }
+    __syncthreads();
+    // stage K: k = f(Sc) on the tile + K; the accumulator on the tile + 1 takes (b h) k and the next
+    // stage state y + (a h) k goes to Sn (after the last stage: y_next = acc + (b3 h) k3)
+    auto stage = [&](auto kk, const float2* Sc, float2* Sn, float bh, float ah) {
+        constexpr int K = decltype(kk)::value, w = TX + 2 * K, h = TY + 2 * K, off = HALO - K;
+        for (int i = threadIdx.x; i < w * h; i += GS_FUSED_THREADS) {
+            const int r = i / w + off, c = i % w + off;
+            const int q = r * W + c;
+            const float2 sc = Sc[q], sl = Sc[q - 1], sr = Sc[q + 1], sd = Sc[q - W], su = Sc[q + W];
+            float du, dv;
+            gs_node<float, POW2>(p, sc.x, sc.y, sl.x, sl.y, sr.x, sr.y, sd.x, sd.y, su.x, su.y, du, dv);
+            if constexpr (K > 1) {
+                if (inner(r, c)) {
+                    const float2 a = As[q];
+                    As[q] = make_float2(gs_f(bh, du, a.x), gs_f(bh, dv, a.y));
+                }
+                const float2 y = Ys[q];
+                Sn[q] = make_float2(gs_f(ah, du, y.x), gs_f(ah, dv, y.y));
+            } else {
+                const float2 a = As[q];
+                Sn[q] = make_float2(gs_f(bh, du, a.x), gs_f(bh, dv, a.y));
+            }
+        }
+    };
+    stage(std::integral_constant<int, 3>{}, S0, S1, cf.bh1, cf.ah2);  // k1 on the tile + 3
+    __syncthreads();
+    stage(std::integral_constant<int, 2>{}, S1, S0, cf.bh2, cf.ah3);  // k2 on the tile + 2
+    __syncthreads();
+    stage(std::integral_constant<int, 1>{}, S0, S1, cf.bh3, 0.0f);    // k3 and y_next on the tile + 1
+    __syncthreads();
+    // k0 of the next step = f(y_next) on the tile; y_next and k0 out
+    for (int i = threadIdx.x; i < TX * TY; i += GS_FUSED_THREADS) {
+        const int r = i / TX + HALO, c = i % TX + HALO;
+        const int q = r * W + c;
+        const float2 sc = S1[q], sl = S1[q - 1], sr = S1[q + 1], sd = S1[q - W], su = S1[q + W];
+        float du, dv;
+        gs_node<float, POW2>(p, sc.x, sc.y, sl.x, sl.y, sr.x, sr.y, sd.x, sd.y, su.x, su.y, du, dv);
+        const int64_t g = (int64_t)(y0 + r - HALO) * nx + (x0 + c - HALO);
+        P.nu[g] = sc.x;
+        P.nv[g] = sc.y;
+        P.knu[g] = du;
+        P.knv[g] = dv;
     }
 }
 

@@ -97,3 +97,33 @@ def test_gray_scott_full_size_properties():
     assert np.all(np.isfinite(a_u)) and a_u.min() >= 0.0 and a_u.max() <= 1.0 + 1e-9
     f_u, f_v = gpu_rk4(gs, abi.MIXED, dt, 50, u, v)
     assert np.max(np.abs(f_u - a_u)) < 1e-4 and np.max(np.abs(f_v - a_v)) < 1e-4
+
+
+def set_fused(on):
+    fn = abi.load().degpu_internal_gs_fused_step
+    fn.argtypes = [C.c_int]
+    fn.restype = C.c_int
+    return fn(1 if on else 0)
+
+
+# (192, 96): fused tiles, but the passes take their one-node-per-thread kernel (nx % 128 != 0)
+@pytest.mark.parametrize("shape,steps", [((4096, 4096), 7), ((256, 128), 5), ((192, 96), 3)])
+def test_gray_scott_fused_fp32_step_equals_four_passes(shape, steps):
+    """The fused FP32 RK4 step (one launch per step, tiles of 64 x 32 nodes with a 4-node halo in
+    shared memory, periodic wrap across the grid's edges) against the four-pass kernels: the same
+    arithmetic in the same order, so the states agree bit for bit, over an odd number of steps
+    (the graph of two steps and a single step after it)."""
+    nx, ny = shape
+    dx = 1.0 / nx
+    gs = gs_struct(nx, ny, dx)
+    dt = 0.2 * dx * dx / W.GRAY_SCOTT["Du"]
+    u, v = W.gray_scott_init(nx, ny) if nx == 4096 else small_state(nx, ny)
+    prev = set_fused(True)
+    try:
+        fu, fv = gpu_rk4(gs, abi.MIXED, dt, steps, u, v)
+        set_fused(False)
+        pu, pv = gpu_rk4(gs, abi.MIXED, dt, steps, u, v)
+    finally:
+        set_fused(prev)
+    assert np.array_equal(fu, pu) and np.array_equal(fv, pv)
+    assert np.all(np.isfinite(fu)) and not np.array_equal(fu, u)
