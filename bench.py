@@ -1275,6 +1275,43 @@ def main():
                 tab = acc_s.table(vy, floor)
                 accuracy["variants"][v] = {"by_family_and_rtol": tab, "rule": acc_s.meets_fp64_floor(tab)}
 
+    # the serial tail: the instance with the most step attempts, solved alone (one lane of one
+    # warp), with the headline variant; however many instances share the GPU, a solve takes at
+    # least this long
+    tail = None
+    if rank == 0:
+        att = acc.astype(np.int64) + rej.astype(np.int64)
+        it = int(np.argmax(att))
+        one = e.subset(np.array([it]))
+        t_in = dict(t0=T(one.t0), tf=T(one.tf), y0=T(one.y0), params=T(one.params), rtol=T(one.rtol),
+                    atol=T(one.atol), family=T(one.family, torch.int32))
+        t_out = {k: torch.empty((3, 1) if k == "y_final" else (1,), dtype=v.dtype, device=dev)
+                 for k, v in d_out.items()}
+        tbi = abi.BatchIn(n=1, t0=abi.ptr(t_in["t0"]), tf=abi.ptr(t_in["tf"]), y0=abi.ptr(t_in["y0"]),
+                          params=abi.ptr(t_in["params"]), rtol=abi.ptr(t_in["rtol"]), atol=abi.ptr(t_in["atol"]),
+                          family=abi.ptr(t_in["family"], C.c_int32), n_eval=0)
+        tbo = abi.BatchOut(y_final=abi.ptr(t_out["y_final"]), t_final=abi.ptr(t_out["t_final"]),
+                           accepted=abi.ptr(t_out["accepted"], C.c_int64),
+                           rejected=abi.ptr(t_out["rejected"], C.c_int64),
+                           fevals=abi.ptr(t_out["fevals"], C.c_int64), status=abi.ptr(t_out["status"], C.c_int32))
+
+        def solve_one():
+            rc = lib.degpu_solve_ensemble(C.byref(prob), C.byref(cfg), C.byref(tbi), C.byref(tbo),
+                                          C.c_void_p(stream.cuda_stream))
+            if rc != abi.OK:
+                raise RuntimeError(f"degpu_solve_ensemble failed: {rc}")
+
+        t1 = _clock_ms(solve_one, stream, torch, 3)
+        a1 = int(t_out["accepted"].item()) + int(t_out["rejected"].item())
+        fam_names = {abi.RHS["VAN_DER_POL"]: "van_der_pol", abi.RHS["PENDULUM"]: "pendulum",
+                     abi.RHS["LORENZ"]: "lorenz"}
+        tail = {"instance": it, "family": fam_names.get(int(e.family[it]), str(int(e.family[it]))),
+                "rtol": float(e.rtol[it]), "t_end": float(e.tf[it]), "step_attempts": int(att[it]),
+                "step_attempts_alone": a1, "alone_ms": t1, "ns_per_attempt_alone": t1 * 1e6 / max(a1, 1),
+                "share_of_solve_time": t1 / ms,
+                "note": "the instance with the most step attempts, solved alone with the headline variant: "
+                        "its serial step count x per-step latency bounds the solve time from below"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -1316,6 +1353,7 @@ def main():
         "clocks": ck,
         "variants": extra,
         "agreement_with_crate": agree,
+        "tail": tail,
         # the headline variant's accuracy against FP64 where FP64 meets 1e-6 (accuracy.*.rule)
         "headline_meets_accuracy_rule": (accuracy["variants"][args.variant]["rule"]["variant_meets_1e-6_there"]
                                          if accuracy and args.variant in accuracy["variants"] else None),
