@@ -16,6 +16,10 @@
 //  - x^(±1/5): one double-double Newton step on r^5 = x from a few-ulp starting value
 //    (quadratic convergence), then the factor x^(2^-54/5) = exp(2^-54 ln(x)/5) that turns 1/5
 //    into the binary64 value 0.2 = (1/5)(1 + 2^-54) (truncated exponential series);
+//  - the controller's x^(-0.2) and x^(-0.125) with few FP64 instructions (pow_ctrl_neg): an FP32
+//    start on the range-reduced exponent, the residual 1 - x s^q in 128-bit fixed point on the
+//    integer pipe, the binomial series of (1 - e)^(-1/q) and Ziv's rounding test (Ziv 1991), with
+//    the double-double power behind it;
 //  - x^(±1/8): three double-double square roots (Karp–Markstein correction);
 //  - x^(±1/q), q = 6, 7, 9: Newton on s^-q = x finished in double-double, reciprocal for the
 //    positive exponent, and the same exp correction for binary64 1/q;

@@ -35,6 +35,15 @@ def test_library_exports_every_declared_symbol():
     assert set(declared_functions()) <= set(abi.SIGNATURES)
 
 
+def test_probe_library_is_separate_from_the_integrator():
+    """The FMA peak probe and the device self-checks live in libdegpu_probe.so, which the benchmark
+    and the tests load; the integrator library exports none of them."""
+    probe = abi.load_probe()
+    for name in ("degpu_internal_fma_peak", "degpu_internal_conv_check", "degpu_internal_pow_ctrl_neg_check"):
+        assert hasattr(probe, name), name
+        assert not hasattr(abi.load(), name), name
+
+
 def test_rust_binding_declares_every_entry_point_and_struct():
     """The Rust sys crate a maintainer would add to the crate binds every function and struct of
     the header (it cannot be compiled here: no Rust toolchain)."""
