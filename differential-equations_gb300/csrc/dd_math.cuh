@@ -361,6 +361,45 @@ DD_HD dd_fx dd_fx_sqr(dd_fx a) {
     return dd_fx_norm(h, l, 2 * a.e + 1);
 }
 
+// e = 1 - x s^q for q = 5 or 8, x and s normal and x s^q in [1/2, 2), on the integer pipe: the
+// mantissas multiplied out in 128-bit fixed point (truncated products, relative error below
+// 2^-120), e rounded toward zero to 53 bits.  ok = false when x s^q lies outside [1/2, 2).
+DD_HD double pow_ctrl_residual(double x, double s, int q, bool& ok) {
+    const long long b = dd_bits(x), sb = dd_bits(s);
+    const int ex = (int)((b >> 52) & 0x7ff) - 1023, es = (int)((sb >> 52) & 0x7ff) - 1023;
+    // x s^q = W 2^(ex + q es) with W = v u^q, u and v the mantissas of s and x in [1, 2)
+    const dd_u64 U = ((dd_u64)sb << 11) | (1ull << 63), V = ((dd_u64)b << 11) | (1ull << 63);
+    dd_fx w = dd_fx_norm(dd_umulhi(U, U), U * U, 1);  // u^2
+    w = dd_fx_sqr(w);                                 // u^4
+    w = q == 5 ? dd_fx_mul64(w, U) : dd_fx_sqr(w);    // u^5 or u^8
+    w = dd_fx_mul64(w, V);
+    const int T = w.e + ex + q * es;  // x s^q = M 2^(T - 127): 0 (x s^q in [1, 2)) or -1
+    ok = T == 0 || T == -1;
+    if (!ok) return 0.0;
+    // D = |1 - x s^q| 2^(127 - T) as a 128-bit integer
+    dd_u64 dh, dl;
+    if (T == 0) {
+        dh = w.h & 0x7fffffffffffffffull;
+        dl = w.l;
+    } else {
+        dl = 0ull - w.l;
+        dh = ~w.h + (w.l == 0);
+    }
+    if (!(dh | dl)) return 0.0;
+    // leading bit p, the 53 bits from it (truncated) and e = +-D 2^(T - 127)
+    const int p = dh ? 127 - dd_clz64(dh) : 63 - dd_clz64(dl);
+    const int n = p - 52;
+    dd_u64 mnt;
+    if (n >= 64)
+        mnt = dh >> (n - 64);
+    else if (n > 0)
+        mnt = (dl >> n) | (dh << (64 - n));
+    else
+        mnt = dl << (-n);
+    const long long eb = ((long long)(p + T - 127 + 1023) << 52) | (long long)(mnt & 0xfffffffffffffull);
+    return dd_from_bits(T == 0 ? (eb | (long long)0x8000000000000000ull) : eb);
+}
+
 // The controller's power x^(-0.2) (DOPRI5 and the order-5 pairs) and x^(-0.125) (DOP853),
 // correctly rounded as pow_ctrl, for the contracted FP64 forms, with as few FP64 instructions as
 // possible (FP64 runs at 1/64 of the FP32 rate on this GPU, integer and FP32 work issues in its
@@ -394,38 +433,9 @@ DD_HD double pow_ctrl_neg(double x, double y) {
     const int es = (int)((fb >> 23) & 0xff) - 127 - k;
     const long long sb = ((long long)(es + 1023) << 52) | ((long long)(fb & 0x7fffff) << 29);
     const double s = dd_from_bits(sb);
-    // x s^q = W 2^(ex + q es) with W = v u^q, u and v the mantissas of s and x in [1, 2)
-    const dd_u64 U = ((dd_u64)sb << 11) | (1ull << 63), V = ((dd_u64)b << 11) | (1ull << 63);
-    dd_fx w = dd_fx_norm(dd_umulhi(U, U), U * U, 1);  // u^2
-    w = dd_fx_sqr(w);                                 // u^4
-    w = fifth ? dd_fx_mul64(w, U) : dd_fx_sqr(w);     // u^5 or u^8
-    w = dd_fx_mul64(w, V);
-    const int T = w.e + ex + q * es;  // x s^q = M 2^(T - 127): 0 (x s^q in [1, 2)) or -1
-    if (T != 0 && T != -1) return pow_ctrl(x, y);
-    // D = |1 - x s^q| 2^(127 - T) as a 128-bit integer
-    dd_u64 dh, dl;
-    if (T == 0) {
-        dh = w.h & 0x7fffffffffffffffull;
-        dl = w.l;
-    } else {
-        dl = 0ull - w.l;
-        dh = ~w.h + (w.l == 0);
-    }
-    double e = 0.0;
-    if (dh | dl) {
-        // leading bit p, the 53 bits from it (truncated) and e = +-D 2^(T - 127)
-        const int p = dh ? 127 - dd_clz64(dh) : 63 - dd_clz64(dl);
-        const int n = p - 52;
-        dd_u64 mnt;
-        if (n >= 64)
-            mnt = dh >> (n - 64);
-        else if (n > 0)
-            mnt = (dl >> n) | (dh << (64 - n));
-        else
-            mnt = dl << (-n);
-        const long long eb = ((long long)(p + T - 127 + 1023) << 52) | (long long)(mnt & 0xfffffffffffffull);
-        e = dd_from_bits(T == 0 ? (eb | (long long)0x8000000000000000ull) : eb);
-    }
+    bool ok;
+    const double e = pow_ctrl_residual(x, s, q, ok);
+    if (!ok) return pow_ctrl(x, y);
     double P;
     if (fifth)  // (1 - e)^(-1/5) - 1: 1/5, 6/50, 66/750, 1056/15000
         P = e * fma(e, fma(e, fma(e, 0.0704, 0.088), 0.12), 0.2);

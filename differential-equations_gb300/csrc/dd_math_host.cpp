@@ -11,6 +11,15 @@ void degpu_host_pow_ctrl(const double* x, double y, double* out, int64_t n) {
 void degpu_host_pow_ctrl_neg(const double* x, double y, double* out, int64_t n) {
     for (int64_t i = 0; i < n; ++i) out[i] = degpu::ddm::pow_ctrl_neg(x[i], y);
 }
+// e[i] = 1 - x[i] s[i]^q through the controller power's fixed-point residual; NaN where x s^q lies
+// outside [1/2, 2)
+void degpu_host_pow_residual(const double* x, const double* s, int q, double* e, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+        bool ok;
+        const double r = degpu::ddm::pow_ctrl_residual(x[i], s[i], q, ok);
+        e[i] = ok ? r : NAN;
+    }
+}
 void degpu_host_sincos_f32(const float* x, float* s, float* c, int64_t n) {
     for (int64_t i = 0; i < n; ++i) {
         s[i] = degpu::f32m::sin_f32(x[i]);

@@ -4,6 +4,7 @@
 // launches instead of 4000 kernel launches.
 #include <math.h>
 
+#include <mutex>
 #include <vector>
 
 #include "../../include/degpu.h"
@@ -31,14 +32,22 @@ static bool is_pow2(double x) {
 constexpr int GS_TX = DEGPU_GS_TX, GS_TY = DEGPU_GS_TY;
 static int g_gs_fused = 1;
 
-// the kernel's shared-memory opt-in (51 KB), set once before its first launch (and so outside any
-// stream capture)
+// the kernel's shared-memory opt-in (92 KB), set on each device before the first launch there
+// (and so outside any stream capture)
 template <bool POW2>
 static cudaError_t gs_fused_prepare() {
-    static cudaError_t attr = cudaFuncSetAttribute(gs_step_fused_kernel<POW2, GS_TX, GS_TY>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)gs_fused_smem<GS_TX, GS_TY>());
-    return attr;
+    static std::mutex mu;
+    static std::vector<int> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (done[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(gs_step_fused_kernel<POW2, GS_TX, GS_TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gs_fused_smem<GS_TX, GS_TY>());
+    if (e == cudaSuccess) done[dev] = 1;
+    return e;
 }
 
 template <bool POW2>

@@ -24,6 +24,7 @@ def H():
     h = C.CDLL(SO)
     h.degpu_host_pow_ctrl.argtypes = [O.DP, C.c_double, O.DP, C.c_int64]
     h.degpu_host_pow_ctrl_neg.argtypes = [O.DP, C.c_double, O.DP, C.c_int64]
+    h.degpu_host_pow_residual.argtypes = [O.DP, O.DP, C.c_int, O.DP, C.c_int64]
     h.degpu_host_sincos_cr.argtypes = [O.DP, O.DP, O.DP, C.c_int64]
     FP = C.POINTER(C.c_float)
     h.degpu_host_sincos_f32.argtypes = [FP, FP, FP, C.c_int64]
@@ -67,6 +68,37 @@ def test_pow_ctrl_neg_correctly_rounded(H, y):
     H.degpu_host_pow_ctrl_neg(O.p(x2), y, O.p(out2), 5)
     ref2 = np.array([O.lib().oracle_cr_pow(v, y) for v in x2])
     assert np.array_equal(out2, ref2, equal_nan=True)
+
+
+@pytest.mark.parametrize("q", [5, 8])
+def test_pow_residual_fixed_point_exact(H, q):
+    """The controller power's residual e = 1 - x s^q, formed in 128-bit fixed point on the
+    integer pipe, against exact rational arithmetic: e is the exact residual rounded toward zero to
+    53 bits (the fixed-point truncation, below 2^-120, never shows), on starting values s within
+    2^-19 of x^(-1/q) and exactly on x^(-1/q) rounded, across the exponent range."""
+    from fractions import Fraction
+    H.degpu_host_pow_residual.argtypes = [O.DP, O.DP, C.c_int, O.DP, C.c_int64]
+    rng = np.random.default_rng(5 + q)
+    n = 3000
+    x = np.exp(rng.uniform(np.log(2.0 ** -800), np.log(2.0 ** 800), n))
+    x[:200] = 2.0 ** rng.integers(-790, 790, 200)
+    s = x ** (-1.0 / q)
+    s[n // 2:] *= 1.0 + rng.uniform(-2.0 ** -19, 2.0 ** -19, n - n // 2)
+    e = np.empty(n)
+    H.degpu_host_pow_residual(O.p(x), O.p(s), q, O.p(e), n)
+    for xi, si, ei in zip(x, s, e):
+        exact = 1 - Fraction(xi) * Fraction(si) ** q
+        if exact == 0:
+            assert ei == 0.0
+            continue
+        assert np.isfinite(ei) and Fraction(ei) * exact >= 0           # same sign
+        assert abs(Fraction(ei)) <= abs(exact)                          # toward zero
+        assert abs(exact - Fraction(ei)) < abs(exact) * Fraction(1, 2 ** 52)  # within 53 bits
+    # outside [1/2, 2) the residual is refused
+    bad = np.array([1.0, 2.0 ** 10]), np.array([2.0, 1.0])
+    out = np.empty(2)
+    H.degpu_host_pow_residual(O.p(bad[0]), O.p(bad[1]), q, O.p(out), 2)
+    assert np.all(np.isnan(out))
 
 
 def test_pow_ctrl_special_values(H):
