@@ -1024,7 +1024,8 @@ def main():
     ap.add_argument("--fpu-slice", type=int, default=16384,
                     help="chains of the FPU-beta configuration timed in the default run")
     ap.add_argument("--n", type=int, default=1 << 20)
-    ap.add_argument("--cpu-sample", type=int, default=12000)
+    # 1/8 of the ensemble, spread over it (every 8th instance): about 3 s on 16 host cores
+    ap.add_argument("--cpu-sample", type=int, default=131072)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--workload", default="uneven",
