@@ -346,7 +346,8 @@ def _oracle_solve(e, method, threads, math_mode=0):
 
 
 # DRAM bytes (read + write) of one FP32 Gray-Scott RK4 step at 4096^2 from ncu captures: the four
-# passes of gs_pass_vec_kernel<float>, and the fused step gs_step_fused_kernel (one launch)
+# passes of gs_pass_vec_kernel<float>, and the fused step gs_step_fused_kernel (one launch; captured
+# on its one-node-per-thread version, which moves the same arrays)
 GS_NCU_TRAFFIC_FP32 = 1.84e9
 GS_NCU_TRAFFIC_FP32_FUSED = 4.937e8
 # FP32 operations per node and RK4 step (FMA = 2): four evaluations of f (44 each: u v^2, the two
@@ -785,7 +786,7 @@ def run_gray_scott(args, torch, dev, lib, emit=True):
                          "traffic": GS_NCU_TRAFFIC_FP32_FUSED, "traffic_unit": "bytes per RK4 step (1 launch)",
                          "bytes_per_node_step": 32, "fp32": res["fp32"]["fp32_algorithmic"],
                          "note": "fused step: y and k0 in, y_next and k0 out; limited by instruction issue "
-                                 "(ncu: 62 %% of cycles issuing, 0.31 of HBM), not by HBM; the four-pass form "
+                                 "(ncu: 62 %% of cycles issuing on its first version), not by HBM; the four-pass form "
                                  "(120 B per node and step, HBM-bound, ncu traffic %.3g B per step) is variant "
                                  "fp32-passes" % GS_NCU_TRAFFIC_FP32},
             "cpu_baseline": {"value": cn * cn * 4 / cdt, "unit": "node-steps/s", "cores": threads, "kind": "port",

@@ -3,6 +3,7 @@
 // graph, because the state is double-buffered) and replayed, so a 1000-step run costs ~500 graph
 // launches instead of 4000 kernel launches.
 #include <math.h>
+#include <stdint.h>
 
 #include <mutex>
 #include <vector>
@@ -23,8 +24,9 @@ static bool is_pow2(double x) {
 // where the grid divides into its tiles (nx % 64 == 0, ny % 32 == 0); degpu_internal_gs_fused_step(0) turns it off (the tests
 // compare the two).
 // tiles of 64 x 32 nodes, 512 threads, two blocks (2 x 92 KB of shared memory) per SM: measured
-// on 4096^2, 0.239 ms per step against 0.246 ms for 32 x 32 tiles with 256 threads, 0.251 ms for
-// 32 x 32 with 512 and 0.300 ms for 64 x 32 with 256 (the four passes: 0.317 ms)
+// on 4096^2 with one node per thread and scalar halo loads, 0.239 ms per step against 0.246 ms for
+// 32 x 32 tiles with 256 threads, 0.251 ms for 32 x 32 with 512 and 0.300 ms for 64 x 32 with 256
+// (the four passes: 0.317 ms); with two rows per thread and 16-byte halo loads, 0.202 ms
 #ifndef DEGPU_GS_TX
 #define DEGPU_GS_TX 64
 #define DEGPU_GS_TY 32
@@ -133,7 +135,9 @@ static degpu_status gs_run(const degpu_gray_scott* gs, typename GsRun<T>::Fn fn,
     R.fn = fn;
     R.h = dt;
     R.pow2 = pow2;
-    R.fused = sizeof(T) == 4 && g_gs_fused && gs->nx % GS_TX == 0 && gs->ny % GS_TY == 0;
+    // the fused step loads y in 16-byte chunks: the caller's planes must start on 16-byte boundaries
+    R.fused = sizeof(T) == 4 && g_gs_fused && gs->nx % GS_TX == 0 && gs->ny % GS_TY == 0 &&
+              ((uintptr_t)u & 15u) == 0 && ((uintptr_t)v & 15u) == 0;
     if (R.fused && (pow2 ? gs_fused_prepare<true>() : gs_fused_prepare<false>()) != cudaSuccess)
         return DEGPU_CUDA_ERROR;
     R.p.nx = gs->nx;

@@ -350,7 +350,9 @@ __global__ void __launch_bounds__(128) gs_pass_vec_kernel(GsPlanes P, GsParams<T
 // is the halo: f is evaluated on (TX+6)(TY+6) + (TX+4)(TY+4) + (TX+2)(TY+2) + TX TY nodes per
 // tile (1.15 x the tile's four evaluations at 64 x 32).  The stage state is double-buffered in
 // shared memory, so each stage's derivative goes straight into the accumulator and the next
-// stage state, and one barrier separates the stages.
+// stage state, and one barrier separates the stages.  The halo comes in with 16-byte loads (four
+// nodes along x), and each thread evaluates two vertically adjacent nodes, which share two of
+// their shared-memory loads.
 // Per node the arithmetic is the passes', in the same order (stage states y + (a h) k, gs_node,
 // the accumulation ((y + (b0 h) k0) + (b1 h) k1) + (b2 h) k2 + (b3 h) k3), so the results equal
 // the four-pass kernels' bit for bit.  Requires nx % TX == 0 and ny % TY == 0.
@@ -384,42 +386,57 @@ template <bool POW2, int TX, int TY>
 __global__ void __launch_bounds__(GS_FUSED_THREADS) gs_step_fused_kernel(GsFusedPlanes P, GsParams<float> p,
                                                                          GsFusedCoef cf) {
     constexpr int HALO = 4, W = TX + 2 * HALO, HH = TY + 2 * HALO, N = W * HH;
+    static_assert(TX % 4 == 0 && TY % 2 == 0, "16-byte row chunks and row pairs");
     extern __shared__ float2 gs_sm[];
     float2* Ys = gs_sm;          // y on the tile + 4
     float2* S0 = gs_sm + N;      // stage states, alternating
     float2* S1 = gs_sm + 2 * N;
-    float2* As = gs_sm + 3 * N;  // accumulator (tile + 1)
+    float2* As = gs_sm + 3 * N;  // accumulator (rows of the tile + 1; other columns unused)
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const int nx = p.nx, ny = p.ny;
-    auto inner = [](int r, int c) { return r >= HALO - 1 && r < HH - HALO + 1 && c >= HALO - 1 && c < W - HALO + 1; };
-    // y and k0 on the tile + 4 (periodic wrap); s1 = y + (a10 h) k0 there, the accumulator's
-    // first term y + (b0 h) k0 on the tile + 1
-    for (int q = threadIdx.x; q < N; q += GS_FUSED_THREADS) {
-        const int r = q / W, c = q - r * W;
+    // y and k0 on the tile + 4 (periodic wrap) in 16-byte chunks of 4 nodes along x (x0 - 4 and nx
+    // are multiples of 4, so a chunk never straddles the wrap); s1 = y + (a10 h) k0 there, the
+    // accumulator's first term y + (b0 h) k0 on the rows of the tile + 1
+    constexpr int CH = W / 4;
+    for (int i = threadIdx.x; i < CH * HH; i += GS_FUSED_THREADS) {
+        const int r = i / CH, c = (i - r * CH) * 4;
         int gx = x0 - HALO + c;
         gx += gx < 0 ? nx : (gx >= nx ? -nx : 0);
         int gy = y0 - HALO + r;
         gy += gy < 0 ? ny : (gy >= ny ? -ny : 0);
         const int64_t g = (int64_t)gy * nx + gx;
-        const float yu = __ldg(P.yu + g), yv = __ldg(P.yv + g);
-        const float ku = __ldg(P.ku + g), kv = __ldg(P.kv + g);
-        Ys[q] = make_float2(yu, yv);
-        S0[q] = make_float2(gs_f(cf.ah1, ku, yu), gs_f(cf.ah1, kv, yv));
-        if (inner(r, c)) As[q] = make_float2(gs_f(cf.bh0, ku, yu), gs_f(cf.bh0, kv, yv));
+        const float4 yu = __ldg(reinterpret_cast<const float4*>(P.yu + g));
+        const float4 yv = __ldg(reinterpret_cast<const float4*>(P.yv + g));
+        const float4 ku = __ldg(reinterpret_cast<const float4*>(P.ku + g));
+        const float4 kv = __ldg(reinterpret_cast<const float4*>(P.kv + g));
+        const int q = r * W + c;  // even: 16-byte aligned pairs of nodes
+        float4* y4 = reinterpret_cast<float4*>(Ys + q);
+        y4[0] = make_float4(yu.x, yv.x, yu.y, yv.y);
+        y4[1] = make_float4(yu.z, yv.z, yu.w, yv.w);
+        float4* s4 = reinterpret_cast<float4*>(S0 + q);
+        s4[0] = make_float4(gs_f(cf.ah1, ku.x, yu.x), gs_f(cf.ah1, kv.x, yv.x), gs_f(cf.ah1, ku.y, yu.y),
+                            gs_f(cf.ah1, kv.y, yv.y));
+        s4[1] = make_float4(gs_f(cf.ah1, ku.z, yu.z), gs_f(cf.ah1, kv.z, yv.z), gs_f(cf.ah1, ku.w, yu.w),
+                            gs_f(cf.ah1, kv.w, yv.w));
+        if (r >= HALO - 1 && r < HH - HALO + 1) {
+            float4* a4 = reinterpret_cast<float4*>(As + q);
+            a4[0] = make_float4(gs_f(cf.bh0, ku.x, yu.x), gs_f(cf.bh0, kv.x, yv.x), gs_f(cf.bh0, ku.y, yu.y),
+                                gs_f(cf.bh0, kv.y, yv.y));
+            a4[1] = make_float4(gs_f(cf.bh0, ku.z, yu.z), gs_f(cf.bh0, kv.z, yv.z), gs_f(cf.bh0, ku.w, yu.w),
+                                gs_f(cf.bh0, kv.w, yv.w));
+        }
     }
     __syncthreads();
-    // stage K: k = f(Sc) on the tile + K; the accumulator on the tile + 1 takes (b h) k and the next
-    // stage state y + (a h) k goes to Sn (after the last stage: y_next = acc + (b3 h) k3)
+    // stage K: k = f(Sc) on the tile + K, two vertically adjacent nodes per thread (rows r and r + 1
+    // share their middle loads); the accumulator on the tile + 1 takes (b h) k and the next stage
+    // state y + (a h) k goes to Sn (after the last stage: y_next = acc + (b3 h) k3)
     auto stage = [&](auto kk, const float2* Sc, float2* Sn, float bh, float ah) {
-        constexpr int K = decltype(kk)::value, w = TX + 2 * K, h = TY + 2 * K, off = HALO - K;
-        for (int i = threadIdx.x; i < w * h; i += GS_FUSED_THREADS) {
-            const int r = i / w + off, c = i % w + off;
-            const int q = r * W + c;
-            const float2 sc = Sc[q], sl = Sc[q - 1], sr = Sc[q + 1], sd = Sc[q - W], su = Sc[q + W];
+        constexpr int K = decltype(kk)::value, w = TX + 2 * K, h2 = (TY + 2 * K) / 2, off = HALO - K;
+        auto node = [&](int r, int c, int q, float2 sc, float2 sl, float2 sr, float2 sd, float2 su) {
             float du, dv;
             gs_node<float, POW2>(p, sc.x, sc.y, sl.x, sl.y, sr.x, sr.y, sd.x, sd.y, su.x, su.y, du, dv);
             if constexpr (K > 1) {
-                if (inner(r, c)) {
+                if (r >= HALO - 1 && r < HH - HALO + 1 && c >= HALO - 1 && c < W - HALO + 1) {
                     const float2 a = As[q];
                     As[q] = make_float2(gs_f(bh, du, a.x), gs_f(bh, dv, a.y));
                 }
@@ -429,6 +446,14 @@ __global__ void __launch_bounds__(GS_FUSED_THREADS) gs_step_fused_kernel(GsFused
                 const float2 a = As[q];
                 Sn[q] = make_float2(gs_f(bh, du, a.x), gs_f(bh, dv, a.y));
             }
+        };
+        for (int i = threadIdx.x; i < w * h2; i += GS_FUSED_THREADS) {
+            const int rp = i / w;
+            const int r = 2 * rp + off, c = i - rp * w + off;
+            const int q = r * W + c;
+            const float2 sd = Sc[q - W], s0 = Sc[q], s1 = Sc[q + W], su = Sc[q + 2 * W];
+            node(r, c, q, s0, Sc[q - 1], Sc[q + 1], sd, s1);
+            node(r + 1, c, q + W, s1, Sc[q + W - 1], Sc[q + W + 1], s0, su);
         }
     };
     stage(std::integral_constant<int, 3>{}, S0, S1, cf.bh1, cf.ah2);  // k1 on the tile + 3
@@ -437,26 +462,41 @@ __global__ void __launch_bounds__(GS_FUSED_THREADS) gs_step_fused_kernel(GsFused
     __syncthreads();
     stage(std::integral_constant<int, 1>{}, S0, S1, cf.bh3, 0.0f);    // k3 and y_next on the tile + 1
     __syncthreads();
-    // k0 of the next step = f(y_next) on the tile; y_next and k0 out
-    for (int i = threadIdx.x; i < TX * TY; i += GS_FUSED_THREADS) {
-        const int r = i / TX + HALO, c = i % TX + HALO;
+    // k0 of the next step = f(y_next) on the tile, two rows per thread; y_next and k0 out
+    for (int i = threadIdx.x; i < TX * (TY / 2); i += GS_FUSED_THREADS) {
+        const int rp = i / TX;
+        const int r = 2 * rp + HALO, c = i - rp * TX + HALO;
         const int q = r * W + c;
-        const float2 sc = S1[q], sl = S1[q - 1], sr = S1[q + 1], sd = S1[q - W], su = S1[q + W];
-        float du, dv;
-        gs_node<float, POW2>(p, sc.x, sc.y, sl.x, sl.y, sr.x, sr.y, sd.x, sd.y, su.x, su.y, du, dv);
+        const float2 sd = S1[q - W], s0 = S1[q], s1 = S1[q + W], su = S1[q + 2 * W];
+        float du0, dv0, du1, dv1;
+        const float2 l0 = S1[q - 1], r0 = S1[q + 1], l1 = S1[q + W - 1], r1 = S1[q + W + 1];
+        gs_node<float, POW2>(p, s0.x, s0.y, l0.x, l0.y, r0.x, r0.y, sd.x, sd.y, s1.x, s1.y, du0, dv0);
+        gs_node<float, POW2>(p, s1.x, s1.y, l1.x, l1.y, r1.x, r1.y, s0.x, s0.y, su.x, su.y, du1, dv1);
         const int64_t g = (int64_t)(y0 + r - HALO) * nx + (x0 + c - HALO);
-        P.nu[g] = sc.x;
-        P.nv[g] = sc.y;
-        P.knu[g] = du;
-        P.knv[g] = dv;
+        P.nu[g] = s0.x;
+        P.nv[g] = s0.y;
+        P.knu[g] = du0;
+        P.knv[g] = dv0;
+        P.nu[g + nx] = s1.x;
+        P.nv[g + nx] = s1.y;
+        P.knu[g + nx] = du1;
+        P.knv[g + nx] = dv1;
     }
 }
 
 // Launchers for one precision (instantiated in stencil.cu and, for the parity build, in
 // inst_parity_stencil.cu with -fmad=false).
+// the vector kernels load and store 16 bytes at a time: every plane must start on a 16-byte boundary
+inline bool gs_planes_aligned16(const GsPlanes& P) {
+    const void* ptrs[] = {P.yu, P.yv, P.ku, P.kv, P.k0u, P.k0v, P.ou, P.ov, P.accu, P.accv, P.ynu, P.ynv};
+    for (const void* q : ptrs)
+        if (((uintptr_t)q & 15u) != 0) return false;
+    return true;
+}
+
 template <class T, bool POW2>
 cudaError_t gs_launch_pass(int pass, const GsPlanes& P, const GsParams<T>& p, cudaStream_t s) {
-    if (p.nx % 128 == 0 && p.ny % 16 == 0) {
+    if (p.nx % 128 == 0 && p.ny % 16 == 0 && gs_planes_aligned16(P)) {
         dim3 blk(128);
         dim3 grd(p.nx / 128, p.ny / 16);
         switch (pass) {
