@@ -5,6 +5,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -32,7 +33,7 @@ static bool is_pow2(double x) {
 #define DEGPU_GS_TY 32
 #endif
 constexpr int GS_TX = DEGPU_GS_TX, GS_TY = DEGPU_GS_TY;
-static int g_gs_fused = 1;
+static std::atomic<int> g_gs_fused{1};
 
 // the kernel's shared-memory opt-in (92 KB), set on each device before the first launch there
 // (and so outside any stream capture)
@@ -224,9 +225,7 @@ degpu_status degpu_gray_scott_rk4(const degpu_gray_scott* gs, int32_t precision,
 
 // Internal: the fused FP32 step on (1) or off (0); returns the previous setting.
 int degpu_internal_gs_fused_step(int on) {
-    const int prev = g_gs_fused;
-    g_gs_fused = on ? 1 : 0;
-    return prev;
+    return g_gs_fused.exchange(on ? 1 : 0);
 }
 
 degpu_status degpu_gray_scott_rhs(const degpu_gray_scott* gs, const double* u, const double* v, double* du, double* dv,
