@@ -350,10 +350,10 @@ def _oracle_solve(e, method, threads, math_mode=0):
 # on its one-node-per-thread version, which moves the same arrays)
 GS_NCU_TRAFFIC_FP32 = 1.84e9
 GS_NCU_TRAFFIC_FP32_FUSED = 4.937e8
-# FP32 operations per node and RK4 step (FMA = 2): four evaluations of f (44 each: u v^2, the two
-# sources, two flux differences per axis and field), three stage states (4) and the four
-# accumulation terms (4)
-GS_FLOPS_PER_NODE_STEP = 4 * 44 + 3 * 4 + 4 * 4
+# FP32 operations per node and RK4 step (FMA = 2) of the FP32 form: four evaluations of f (26 each:
+# u v^2, the two 4-neighbour difference sums, 1 - u and F + k, two fused terms per field), three
+# stage states (4 each) and four accumulation terms (4 each)
+GS_FLOPS_PER_NODE_STEP = 4 * 26 + 3 * 4 + 4 * 4
 
 # the hyperplane workload's plane: pos = (y0, y1) through (0.1, -0.2) with normal (1, 1)
 PLANE = ([0, 1], [0.1, -0.2], [1.0, 1.0])
